@@ -1,0 +1,258 @@
+"""The CPU oracle pinned against the reference's known-answer tests and against
+independent numpy restatements of each block operation (CPU only)."""
+import zlib
+
+import numpy as np
+import pytest
+
+from oracle import oracle
+from tests import kat
+
+
+def _einsum_labels(dl, ll, rl):
+    letters = {}
+    for lab in list(dl) + list(ll) + list(rl):
+        letters.setdefault(lab, "abcdefghijklmnopqrstuvwxyz"[len(letters)])
+    f = lambda labs: "".join(letters[x] for x in labs)
+    return f"{f(ll)},{f(rl)}->{f(dl)}"
+
+
+def _blk(flat, ext):
+    return flat.reshape(ext, order="F") if len(ext) else flat.reshape(())
+
+
+@pytest.mark.parametrize("name", ["contraction_small_test", "contraction_small_test2", "contract_to_scalar"])
+def test_kat_contractions(name):
+    c = kat.case(name)
+    L = kat.fill(c["l_fill"], kat.size(c["l_ext"]))
+    R = kat.fill(c["r_fill"], kat.size(c["r_ext"]))
+    ierr, D = oracle.contract_labels(c["d_labels"], c["l_labels"], c["r_labels"], L, c["l_ext"], R,
+                                     c["r_ext"], c["d_ext"])
+    assert ierr == 0
+    np.testing.assert_array_equal(D, np.array(c["expected"]))
+
+
+@pytest.mark.parametrize("name", ["transpose_tmp", "transpose4d_tmp", "transpose4d_square_tmp"])
+def test_kat_permutes(name):
+    c = kat.case(name)
+    S = kat.fill(c["s_fill"], kat.size(c["s_ext"]))
+    perm = kat.perm_from_labels(c["d_labels"], c["s_labels"])
+    ierr, D = oracle.tensor_block_copy(c["s_ext"], perm, S)
+    assert ierr == 0
+    np.testing.assert_array_equal(D, np.array(c["expected"]))
+    if "esum" in c:
+        sl, dl = c["s_labels"], c["d_labels"]
+        e1 = oracle.contract_labels([], sl, sl, S, c["s_ext"], S, c["s_ext"], [])[1][0]
+        e2 = oracle.contract_labels([], dl, dl, D, c["d_ext"], D, c["d_ext"], [])[1][0]
+        e3 = oracle.contract_labels([], sl, dl, S, c["s_ext"], D, c["d_ext"], [])[1][0]
+        assert [e1, e2, e3] == c["esum"]
+
+
+def test_kat_sum_op_and_self_multiply():
+    c = kat.case("sum_op")
+    n = kat.size(c["ext"])
+    a = kat.fill(c["a_fill"], n)
+    cc = kat.fill(c["c_fill"], n)
+    d = np.empty(n)
+    e = np.empty(n)
+    ids = [1, 2]
+    assert oracle.block_add_sub(0, ids, ids, ids, c["ext"], 0, d, a, cc) == 0
+    assert oracle.block_add_sub(1, ids, ids, ids, c["ext"], 0, e, d, cc) == 0
+    np.testing.assert_array_equal(d, c["expected_d"])
+    np.testing.assert_array_equal(e, c["expected_e"])
+
+    s = kat.case("self_multiply_test")
+    a = kat.fill(s["a_fill"], n)
+    assert oracle.block_add_sub(0, ids, ids, ids, s["ext"], 1, a, a.copy(), a.copy()) == 0
+    assert oracle.tensor_block_scale(a, s["ext"], s["factor"]) == 0
+    np.testing.assert_array_equal(a, s["expected"])
+
+
+def test_get_contraction_ptrn_errors():
+    # ierr 1: negative rank; 2: odd label count; 3: no operands; 4: unpaired
+    # label; 5: label used more than twice; 6: trace / operand-only pairing
+    assert oracle.get_contraction_ptrn(-1, 1, 1, [1, 1])[0] == 1
+    assert oracle.get_contraction_ptrn(1, 1, 1, [1, 1, 2])[0] == 2
+    assert oracle.get_contraction_ptrn(2, 0, 0, [1, 1])[0] == 3
+    assert oracle.get_contraction_ptrn(0, 0, 0, [])[0] == 0
+    assert oracle.get_contraction_ptrn(1, 1, 2, [1, 2, 1, 3])[0] == 4
+    assert oracle.get_contraction_ptrn(0, 2, 2, [1, 1, 1, 1])[0] == 5
+    assert oracle.get_contraction_ptrn(2, 2, 0, [1, 2, 1, 1])[0] == 4  # sorted 1,1,1,2
+    assert oracle.get_contraction_ptrn(2, 2, 0, [1, 1, 1, 1])[0] == 5
+    assert oracle.get_contraction_ptrn(0, 2, 2, [1, 1, 2, 2])[0] == 6  # trace in left
+    assert oracle.get_contraction_ptrn(2, 1, 1, [1, 1, 2, 2])[0] == 6  # repeated dest label
+
+
+def test_get_contraction_ptrn_values():
+    # ladder: R(a,b,i,j) = V(a,b,c,d) T(c,d,i,j)
+    ierr, p = oracle.get_contraction_ptrn(4, 4, 4, [1, 2, 3, 4, 1, 2, 5, 6, 5, 6, 3, 4])
+    assert ierr == 0 and p == [1, 2, -1, -2, -3, -4, 3, 4]
+    # ring: R(a,i,b,j) = V(a,k,c,i) T(c,b,k,j)
+    ierr, p = oracle.get_contraction_ptrn(4, 4, 4, [1, 2, 3, 4, 1, 5, 6, 2, 6, 3, 5, 4])
+    assert ierr == 0 and p == [1, -3, -1, 2, -3, 3, -2, 4]
+
+
+def test_contr_ptrn_ok():
+    assert oracle.contr_ptrn_ok([1, 2, -1, -2, -3, -4, 3, 4], [3, 3, 4, 4], [4, 4, 5, 5], [3, 3, 5, 5])
+    assert not oracle.contr_ptrn_ok([1, 2, -1, -2, -3, -4, 3, 4], [3, 3, 4, 4], [4, 9, 5, 5], [3, 3, 5, 5])
+    assert not oracle.contr_ptrn_ok([1, 1, -1, -2, -3, -4, 3, 4], [3, 3, 4, 4], [4, 4, 5, 5], [3, 3, 5, 5])
+
+
+RANDOM_PATTERNS = [
+    # (d labels, l labels, r labels)
+    ("abij", "abcd", "cdij"),      # ladder
+    ("aibj", "akci", "cbkj"),      # ring (both operands permuted)
+    ("abcijk", "bcdk", "adij"),    # triples term 1
+    ("il", "ijkl", "jk"),
+    ("ba", "ac", "cb"),            # destination permuted
+    ("", "abc", "cab"),            # full contraction, permuted right
+    ("ab", "a", "b"),              # outer product
+    ("ab", "ab", ""),              # right scalar
+    ("ba", "", "ab"),              # left scalar, permuted dest
+    ("", "", ""),                  # scalar * scalar
+    ("fedcba", "abcx", "xdef"),    # rank 6 destination
+]
+
+
+@pytest.mark.parametrize("dl,ll,rl", RANDOM_PATTERNS)
+def test_contract_random_vs_einsum(dl, ll, rl):
+    rng = np.random.default_rng(zlib.crc32((dl + "|" + ll + "|" + rl).encode()))
+    ext = {lab: int(rng.integers(2, 6)) for lab in set(dl + ll + rl)}
+    lid = {lab: i + 1 for i, lab in enumerate(sorted(set(dl + ll + rl)))}
+    le, re, de = [ext[x] for x in ll], [ext[x] for x in rl], [ext[x] for x in dl]
+    L = rng.standard_normal(kat.size(le))
+    R = rng.standard_normal(kat.size(re))
+    ierr, D = oracle.contract_labels([lid[x] for x in dl], [lid[x] for x in ll], [lid[x] for x in rl],
+                                     L, le, R, re, de)
+    assert ierr == 0
+    ref = np.einsum(_einsum_labels(dl, ll, rl), _blk(L, le), _blk(R, re))
+    np.testing.assert_allclose(D, np.asarray(ref).ravel(order="F"), rtol=1e-12, atol=1e-12)
+    # the BLAS-path restatement used as the CPU baseline agrees too
+    if dl and ll and rl:
+        _, p = oracle.get_contraction_ptrn(len(dl), len(ll), len(rl),
+                                           [lid[x] for x in dl + ll + rl])
+        D2 = oracle.contract_blas(p, L, le, R, re, de)
+        np.testing.assert_allclose(D2, D, rtol=1e-12, atol=1e-12)
+
+
+def test_contract_overwrites_and_bad_pattern():
+    L = np.ones(6)
+    R = np.ones(6)
+    D = np.full(4, 7.0)
+    # D(a,b) = L(a,c) R(c,b): 2x3 * 3x2
+    assert oracle.tensor_block_contract([1, -1, -2, 2], L, [2, 3], R, [3, 2], D, [2, 2]) == 0
+    np.testing.assert_array_equal(D, 3.0)
+    # extent mismatch -> ierr 1, negative rank -> -1
+    assert oracle.tensor_block_contract([1, -1, -2, 2], L, [2, 3], R, [4, 2], D, [2, 2]) == 1
+
+
+def test_permute_random_vs_numpy():
+    rng = np.random.default_rng(3)
+    for rank in range(1, 7):
+        ext = [int(x) for x in rng.integers(1, 6, rank)]
+        perm = [int(x) + 1 for x in rng.permutation(rank)]
+        S = rng.standard_normal(kat.size(ext))
+        ierr, D = oracle.tensor_block_copy(ext, perm, S)
+        assert ierr == 0
+        n2o = [0] * rank
+        for i, p in enumerate(perm):
+            n2o[p - 1] = i
+        ref = np.transpose(S.reshape(ext, order="F"), n2o).ravel(order="F")
+        np.testing.assert_array_equal(D, ref)
+
+
+def test_elementwise_ops():
+    rng = np.random.default_rng(5)
+    ext = [3, 4, 5]
+    t0 = rng.standard_normal(60)
+    t1 = rng.standard_normal(60)
+    a = t0.copy()
+    assert oracle.tensor_block_add(ext, a, t1, 0.5) == 0
+    np.testing.assert_array_equal(a, t0 + t1 * 0.5)
+    a = t0.copy()
+    oracle.tensor_block_add(ext, a, t1, 1.0 + 5e-14)  # treated as exactly 1
+    np.testing.assert_array_equal(a, t0 + t1)
+    a = t0.copy()
+    oracle.tensor_block_scale(a, ext, -2.5)
+    np.testing.assert_array_equal(a, t0 * -2.5)
+    v, ierr = oracle.tensor_block_norm2(t0, ext)
+    assert ierr == 0 and abs(v - float(np.sum(t0 * t0))) < 1e-12
+    a = t0.copy()
+    oracle.tensor_block_init(a, ext, 3.25)
+    np.testing.assert_array_equal(a, 3.25)
+    d = np.empty(60)
+    oracle.block_scale_and_copy(d, t0, 3.0)
+    np.testing.assert_array_equal(d, t0 * 3.0)
+    a = t0.copy()
+    oracle.block_increment(a, 0.125)
+    np.testing.assert_array_equal(a, t0 + 0.125)
+    a = t0.copy()
+    oracle.block_accumulate(a, t1)
+    np.testing.assert_array_equal(a, t0 + t1)
+
+
+def test_slice_insert():
+    rng = np.random.default_rng(6)
+    text, sext, beg = [6, 5, 4], [3, 2, 2], [2, 1, 1]
+    T = rng.standard_normal(120)
+    ierr, S = oracle.tensor_block_slice(T, text, sext, beg)
+    assert ierr == 0
+    Tb = T.reshape(text, order="F")
+    np.testing.assert_array_equal(S, Tb[2:5, 1:3, 1:3].ravel(order="F"))
+    T2 = np.zeros(120)
+    assert oracle.tensor_block_insert(T2, text, S, sext, beg) == 0
+    ref = np.zeros(text)
+    ref[2:5, 1:3, 1:3] = Tb[2:5, 1:3, 1:3]
+    np.testing.assert_array_equal(T2, ref.ravel(order="F"))
+
+
+def test_block_add_permuted_rhs():
+    rng = np.random.default_rng(7)
+    ext_d = [3, 4, 5]  # d(i,j,k) += r(k,i,j)
+    r_ext = [5, 3, 4]
+    d = rng.standard_normal(60)
+    r = rng.standard_normal(60)
+    out = d.copy()
+    assert oracle.block_add_sub(0, [1, 2, 3], [1, 2, 3], [3, 1, 2], r_ext, 1, out, d.copy(), r) == 0
+    ref = d.reshape(ext_d, order="F") + np.transpose(r.reshape(r_ext, order="F"), (1, 2, 0))
+    np.testing.assert_array_equal(out, ref.ravel(order="F"))
+    # without the += form the labels must agree
+    assert oracle.block_add_sub(0, [1, 2, 3], [1, 2, 3], [3, 1, 2], r_ext, 0, out, d, r) == 2
+
+
+@pytest.mark.parametrize("rank0,rank1", [(2, 2), (2, 1), (4, 2), (4, 1), (6, 2)])
+def test_energy_denominator(rank0, rank1):
+    rng = np.random.default_rng(rank0 * 10 + rank1)
+    segs = [3, 4, 2, 5]
+    norb = sum(segs)
+    eps = np.sort(rng.uniform(-2, 5, norb))
+    fock = np.diag(eps) + 0.01 * rng.standard_normal((norb, norb))
+    f1 = fock.ravel(order="F") if rank1 == 2 else eps.copy()
+    ext1 = [norb, norb] if rank1 == 2 else [norb]
+    iv = [int(x) for x in rng.integers(1, len(segs) + 1, rank0)]
+    ext0 = [segs[v - 1] for v in iv]
+    if rank0 == 6:
+        ext0[4] = 1  # a simple index: offset = value - 1
+        iv[4] = 7
+    data = rng.standard_normal(kat.size(ext0))
+    out = data.copy()
+    assert oracle.energy_denominator_rhf(iv, ext0, out, ext1, f1, segs) == 0
+    e = np.diag(fock) if rank1 == 2 else eps
+    offs = []
+    for q in range(rank0):
+        if rank0 == 6 and ext0[q] == 1:
+            offs.append(iv[q] - 1)
+        else:
+            offs.append(sum(segs[: iv[q] - 1]))
+    blk = data.reshape(ext0, order="F")
+    ref = np.empty_like(blk)
+    for idx in np.ndindex(*ext0):
+        ev = [e[idx[q] + offs[q]] for q in range(rank0)]
+        if rank0 == 2:
+            den = ev[1] - ev[0]
+        elif rank0 == 4:
+            den = ev[1] + ev[3] - ev[0] - ev[2]
+        else:
+            den = ev[1] + ev[3] + ev[5] - ev[0] - ev[2] - ev[4]
+        ref[idx] = blk[idx] / den
+    np.testing.assert_array_equal(out, ref.ravel(order="F"))
