@@ -1,0 +1,614 @@
+// extern "C" entry points: the drop-in replacements of the reference's
+// Fortran kernels (host buffers), of its legacy GPU API (device buffers), the
+// energy-denominator super instruction, and the device-resident a4g_* API.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <map>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "a4g_internal.h"
+
+using namespace a4g;
+
+namespace {
+
+int64_t count(int rank, const int* ext) {
+  int64_t n = 1;
+  for (int i = 0; i < rank; ++i) n *= ext[i];
+  return n;
+}
+
+bool extents_ok(int rank, const int* ext) {
+  if (rank > 0 && !ext) return false;
+  for (int i = 0; i < rank; ++i)
+    if (ext[i] <= 0) return false;
+  return true;
+}
+
+// Maps an a4g status onto the reference's ierr convention for the drop-ins:
+// argument/pattern problems keep the reference's own codes (set by callers);
+// runtime failures are reported as negative codes the reference never uses.
+int runtime_ierr(int rc) { return rc == A4G_OK ? 0 : -100 - rc; }
+
+// Host-buffer staging through the library arena: copy in, run, copy out, sync.
+struct Staged {
+  char* base = nullptr;
+  size_t used = 0;
+  double* take(int64_t n) {
+    double* p = reinterpret_cast<double*>(base + used);
+    used += (size_t(n) * sizeof(double) + 255) & ~size_t(255);
+    return p;
+  }
+};
+
+int stage(size_t bytes, Staged* st) {
+  void* p = nullptr;
+  int rc = arena_reserve(bytes, &p);
+  if (rc) return rc;
+  st->base = static_cast<char*>(p);
+  st->used = 0;
+  return A4G_OK;
+}
+
+size_t rounded(int64_t n) { return (size_t(n) * sizeof(double) + 255) & ~size_t(255); }
+
+int h2d(double* d, const double* h, int64_t n, cudaStream_t s) {
+  A4G_CUDA(cudaMemcpyAsync(d, h, size_t(n) * sizeof(double), cudaMemcpyHostToDevice, s));
+  return A4G_OK;
+}
+int d2h(double* h, const double* d, int64_t n, cudaStream_t s) {
+  A4G_CUDA(cudaMemcpyAsync(h, d, size_t(n) * sizeof(double), cudaMemcpyDeviceToHost, s));
+  return A4G_OK;
+}
+
+std::mutex g_host_mu;  // host-buffer entries share one arena
+
+std::map<std::string, std::vector<int>> g_predefined;
+std::mutex g_predef_mu;
+
+// o2n (1-based) from two label lists: source dim j goes to the destination
+// dim i carrying the same label (permute_rhs_to_lhs, interpreter.cpp:2049-2084).
+bool perm_from_labels(int rank, const int* dst_labels, const int* src_labels, int* o2n) {
+  for (int j = 0; j < rank; ++j) o2n[j] = 0;
+  for (int i = 0; i < rank; ++i) {
+    int j = 0;
+    while (j < rank && src_labels[j] != dst_labels[i]) ++j;
+    if (j >= rank || o2n[j] != 0) return false;
+    o2n[j] = i + 1;
+  }
+  return true;
+}
+
+int contract_device(const int* ptrn, const double* l, int lrank, const int* lext, const double* r,
+                    int rrank, const int* rext, double* d, int drank, const int* dext, int beta,
+                    double* scratch, cudaStream_t s) {
+  const DevPlan* p = nullptr;
+  int rc = get_dev_plan(ptrn, lrank, lext, rrank, rext, drank, dext, &p);
+  if (rc) return rc;
+  if (p->host.kind == ContractKind::kTensorTensor) return launch_contract_f64(p, l, r, d, beta, s);
+  return launch_scalar_cases(p, l, r, d, beta, scratch, s);
+}
+
+// Per-context scratch for the deterministic reductions of the device API.
+double* reduction_scratch() {
+  static double* p = nullptr;
+  if (!p) {
+    if (cudaMalloc(&p, sizeof(double) * (dot_scratch_len() + 8)) != cudaSuccess) p = nullptr;
+  }
+  return p;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* a4g_version(void) { return "aces4_gb300 0.1 (sm_103a)"; }
+
+const char* a4g_last_error(void) { return last_error_text(); }
+
+// ============================================================ drop-in (host)
+long long tensor_size_by_shape_(int* num_dim, int* dims, int* ierr) {
+  *ierr = 0;
+  long long s = 1;
+  if (*num_dim > 0) {
+    for (int i = 0; i < *num_dim; ++i) s *= dims[i];
+    if (s <= 0) *ierr = 2;
+  } else if (*num_dim < 0) {
+    *ierr = 1;
+    s = 0;
+  }
+  return s;
+}
+
+void get_contraction_ptrn_(int* drank, int* lrank, int* rrank, int* aces_ptrn, int* my_ptrn,
+                           int* ierr) {
+  *ierr = a4g::get_contraction_ptrn(*drank, *lrank, *rrank, aces_ptrn, my_ptrn);
+}
+
+void tensor_block_init__(int* nthreads, double* tens, int* tens_rank, int* ext, double* sval,
+                         int* ierr) {
+  (void)nthreads;
+  if (*tens_rank < 0) return void(*ierr = -1);
+  if (!extents_ok(*tens_rank, ext) || !tens) return void(*ierr = -1);
+  std::lock_guard<std::mutex> lock(g_host_mu);
+  int rc = ensure_init();
+  const int64_t n = count(*tens_rank, ext);
+  Staged st;
+  if (!rc) rc = stage(rounded(n), &st);
+  if (!rc) {
+    cudaStream_t s = ctx()->stream;
+    double* d = st.take(n);
+    rc = launch_fill(d, n, *sval, s);
+    if (!rc) rc = d2h(tens, d, n, s);
+    if (!rc) rc = check_device_flag(s);
+  }
+  *ierr = runtime_ierr(rc);
+}
+
+void tensor_block_scale__(int* nthreads, double* tens, int* tens_rank, int* ext, double* f,
+                          int* ierr) {
+  (void)nthreads;
+  if (*tens_rank < 0 || !extents_ok(*tens_rank, ext) || !tens) return void(*ierr = -1);
+  std::lock_guard<std::mutex> lock(g_host_mu);
+  int rc = ensure_init();
+  const int64_t n = count(*tens_rank, ext);
+  Staged st;
+  if (!rc) rc = stage(rounded(n), &st);
+  if (!rc) {
+    cudaStream_t s = ctx()->stream;
+    double* d = st.take(n);
+    rc = h2d(d, tens, n, s);
+    if (!rc) rc = launch_scale(d, n, *f, s);
+    if (!rc) rc = d2h(tens, d, n, s);
+    if (!rc) rc = check_device_flag(s);
+  }
+  *ierr = runtime_ierr(rc);
+}
+
+double tensor_block_norm2__(int* nthreads, double* tens, int* tens_rank, int* ext, int* ierr) {
+  (void)nthreads;
+  if (*tens_rank < 0 || !extents_ok(*tens_rank, ext) || !tens) {
+    *ierr = -1;
+    return 0.0;
+  }
+  std::lock_guard<std::mutex> lock(g_host_mu);
+  int rc = ensure_init();
+  const int64_t n = count(*tens_rank, ext);
+  double result = 0.0;
+  Staged st;
+  if (!rc) rc = stage(rounded(n) + rounded(dot_scratch_len() + 1), &st);
+  if (!rc) {
+    cudaStream_t s = ctx()->stream;
+    double* d = st.take(n);
+    double* scratch = st.take(dot_scratch_len());
+    double* out = st.take(1);
+    rc = h2d(d, tens, n, s);
+    if (!rc) rc = launch_dot(d, d, nullptr, nullptr, n, out, scratch, dot_scratch_len(), s);
+    if (!rc) rc = d2h(&result, out, 1, s);
+    if (!rc) rc = check_device_flag(s);
+  }
+  *ierr = runtime_ierr(rc);
+  return result;
+}
+
+static void slice_insert_host(int insert, int* dim_num, double* tens, int* text, double* slice,
+                              int* sext, int* beg, int* ierr) {
+  if (*dim_num < 0) return void(*ierr = 1);
+  if (!tens || !slice) return void(*ierr = 1);
+  std::lock_guard<std::mutex> lock(g_host_mu);
+  int rc = ensure_init();
+  const int64_t nt = count(*dim_num, text), ns = count(*dim_num, sext);
+  Staged st;
+  if (!rc) rc = stage(rounded(nt) + rounded(ns), &st);
+  if (!rc) {
+    cudaStream_t s = ctx()->stream;
+    double* dt = st.take(nt);
+    double* ds = st.take(ns);
+    if (*dim_num == 0) {
+      rc = insert ? h2d(dt, slice, 1, s) : h2d(ds, tens, 1, s);
+      if (!rc) rc = insert ? d2h(tens, dt, 1, s) : d2h(slice, ds, 1, s);
+    } else {
+      rc = h2d(dt, tens, nt, s);
+      if (!rc && insert) rc = h2d(ds, slice, ns, s);
+      if (!rc) rc = launch_slice_insert(insert, *dim_num, dt, text, ds, sext, beg, s);
+      if (!rc) rc = insert ? d2h(tens, dt, nt, s) : d2h(slice, ds, ns, s);
+    }
+    if (!rc) rc = check_device_flag(s);
+  }
+  *ierr = rc == A4G_ERR_ARG ? 1 : runtime_ierr(rc);
+}
+
+void tensor_block_slice__(int* nthreads, int* dim_num, double* tens, int* tens_ext, double* slice,
+                          int* slice_ext, int* ext_beg, int* ierr) {
+  (void)nthreads;
+  slice_insert_host(0, dim_num, tens, tens_ext, slice, slice_ext, ext_beg, ierr);
+}
+
+void tensor_block_insert__(int* nthreads, int* dim_num, double* tens, int* tens_ext, double* slice,
+                           int* slice_ext, int* ext_beg, int* ierr) {
+  (void)nthreads;
+  slice_insert_host(1, dim_num, tens, tens_ext, slice, slice_ext, ext_beg, ierr);
+}
+
+void tensor_block_add__(const int* nthreads, const int* dim_num, int* ext, double* t0, double* t1,
+                        const double* scale_fac, int* ierr) {
+  (void)nthreads;
+  if (*dim_num < 0 || !extents_ok(*dim_num, ext) || !t0 || !t1) return void(*ierr = -1);
+  std::lock_guard<std::mutex> lock(g_host_mu);
+  int rc = ensure_init();
+  const int64_t n = count(*dim_num, ext);
+  Staged st;
+  if (!rc) rc = stage(2 * rounded(n), &st);
+  if (!rc) {
+    cudaStream_t s = ctx()->stream;
+    double* d0 = st.take(n);
+    double* d1 = st.take(n);
+    rc = h2d(d0, t0, n, s);
+    if (!rc) rc = h2d(d1, t1, n, s);
+    if (!rc) rc = launch_add_scaled(d0, d1, n, *scale_fac, s);
+    if (!rc) rc = d2h(t0, d0, n, s);
+    if (!rc) rc = check_device_flag(s);
+  }
+  *ierr = runtime_ierr(rc);
+}
+
+void tensor_block_copy__(int* nthreads, int* dim_num, int* ext, int* dim_transp, double* tin,
+                         double* tout, int* ierr) {
+  (void)nthreads;
+  if (*dim_num < 0) return void(*ierr = *dim_num);
+  if (!tin || !tout || !extents_ok(*dim_num, ext)) return void(*ierr = 1);
+  std::lock_guard<std::mutex> lock(g_host_mu);
+  int rc = ensure_init();
+  const int64_t n = count(*dim_num, ext);
+  Staged st;
+  if (!rc) rc = stage(2 * rounded(n), &st);
+  if (!rc) {
+    cudaStream_t s = ctx()->stream;
+    double* din = st.take(n);
+    double* dout = st.take(n);
+    rc = h2d(din, tin, n, s);
+    if (!rc) rc = launch_permute(*dim_num, ext, dim_transp + 1, din, dout, s);
+    if (!rc) rc = d2h(tout, dout, n, s);
+    if (!rc) rc = check_device_flag(s);
+  }
+  *ierr = rc == A4G_ERR_ARG ? 1 : runtime_ierr(rc);
+}
+
+void tensor_block_contract__(int* nthreads, int* ptrn, double* ltens, int* lrank, int* lext,
+                             double* rtens, int* rrank, int* rext, double* dtens, int* drank,
+                             int* dext, int* ierr) {
+  (void)nthreads;
+  if (!(*lrank >= 0 && *lrank <= kMaxRank && *rrank >= 0 && *rrank <= kMaxRank && *drank >= 0 &&
+        *drank <= kMaxRank))
+    return void(*ierr = -1);
+  if (!a4g::contr_ptrn_ok(ptrn, *lrank, *rrank, *drank, lext, rext, dext)) return void(*ierr = 1);
+  if (!ltens || !rtens || !dtens || !extents_ok(*lrank, lext) || !extents_ok(*rrank, rext))
+    return void(*ierr = 1);
+  std::lock_guard<std::mutex> lock(g_host_mu);
+  int rc = ensure_init();
+  const int64_t nl = count(*lrank, lext), nr = count(*rrank, rext), nd = count(*drank, dext);
+  Staged st;
+  if (!rc) rc = stage(rounded(nl) + rounded(nr) + rounded(nd) + rounded(dot_scratch_len()), &st);
+  if (!rc) {
+    cudaStream_t s = ctx()->stream;
+    double* dl = st.take(nl);
+    double* dr = st.take(nr);
+    double* dd = st.take(nd);
+    double* scratch = st.take(dot_scratch_len());
+    rc = h2d(dl, ltens, nl, s);
+    if (!rc) rc = h2d(dr, rtens, nr, s);
+    if (!rc)
+      rc = contract_device(ptrn, dl, *lrank, lext, dr, *rrank, rext, dd, *drank, dext, 0, scratch, s);
+    if (!rc) rc = d2h(dtens, dd, nd, s);
+    if (!rc) rc = check_device_flag(s);
+  }
+  *ierr = rc == A4G_ERR_PATTERN ? 1 : runtime_ierr(rc);
+}
+
+// ============================================================ legacy GPU API
+void _init_gpu(int* devid, int* myRank) {
+  int n = 0;
+  if (cudaGetDeviceCount(&n) != cudaSuccess || n == 0) {
+    *devid = -1;
+    set_error("no CUDA device");
+    return;
+  }
+  const int dev = (*myRank) % n;
+  if (cudaSetDevice(dev) != cudaSuccess) {
+    *devid = -1;
+    set_error("cudaSetDevice failed");
+    return;
+  }
+  *devid = dev;
+  ensure_init();
+}
+
+void _gpu_axpy(double* y, double* x, const double alpha, const int numElems) {
+  if (ensure_init()) return;
+  if (!launch_axpy(y, x, numElems, alpha, ctx()->stream)) check_device_flag(ctx()->stream);
+}
+
+void _gpu_double_memset(double* g, double value, const int numElems) {
+  if (ensure_init()) return;
+  if (!launch_fill(g, numElems, value, ctx()->stream)) check_device_flag(ctx()->stream);
+}
+
+void _gpu_selfmultiply(double* x, const double alpha, const int numElems) {
+  if (ensure_init()) return;
+  if (!launch_scale(x, numElems, alpha, ctx()->stream)) check_device_flag(ctx()->stream);
+}
+
+void _gpu_contract(double* y, const int ny, const int* yDims, const int* yInds, double* x1,
+                   const int n1, const int* x1Dims, const int* x1Inds, double* x2, const int n2,
+                   const int* x2Dims, const int* x2Inds) {
+  if (ensure_init()) return;
+  a4g_contract_labels(yInds, x1Inds, x2Inds, x1, n1, x1Dims, x2, n2, x2Dims, y, ny, yDims, 0,
+                      nullptr);
+  check_device_flag(ctx()->stream);
+}
+
+void _gpu_permute(double* y, const int ny, const int* yDims, const int* yInds, double* x,
+                  const int nx, const int* xDims, const int* xInds) {
+  (void)yDims;
+  if (ensure_init()) return;
+  if (ny != nx) return set_error("_gpu_permute: rank mismatch");
+  int o2n[kMaxRank + 1];
+  o2n[0] = 1;
+  if (!perm_from_labels(nx, yInds, xInds, o2n + 1)) return set_error("_gpu_permute: labels differ");
+  if (!launch_permute(nx, xDims, o2n + 1, x, y, ctx()->stream)) check_device_flag(ctx()->stream);
+}
+
+void _gpu_host_to_device(double* c_addr, double* g_addr, const int numElems) {
+  cudaError_t e = cudaMemcpy(g_addr, c_addr, size_t(numElems) * sizeof(double), cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) cuda_fail(e, "_gpu_host_to_device");
+}
+
+double* _gpu_allocate(const int numElems) {
+  double* p = nullptr;
+  cudaError_t e = cudaMalloc(&p, size_t(numElems > 0 ? numElems : 1) * sizeof(double));
+  if (e != cudaSuccess) {
+    cuda_fail(e, "_gpu_allocate");
+    return nullptr;
+  }
+  e = cudaMemset(p, 0, size_t(numElems > 0 ? numElems : 1) * sizeof(double));
+  if (e != cudaSuccess) cuda_fail(e, "_gpu_allocate memset");
+  return p;
+}
+
+void _gpu_device_to_host(double* c_addr, double* g_addr, const int numElems) {
+  cudaError_t e = cudaMemcpy(c_addr, g_addr, size_t(numElems) * sizeof(double), cudaMemcpyDeviceToHost);
+  if (e != cudaSuccess) cuda_fail(e, "_gpu_device_to_host");
+}
+
+void _gpu_device_to_device(double* dst, double* src, const int numElems) {
+  cudaError_t e = cudaMemcpy(dst, src, size_t(numElems) * sizeof(double), cudaMemcpyDeviceToDevice);
+  if (e != cudaSuccess) cuda_fail(e, "_gpu_device_to_device");
+}
+
+void _gpu_free(double* g_addr) {
+  if (g_addr) cudaFree(g_addr);
+}
+
+// ============================================================ super instruction
+int a4g_set_predefined_int_array(const char* name, int n, const int* values) {
+  if (!name || n < 0 || (n > 0 && !values)) return fail(A4G_ERR_ARG, "bad predefined array");
+  std::lock_guard<std::mutex> lock(g_predef_mu);
+  g_predefined[name] = std::vector<int>(values, values + n);
+  return A4G_OK;
+}
+
+// Orbital offsets of each block dimension (energy_denominator_rhf.F:57-88,
+// 140-220): the sum of the segment sizes before the block's segment; for rank
+// 6 an extent of 1 marks a simple index whose offset is its value - 1.
+// Every orbital index the kernel will read is checked against the energy /
+// Fock block here, on the host, so the device never reads out of bounds.
+static int denominator_offsets(int rank0, const int* iv, const int* ext0, int rank1, const int* ext1,
+                               const std::vector<int>& segs, int* off) {
+  const int norb = rank1 == 2 ? std::min(ext1[0], ext1[1]) : ext1[0];
+  for (int q = 0; q < rank0; ++q) {
+    off[q] = 0;
+    if (ext0[q] <= 0) return fail(A4G_ERR_ARG, "non-positive extent");
+    if (rank0 == 6 && ext0[q] == 1) {
+      off[q] = iv[q] - 1;
+    } else {
+      for (int i = 1; i <= iv[q] - 1; ++i) {
+        if (i > int(segs.size())) return fail(A4G_ERR_ARG, "segment number beyond moa_seg_ranges");
+        off[q] += segs[i - 1];
+      }
+    }
+    if (off[q] < 0 || off[q] + ext0[q] > norb)
+      return fail(A4G_ERR_ARG, "block orbital range exceeds the orbital-energy array");
+  }
+  return A4G_OK;
+}
+
+void energy_denominator_rhf(int* array_slot_0, int* rank_0, int* index_values_0, int* size_0,
+                            int* extents_0, double* data_0, int* array_slot_1, int* rank_1,
+                            int* index_values_1, int* size_1, int* extents_1, double* data_1,
+                            int* ierr) {
+  (void)array_slot_0, (void)array_slot_1, (void)index_values_1;
+  *ierr = 0;
+  const int r0 = *rank_0, r1 = *rank_1;
+  // the reference acts only on these rank combinations and leaves data untouched otherwise
+  if (!((r0 == 2 || r0 == 4) && (r1 == 1 || r1 == 2)) && !(r0 == 6 && r1 == 2)) return;
+  std::vector<int> segs;
+  {
+    std::lock_guard<std::mutex> lock(g_predef_mu);
+    auto it = g_predefined.find("moa_seg_ranges");
+    if (it == g_predefined.end()) {
+      set_error("energy_denominator_rhf: predefined array moa_seg_ranges not registered");
+      *ierr = 1;
+      return;
+    }
+    segs = it->second;
+  }
+  int off[6];
+  if (denominator_offsets(r0, index_values_0, extents_0, r1, extents_1, segs, off))
+    return void(*ierr = 1);
+  std::lock_guard<std::mutex> lock(g_host_mu);
+  int rc = ensure_init();
+  const int64_t n0 = count(r0, extents_0), n1 = count(r1, extents_1);
+  (void)size_0, (void)size_1;
+  Staged st;
+  if (!rc) rc = stage(rounded(n0) + rounded(n1), &st);
+  if (!rc) {
+    cudaStream_t s = ctx()->stream;
+    double* d0 = st.take(n0);
+    double* d1 = st.take(n1);
+    rc = h2d(d0, data_0, n0, s);
+    if (!rc) rc = h2d(d1, data_1, n1, s);
+    if (!rc) rc = launch_denominator(r0, off, extents_0, d0, r1, extents_1[0], d1, s);
+    if (!rc) rc = d2h(data_0, d0, n0, s);
+    if (!rc) rc = check_device_flag(s);
+  }
+  *ierr = runtime_ierr(rc);
+}
+
+// ============================================================ device API
+int a4g_init(int device) {
+  if (device >= 0) A4G_CUDA(cudaSetDevice(device));
+  return ensure_init();
+}
+
+int a4g_sync(void* stream) {
+  int rc = ensure_init();
+  if (rc) return rc;
+  return check_device_flag(pick(stream));
+}
+
+void* a4g_default_stream(void) {
+  if (ensure_init()) return nullptr;
+  return ctx()->stream;
+}
+
+int a4g_contract(const int* ptrn, const double* l, int lrank, const int* lext, const double* r,
+                 int rrank, const int* rext, double* d, int drank, const int* dext, int beta,
+                 void* stream) {
+  int rc = ensure_init();
+  if (rc) return rc;
+  if (!l || !r || !d || !ptrn) return fail(A4G_ERR_ARG, "null pointer");
+  double* scratch = reduction_scratch();
+  if (!scratch) return fail(A4G_ERR_NOMEM, "reduction scratch");
+  return contract_device(ptrn, l, lrank, lext, r, rrank, rext, d, drank, dext, beta ? 1 : 0,
+                         scratch, pick(stream));
+}
+
+int a4g_contract_labels(const int* d_labels, const int* l_labels, const int* r_labels,
+                        const double* l, int lrank, const int* lext, const double* r, int rrank,
+                        const int* rext, double* d, int drank, const int* dext, int beta,
+                        void* stream) {
+  if (drank < 0 || lrank < 0 || rrank < 0 || drank + lrank + rrank > 3 * kMaxRank)
+    return fail(A4G_ERR_ARG, "rank out of range");
+  int aces[3 * kMaxRank], ptrn[2 * kMaxRank + 1];
+  for (int i = 0; i < drank; ++i) aces[i] = d_labels[i];
+  for (int i = 0; i < lrank; ++i) aces[drank + i] = l_labels[i];
+  for (int i = 0; i < rrank; ++i) aces[drank + lrank + i] = r_labels[i];
+  const int ierr = a4g::get_contraction_ptrn(drank, lrank, rrank, aces, ptrn);
+  if (ierr) return fail(A4G_ERR_PATTERN, "get_contraction_ptrn ierr " + std::to_string(ierr));
+  return a4g_contract(ptrn, l, lrank, lext, r, rrank, rext, d, drank, dext, beta, stream);
+}
+
+int a4g_permute(int rank, const int* ext, const int* dim_transp, const double* in, double* out,
+                void* stream) {
+  int rc = ensure_init();
+  if (rc) return rc;
+  return launch_permute(rank, ext, dim_transp + 1, in, out, pick(stream));
+}
+
+int a4g_fill(double* d, int64_t n, double v, void* stream) {
+  int rc = ensure_init();
+  return rc ? rc : launch_fill(d, n, v, pick(stream));
+}
+int a4g_scale(double* d, int64_t n, double f, void* stream) {
+  int rc = ensure_init();
+  return rc ? rc : launch_scale(d, n, f, pick(stream));
+}
+int a4g_scale_copy(double* d, const double* s, int64_t n, double f, void* stream) {
+  int rc = ensure_init();
+  return rc ? rc : launch_scale_copy(d, s, n, f, pick(stream));
+}
+int a4g_increment(double* d, int64_t n, double delta, void* stream) {
+  int rc = ensure_init();
+  return rc ? rc : launch_increment(d, n, delta, pick(stream));
+}
+int a4g_add_scaled(double* t0, const double* t1, int64_t n, double scale, void* stream) {
+  int rc = ensure_init();
+  return rc ? rc : launch_add_scaled(t0, t1, n, scale, pick(stream));
+}
+
+int a4g_add_sub(int subtract, int rank, const int* d_labels, const int* r_labels, const int* r_ext,
+                double* d, const double* l, const double* r, void* stream) {
+  int rc = ensure_init();
+  if (rc) return rc;
+  if (rank < 0 || rank > kMaxRank) return fail(A4G_ERR_ARG, "rank out of range");
+  int o2n[kMaxRank];
+  if (!perm_from_labels(rank, d_labels, r_labels, o2n))
+    return fail(A4G_ERR_ARG, "incompatible indices for LHS and RHS");
+  bool trivial = true;
+  for (int i = 0; i < rank; ++i) trivial &= o2n[i] == i + 1;
+  const int64_t n = count(rank, r_ext);
+  cudaStream_t s = pick(stream);
+  const char *rb = reinterpret_cast<const char*>(r), *db = reinterpret_cast<const char*>(d);
+  const bool overlap = rb < db + n * sizeof(double) && db < rb + n * sizeof(double);
+  if (!trivial && overlap) {
+    // d[i,j] += d[j,i]: the right operand must be read before d is written,
+    // as the reference does with its temporary block (interpreter.cpp:1919-1927)
+    double* tmp = nullptr;
+    A4G_CUDA(cudaMallocAsync(reinterpret_cast<void**>(&tmp), size_t(n) * sizeof(double), s));
+    rc = launch_permute(rank, r_ext, o2n, r, tmp, s);
+    int ident[kMaxRank];
+    for (int i = 0; i < rank; ++i) ident[i] = i + 1;
+    int dext[kMaxRank];
+    for (int i = 0; i < rank; ++i) dext[o2n[i] - 1] = r_ext[i];
+    if (!rc) rc = launch_add_sub_permuted(subtract, rank, dext, ident, d, l, tmp, s);
+    cudaFreeAsync(tmp, s);
+    return rc;
+  }
+  return launch_add_sub_permuted(subtract, rank, r_ext, o2n, d, l, r, s);
+}
+
+int a4g_norm2(const double* t, int64_t n, double* h_result, void* stream) {
+  int rc = ensure_init();
+  if (rc) return rc;
+  double* scratch = reduction_scratch();
+  if (!scratch) return fail(A4G_ERR_NOMEM, "reduction scratch");
+  cudaStream_t s = pick(stream);
+  double* out = scratch + dot_scratch_len();
+  rc = launch_dot(t, t, nullptr, nullptr, n, out, scratch, dot_scratch_len(), s);
+  if (rc) return rc;
+  A4G_CUDA(cudaMemcpyAsync(h_result, out, sizeof(double), cudaMemcpyDeviceToHost, s));
+  return check_device_flag(s);
+}
+
+int a4g_slice(int rank, const double* tens, const int* text, double* slice, const int* sext,
+              const int* beg, void* stream) {
+  int rc = ensure_init();
+  return rc ? rc
+            : launch_slice_insert(0, rank, const_cast<double*>(tens), text, slice, sext, beg,
+                                  pick(stream));
+}
+int a4g_insert(int rank, double* tens, const int* text, const double* slice, const int* sext,
+               const int* beg, void* stream) {
+  int rc = ensure_init();
+  return rc ? rc
+            : launch_slice_insert(1, rank, tens, text, const_cast<double*>(slice), sext, beg,
+                                  pick(stream));
+}
+
+int a4g_energy_denominator(int rank0, const int* iv, const int* ext0, double* data0, int rank1,
+                           const int* ext1, const double* e, int nsegs, const int* segs,
+                           void* stream) {
+  int rc = ensure_init();
+  if (rc) return rc;
+  if (!((rank0 == 2 || rank0 == 4) && (rank1 == 1 || rank1 == 2)) && !(rank0 == 6 && rank1 == 2))
+    return fail(A4G_ERR_UNSUPPORTED, "energy denominator: unsupported rank combination");
+  int off[6];
+  rc = denominator_offsets(rank0, iv, ext0, rank1, ext1, std::vector<int>(segs, segs + nsegs), off);
+  if (rc) return rc;
+  return launch_denominator(rank0, off, ext0, data0, rank1, ext1[0], e, pick(stream));
+}
+
+}  // extern "C"

@@ -1,0 +1,218 @@
+/*
+ * aces4_gb300 — GB300 (sm_103a) implementation of the ACES4 SIP block-contraction path.
+ *
+ * C ABI.  Plain pointers and sizes only.  Three groups of entry points:
+ *
+ *  1. Drop-in replacements for the reference's Fortran kernels
+ *     (src/sip/tensor_algebra/tensor_ops_c_prototypes.h).  Same symbol names,
+ *     same argument meaning, HOST buffers, synchronous, same ierr values.  The
+ *     reference declares scalars as C++ references (int&); a reference and a
+ *     pointer have the same calling convention, so the reference's own header
+ *     links against these definitions unchanged.
+ *  2. Drop-in replacements for the reference's legacy GPU API
+ *     (src/sip/cuda/gpu_super_instructions.h), DEVICE buffers.  The reference
+ *     exits the process on a CUDA error; these record the error (a4g_last_error)
+ *     and return instead.
+ *  3. New a4g_* entry points: device-resident, stream-ordered block operations,
+ *     the batched (one pardo step per call) contraction, and the split-precision
+ *     (Ozaki, BF16 tensor-core) contraction.  Every a4g_* call returns an int
+ *     status (A4G_OK = 0) and never exits or traps.
+ *
+ * Data layout everywhere: a block is a dense column-major array of doubles
+ * (first index fastest) whose extents are the segment sizes of its indices
+ * (reference: src/sip/dynamic_data/block_shape.cpp:25-49).  Rank <= 32 for the
+ * Fortran-compatible entries (tensor_dil_omp.F90:58), <= 6 for SIAL blocks.
+ */
+#ifndef ACES4_GB300_H
+#define ACES4_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ----------------------------------------------------------------------------
+ * Status codes of the a4g_* API
+ * ------------------------------------------------------------------------- */
+#define A4G_OK 0
+#define A4G_ERR_ARG 1        /* invalid argument (rank, extent, pattern, null pointer)        */
+#define A4G_ERR_PATTERN 2    /* contraction pattern rejected (reference ierr 1)               */
+#define A4G_ERR_CUDA 3       /* a CUDA runtime/driver call failed                             */
+#define A4G_ERR_NOMEM 4      /* device or host allocation failed                              */
+#define A4G_ERR_TIMEOUT 5    /* a device-side wait hit its iteration limit; kernel bailed out */
+#define A4G_ERR_UNSUPPORTED 6
+#define A4G_ERR_RANGE 7      /* size beyond a documented maximum                              */
+
+/* Text of the last error on the calling thread ("" when none). */
+const char* a4g_last_error(void);
+/* Library version string. */
+const char* a4g_version(void);
+
+/* ============================================================================
+ * 1. Drop-in replacements: src/sip/tensor_algebra/tensor_ops_c_prototypes.h
+ *    (HOST buffers; each call copies to the GPU, computes there, copies back)
+ * ========================================================================= */
+
+/* tensor_ops_c_prototypes.h:42 / tensor_dil_omp.F90:66 */
+long long tensor_size_by_shape_(int* num_dim, int* dims, int* ierr);
+/* tensor_ops_c_prototypes.h:55 / tensor_dil_omp.F90:87.  Host-only integer work. */
+void get_contraction_ptrn_(int* drank, int* lrank, int* rrank, int* aces_ptrn, int* my_ptrn,
+                           int* ierr);
+/* tensor_ops_c_prototypes.h:70 / tensor_dil_omp.F90:144 */
+void tensor_block_init__(int* nthreads, double* tens, int* tens_rank, int* tens_dim_extents,
+                         double* sval, int* ierr);
+/* tensor_ops_c_prototypes.h:84 / tensor_dil_omp.F90:193 */
+void tensor_block_scale__(int* nthreads, double* tens, int* tens_rank, int* tens_dim_extents,
+                          double* scale_fac, int* ierr);
+/* tensor_ops_c_prototypes.h:86 / tensor_dil_omp.F90:230 */
+double tensor_block_norm2__(int* nthreads, double* tens, int* tens_rank, int* tens_dim_extents,
+                            int* ierr);
+/* tensor_ops_c_prototypes.h:101 / tensor_dil_omp.F90:271 */
+void tensor_block_slice__(int* nthreads, int* dim_num, double* tens, int* tens_ext, double* slice,
+                          int* slice_ext, int* ext_beg, int* ierr);
+/* tensor_ops_c_prototypes.h:117 / tensor_dil_omp.F90:332 */
+void tensor_block_insert__(int* nthreads, int* dim_num, double* tens, int* tens_ext, double* slice,
+                           int* slice_ext, int* ext_beg, int* ierr);
+/* tensor_ops_c_prototypes.h:133 / tensor_dil_omp.F90:394  (tens0 += tens1*scale_fac) */
+void tensor_block_add__(const int* nthreads, const int* dim_num, int* dim_extents, double* tens0,
+                        double* tens1, const double* scale_fac, int* ierr);
+/* tensor_ops_c_prototypes.h:152 / tensor_dil_omp.F90:438  (dim_transp: sign slot + 1-based O2N) */
+void tensor_block_copy__(int* nthreads, int* dim_num, int* dim_extents, int* dim_transp,
+                         double* tens_in, double* tens_out, int* ierr);
+/* tensor_ops_c_prototypes.h:178 / tensor_dil_omp.F90:662.  D is OVERWRITTEN. */
+void tensor_block_contract__(int* nthreads, int* contr_ptrn, double* ltens, int* ltens_num_dim,
+                             int* ltens_dim_extent, double* rtens, int* rtens_num_dim,
+                             int* rtens_dim_extent, double* dtens, int* dtens_num_dim,
+                             int* dtens_dim_extent, int* ierr);
+
+/* ============================================================================
+ * 2. Drop-in replacements: src/sip/cuda/gpu_super_instructions.h:26-126
+ *    (DEVICE buffers; synchronous like the reference)
+ * ========================================================================= */
+void _init_gpu(int* devid, int* myRank);                                         /* .h:26  */
+void _gpu_axpy(double* y, double* x, const double alpha, const int numElems);   /* .h:35  */
+void _gpu_double_memset(double* g_addr, double value, const int numElems);      /* .h:44  */
+void _gpu_selfmultiply(double* x, const double alpha, const int numElems);      /* .h:53  */
+/* .h:70: y = x1 * x2, indices given as labels (overwrite, like the reference) */
+void _gpu_contract(double* y, const int ny, const int* yDims, const int* yInds, double* x1,
+                   const int n1, const int* x1Dims, const int* x1Inds, double* x2, const int n2,
+                   const int* x2Dims, const int* x2Inds);
+/* .h:86: y = x with the index order given by the labels */
+void _gpu_permute(double* y, const int ny, const int* yDims, const int* yInds, double* x,
+                  const int nx, const int* xDims, const int* xInds);
+void _gpu_host_to_device(double* c_addr, double* g_addr, const int numElems);   /* .h:96  */
+double* _gpu_allocate(const int numElems);                                       /* .h:103 */
+void _gpu_device_to_host(double* c_addr, double* g_addr, const int numElems);   /* .h:111 */
+void _gpu_device_to_device(double* dst, double* src, const int numElems);       /* .h:120 */
+void _gpu_free(double* g_addr);                                                  /* .h:126 */
+
+/* ============================================================================
+ * Super instruction: energy_denominator_rhf
+ * (src/sip/super_instructions/qm/qm-generic/energy_denominator_rhf.F:15, the
+ *  "fp2" ABI of src/sip/super_instructions/special_instructions.h:73-74).
+ * data_0 (HOST, the amplitude block) is divided in place by orbital-energy
+ * denominators read from data_1 (2-D Fock block: its diagonal; or 1-D energies).
+ * The segment sizes come from the predefined integer array "moa_seg_ranges",
+ * registered with a4g_set_predefined_int_array (sip_interface.h:17-48 role).
+ * ========================================================================= */
+void energy_denominator_rhf(int* array_slot_0, int* rank_0, int* index_values_0, int* size_0,
+                            int* extents_0, double* data_0, int* array_slot_1, int* rank_1,
+                            int* index_values_1, int* size_1, int* extents_1, double* data_1,
+                            int* ierr);
+/* Registers (copies) a predefined integer array by name, e.g. "moa_seg_ranges". */
+int a4g_set_predefined_int_array(const char* name, int n, const int* values);
+
+/* ============================================================================
+ * 3. Device-resident API (a4g_*).  All pointers are device pointers unless
+ *    named h_*; `stream` is a cudaStream_t (NULL = the library's own stream).
+ *    Calls are asynchronous on `stream`; a4g_sync(stream) waits and reports
+ *    any device-side error flag.
+ * ========================================================================= */
+int a4g_init(int device);
+int a4g_sync(void* stream);
+void* a4g_default_stream(void);
+
+/* Contraction of two blocks, reference pattern format (get_contraction_ptrn_).
+ * beta = 0: D = L*R (reference overwrite semantics, tensor_dil_omp.F90:752);
+ * beta = 1: D += L*R (the contract-accumulate the interpreter lacks,
+ * src/sip/worker/interpreter.cpp:743-747).  Plain FP64 on the GPU (DMMA). */
+int a4g_contract(const int* contr_ptrn, const double* l, int lrank, const int* lext,
+                 const double* r, int rrank, const int* rext, double* d, int drank,
+                 const int* dext, int beta, void* stream);
+/* Same, indices given as labels like the interpreter's selectors
+ * (src/sip/worker/interpreter.cpp:1210-1262). */
+int a4g_contract_labels(const int* d_labels, const int* l_labels, const int* r_labels,
+                        const double* l, int lrank, const int* lext, const double* r, int rrank,
+                        const int* rext, double* d, int drank, const int* dext, int beta,
+                        void* stream);
+/* tensor_block_copy: out = permute(in), dim_transp = sign slot + 1-based O2N. */
+int a4g_permute(int rank, const int* ext, const int* dim_transp, const double* in, double* out,
+                void* stream);
+/* Element-wise ops on n doubles (block.cpp:153-270, tensor_dil_omp.F90:144-436). */
+int a4g_fill(double* d, int64_t n, double value, void* stream);
+int a4g_scale(double* d, int64_t n, double factor, void* stream);
+int a4g_scale_copy(double* d, const double* s, int64_t n, double factor, void* stream);
+int a4g_increment(double* d, int64_t n, double delta, void* stream);
+/* tensor_block_add_: t0 += t1*scale (a factor within 1e-13 of one counts as one). */
+int a4g_add_scaled(double* t0, const double* t1, int64_t n, double scale, void* stream);
+/* d = l +/- r, r given in its own index order (labels); interpreter.cpp:1874-1997.
+ * d may alias l (the "+=" form); r is then permuted on the fly, no temp block. */
+int a4g_add_sub(int subtract, int rank, const int* d_labels, const int* r_labels, const int* r_ext,
+                double* d, const double* l, const double* r, void* stream);
+/* Sum of squares into *h_result (host), tensor_block_norm2_. Synchronous. */
+int a4g_norm2(const double* t, int64_t n, double* h_result, void* stream);
+/* Slice / insert of a rectangular sub-block (tensor_dil_omp.F90:271-392). */
+int a4g_slice(int rank, const double* tens, const int* tens_ext, double* slice,
+              const int* slice_ext, const int* ext_beg, void* stream);
+int a4g_insert(int rank, double* tens, const int* tens_ext, const double* slice,
+               const int* slice_ext, const int* ext_beg, void* stream);
+/* energy_denominator_rhf on device data.  e_or_fock: 1-D energies (rank1 = 1)
+ * or the 2-D Fock block (rank1 = 2, leading dimension ext1[0]). */
+int a4g_energy_denominator(int rank0, const int* index_values0, const int* ext0, double* data0,
+                           int rank1, const int* ext1, const double* e_or_fock, int nsegs,
+                           const int* seg_sizes, void* stream);
+
+/* ----------------------------------------------------------------------------
+ * Batched contraction of one pardo step (one call, many block triples).
+ * Every triple uses the same contraction pattern (one SIAL statement); block
+ * extents may differ per triple (uneven segments).  Triples that share the
+ * same D pointer are summed into that block.  A triple whose L or R pointer
+ * is NULL is a zero block and is skipped (the `where`-clause skip).
+ * ------------------------------------------------------------------------- */
+typedef struct a4g_triple {
+  double* d;
+  const double* l;
+  const double* r;
+  int dext[6];
+  int lext[6];
+  int rext[6];
+} a4g_triple;
+
+#define A4G_PREC_FP64 0       /* plain FP64 (DMMA)                                  */
+#define A4G_PREC_OZAKI_BF16 1 /* split-precision: BF16 slices on tcgen05 tensor cores */
+
+typedef struct a4g_batch_opts {
+  int precision;   /* A4G_PREC_*                                              */
+  int slices;      /* number of BF16 slices per operand (Ozaki), 2..8       */
+  int beta;        /* 0: D = sum of products (overwrite); 1: D += sum        */
+  int reserved[5];
+} a4g_batch_opts;
+
+/* Opaque handle of a planned pardo step: pattern + triple list + workspace. */
+typedef struct a4g_batch a4g_batch;
+
+int a4g_batch_create(a4g_batch** out, const int* contr_ptrn, int drank, int lrank, int rrank,
+                     const a4g_triple* h_triples, int64_t n_triples, const a4g_batch_opts* opts);
+int a4g_batch_run(a4g_batch* b, void* stream);
+/* Capture a4g_batch_run into a CUDA graph once; later runs replay it. */
+int a4g_batch_run_graph(a4g_batch* b, void* stream);
+/* Number of block pairs executed (zero blocks skipped) and FP64 flops. */
+int a4g_batch_info(const a4g_batch* b, int64_t* pairs, double* flops, int64_t* workspace_bytes);
+void a4g_batch_destroy(a4g_batch* b);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* ACES4_GB300_H */
