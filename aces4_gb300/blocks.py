@@ -1,0 +1,94 @@
+"""Segmented block arrays for driving a pardo step (host-side helper).
+
+A SIAL array is a set of dense column-major blocks, one per tuple of segment
+numbers, whose extents are the segment sizes (the reference's BlockManager /
+SipTables role, src/sip/dynamic_data/block_manager.cpp,
+src/sip/static_data/sip_tables.cpp:296).  ``BlockArray`` keeps every block of
+an array in one device allocation (contiguous, 256-byte aligned blocks) and
+hands out per-block views; a block may be marked zero (absent), which is how
+`where`-clause sparsity reaches the batched contraction.
+"""
+from __future__ import annotations
+
+import itertools
+
+import numpy as np
+
+
+def _align(n: int, a: int) -> int:
+    return (n + a - 1) // a * a
+
+
+class BlockArray:
+    """All blocks of one array, by segment tuple, in one CUDA buffer."""
+
+    def __init__(self, segs_per_index, present=None, device="cuda", dtype=None):
+        import torch
+
+        self.segs = [list(s) for s in segs_per_index]
+        self.rank = len(self.segs)
+        keys = list(itertools.product(*[range(len(s)) for s in self.segs]))
+        self.present = {k: (present(k) if present else True) for k in keys}
+        self.offsets, off = {}, 0
+        for k in keys:
+            if self.present[k]:
+                self.offsets[k] = off
+                off = _align(off + self.size(k), 32)  # 256-byte aligned blocks
+        self.total = max(off, 1)
+        self.buf = torch.zeros(self.total, dtype=dtype or torch.float64, device=device)
+
+    def ext(self, key):
+        return [self.segs[q][key[q]] for q in range(self.rank)]
+
+    def size(self, key) -> int:
+        return int(np.prod(self.ext(key)))
+
+    def keys(self):
+        return [k for k, p in self.present.items() if p]
+
+    def block(self, key):
+        """Flat device view of block `key`, or None for a zero block."""
+        if not self.present.get(key, False):
+            return None
+        o = self.offsets[key]
+        return self.buf[o:o + self.size(key)]
+
+    def fill_from(self, fn):
+        """fn(key, ext) -> flat float64 numpy array; copied to the device."""
+        import torch
+
+        for k in self.keys():
+            self.block(k).copy_(torch.from_numpy(np.ascontiguousarray(fn(k, self.ext(k)))))
+
+
+def ladder_triples(R: BlockArray, V: BlockArray, T: BlockArray):
+    """R(a,b,i,j) += V(a,b,c,d) T(c,d,i,j) over every segment tuple: the
+    particle-particle ladder statement of rlccd_rhf.sialx:399-433 as block
+    triples (zero V or T blocks give a NULL operand, skipped by the batch)."""
+    nv = len(V.segs[0])
+    no = len(T.segs[2])
+    out = []
+    for a, b, i, j in itertools.product(range(nv), range(nv), range(no), range(no)):
+        for c, d in itertools.product(range(nv), range(nv)):
+            rk, vk, tk = (a, b, i, j), (a, b, c, d), (c, d, i, j)
+            out.append((R.block(rk), V.block(vk), T.block(tk), R.ext(rk), V.ext(vk), T.ext(tk)))
+    return out
+
+
+# labels: a=1 b=2 i=3 j=4 c=5 d=6 (k=7 for the ring)
+LADDER_LABELS = ([1, 2, 3, 4], [1, 2, 5, 6], [5, 6, 3, 4])
+# R(a,i,b,j) = V(a,k,c,i) T(c,b,k,j)
+RING_LABELS = ([1, 3, 2, 4], [1, 7, 5, 3], [5, 2, 7, 4])
+
+
+def ring_triples(R: BlockArray, V: BlockArray, T: BlockArray):
+    """R(a,i,b,j) += V(a,k,c,i) T(c,b,k,j): ring term with both operands
+    permuted relative to the matrix form."""
+    nv = len(V.segs[0])
+    no = len(V.segs[1])
+    out = []
+    for a, i, b, j in itertools.product(range(nv), range(no), range(nv), range(no)):
+        for k, c in itertools.product(range(no), range(nv)):
+            rk, vk, tk = (a, i, b, j), (a, k, c, i), (c, b, k, j)
+            out.append((R.block(rk), V.block(vk), T.block(tk), R.ext(rk), V.ext(vk), T.ext(tk)))
+    return out

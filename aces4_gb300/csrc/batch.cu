@@ -1,18 +1,423 @@
-// Batched (one pardo step) contraction: placeholder until the grouped kernel lands.
+// Batched contraction of one pardo step (a4g_batch_*): planning on the host,
+// one grouped kernel (FP64) or the split-precision pipeline (Ozaki, BF16
+// tcgen05) on the device, optionally captured once into a CUDA graph.
+//
+// The reference runs one tensor_block_contract__ per block pair from the
+// interpreter loop (src/sip/worker/interpreter.cpp:734-742, one pardo
+// iteration at a time, loop_manager.cpp:289-314) and accumulates partial
+// results with a separate += (rlccd_rhf.sialx:408-412).  Here the whole step
+// is one call: pairs that feed the same destination block are summed in the
+// kernel, zero blocks (NULL operand) are never touched.
+#include <algorithm>
+#include <cstring>
+#include <map>
+#include <memory>
+#include <vector>
+
 #include "a4g_internal.h"
+#include "grouped.h"
+#include "ozaki.h"
 
 using namespace a4g;
 
+struct a4g_batch {
+  int precision = A4G_PREC_FP64;
+  int slices = 6;
+  int beta = 0;
+  int64_t pairs = 0;
+  double flops = 0.0;
+  int64_t device_bytes = 0;
+  std::vector<void*> allocs;
+  std::vector<std::pair<double*, int64_t>> zero_blocks;  // D blocks with no live pair (beta = 0)
+  PlanRef* d_plans = nullptr;
+  // FP64 grouped
+  GroupedF64Tile* d_f64_tiles = nullptr;
+  GroupedPair* d_f64_pairs = nullptr;
+  int n_f64_tiles = 0;
+  // split precision
+  OzPanel* d_pa = nullptr;
+  OzPanel* d_pb = nullptr;
+  int* d_exps = nullptr;
+  size_t exps_bytes = 0;
+  OzSplitJob *d_jobs_a = nullptr, *d_jobs_b = nullptr;
+  int64_t *d_prefix_a = nullptr, *d_prefix_b = nullptr;
+  int njobs_a = 0, njobs_b = 0;
+  int64_t jtiles_a = 0, jtiles_b = 0;
+  OzTile* d_tiles = nullptr;
+  int n_tiles = 0;
+  OzDBlock* d_dblocks = nullptr;
+  float2* d_ws = nullptr;
+  OzGemmArgs gemm{};
+  int grid = 0;
+  cudaGraphExec_t graph = nullptr;
+
+  ~a4g_batch() {
+    if (graph) cudaGraphExecDestroy(graph);
+    for (void* p : allocs) cudaFree(p);
+  }
+};
+
+namespace {
+
+template <class T>
+int upload(a4g_batch* b, const std::vector<T>& v, T** out) {
+  *out = nullptr;
+  if (v.empty()) return A4G_OK;
+  const size_t bytes = v.size() * sizeof(T);
+  void* p = nullptr;
+  A4G_CUDA(cudaMalloc(&p, bytes));
+  b->allocs.push_back(p);
+  b->device_bytes += int64_t(bytes);
+  A4G_CUDA(cudaMemcpy(p, v.data(), bytes, cudaMemcpyHostToDevice));
+  *out = static_cast<T*>(p);
+  return A4G_OK;
+}
+
+int device_alloc(a4g_batch* b, size_t bytes, void** out, bool zero) {
+  void* p = nullptr;
+  A4G_CUDA(cudaMalloc(&p, std::max<size_t>(bytes, 256)));
+  b->allocs.push_back(p);
+  b->device_bytes += int64_t(bytes);
+  if (zero) A4G_CUDA(cudaMemset(p, 0, bytes));
+  *out = p;
+  return A4G_OK;
+}
+
+PlanRef ref_of(const DevPlan* p) {
+  PlanRef r;
+  r.offLm = p->offLm, r.offLk = p->offLk, r.offRk = p->offRk, r.offRn = p->offRn;
+  r.offDm = p->offDm, r.offDn = p->offDn;
+  r.M = int(p->host.M), r.N = int(p->host.N), r.K = int(p->host.K);
+  r.a_kfast = p->host.a_kfast, r.b_kfast = p->host.b_kfast;
+  return r;
+}
+
+struct Pair {
+  const double* l;
+  const double* r;
+  int plan;
+};
+struct DGroup {
+  double* d;
+  std::vector<Pair> pairs;
+  int plan = -1;  // any pair's plan: D-side tables are identical for all
+};
+
+int64_t ceil_to(int64_t x, int64_t m) { return (x + m - 1) / m * m; }
+
+struct alignas(64) MapBytes {  // host image of one CUtensorMap (128 bytes, 64-byte aligned)
+  uint8_t b[128];
+};
+
+// Panel of one operand side: the distinct blocks feeding a set of destination
+// rows (A) or columns (B), each with its k offset inside the panel.
+struct PanelBuild {
+  std::vector<const double*> key;  // sorted block pointers
+  std::map<const double*, int64_t> koff;
+  std::map<const double*, int> plan;
+  int rows = 0;
+  int64_t kpad = 0;
+};
+
+int find_or_add_panel(std::vector<PanelBuild>& panels, std::map<std::vector<const double*>, int>& index,
+                      const std::vector<std::pair<const double*, int>>& blocks, int rows,
+                      const std::vector<DevPlan const*>& plans, bool left) {
+  std::vector<const double*> key;
+  for (auto& b : blocks) key.push_back(b.first);
+  std::sort(key.begin(), key.end());
+  key.erase(std::unique(key.begin(), key.end()), key.end());
+  auto it = index.find(key);
+  if (it != index.end()) return it->second;
+  PanelBuild pb;
+  pb.key = key;
+  pb.rows = rows;
+  for (auto& b : blocks) {
+    if (pb.koff.count(b.first)) continue;
+    pb.koff[b.first] = pb.kpad;
+    pb.plan[b.first] = b.second;
+    pb.kpad += ceil_to(plans[b.second]->host.K, kOzBK);
+  }
+  (void)left;
+  panels.push_back(pb);
+  index[key] = int(panels.size()) - 1;
+  return int(panels.size()) - 1;
+}
+
+int build_f64(a4g_batch* b, const std::vector<DGroup>& groups, const std::vector<const DevPlan*>& plans) {
+  std::vector<GroupedF64Tile> tiles;
+  std::vector<GroupedPair> pairs;
+  const int TM = grouped_f64_tile_m(), TN = grouped_f64_tile_n();
+  for (const DGroup& g : groups) {
+    const int begin = int(pairs.size());
+    for (const Pair& p : g.pairs) pairs.push_back({p.l, p.r, p.plan, 0});
+    const int end = int(pairs.size());
+    const GemmPlan& h = plans[g.plan]->host;
+    for (int64_t n0 = 0; n0 < h.N; n0 += TN)
+      for (int64_t m0 = 0; m0 < h.M; m0 += TM)
+        tiles.push_back({g.d, int(m0), int(n0), begin, end, g.plan, 0});
+  }
+  if (tiles.size() > 0x7fffffffu) return fail(A4G_ERR_RANGE, "too many tiles");
+  b->n_f64_tiles = int(tiles.size());
+  int rc = upload(b, tiles, &b->d_f64_tiles);
+  if (!rc) rc = upload(b, pairs, &b->d_f64_pairs);
+  return rc;
+}
+
+int build_ozaki(a4g_batch* b, const std::vector<DGroup>& groups, const std::vector<const DevPlan*>& plans) {
+  std::vector<PanelBuild> pa, pb;
+  std::map<std::vector<const double*>, int> ia, ib;
+  std::vector<OzDBlock> dblocks;
+  std::vector<OzTile> tiles;
+  std::vector<OzTrip> trips;
+  for (const DGroup& g : groups) {
+    const GemmPlan& h = plans[g.plan]->host;
+    std::vector<std::pair<const double*, int>> ls, rs;
+    for (const Pair& p : g.pairs) ls.push_back({p.l, p.plan}), rs.push_back({p.r, p.plan});
+    const int a = find_or_add_panel(pa, ia, ls, int(h.M), plans, true);
+    const int c = find_or_add_panel(pb, ib, rs, int(h.N), plans, false);
+    const int db = int(dblocks.size());
+    dblocks.push_back({g.d, g.plan, a, c});
+    const int tb = int(trips.size());
+    int kb_total = 0;
+    for (const Pair& p : g.pairs) {
+      const int nkb = int(ceil_to(plans[p.plan]->host.K, kOzBK) / kOzBK);
+      trips.push_back({pa[a].koff.at(p.l), pb[c].koff.at(p.r), nkb, 0});
+      kb_total += nkb;
+    }
+    const int te = int(trips.size());
+    for (int64_t n0 = 0; n0 < h.N; n0 += kOzBN)
+      for (int64_t m0 = 0; m0 < h.M; m0 += kOzBM)
+        tiles.push_back({db, int(m0), int(n0), a, c, tb, te, kb_total});
+  }
+  const int S = b->slices;
+  int rc0 = oz_prepare();
+  if (rc0) return rc0;
+  // panels: slices (BF16, zero padded), exponents, tensor maps
+  std::vector<OzPanel> hpa, hpb;
+  std::vector<MapBytes> maps_a(pa.size()), maps_b(pb.size());
+  size_t exps_total = 0;
+  for (auto& p : pa) exps_total += ceil_to(p.rows, kOzBM);
+  for (auto& p : pb) exps_total += ceil_to(p.rows, kOzBN);
+  void* exps = nullptr;
+  int rc = device_alloc(b, exps_total * sizeof(int), &exps, true);
+  if (rc) return rc;
+  b->d_exps = static_cast<int*>(exps);
+  b->exps_bytes = exps_total * sizeof(int);
+  size_t eoff = 0;
+  auto make_panels = [&](std::vector<PanelBuild>& src, std::vector<OzPanel>& dst, std::vector<MapBytes>& maps,
+                         int rows_tile) -> int {
+    for (size_t i = 0; i < src.size(); ++i) {
+      OzPanel p{};
+      p.rows = src[i].rows;
+      p.rows_pad = int(ceil_to(src[i].rows, rows_tile));
+      p.kpad = src[i].kpad;
+      const size_t bytes = size_t(S) * p.rows_pad * size_t(p.kpad) * 2;
+      void* mem = nullptr;
+      int r = device_alloc(b, bytes, &mem, true);
+      if (r) return r;
+      p.base = static_cast<__nv_bfloat16*>(mem);
+      p.exps = b->d_exps + eoff;
+      eoff += p.rows_pad;
+      r = oz_make_tensor_map(maps[i].b, mem, p.kpad, int64_t(S) * p.rows_pad);
+      if (r) return r;
+      dst.push_back(p);
+    }
+    return A4G_OK;
+  };
+  if ((rc = make_panels(pa, hpa, maps_a, kOzBM))) return rc;
+  if ((rc = make_panels(pb, hpb, maps_b, kOzBN))) return rc;
+  for (auto& p : hpa)
+    if (p.kpad > 0x7fffffffLL || int64_t(S) * p.rows_pad > 0x7fffffffLL)
+      return fail(A4G_ERR_RANGE, "panel exceeds TMA coordinate range");
+  for (auto& p : hpb)
+    if (p.kpad > 0x7fffffffLL || int64_t(S) * p.rows_pad > 0x7fffffffLL)
+      return fail(A4G_ERR_RANGE, "panel exceeds TMA coordinate range");
+  // split jobs (one per block per panel) and their 64x64 tile prefix sums
+  auto jobs_of = [&](std::vector<PanelBuild>& src, bool left, std::vector<OzSplitJob>& jobs,
+                     std::vector<int64_t>& prefix) {
+    prefix.assign(1, 0);
+    for (size_t pi = 0; pi < src.size(); ++pi) {
+      for (auto& kv : src[pi].koff) {
+        const DevPlan* dp = plans[src[pi].plan.at(kv.first)];
+        OzSplitJob j{};
+        j.src = kv.first;
+        j.offRow = left ? dp->offLm : dp->offRn;
+        j.offK = left ? dp->offLk : dp->offRk;
+        j.rows = int(left ? dp->host.M : dp->host.N);
+        j.K = int(dp->host.K);
+        j.kfast = left ? dp->host.a_kfast : dp->host.b_kfast;
+        j.panel = int(pi);
+        j.koff = kv.second;
+        jobs.push_back(j);
+        prefix.push_back(prefix.back() + ceil_to(j.rows, 64) / 64 * (ceil_to(j.K, 64) / 64));
+      }
+    }
+  };
+  std::vector<OzSplitJob> ja, jb;
+  std::vector<int64_t> xa, xb;
+  jobs_of(pa, true, ja, xa);
+  jobs_of(pb, false, jb, xb);
+  b->njobs_a = int(ja.size()), b->njobs_b = int(jb.size());
+  b->jtiles_a = xa.back(), b->jtiles_b = xb.back();
+  void *dmaps_a = nullptr, *dmaps_b = nullptr;
+  const size_t mbytes_a = maps_a.size() * sizeof(MapBytes), mbytes_b = maps_b.size() * sizeof(MapBytes);
+  if ((rc = device_alloc(b, mbytes_a, &dmaps_a, false))) return rc;
+  if ((rc = device_alloc(b, mbytes_b, &dmaps_b, false))) return rc;
+  A4G_CUDA(cudaMemcpy(dmaps_a, maps_a.data(), mbytes_a, cudaMemcpyHostToDevice));
+  A4G_CUDA(cudaMemcpy(dmaps_b, maps_b.data(), mbytes_b, cudaMemcpyHostToDevice));
+  OzTrip* d_trips = nullptr;
+  if ((rc = upload(b, hpa, &b->d_pa)) || (rc = upload(b, hpb, &b->d_pb)) || (rc = upload(b, ja, &b->d_jobs_a)) ||
+      (rc = upload(b, jb, &b->d_jobs_b)) || (rc = upload(b, xa, &b->d_prefix_a)) ||
+      (rc = upload(b, xb, &b->d_prefix_b)) || (rc = upload(b, tiles, &b->d_tiles)) ||
+      (rc = upload(b, trips, &d_trips)) || (rc = upload(b, dblocks, &b->d_dblocks)))
+    return rc;
+  b->n_tiles = int(tiles.size());
+  void* ws = nullptr;
+  if ((rc = device_alloc(b, size_t(b->n_tiles) * S * kOzBM * kOzBN * sizeof(float2), &ws, false))) return rc;
+  b->d_ws = static_cast<float2*>(ws);
+  OzGemmArgs& ga = b->gemm;
+  ga.maps_a = dmaps_a, ga.maps_b = dmaps_b;
+  ga.panels_a = b->d_pa, ga.panels_b = b->d_pb;
+  ga.tiles = b->d_tiles, ga.trips = d_trips;
+  ga.n_tiles = b->n_tiles;
+  ga.n_units = b->n_tiles * S;
+  ga.slices = S;
+  for (int t = 0; t < kOzMaxSlices; ++t) ga.chunk_kb[t] = t < S ? oz_chunk_kb(t) : 1;
+  for (int t = 0; t < S; ++t)
+    if (ga.chunk_kb[t] < 1) return fail(A4G_ERR_ARG, "slice count too large for exact accumulation");
+  ga.ws = b->d_ws;
+  ga.err_flag = ctx()->d_error_flag;
+  b->grid = std::min(ga.n_units, ctx()->num_sms);
+  return A4G_OK;
+}
+
+int run(a4g_batch* b, cudaStream_t s) {
+  int rc = A4G_OK;
+  if (b->beta == 0)
+    for (auto& z : b->zero_blocks)
+      if ((rc = launch_fill(z.first, z.second, 0.0, s))) return rc;
+  if (b->precision == A4G_PREC_FP64)
+    return launch_grouped_f64(b->d_f64_tiles, b->n_f64_tiles, b->d_f64_pairs, b->d_plans, b->beta, s);
+  if (b->n_tiles == 0) return A4G_OK;
+  A4G_CUDA(cudaMemsetAsync(b->d_exps, 0, b->exps_bytes, s));
+  if ((rc = oz_launch_exp(b->d_jobs_a, b->d_prefix_a, b->njobs_a, b->jtiles_a, b->d_pa, s))) return rc;
+  if ((rc = oz_launch_exp(b->d_jobs_b, b->d_prefix_b, b->njobs_b, b->jtiles_b, b->d_pb, s))) return rc;
+  if ((rc = oz_launch_split(b->d_jobs_a, b->d_prefix_a, b->njobs_a, b->jtiles_a, b->d_pa, b->slices, s))) return rc;
+  if ((rc = oz_launch_split(b->d_jobs_b, b->d_prefix_b, b->njobs_b, b->jtiles_b, b->d_pb, b->slices, s))) return rc;
+  if ((rc = oz_launch_gemm(b->gemm, b->grid, s))) return rc;
+  return oz_launch_recombine(b->d_tiles, b->n_tiles, b->d_dblocks, b->d_plans, b->d_pa, b->d_pb, b->d_ws,
+                             b->slices, b->beta, s);
+}
+
+}  // namespace
+
 extern "C" {
-int a4g_batch_create(a4g_batch** out, const int*, int, int, int, const a4g_triple*, int64_t,
-                     const a4g_batch_opts*) {
-  if (out) *out = nullptr;
-  return fail(A4G_ERR_UNSUPPORTED, "batched contraction not built yet");
+
+int a4g_batch_create(a4g_batch** out, const int* ptrn, int drank, int lrank, int rrank,
+                     const a4g_triple* trip, int64_t n, const a4g_batch_opts* opts) {
+  if (!out) return fail(A4G_ERR_ARG, "null output handle");
+  *out = nullptr;
+  int rc = ensure_init();
+  if (rc) return rc;
+  if (!ptrn || (n > 0 && !trip)) return fail(A4G_ERR_ARG, "null argument");
+  if (drank < 1 || drank > 6 || lrank < 1 || lrank > 6 || rrank < 1 || rrank > 6)
+    return fail(A4G_ERR_UNSUPPORTED, "batched contraction needs tensor operands of rank 1..6");
+  std::unique_ptr<a4g_batch> b(new a4g_batch());
+  if (opts) {
+    b->precision = opts->precision;
+    b->slices = opts->slices > 0 ? opts->slices : 6;
+    b->beta = opts->beta ? 1 : 0;
+  }
+  if (b->precision != A4G_PREC_FP64 && b->precision != A4G_PREC_OZAKI_BF16)
+    return fail(A4G_ERR_ARG, "unknown precision mode");
+  if (b->slices < 1 || b->slices > kOzMaxUsableSlices) return fail(A4G_ERR_ARG, "slices must be 1..7");
+
+  std::vector<const DevPlan*> plans;
+  std::map<const DevPlan*, int> plan_index;
+  std::vector<DGroup> groups;
+  std::map<double*, int> gindex;
+  std::map<double*, int64_t> all_d;
+  for (int64_t i = 0; i < n; ++i) {
+    const a4g_triple& t = trip[i];
+    if (!t.d) return fail(A4G_ERR_ARG, "triple with NULL destination");
+    int64_t dsize = 1;
+    for (int q = 0; q < drank; ++q) dsize *= t.dext[q];
+    all_d[t.d] = dsize;
+    if (!t.l || !t.r) continue;  // zero block: skipped
+    const DevPlan* p = nullptr;
+    if ((rc = get_dev_plan(ptrn, lrank, t.lext, rrank, t.rext, drank, t.dext, &p))) return rc;
+    if (p->host.kind != ContractKind::kTensorTensor)
+      return fail(A4G_ERR_UNSUPPORTED, "batched contraction of scalar operands");
+    if (p->host.M > 0x7fffffff || p->host.N > 0x7fffffff || p->host.K > 0x7fffffff)
+      return fail(A4G_ERR_RANGE, "block too large");
+    auto pit = plan_index.find(p);
+    int pi;
+    if (pit == plan_index.end()) {
+      pi = int(plans.size());
+      plans.push_back(p);
+      plan_index[p] = pi;
+    } else {
+      pi = pit->second;
+    }
+    auto git = gindex.find(t.d);
+    if (git == gindex.end()) {
+      gindex[t.d] = int(groups.size());
+      groups.push_back(DGroup{t.d, {}, pi});
+      git = gindex.find(t.d);
+    }
+    DGroup& g = groups[git->second];
+    const GemmPlan& h0 = plans[g.plan]->host;
+    if (h0.M != p->host.M || h0.N != p->host.N)
+      return fail(A4G_ERR_ARG, "triples sharing a destination block disagree on its extents");
+    g.pairs.push_back({t.l, t.r, pi});
+    b->pairs += 1;
+    b->flops += 2.0 * double(p->host.M) * double(p->host.N) * double(p->host.K);
+  }
+  for (auto& kv : all_d)
+    if (!gindex.count(kv.first)) b->zero_blocks.push_back({kv.first, kv.second});
+  std::vector<PlanRef> refs;
+  for (const DevPlan* p : plans) refs.push_back(ref_of(p));
+  if ((rc = upload(b.get(), refs, &b->d_plans))) return rc;
+  rc = b->precision == A4G_PREC_FP64 ? build_f64(b.get(), groups, plans) : build_ozaki(b.get(), groups, plans);
+  if (rc) return rc;
+  *out = b.release();
+  return A4G_OK;
 }
-int a4g_batch_run(a4g_batch*, void*) { return fail(A4G_ERR_UNSUPPORTED, "not built"); }
-int a4g_batch_run_graph(a4g_batch*, void*) { return fail(A4G_ERR_UNSUPPORTED, "not built"); }
-int a4g_batch_info(const a4g_batch*, int64_t*, double*, int64_t*) {
-  return fail(A4G_ERR_UNSUPPORTED, "not built");
+
+int a4g_batch_run(a4g_batch* b, void* stream) {
+  if (!b) return fail(A4G_ERR_ARG, "null batch");
+  return run(b, pick(stream));
 }
-void a4g_batch_destroy(a4g_batch*) {}
+
+int a4g_batch_run_graph(a4g_batch* b, void* stream) {
+  if (!b) return fail(A4G_ERR_ARG, "null batch");
+  cudaStream_t s = pick(stream);
+  if (!b->graph) {
+    cudaGraph_t g = nullptr;
+    A4G_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+    const int rc = run(b, s);
+    cudaError_t e = cudaStreamEndCapture(s, &g);
+    if (rc) {
+      if (g) cudaGraphDestroy(g);
+      return rc;
+    }
+    if (e != cudaSuccess) return cuda_fail(e, "cudaStreamEndCapture");
+    e = cudaGraphInstantiate(&b->graph, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaGraphInstantiate");
+  }
+  A4G_CUDA(cudaGraphLaunch(b->graph, s));
+  return A4G_OK;
 }
+
+int a4g_batch_info(const a4g_batch* b, int64_t* pairs, double* flops, int64_t* workspace_bytes) {
+  if (!b) return fail(A4G_ERR_ARG, "null batch");
+  if (pairs) *pairs = b->pairs;
+  if (flops) *flops = b->flops;
+  if (workspace_bytes) *workspace_bytes = b->device_bytes;
+  return A4G_OK;
+}
+
+void a4g_batch_destroy(a4g_batch* b) { delete b; }
+
+}  // extern "C"

@@ -1,0 +1,100 @@
+// Device-visible descriptors of a planned pardo step (batched contraction):
+// the FP64 grouped kernel and the split-precision (Ozaki) pipeline.
+#pragma once
+
+#include <cuda_bf16.h>
+#include <stdint.h>
+
+namespace a4g {
+
+// Device copy of one contraction plan's address tables (see GemmPlan).
+struct PlanRef {
+  const int64_t *offLm, *offLk, *offRk, *offRn, *offDm, *offDn;
+  int M, N, K;
+  int a_kfast, b_kfast;
+};
+
+// ------------------------------------------------------------ FP64 grouped
+struct GroupedPair {
+  const double* l;
+  const double* r;
+  int plan;
+  int pad;
+};
+struct GroupedF64Tile {
+  double* d;
+  int m0, n0;
+  int pair_begin, pair_end;  // pairs summed into this tile
+  int dplan;                 // plan giving D's tables and M, N
+  int pad;
+};
+int launch_grouped_f64(const GroupedF64Tile* tiles, int ntiles, const GroupedPair* pairs,
+                       const PlanRef* plans, int beta, cudaStream_t s);
+int grouped_f64_tile_m();
+int grouped_f64_tile_n();
+
+// ------------------------------------------------------------ split precision
+// A panel holds the BF16 slices of every left block that feeds one group of
+// destination rows, K-major: slice i, row m, column k at
+//   base[(i * rows_pad + m) * kpad + k];
+// the same layout with n for right-operand (B) panels.  Row exponents E (|x| <
+// 2^E over the whole row of the panel) are kept per row.
+struct OzPanel {
+  __nv_bfloat16* base;
+  int* exps;   // biased max exponent per row (atomicMax target)
+  int rows;    // live rows
+  int rows_pad;
+  int64_t kpad;
+};
+
+// One operand block to slice into a panel (left blocks into A panels, right
+// blocks into B panels).  Element (row, k) of the block is
+//   src[offRow[row] + offK[k]].
+struct OzSplitJob {
+  const double* src;
+  const int64_t* offRow;
+  const int64_t* offK;
+  int rows, K;
+  int kfast;  // src is unit-stride along k
+  int panel;
+  int64_t koff;  // first k column of this block inside the panel (multiple of 64)
+};
+
+// One 128x128 output tile of one destination block.
+struct OzTile {
+  int dblock;
+  int m0, n0;
+  int panel_a, panel_b;
+  int trip_begin, trip_end;  // range of OzTrip (one per block pair feeding the tile)
+  int kb_total;              // sum of the pairs' 64-wide k blocks
+};
+// k position of one block pair inside the A and B panels.
+struct OzTrip {
+  int64_t koff_a, koff_b;
+  int nkb;
+  int pad;
+};
+struct OzDBlock {
+  double* d;
+  int plan;  // PlanRef index for offDm/offDn and M, N
+  int panel_a, panel_b;
+};
+
+constexpr int kOzBM = 128, kOzBN = 128, kOzBK = 64, kOzMaxSlices = 8;
+
+struct OzGemmArgs {
+  const void* maps_a;  // CUtensorMap[n_panels_a], 64-byte aligned, device memory
+  const void* maps_b;
+  const OzPanel* panels_a;
+  const OzPanel* panels_b;
+  const OzTile* tiles;
+  const OzTrip* trips;
+  int n_units;  // units = (tile, level), level-major order: unit u -> tile u % n_tiles, level u / n_tiles
+  int n_tiles;
+  int slices;
+  int chunk_kb[kOzMaxSlices];  // k blocks per exact flush at each level
+  float2* ws;                  // [tile][level][col 128][row 128] (hi, lo)
+  int* err_flag;
+};
+
+}  // namespace a4g

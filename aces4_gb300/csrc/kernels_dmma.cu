@@ -10,7 +10,12 @@
 // registers, then staged in double-buffered shared memory.  FP64 throughput on
 // GB300 is ~2 FMA/clk/SM, so the kernel is bound by the FP64 pipe; the gather
 // traffic is small in comparison.
+//
+// The grouped form runs a whole pardo step: one CTA owns one 64x64 tile of one
+// destination block and sums the products of every block pair that feeds that
+// block (the contract-accumulate the interpreter lacks), then writes D once.
 #include "a4g_internal.h"
+#include "grouped.h"
 
 namespace a4g {
 namespace {
@@ -24,108 +29,92 @@ __device__ __forceinline__ void dmma_8x8x4(double (&c)[2], double a, double b) {
                : "d"(a), "d"(b));
 }
 
-// Gathers one BMxBK (or BKxBN) operand tile into 8 registers per thread.
+// Gathers one 64x16 operand tile (rows x k) into 8 registers per thread.
 // KFAST: the operand is unit-stride along k, so threads walk k fastest.
-template <bool KFAST>
-__device__ __forceinline__ void gather_tile(double (&reg)[8], const double* __restrict__ X,
-                                            const int64_t* __restrict__ offRow,  // per m (or n), smem
+__device__ __forceinline__ void gather_tile(bool kfast, double (&reg)[8], const double* __restrict__ X,
+                                            const int64_t* __restrict__ offRow,  // smem, per row
                                             const int64_t* __restrict__ offK,    // global, per k
-                                            int row0, int rows, int k0, int K) {
+                                            int rows_left, int k0, int K) {
   const int t = threadIdx.x;
 #pragma unroll
   for (int i = 0; i < 8; ++i) {
-    int r, kk;
-    if (KFAST) {
-      kk = t & (BK - 1);
-      r = (t >> 4) + 8 * i;
-    } else {
-      r = t & (BM - 1);
-      kk = (t >> 6) + 2 * i;
-    }
+    const int kk = kfast ? (t & (BK - 1)) : ((t >> 6) + 2 * i);
+    const int r = kfast ? ((t >> 4) + 8 * i) : (t & (BM - 1));
     const int k = k0 + kk;
-    reg[i] = (row0 + r < rows && k < K) ? __ldg(&X[offRow[r] + __ldg(&offK[k])]) : 0.0;
+    reg[i] = (r < rows_left && k < K) ? __ldg(&X[offRow[r] + __ldg(&offK[k])]) : 0.0;
   }
 }
 
-template <bool KFAST>
-__device__ __forceinline__ void store_tile(double (*S)[LDS], const double (&reg)[8]) {
+__device__ __forceinline__ void store_tile(bool kfast, double (*S)[LDS], const double (&reg)[8]) {
   const int t = threadIdx.x;
 #pragma unroll
   for (int i = 0; i < 8; ++i) {
-    int r, kk;
-    if (KFAST) {
-      kk = t & (BK - 1);
-      r = (t >> 4) + 8 * i;
-    } else {
-      r = t & (BM - 1);
-      kk = (t >> 6) + 2 * i;
-    }
+    const int kk = kfast ? (t & (BK - 1)) : ((t >> 6) + 2 * i);
+    const int r = kfast ? ((t >> 4) + 8 * i) : (t & (BM - 1));
     S[kk][r] = reg[i];
   }
 }
 
-template <bool A_KFAST, bool B_KFAST>
-__global__ void __launch_bounds__(kThreadsF64) contract_f64_kernel(
-    const double* __restrict__ L, const double* __restrict__ R, double* __restrict__ D,
-    const int64_t* __restrict__ offLm, const int64_t* __restrict__ offLk,
-    const int64_t* __restrict__ offRk, const int64_t* __restrict__ offRn,
-    const int64_t* __restrict__ offDm, const int64_t* __restrict__ offDn, int M, int N, int K,
-    int tiles_m, int beta) {
-  __shared__ __align__(16) double As[2][BK][LDS];
-  __shared__ __align__(16) double Bs[2][BK][LDS];
-  __shared__ int64_t sLm[BM], sRn[BN];
+struct Smem {
+  double As[2][BK][LDS];
+  double Bs[2][BK][LDS];
+  int64_t sLm[BM], sRn[BN];
+};
 
-  const int tm = blockIdx.x % tiles_m, tn = blockIdx.x / tiles_m;
-  const int m0 = tm * BM, n0 = tn * BN;
+// acc += L_tile * R_tile over all K of one block pair.
+__device__ void accumulate_pair(Smem& sm, double (&acc)[4][4][2], const double* __restrict__ L,
+                                const double* __restrict__ R, const int64_t* __restrict__ offLm,
+                                const int64_t* __restrict__ offLk, const int64_t* __restrict__ offRk,
+                                const int64_t* __restrict__ offRn, int M, int N, int K, int m0, int n0,
+                                bool a_kfast, bool b_kfast) {
   const int t = threadIdx.x;
-  if (t < BM) sLm[t] = (m0 + t < M) ? offLm[m0 + t] : 0;
-  else sRn[t - BM] = (n0 + t - BM < N) ? offRn[n0 + t - BM] : 0;
+  __syncthreads();  // previous pair done with the tables / tiles
+  if (t < BM) sm.sLm[t] = (m0 + t < M) ? offLm[m0 + t] : 0;
+  else sm.sRn[t - BM] = (n0 + t - BM < N) ? offRn[n0 + t - BM] : 0;
   __syncthreads();
 
   const int warp = t >> 5, lane = t & 31;
   const int g = lane >> 2, tig = lane & 3;
   const int wm = (warp & 1) * 32, wn = (warp >> 1) * 32;
-
-  double acc[4][4][2];
-#pragma unroll
-  for (int i = 0; i < 4; ++i)
-#pragma unroll
-    for (int j = 0; j < 4; ++j) acc[i][j][0] = acc[i][j][1] = 0.0;
-
   double ra[8], rb[8];
   const int ksteps = (K + BK - 1) / BK;
-  gather_tile<A_KFAST>(ra, L, sLm, offLk, m0, M, 0, K);
-  gather_tile<B_KFAST>(rb, R, sRn, offRk, n0, N, 0, K);
-  store_tile<A_KFAST>(As[0], ra);
-  store_tile<B_KFAST>(Bs[0], rb);
+  gather_tile(a_kfast, ra, L, sm.sLm, offLk, M - m0, 0, K);
+  gather_tile(b_kfast, rb, R, sm.sRn, offRk, N - n0, 0, K);
+  store_tile(a_kfast, sm.As[0], ra);
+  store_tile(b_kfast, sm.Bs[0], rb);
   __syncthreads();
-
   for (int ks = 0; ks < ksteps; ++ks) {
     const int cur = ks & 1;
     if (ks + 1 < ksteps) {
-      gather_tile<A_KFAST>(ra, L, sLm, offLk, m0, M, (ks + 1) * BK, K);
-      gather_tile<B_KFAST>(rb, R, sRn, offRk, n0, N, (ks + 1) * BK, K);
+      gather_tile(a_kfast, ra, L, sm.sLm, offLk, M - m0, (ks + 1) * BK, K);
+      gather_tile(b_kfast, rb, R, sm.sRn, offRk, N - n0, (ks + 1) * BK, K);
     }
 #pragma unroll
     for (int kk = 0; kk < BK; kk += 4) {
       double af[4], bf[4];
 #pragma unroll
-      for (int i = 0; i < 4; ++i) af[i] = As[cur][kk + tig][wm + i * 8 + g];
+      for (int i = 0; i < 4; ++i) af[i] = sm.As[cur][kk + tig][wm + i * 8 + g];
 #pragma unroll
-      for (int j = 0; j < 4; ++j) bf[j] = Bs[cur][kk + tig][wn + j * 8 + g];
+      for (int j = 0; j < 4; ++j) bf[j] = sm.Bs[cur][kk + tig][wn + j * 8 + g];
 #pragma unroll
       for (int i = 0; i < 4; ++i)
 #pragma unroll
         for (int j = 0; j < 4; ++j) dmma_8x8x4(acc[i][j], af[i], bf[j]);
     }
     if (ks + 1 < ksteps) {
-      store_tile<A_KFAST>(As[cur ^ 1], ra);
-      store_tile<B_KFAST>(Bs[cur ^ 1], rb);
+      store_tile(a_kfast, sm.As[cur ^ 1], ra);
+      store_tile(b_kfast, sm.Bs[cur ^ 1], rb);
     }
     __syncthreads();
   }
+}
 
-  // Epilogue: scatter into D through the destination offset tables.
+__device__ void write_tile(const double (&acc)[4][4][2], double* __restrict__ D,
+                           const int64_t* __restrict__ offDm, const int64_t* __restrict__ offDn,
+                           int M, int N, int m0, int n0, int beta) {
+  const int t = threadIdx.x, warp = t >> 5, lane = t & 31;
+  const int g = lane >> 2, tig = lane & 3;
+  const int wm = (warp & 1) * 32, wn = (warp >> 1) * 32;
 #pragma unroll
   for (int i = 0; i < 4; ++i) {
     const int m = m0 + wm + i * 8 + g;
@@ -144,6 +133,46 @@ __global__ void __launch_bounds__(kThreadsF64) contract_f64_kernel(
   }
 }
 
+__global__ void __launch_bounds__(kThreadsF64) contract_f64_kernel(
+    const double* __restrict__ L, const double* __restrict__ R, double* __restrict__ D,
+    const int64_t* __restrict__ offLm, const int64_t* __restrict__ offLk,
+    const int64_t* __restrict__ offRk, const int64_t* __restrict__ offRn,
+    const int64_t* __restrict__ offDm, const int64_t* __restrict__ offDn, int M, int N, int K,
+    int tiles_m, int beta, int a_kfast, int b_kfast) {
+  __shared__ __align__(16) Smem sm;
+  const int tm = blockIdx.x % tiles_m, tn = blockIdx.x / tiles_m;
+  const int m0 = tm * BM, n0 = tn * BN;
+  double acc[4][4][2];
+#pragma unroll
+  for (int i = 0; i < 4; ++i)
+#pragma unroll
+    for (int j = 0; j < 4; ++j) acc[i][j][0] = acc[i][j][1] = 0.0;
+  accumulate_pair(sm, acc, L, R, offLm, offLk, offRk, offRn, M, N, K, m0, n0, a_kfast, b_kfast);
+  write_tile(acc, D, offDm, offDn, M, N, m0, n0, beta);
+}
+
+// One CTA per (destination block, 64x64 tile); the block's pairs are summed.
+__global__ void __launch_bounds__(kThreadsF64) grouped_f64_kernel(const GroupedF64Tile* __restrict__ tiles,
+                                                                  const GroupedPair* __restrict__ pairs,
+                                                                  const PlanRef* __restrict__ plans,
+                                                                  int beta) {
+  __shared__ __align__(16) Smem sm;
+  const GroupedF64Tile tl = tiles[blockIdx.x];
+  double acc[4][4][2];
+#pragma unroll
+  for (int i = 0; i < 4; ++i)
+#pragma unroll
+    for (int j = 0; j < 4; ++j) acc[i][j][0] = acc[i][j][1] = 0.0;
+  for (int q = tl.pair_begin; q < tl.pair_end; ++q) {
+    const GroupedPair pr = pairs[q];
+    const PlanRef pl = plans[pr.plan];
+    accumulate_pair(sm, acc, pr.l, pr.r, pl.offLm, pl.offLk, pl.offRk, pl.offRn, pl.M, pl.N, pl.K,
+                    tl.m0, tl.n0, pl.a_kfast, pl.b_kfast);
+  }
+  const PlanRef dp = plans[tl.dplan];
+  write_tile(acc, tl.d, dp.offDm, dp.offDn, dp.M, dp.N, tl.m0, tl.n0, beta);
+}
+
 }  // namespace
 
 int launch_contract_f64(const DevPlan* p, const double* L, const double* R, double* D, int beta,
@@ -155,16 +184,22 @@ int launch_contract_f64(const DevPlan* p, const double* L, const double* R, doub
   const int64_t tiles_m = (M + BM - 1) / BM, tiles_n = (N + BN - 1) / BN;
   const int64_t grid = tiles_m * tiles_n;
   if (grid > 0x7fffffffLL) return fail(A4G_ERR_RANGE, "contraction grid too large");
-  auto args = [&](auto kern) {
-    kern<<<unsigned(grid), kThreadsF64, 0, s>>>(L, R, D, p->offLm, p->offLk, p->offRk, p->offRn,
-                                                p->offDm, p->offDn, M, N, K, int(tiles_m), beta);
-  };
-  if (h.a_kfast && h.b_kfast) args(contract_f64_kernel<true, true>);
-  else if (h.a_kfast) args(contract_f64_kernel<true, false>);
-  else if (h.b_kfast) args(contract_f64_kernel<false, true>);
-  else args(contract_f64_kernel<false, false>);
+  contract_f64_kernel<<<unsigned(grid), kThreadsF64, 0, s>>>(L, R, D, p->offLm, p->offLk, p->offRk,
+                                                            p->offRn, p->offDm, p->offDn, M, N, K,
+                                                            int(tiles_m), beta, h.a_kfast, h.b_kfast);
   A4G_CUDA(cudaGetLastError());
   return A4G_OK;
 }
+
+int launch_grouped_f64(const GroupedF64Tile* tiles, int ntiles, const GroupedPair* pairs,
+                       const PlanRef* plans, int beta, cudaStream_t s) {
+  if (ntiles <= 0) return A4G_OK;
+  grouped_f64_kernel<<<ntiles, kThreadsF64, 0, s>>>(tiles, pairs, plans, beta);
+  A4G_CUDA(cudaGetLastError());
+  return A4G_OK;
+}
+
+int grouped_f64_tile_m() { return BM; }
+int grouped_f64_tile_n() { return BN; }
 
 }  // namespace a4g

@@ -1,0 +1,584 @@
+// Split-precision (Ozaki scheme) block contraction on the tcgen05 tensor cores.
+//
+// Each FP64 operand row (left blocks) / column (right blocks) is scaled by a
+// power of two 2^E with |x| < 2^E over the whole row of the pardo step, then
+// cut into `slices` signed 7-bit digits:
+//     x = sign * sum_i d_i * 2^(E - 7(i+1)) + truncation,   d_i in [0, 127].
+// Digits are exact BF16 values.  The product of two slices is an integer
+// matrix, so   L*R ~= sum_t 2^(E_m + F_n - 7(t+2)) * S_t,   S_t = sum_{i+j=t} A_i B_j
+// over levels t < slices (triangular truncation).  Each S_t is computed on the
+// tensor cores (kind::f16, BF16 x BF16 -> FP32) in chunks of k short enough
+// that every FP32 partial sum is an integer below 2^24 and therefore exact;
+// the epilogue warps fold each chunk into an exact FP32 (hi, lo) pair with
+// TwoSum.  A final FP64 kernel applies the powers of two and writes D.
+//
+// Published method: Ozaki, Ogita, Oishi, Rump, "Error-free transformations of
+// matrix multiplication by using fast routines of matrix multiplication and
+// its applications", Numer. Algorithms 59 (2012); Mukunoki, Ozaki, Ogita,
+// Imamura, "DGEMM using Tensor Cores, and Its Accurate and Reproducible
+// Versions", ISC 2020 (slices on tensor cores with exact FP32 accumulation).
+//
+// Kernels:
+//   oz_exp_kernel       max exponent per panel row          (HBM: 8 B/elem read)
+//   oz_split_kernel     FP64 -> BF16 digit slices, K-major   (HBM: 8 B read + 2*slices B write)
+//                       with the block's index permute folded into the gather
+//   oz_gemm_kernel      persistent warp-specialised tcgen05 GEMM: TMA (SW128)
+//                       -> 6-stage smem ring -> tcgen05.mma into TMEM (2 buffers)
+//                       -> epilogue warps fold each chunk into (hi, lo) sums
+//                       that also live in TMEM (tcgen05.ld / tcgen05.st)
+//   oz_recombine_kernel FP64 combination of the levels, scaled store into D
+#include <cuda.h>
+#include <cuda_bf16.h>
+#include <cudaTypedefs.h>
+
+#include "a4g_internal.h"
+#include "grouped.h"
+#include "ozaki.h"
+
+namespace a4g {
+namespace {
+
+constexpr int kDigitBits = 7;
+constexpr int kStages = 6;
+constexpr int kThreadsOz = 192;  // warp 0 TMA, warp 1 MMA, warps 2..5 epilogue
+constexpr uint32_t kTileBytes = kOzBM * kOzBK * 2;  // 16 KB per operand tile
+constexpr uint32_t kStageBytes = 2 * kTileBytes;
+// TMEM columns: [0,128) and [128,256) are the two FP32 MMA accumulators; [256,384)
+// and [384,512) hold the running exact (hi, lo) sums of the current level.
+constexpr uint32_t kTmemCols = 512;
+constexpr uint32_t kTmemHi = 256, kTmemLo = 384;
+constexpr unsigned long long kWaitLimitNs = 20ull * 1000 * 1000 * 1000;  // 20 s
+
+// tcgen05 instruction descriptor, kind::f16: D F32 (bits 4-5 = 1), A BF16
+// (bits 7-9 = 1), B BF16 (bits 10-12 = 1), both K-major (bits 15/16 = 0),
+// N>>3 at bits 17-22, M>>4 at bits 24-28.
+constexpr uint32_t kIdesc = (1u << 4) | (1u << 7) | (1u << 10) | (uint32_t(kOzBN >> 3) << 17) |
+                            (uint32_t(kOzBM >> 4) << 24);
+
+struct __align__(1024) OzSmem {
+  uint8_t a[kStages][kTileBytes];
+  uint8_t b[kStages][kTileBytes];
+  uint64_t full[kStages], empty[kStages];
+  uint64_t acc_full[2], acc_empty[2];
+  uint64_t drain;
+  uint32_t tmem_base;
+  volatile int abort;
+};
+
+// ------------------------------------------------------------------ PTX helpers
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+__device__ __forceinline__ unsigned long long now_ns() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %globaltimer;" : "=l"(t));
+  return t;
+}
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count));
+}
+__device__ __forceinline__ void fence_mbar_init() {
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
+               : "memory");
+}
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}\n"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+// Bounded wait: gives up after kWaitLimitNs or when another role aborted.
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, OzSmem& sm, int* err,
+                                          int code) {
+  if (mbar_try_wait(bar, parity)) return true;
+  const unsigned long long t0 = now_ns();
+#pragma unroll 1
+  for (uint32_t it = 1;; ++it) {
+    if (mbar_try_wait(bar, parity)) return true;
+    if ((it & 255) == 0) {
+      if (sm.abort) return false;
+      if (now_ns() - t0 > kWaitLimitNs) {
+        sm.abort = 1;
+        atomicExch(err, code);
+        return false;
+      }
+    }
+  }
+}
+__device__ __forceinline__ void tma_load_2d(void* dst, const void* map, uint64_t* bar, int c0, int c1) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%3, %4}], [%2];" ::"r"(
+          smem_u32(dst)),
+      "l"(map), "r"(smem_u32(bar)), "r"(c0), "r"(c1)
+      : "memory");
+}
+__device__ __forceinline__ void tc_fence_before() {
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+}
+__device__ __forceinline__ void tc_fence_after() {
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+}
+__device__ __forceinline__ void tc_commit(uint64_t* bar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                   smem_u32(bar))
+               : "memory");
+}
+__device__ __forceinline__ void tc_mma(uint32_t d_tmem, uint64_t adesc, uint64_t bdesc, uint32_t accum) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "setp.ne.b32 p, %4, 0;\n\t"
+      "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(d_tmem),
+      "l"(adesc), "l"(bdesc), "r"(kIdesc), "r"(accum));
+}
+// Shared-memory matrix descriptor: K-major, 128-byte swizzle, rows of 128 B,
+// 8-row core groups 1024 B apart (SBO), descriptor version 1 (bits 46-48).
+__device__ __forceinline__ uint64_t sw128_desc(const void* tile) {
+  const uint32_t addr = smem_u32(tile);
+  uint64_t d = uint64_t((addr & 0x3FFFF) >> 4);
+  d |= uint64_t(1) << 16;            // leading byte offset (unused for SW128 K-major)
+  d |= uint64_t(1024 >> 4) << 32;    // stride byte offset
+  d |= uint64_t(1) << 46;
+  d |= uint64_t(2) << 61;            // SWIZZLE_128B
+  return d;
+}
+__device__ __forceinline__ void tc_ld32(uint32_t taddr, uint32_t (&r)[32]) {
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x32.b32 "
+      "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+      "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+        "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]),
+        "=r"(r[14]), "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]),
+        "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]), "=r"(r[25]),
+        "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+      : "r"(taddr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+}
+
+// Exact accumulation of an integer-valued float x (|x| < 2^24) into hi + lo.
+__device__ __forceinline__ void two_sum_acc(float& hi, float& lo, float x) {
+  const float s = __fadd_rn(hi, x);
+  const float bp = __fsub_rn(s, hi);
+  const float e = __fadd_rn(__fsub_rn(hi, __fsub_rn(s, bp)), __fsub_rn(x, bp));
+  hi = s;
+  lo = __fadd_rn(lo, e);
+}
+
+// ------------------------------------------------------------------ roles
+__device__ void producer(const OzGemmArgs& a, OzSmem& sm) {
+  uint32_t it = 0;
+  for (int u = blockIdx.x; u < a.n_units; u += gridDim.x) {
+    const int tile = u % a.n_tiles, level = u / a.n_tiles;
+    const OzTile tl = a.tiles[tile];
+    const void* ma = static_cast<const uint8_t*>(a.maps_a) + size_t(tl.panel_a) * 128;
+    const void* mb = static_cast<const uint8_t*>(a.maps_b) + size_t(tl.panel_b) * 128;
+    const int rpa = a.panels_a[tl.panel_a].rows_pad, rpb = a.panels_b[tl.panel_b].rows_pad;
+    for (int q = tl.trip_begin; q < tl.trip_end; ++q) {
+      const OzTrip tr = a.trips[q];
+      for (int j = 0; j < tr.nkb; ++j) {
+        const int ka = int(tr.koff_a) + j * kOzBK, kb = int(tr.koff_b) + j * kOzBK;
+        for (int i = 0; i <= level; ++i) {
+          const int s = it % kStages;
+          const uint32_t ph = (it / kStages) & 1;
+          if (!mbar_wait(&sm.empty[s], ph ^ 1, sm, a.err_flag, 1)) return;
+          mbar_expect_tx(&sm.full[s], kStageBytes);
+          tma_load_2d(sm.a[s], ma, &sm.full[s], ka, i * rpa + tl.m0);
+          tma_load_2d(sm.b[s], mb, &sm.full[s], kb, (level - i) * rpb + tl.n0);
+          ++it;
+        }
+      }
+    }
+  }
+}
+
+__device__ void mma_issuer(const OzGemmArgs& a, OzSmem& sm, uint32_t tmem) {
+  uint32_t it = 0, chunk = 0;
+  for (int u = blockIdx.x; u < a.n_units; u += gridDim.x) {
+    const int tile = u % a.n_tiles, level = u / a.n_tiles;
+    const OzTile tl = a.tiles[tile];
+    const int ckb = a.chunk_kb[level];
+    int kb_done = 0, in_chunk = 0;
+    uint32_t buf = 0;
+    for (int q = tl.trip_begin; q < tl.trip_end; ++q) {
+      const int nkb = a.trips[q].nkb;
+      for (int j = 0; j < nkb; ++j) {
+        if (in_chunk == 0) {
+          buf = chunk & 1;
+          if (!mbar_wait(&sm.acc_empty[buf], ((chunk >> 1) & 1) ^ 1, sm, a.err_flag, 2)) return;
+          tc_fence_after();
+        }
+        const uint32_t d_tmem = tmem + buf * kOzBN;
+        for (int i = 0; i <= level; ++i) {
+          const int s = it % kStages;
+          const uint32_t ph = (it / kStages) & 1;
+          if (!mbar_wait(&sm.full[s], ph, sm, a.err_flag, 3)) return;
+          tc_fence_after();
+          const uint64_t ad = sw128_desc(sm.a[s]), bd = sw128_desc(sm.b[s]);
+#pragma unroll
+          for (int kk = 0; kk < kOzBK / 16; ++kk)
+            tc_mma(d_tmem, ad + 2 * kk, bd + 2 * kk, (in_chunk == 0 && i == 0 && kk == 0) ? 0u : 1u);
+          tc_commit(&sm.empty[s]);
+          ++it;
+        }
+        ++kb_done;
+        ++in_chunk;
+        if (in_chunk == ckb || kb_done == tl.kb_total) {
+          tc_commit(&sm.acc_full[buf]);
+          ++chunk;
+          in_chunk = 0;
+        }
+      }
+    }
+  }
+}
+
+__device__ __forceinline__ void tc_st32(uint32_t taddr, const uint32_t (&r)[32]) {
+  asm volatile(
+      "tcgen05.st.sync.aligned.32x32b.x32.b32 [%0], "
+      "{%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16,"
+      "%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31,%32};" ::"r"(taddr),
+      "r"(r[0]), "r"(r[1]), "r"(r[2]), "r"(r[3]), "r"(r[4]), "r"(r[5]), "r"(r[6]), "r"(r[7]),
+      "r"(r[8]), "r"(r[9]), "r"(r[10]), "r"(r[11]), "r"(r[12]), "r"(r[13]), "r"(r[14]),
+      "r"(r[15]), "r"(r[16]), "r"(r[17]), "r"(r[18]), "r"(r[19]), "r"(r[20]), "r"(r[21]),
+      "r"(r[22]), "r"(r[23]), "r"(r[24]), "r"(r[25]), "r"(r[26]), "r"(r[27]), "r"(r[28]),
+      "r"(r[29]), "r"(r[30]), "r"(r[31])
+      : "memory");
+}
+
+// Four warps, one per TMEM lane quadrant; each thread owns one accumulator
+// row and walks its 128 columns in groups of 32.
+__device__ void epilogue(const OzGemmArgs& a, OzSmem& sm, uint32_t tmem, int warp, int lane) {
+  const int q = warp & 3;
+  const int row = 32 * q + lane;
+  const uint32_t lane_addr = tmem + (uint32_t(32 * q) << 16);
+  uint32_t chunk = 0;
+  for (int u = blockIdx.x; u < a.n_units; u += gridDim.x) {
+    const int tile = u % a.n_tiles, level = u / a.n_tiles;
+    const int kb_total = a.tiles[tile].kb_total;
+    const int ckb = a.chunk_kb[level];
+    const int nchunks = (kb_total + ckb - 1) / ckb;
+    float2* w = a.ws + (size_t(tile) * a.slices + level) * kOzBN * kOzBM + row;
+    for (int c = 0; c < nchunks; ++c) {
+      const uint32_t buf = chunk & 1;
+      if (!mbar_wait(&sm.acc_full[buf], (chunk >> 1) & 1, sm, a.err_flag, 4)) return;
+      tc_fence_after();
+      const bool first = c == 0, last = c == nchunks - 1;
+#pragma unroll 1
+      for (int g = 0; g < kOzBN / 32; ++g) {
+        uint32_t x[32], hi[32], lo[32];
+        tc_ld32(lane_addr + buf * kOzBN + 32 * g, x);
+        if (first) {
+#pragma unroll
+          for (int j = 0; j < 32; ++j) hi[j] = x[j], lo[j] = 0u;
+        } else {
+          tc_ld32(lane_addr + kTmemHi + 32 * g, hi);
+          tc_ld32(lane_addr + kTmemLo + 32 * g, lo);
+#pragma unroll
+          for (int j = 0; j < 32; ++j) {
+            float h = __uint_as_float(hi[j]), l = __uint_as_float(lo[j]);
+            two_sum_acc(h, l, __uint_as_float(x[j]));
+            hi[j] = __float_as_uint(h), lo[j] = __float_as_uint(l);
+          }
+        }
+        if (!last) {
+          tc_st32(lane_addr + kTmemHi + 32 * g, hi);
+          tc_st32(lane_addr + kTmemLo + 32 * g, lo);
+          asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
+        } else {
+#pragma unroll
+          for (int j = 0; j < 32; ++j)
+            w[size_t(32 * g + j) * kOzBM] = make_float2(__uint_as_float(hi[j]), __uint_as_float(lo[j]));
+        }
+      }
+      tc_fence_before();
+      __syncwarp();
+      if (lane == 0) mbar_arrive(&sm.acc_empty[buf]);
+      ++chunk;
+    }
+  }
+}
+
+__global__ void __launch_bounds__(kThreadsOz, 1) oz_gemm_kernel(const __grid_constant__ OzGemmArgs a) {
+  extern __shared__ uint8_t smem_raw[];
+  OzSmem& sm = *reinterpret_cast<OzSmem*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < kStages; ++s) {
+      mbar_init(&sm.full[s], 1);
+      mbar_init(&sm.empty[s], 1);
+    }
+    for (int b = 0; b < 2; ++b) {
+      mbar_init(&sm.acc_full[b], 1);
+      mbar_init(&sm.acc_empty[b], 4);  // one arrive per epilogue warp
+    }
+    mbar_init(&sm.drain, 1);
+    sm.abort = 0;
+    fence_mbar_init();
+  }
+  if (warp == 1) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                     smem_u32(&sm.tmem_base)),
+                 "r"(kTmemCols));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = sm.tmem_base;
+
+  if (warp == 0) {
+    if (lane == 0) producer(a, sm);
+  } else if (warp == 1) {
+    if (lane == 0) {
+      mma_issuer(a, sm, tmem);
+      // all MMAs this thread issued have completed before TMEM is released
+      tc_commit(&sm.drain);
+      mbar_wait(&sm.drain, 0, sm, a.err_flag, 5);
+    }
+  } else {
+    epilogue(a, sm, tmem, warp, lane);
+  }
+  tc_fence_before();
+  __syncthreads();
+  if (warp == 1) {
+    tc_fence_after();
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kTmemCols));
+  }
+}
+
+// ------------------------------------------------------------------ split side
+// Tiles of 64 rows x 64 k over the jobs; job_tiles[j] is the prefix count.
+__device__ __forceinline__ int find_job(const int64_t* prefix, int njobs, int64_t t) {
+  int lo = 0, hi = njobs;  // prefix[lo] <= t < prefix[hi]
+  while (hi - lo > 1) {
+    const int mid = (lo + hi) >> 1;
+    if (prefix[mid] <= t) lo = mid;
+    else hi = mid;
+  }
+  return lo;
+}
+
+constexpr int kSplitT = 64;
+
+// Loads one 64x64 (row, k) tile of a job into shared memory as raw bits.
+__device__ __forceinline__ void load_job_tile(const OzSplitJob& jb, int r0, int k0,
+                                              unsigned long long (*tile)[kSplitT + 1]) {
+  const int t = threadIdx.x;  // 256 threads
+  for (int p = 0; p < 16; ++p) {
+    int r, k;
+    if (jb.kfast) {
+      k = t & 63;
+      r = (t >> 6) + 4 * p;
+    } else {
+      r = t & 63;
+      k = (t >> 6) + 4 * p;
+    }
+    unsigned long long v = 0;
+    if (r0 + r < jb.rows && k0 + k < jb.K)
+      v = __double_as_longlong(__ldg(&jb.src[__ldg(&jb.offRow[r0 + r]) + __ldg(&jb.offK[k0 + k])]));
+    tile[r][k] = v;
+  }
+}
+
+__global__ void __launch_bounds__(256) oz_exp_kernel(const OzSplitJob* __restrict__ jobs,
+                                                     const int64_t* __restrict__ prefix, int njobs,
+                                                     const OzPanel* __restrict__ panels) {
+  __shared__ unsigned long long tile[kSplitT][kSplitT + 1];
+  const int64_t t = blockIdx.x;
+  const int j = find_job(prefix, njobs, t);
+  const OzSplitJob jb = jobs[j];
+  const int64_t local = t - prefix[j];
+  const int ktiles = (jb.K + kSplitT - 1) / kSplitT;
+  const int r0 = int(local / ktiles) * kSplitT, k0 = int(local % ktiles) * kSplitT;
+  load_job_tile(jb, r0, k0, tile);
+  __syncthreads();
+  // 4 threads per row, 16 k each
+  const int r = threadIdx.x >> 2, part = threadIdx.x & 3;
+  int m = 0;
+  for (int k = part * 16; k < part * 16 + 16; ++k) m = max(m, int((tile[r][k] >> 52) & 0x7FF));
+  m = max(m, __shfl_xor_sync(0xffffffffu, m, 1));
+  m = max(m, __shfl_xor_sync(0xffffffffu, m, 2));
+  if (part == 0 && r0 + r < jb.rows && m > 0) atomicMax(&panels[jb.panel].exps[r0 + r], m);
+}
+
+// Digits of one double against the row exponent (biased max exponent mx):
+// q = floor(|x| * 2^(7*slices - E)) with E = mx - 1022, so |x| < 2^E and
+// q < 2^(7*slices); digit i is bits [7(slices-1-i), 7(slices-i)) of q.
+__device__ __forceinline__ unsigned long long quantize(unsigned long long bits, int mx, int slices) {
+  const int be = int((bits >> 52) & 0x7FF);
+  const unsigned long long frac = bits & ((1ull << 52) - 1);
+  const unsigned long long mant = be ? (frac | (1ull << 52)) : frac;
+  const int ex = be ? be : 1;
+  const int E = (mx ? mx : 1) - 1022;
+  const int sh = ex - 1075 + kDigitBits * slices - E;  // always <= 7*slices - 53 < 0
+  const int rs = -sh;
+  return rs >= 64 ? 0ull : (mant >> rs);
+}
+
+__global__ void __launch_bounds__(256) oz_split_kernel(const OzSplitJob* __restrict__ jobs,
+                                                       const int64_t* __restrict__ prefix, int njobs,
+                                                       const OzPanel* __restrict__ panels, int slices) {
+  __shared__ unsigned long long tile[kSplitT][kSplitT + 1];
+  const int64_t t = blockIdx.x;
+  const int j = find_job(prefix, njobs, t);
+  const OzSplitJob jb = jobs[j];
+  const int64_t local = t - prefix[j];
+  const int ktiles = (jb.K + kSplitT - 1) / kSplitT;
+  const int r0 = int(local / ktiles) * kSplitT, k0 = int(local % ktiles) * kSplitT;
+  load_job_tile(jb, r0, k0, tile);
+  __syncthreads();
+  const OzPanel pn = panels[jb.panel];
+  // each thread: one row, two consecutive k -> one bf16x2 store per slice
+  const int kp = threadIdx.x & 31;
+  for (int p = 0; p < 8; ++p) {
+    const int r = (threadIdx.x >> 5) + 8 * p;
+    if (r0 + r >= jb.rows) continue;
+    const int k = 2 * kp;
+    if (k0 + k >= jb.K) continue;
+    const int mx = pn.exps[r0 + r];
+    const unsigned long long b0 = tile[r][k], b1 = (k0 + k + 1 < jb.K) ? tile[r][k + 1] : 0ull;
+    const unsigned long long q0 = quantize(b0, mx, slices), q1 = quantize(b1, mx, slices);
+    const float s0 = (b0 >> 63) ? -1.f : 1.f, s1 = (b1 >> 63) ? -1.f : 1.f;
+    __nv_bfloat162* dst = reinterpret_cast<__nv_bfloat162*>(
+        pn.base + (size_t(r0 + r) * pn.kpad + jb.koff + k0 + k));
+    const size_t slice_stride = size_t(pn.rows_pad) * pn.kpad / 2;
+    for (int i = 0; i < slices; ++i) {
+      const int sh = kDigitBits * (slices - 1 - i);
+      const float d0 = s0 * float((q0 >> sh) & 127ull), d1 = s1 * float((q1 >> sh) & 127ull);
+      dst[i * slice_stride] = __floats2bfloat162_rn(d0, d1);
+    }
+  }
+}
+
+// ------------------------------------------------------------------ recombine
+__global__ void __launch_bounds__(256) oz_recombine_kernel(const OzTile* __restrict__ tiles,
+                                                           const OzDBlock* __restrict__ dblocks,
+                                                           const PlanRef* __restrict__ plans,
+                                                           const OzPanel* __restrict__ pa,
+                                                           const OzPanel* __restrict__ pb,
+                                                           const float2* __restrict__ ws, int slices,
+                                                           int beta) {
+  const int tile = blockIdx.x;
+  const OzTile tl = tiles[tile];
+  const OzDBlock db = dblocks[tl.dblock];
+  const PlanRef pl = plans[db.plan];
+  const int* ea = pa[tl.panel_a].exps;
+  const int* eb = pb[tl.panel_b].exps;
+  for (int e = threadIdx.x; e < kOzBM * kOzBN; e += blockDim.x) {
+    const int row = e & (kOzBM - 1), col = e >> 7;
+    const int m = tl.m0 + row, n = tl.n0 + col;
+    if (m >= pl.M || n >= pl.N) continue;
+    double v = 0.0;
+    for (int lv = slices - 1; lv >= 0; --lv) {
+      const float2 p = ws[((size_t(tile) * slices + lv) * kOzBN + col) * kOzBM + row];
+      const double s = double(p.x) + double(p.y);  // exact: both integers, sum < 2^53
+      v += ldexp(s, -kDigitBits * (lv + 2));
+    }
+    const int E = (ea[m] ? ea[m] : 1) - 1022, F = (eb[n] ? eb[n] : 1) - 1022;
+    v = ldexp(v, E + F);
+    double* dst = db.d + pl.offDm[m] + pl.offDn[n];
+    *dst = beta ? *dst + v : v;
+  }
+}
+
+using EncodeTiled = PFN_cuTensorMapEncodeTiled_v12000;
+EncodeTiled get_encoder() {
+  static EncodeTiled fn = nullptr;
+  if (!fn) {
+    cudaDriverEntryPointQueryResult q;
+    void* p = nullptr;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+            cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<EncodeTiled>(p);
+  }
+  return fn;
+}
+
+}  // namespace
+
+int oz_chunk_kb(int level) {
+  // largest multiple of 64 k such that (level+1) * 127^2 * k < 2^24
+  const long long per = (long long)(level + 1) * 127 * 127;
+  const long long k = ((1LL << 24) - 1) / per;
+  return int(k / kOzBK);
+}
+
+int oz_make_tensor_map(void* map128, const void* base, int64_t kpad, int64_t rows_total) {
+  EncodeTiled enc = get_encoder();
+  if (!enc) return fail(A4G_ERR_CUDA, "cuTensorMapEncodeTiled unavailable");
+  if (kpad % kOzBK != 0 || (reinterpret_cast<uintptr_t>(base) & 15) != 0)
+    return fail(A4G_ERR_ARG, "panel not aligned for TMA");
+  cuuint64_t dims[2] = {cuuint64_t(kpad), cuuint64_t(rows_total)};
+  cuuint64_t strides[1] = {cuuint64_t(kpad) * 2};
+  cuuint32_t box[2] = {kOzBK, kOzBM};
+  cuuint32_t estr[2] = {1, 1};
+  CUresult r = enc(reinterpret_cast<CUtensorMap*>(map128), CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2,
+                   const_cast<void*>(base), dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                   CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                   CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS) return fail(A4G_ERR_CUDA, "cuTensorMapEncodeTiled failed: " + std::to_string(int(r)));
+  return A4G_OK;
+}
+
+int oz_launch_exp(const OzSplitJob* jobs, const int64_t* prefix, int njobs, int64_t ntiles,
+                  const OzPanel* panels, cudaStream_t s) {
+  if (ntiles <= 0) return A4G_OK;
+  if (ntiles > 0x7fffffffLL) return fail(A4G_ERR_RANGE, "too many split tiles");
+  oz_exp_kernel<<<unsigned(ntiles), 256, 0, s>>>(jobs, prefix, njobs, panels);
+  A4G_CUDA(cudaGetLastError());
+  return A4G_OK;
+}
+
+int oz_launch_split(const OzSplitJob* jobs, const int64_t* prefix, int njobs, int64_t ntiles,
+                    const OzPanel* panels, int slices, cudaStream_t s) {
+  if (ntiles <= 0) return A4G_OK;
+  if (ntiles > 0x7fffffffLL) return fail(A4G_ERR_RANGE, "too many split tiles");
+  oz_split_kernel<<<unsigned(ntiles), 256, 0, s>>>(jobs, prefix, njobs, panels, slices);
+  A4G_CUDA(cudaGetLastError());
+  return A4G_OK;
+}
+
+int oz_prepare() {
+  static bool done = false;
+  if (!done) {
+    A4G_CUDA(cudaFuncSetAttribute(oz_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  int(sizeof(OzSmem)) + 1024));
+    done = true;
+  }
+  return A4G_OK;
+}
+
+int oz_launch_gemm(const OzGemmArgs& args, int grid, cudaStream_t s) {
+  if (args.slices > kOzMaxUsableSlices) return fail(A4G_ERR_ARG, "at most 7 slices");
+  const int smem = int(sizeof(OzSmem)) + 1024;
+  int rc = oz_prepare();
+  if (rc) return rc;
+  if (args.slices < 1 || args.slices > kOzMaxSlices) return fail(A4G_ERR_ARG, "slices out of range");
+  if (args.n_units <= 0) return A4G_OK;
+  oz_gemm_kernel<<<grid, kThreadsOz, smem, s>>>(args);
+  A4G_CUDA(cudaGetLastError());
+  return A4G_OK;
+}
+
+int oz_launch_recombine(const OzTile* tiles, int ntiles, const OzDBlock* dblocks, const PlanRef* plans,
+                        const OzPanel* pa, const OzPanel* pb, const float2* ws, int slices, int beta,
+                        cudaStream_t s) {
+  if (ntiles <= 0) return A4G_OK;
+  oz_recombine_kernel<<<ntiles, 256, 0, s>>>(tiles, dblocks, plans, pa, pb, ws, slices, beta);
+  A4G_CUDA(cudaGetLastError());
+  return A4G_OK;
+}
+
+}  // namespace a4g

@@ -142,3 +142,70 @@ def gpu_contract(y, ydims, yinds, x1, x1dims, x1inds, x2, x2dims, x2inds):
 def gpu_permute(y, ydims, yinds, x, xdims, xinds):
     lib()._gpu_permute(ctypes.c_void_p(_ptr(y)), _i(len(ydims)), _iarr(ydims), _iarr(yinds),
                        ctypes.c_void_p(_ptr(x)), _i(len(xdims)), _iarr(xdims), _iarr(xinds))
+
+
+# ------------------------------------------------ batched pardo step
+PREC_FP64 = 0
+PREC_OZAKI_BF16 = 1
+
+
+class _Triple(ctypes.Structure):
+    _fields_ = [("d", ctypes.c_void_p), ("l", ctypes.c_void_p), ("r", ctypes.c_void_p),
+                ("dext", ctypes.c_int * 6), ("lext", ctypes.c_int * 6), ("rext", ctypes.c_int * 6)]
+
+
+class _Opts(ctypes.Structure):
+    _fields_ = [("precision", ctypes.c_int), ("slices", ctypes.c_int), ("beta", ctypes.c_int),
+                ("reserved", ctypes.c_int * 5)]
+
+
+def _ext6(e):
+    e = list(e) + [1] * (6 - len(e))
+    return (ctypes.c_int * 6)(*e)
+
+
+class Batch:
+    """One pardo step: every (D, L, R) block triple of one SIAL contraction
+    statement, executed by one call.  Triples with the same D are summed into
+    it; a triple whose L or R is None is a zero block and is skipped.
+
+    triples: iterable of (d, l, r, dext, lext, rext) with CUDA tensors (or
+    device addresses) and per-block extents.
+    """
+
+    def __init__(self, ptrn, drank, lrank, rrank, triples, precision=PREC_FP64, slices=6, beta=0):
+        tl = list(triples)
+        arr = (_Triple * max(1, len(tl)))()
+        for i, (d, l, r, de, le, re) in enumerate(tl):
+            arr[i].d, arr[i].l, arr[i].r = _ptr(d), _ptr(l), _ptr(r)
+            arr[i].dext, arr[i].lext, arr[i].rext = _ext6(de), _ext6(le), _ext6(re)
+        opts = _Opts(precision, slices, beta)
+        h = ctypes.c_void_p(0)
+        rc = lib().a4g_batch_create(ctypes.byref(h), _iarr(ptrn), _i(drank), _i(lrank), _i(rrank), arr,
+                                    ctypes.c_int64(len(tl)), ctypes.byref(opts))
+        _check(rc, "a4g_batch_create")
+        self._h = h
+        self._keep = tl  # the caller's buffers must outlive the batch
+
+    def run(self, stream=None):
+        _check(lib().a4g_batch_run(self._h, _stream(stream)), "a4g_batch_run")
+
+    def run_graph(self, stream=None):
+        _check(lib().a4g_batch_run_graph(self._h, _stream(stream)), "a4g_batch_run_graph")
+
+    def info(self):
+        pairs, flops, ws = ctypes.c_int64(0), ctypes.c_double(0), ctypes.c_int64(0)
+        _check(lib().a4g_batch_info(self._h, ctypes.byref(pairs), ctypes.byref(flops), ctypes.byref(ws)),
+               "a4g_batch_info")
+        return {"pairs": pairs.value, "flops": flops.value, "device_bytes": ws.value}
+
+    def close(self):
+        if getattr(self, "_h", None) and self._h.value:
+            lib().a4g_batch_destroy(self._h)
+            self._h = ctypes.c_void_p(0)
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

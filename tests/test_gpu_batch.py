@@ -1,0 +1,202 @@
+"""Batched (one pardo step) contraction through the C ABI: the grouped FP64
+kernel and the split-precision tcgen05 pipeline, against the CPU oracle's BLAS
+path per destination block.
+
+Tolerances (relative Frobenius error per destination block):
+  plain FP64 grouped kernel   1e-12
+  split precision, 6 slices   1e-10   (the stated bound of the split form)
+  split precision, 1 slice on integer data in [-127, 127]: bit-exact
+"""
+import itertools
+
+import numpy as np
+import pytest
+
+from oracle import oracle
+
+pytestmark = pytest.mark.gpu
+
+TOL_FP64 = 1e-12
+TOL_SPLIT = 1e-10
+
+
+@pytest.fixture(scope="module")
+def a4():
+    import aces4_gb300
+
+    aces4_gb300.build()
+    aces4_gb300.device.init(0)
+    return aces4_gb300
+
+
+def _ptrn(labels):
+    d, l, r = labels
+    ierr, p = oracle.get_contraction_ptrn(len(d), len(l), len(r), d + l + r)
+    assert ierr == 0
+    return p
+
+
+def _make(a4, kind, vsegs, osegs, zero_frac, seed, outliers=False, integer=False):
+    from aces4_gb300.blocks import BlockArray, ladder_triples, ring_triples, LADDER_LABELS, RING_LABELS
+
+    rng = np.random.default_rng(seed)
+    v = sum(vsegs)
+    o = sum(osegs)
+    zero = {}
+
+    def vpresent(k):
+        zero.setdefault(k, rng.random() < zero_frac)
+        return not zero[k]
+
+    def vfill(k, e):
+        n = int(np.prod(e))
+        if integer:
+            return rng.integers(-127, 128, n).astype(np.float64)
+        return rng.uniform(-1, 1, n) / (v if kind == "ladder" else np.sqrt(o * v))
+
+    def tfill(k, e):
+        n = int(np.prod(e))
+        if integer:
+            return rng.integers(-127, 128, n).astype(np.float64)
+        x = rng.normal(0.0, 0.1, n)
+        if outliers:
+            x[rng.random(n) < 0.01] *= 1e3
+        return x
+
+    if kind == "ladder":
+        V = BlockArray([vsegs] * 4, present=vpresent)
+        T = BlockArray([vsegs, vsegs, osegs, osegs])
+        R = BlockArray([vsegs, vsegs, osegs, osegs])
+        V.fill_from(vfill)
+        T.fill_from(tfill)
+        trip = ladder_triples(R, V, T)
+        labels = LADDER_LABELS
+    else:
+        V = BlockArray([vsegs, osegs, vsegs, osegs], present=vpresent)
+        T = BlockArray([vsegs, vsegs, osegs, osegs])
+        R = BlockArray([vsegs, osegs, vsegs, osegs])
+        V.fill_from(vfill)
+        T.fill_from(tfill)
+        trip = ring_triples(R, V, T)
+        labels = RING_LABELS
+    return R, V, T, trip, labels
+
+
+def _reference(R, trip, labels):
+    """Per destination block: sum over live pairs of the BLAS-path oracle."""
+    p = _ptrn(labels)
+    ref = {}
+    ptr_to_key = {R.block(k).data_ptr(): k for k in R.keys()}
+    for d, l, r, de, le, re in trip:
+        key = ptr_to_key[d.data_ptr()]
+        acc = ref.setdefault(key, np.zeros(int(np.prod(de))))
+        if l is None or r is None:
+            continue
+        acc += oracle.contract_blas(p, l.cpu().numpy(), le, r.cpu().numpy(), re, de)
+    return ref
+
+
+def _errors(R, ref):
+    errs = []
+    for k, want in ref.items():
+        got = R.block(k).cpu().numpy()
+        nb = np.linalg.norm(want)
+        errs.append(np.linalg.norm(got - want) / (nb if nb > 0 else 1.0))
+    return np.array(errs)
+
+
+def _run(a4, R, trip, labels, precision, slices=6, beta=0, graph=False):
+    import torch
+
+    b = a4.device.Batch(_ptrn(labels), 4, 4, 4, trip, precision=precision, slices=slices, beta=beta)
+    if graph:
+        b.run_graph()
+    else:
+        b.run()
+    a4.device.sync()
+    torch.cuda.synchronize()
+    return b
+
+
+def test_fp64_ladder_config1_shape(a4):
+    # o=10 as 2 segments of 5, v=48 as 4 segments of 12, all blocks dense
+    R, V, T, trip, labels = _make(a4, "ladder", [12] * 4, [5, 5], 0.0, 1)
+    R.buf.fill_(np.nan)
+    b = _run(a4, R, trip, labels, a4.device.PREC_FP64)
+    info = b.info()
+    assert info["pairs"] == 4 ** 4 * 2 ** 2
+    assert abs(info["flops"] - 2 * 48 ** 4 * 10 ** 2) < 1
+    assert _errors(R, _reference(R, trip, labels)).max() <= TOL_FP64
+
+
+def test_fp64_uneven_sparse_ring(a4):
+    R, V, T, trip, labels = _make(a4, "ring", [12, 16, 24], [5, 8], 0.3, 2)
+    R.buf.fill_(np.nan)
+    _run(a4, R, trip, labels, a4.device.PREC_FP64)
+    errs = _errors(R, _reference(R, trip, labels))
+    assert errs.max() <= TOL_FP64
+
+
+def test_split_one_slice_integer_exact(a4):
+    # integers in [-127, 127] are exact single 7-bit digits: the tensor-core
+    # products and the chunked FP32 accumulation must reproduce FP64 exactly
+    R, V, T, trip, labels = _make(a4, "ladder", [32, 32], [16, 16], 0.0, 3, integer=True)
+    _run(a4, R, trip, labels, a4.device.PREC_OZAKI_BF16, slices=1)
+    ref = _reference(R, trip, labels)
+    for k, want in ref.items():
+        np.testing.assert_array_equal(R.block(k).cpu().numpy(), want)
+
+
+def test_split_long_k_integer_exact(a4):
+    # K per destination row = 16 * 48^2 = 36864 (several exact flush chunks,
+    # several levels' chunk sizes) with 2 slices on integer data
+    R, V, T, trip, labels = _make(a4, "ladder", [48] * 4, [8], 0.0, 4, integer=True)
+    _run(a4, R, trip, labels, a4.device.PREC_OZAKI_BF16, slices=2)
+    ref = _reference(R, trip, labels)
+    for k, want in ref.items():
+        np.testing.assert_array_equal(R.block(k).cpu().numpy(), want)
+
+
+@pytest.mark.parametrize("slices,tol", [(4, 1e-6), (5, 1e-8), (6, TOL_SPLIT), (7, 1e-12)])
+def test_split_ladder_outliers(a4, slices, tol):
+    # config-4 distributions (V ~ U[-1,1]/v, T ~ N(0,1e-2) with 1% x1e3) on a
+    # smaller ladder: v=64 in 2 segments of 32, o=32 in 2 segments of 16
+    R, V, T, trip, labels = _make(a4, "ladder", [32, 32], [16, 16], 0.0, 5, outliers=True)
+    _run(a4, R, trip, labels, a4.device.PREC_OZAKI_BF16, slices=slices)
+    errs = _errors(R, _reference(R, trip, labels))
+    assert errs.max() <= tol, (slices, errs.max())
+
+
+def test_split_uneven_sparse_ring_graph_and_beta(a4):
+    import torch
+
+    R, V, T, trip, labels = _make(a4, "ring", [12, 16, 24, 32], [5, 8], 0.3, 6)
+    ref = _reference(R, trip, labels)
+    _run(a4, R, trip, labels, a4.device.PREC_OZAKI_BF16, slices=6, graph=True)
+    assert _errors(R, ref).max() <= TOL_SPLIT
+    first = R.buf.clone()
+    # replaying the captured graph gives identical bits
+    b = a4.device.Batch(_ptrn(labels), 4, 4, 4, trip, precision=a4.device.PREC_OZAKI_BF16, slices=6)
+    b.run_graph()
+    b.run_graph()
+    a4.device.sync()
+    assert torch.equal(first, R.buf)
+    # beta = 1 accumulates on top of the existing blocks
+    base = R.buf.clone()
+    bb = a4.device.Batch(_ptrn(labels), 4, 4, 4, trip, precision=a4.device.PREC_OZAKI_BF16, slices=6, beta=1)
+    bb.run()
+    a4.device.sync()
+    for k, want in ref.items():
+        got = R.block(k).cpu().numpy()
+        want2 = want + base[R.offsets[k]:R.offsets[k] + want.size].cpu().numpy()
+        assert np.linalg.norm(got - want2) <= TOL_SPLIT * np.linalg.norm(want2)
+
+
+def test_zero_destination_blocks_are_cleared(a4):
+    # every V block zero -> R blocks receive no pair and are overwritten with 0
+    R, V, T, trip, labels = _make(a4, "ladder", [12, 12], [5], 1.0, 7)
+    for prec in (a4.device.PREC_FP64, a4.device.PREC_OZAKI_BF16):
+        R.buf.fill_(5.0)
+        b = _run(a4, R, trip, labels, prec)
+        assert b.info()["pairs"] == 0
+        assert all(float(R.block(k).abs().max()) == 0.0 for k in R.keys())
