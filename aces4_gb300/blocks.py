@@ -65,11 +65,11 @@ def ladder_triples(R: BlockArray, V: BlockArray, T: BlockArray):
     """R(a,b,i,j) += V(a,b,c,d) T(c,d,i,j) over every segment tuple: the
     particle-particle ladder statement of rlccd_rhf.sialx:399-433 as block
     triples (zero V or T blocks give a NULL operand, skipped by the batch)."""
-    nv = len(V.segs[0])
-    no = len(T.segs[2])
+    na, nb, nc, nd = (len(V.segs[q]) for q in range(4))
+    ni, nj = len(T.segs[2]), len(T.segs[3])
     out = []
-    for a, b, i, j in itertools.product(range(nv), range(nv), range(no), range(no)):
-        for c, d in itertools.product(range(nv), range(nv)):
+    for a, b, i, j in itertools.product(range(na), range(nb), range(ni), range(nj)):
+        for c, d in itertools.product(range(nc), range(nd)):
             rk, vk, tk = (a, b, i, j), (a, b, c, d), (c, d, i, j)
             out.append((R.block(rk), V.block(vk), T.block(tk), R.ext(rk), V.ext(vk), T.ext(tk)))
     return out
@@ -84,11 +84,11 @@ RING_LABELS = ([1, 3, 2, 4], [1, 7, 5, 3], [5, 2, 7, 4])
 def ring_triples(R: BlockArray, V: BlockArray, T: BlockArray):
     """R(a,i,b,j) += V(a,k,c,i) T(c,b,k,j): ring term with both operands
     permuted relative to the matrix form."""
-    nv = len(V.segs[0])
-    no = len(V.segs[1])
+    na, nk, nc, ni = (len(V.segs[q]) for q in range(4))
+    nb, nj = len(T.segs[1]), len(T.segs[3])
     out = []
-    for a, i, b, j in itertools.product(range(nv), range(no), range(nv), range(no)):
-        for k, c in itertools.product(range(no), range(nv)):
+    for a, i, b, j in itertools.product(range(na), range(ni), range(nb), range(nj)):
+        for k, c in itertools.product(range(nk), range(nc)):
             rk, vk, tk = (a, i, b, j), (a, k, c, i), (c, b, k, j)
             out.append((R.block(rk), V.block(vk), T.block(tk), R.ext(rk), V.ext(vk), T.ext(tk)))
     return out

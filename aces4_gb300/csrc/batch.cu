@@ -50,8 +50,13 @@ struct a4g_batch {
   OzGemmArgs gemm{};
   int grid = 0;
   cudaGraphExec_t graph = nullptr;
+  // phase timing: events[run][6] recorded by a4g_batch_run_timed
+  std::vector<std::vector<cudaEvent_t>> events;
+  int timed_runs = 0;
 
   ~a4g_batch() {
+    for (auto& ev : events)
+      for (cudaEvent_t e : ev) cudaEventDestroy(e);
     if (graph) cudaGraphExecDestroy(graph);
     for (void* p : allocs) cudaFree(p);
   }
@@ -291,22 +296,43 @@ int build_ozaki(a4g_batch* b, const std::vector<DGroup>& groups, const std::vect
   return A4G_OK;
 }
 
-int run(a4g_batch* b, cudaStream_t s) {
+// ev (optional) receives 6 events: before phase 0 and after each of phases 0..4.
+int run(a4g_batch* b, cudaStream_t s, const cudaEvent_t* ev = nullptr) {
   int rc = A4G_OK;
+  auto mark = [&](int i) -> int {
+    if (ev) A4G_CUDA(cudaEventRecord(ev[i], s));
+    return A4G_OK;
+  };
+  if ((rc = mark(0))) return rc;
   if (b->beta == 0)
     for (auto& z : b->zero_blocks)
       if ((rc = launch_fill(z.first, z.second, 0.0, s))) return rc;
-  if (b->precision == A4G_PREC_FP64)
-    return launch_grouped_f64(b->d_f64_tiles, b->n_f64_tiles, b->d_f64_pairs, b->d_plans, b->beta, s);
-  if (b->n_tiles == 0) return A4G_OK;
-  A4G_CUDA(cudaMemsetAsync(b->d_exps, 0, b->exps_bytes, s));
-  if ((rc = oz_launch_exp(b->d_jobs_a, b->d_prefix_a, b->njobs_a, b->jtiles_a, b->d_pa, s))) return rc;
-  if ((rc = oz_launch_exp(b->d_jobs_b, b->d_prefix_b, b->njobs_b, b->jtiles_b, b->d_pb, s))) return rc;
-  if ((rc = oz_launch_split(b->d_jobs_a, b->d_prefix_a, b->njobs_a, b->jtiles_a, b->d_pa, b->slices, s))) return rc;
-  if ((rc = oz_launch_split(b->d_jobs_b, b->d_prefix_b, b->njobs_b, b->jtiles_b, b->d_pb, b->slices, s))) return rc;
-  if ((rc = oz_launch_gemm(b->gemm, b->grid, s))) return rc;
-  return oz_launch_recombine(b->d_tiles, b->n_tiles, b->d_dblocks, b->d_plans, b->d_pa, b->d_pb, b->d_ws,
-                             b->slices, b->beta, s);
+  if ((rc = mark(1))) return rc;
+  if (b->precision == A4G_PREC_FP64) {
+    if ((rc = mark(2)) || (rc = mark(3))) return rc;
+    rc = launch_grouped_f64(b->d_f64_tiles, b->n_f64_tiles, b->d_f64_pairs, b->d_plans, b->beta, s);
+    if (rc) return rc;
+    if ((rc = mark(4)) || (rc = mark(5))) return rc;
+    return A4G_OK;
+  }
+  if (b->n_tiles > 0) {
+    A4G_CUDA(cudaMemsetAsync(b->d_exps, 0, b->exps_bytes, s));
+    if ((rc = oz_launch_exp(b->d_jobs_a, b->d_prefix_a, b->njobs_a, b->jtiles_a, b->d_pa, s))) return rc;
+    if ((rc = oz_launch_exp(b->d_jobs_b, b->d_prefix_b, b->njobs_b, b->jtiles_b, b->d_pb, s))) return rc;
+  }
+  if ((rc = mark(2))) return rc;
+  if (b->n_tiles > 0) {
+    if ((rc = oz_launch_split(b->d_jobs_a, b->d_prefix_a, b->njobs_a, b->jtiles_a, b->d_pa, b->slices, s))) return rc;
+    if ((rc = oz_launch_split(b->d_jobs_b, b->d_prefix_b, b->njobs_b, b->jtiles_b, b->d_pb, b->slices, s))) return rc;
+  }
+  if ((rc = mark(3))) return rc;
+  if (b->n_tiles > 0 && (rc = oz_launch_gemm(b->gemm, b->grid, s))) return rc;
+  if ((rc = mark(4))) return rc;
+  if (b->n_tiles > 0 &&
+      (rc = oz_launch_recombine(b->d_tiles, b->n_tiles, b->d_dblocks, b->d_plans, b->d_pa, b->d_pb, b->d_ws,
+                                b->slices, b->beta, s)))
+    return rc;
+  return mark(5);
 }
 
 }  // namespace
@@ -407,6 +433,33 @@ int a4g_batch_run_graph(a4g_batch* b, void* stream) {
     if (e != cudaSuccess) return cuda_fail(e, "cudaGraphInstantiate");
   }
   A4G_CUDA(cudaGraphLaunch(b->graph, s));
+  return A4G_OK;
+}
+
+int a4g_batch_run_timed(a4g_batch* b, void* stream) {
+  if (!b) return fail(A4G_ERR_ARG, "null batch");
+  if (int(b->events.size()) <= b->timed_runs) {
+    std::vector<cudaEvent_t> ev(6);
+    for (auto& e : ev) A4G_CUDA(cudaEventCreate(&e));
+    b->events.push_back(ev);
+  }
+  const int rc = run(b, pick(stream), b->events[b->timed_runs].data());
+  if (!rc) ++b->timed_runs;
+  return rc;
+}
+
+int a4g_batch_timings(a4g_batch* b, float* phase_ms, int nphase, int* runs) {
+  if (!b || !phase_ms || nphase < 0) return fail(A4G_ERR_ARG, "bad timing query");
+  for (int p = 0; p < nphase; ++p) phase_ms[p] = 0.f;
+  if (runs) *runs = b->timed_runs;
+  if (b->timed_runs > 0) A4G_CUDA(cudaEventSynchronize(b->events[b->timed_runs - 1][5]));
+  for (int r = 0; r < b->timed_runs; ++r)
+    for (int p = 0; p < std::min(nphase, 5); ++p) {
+      float ms = 0.f;
+      A4G_CUDA(cudaEventElapsedTime(&ms, b->events[r][p], b->events[r][p + 1]));
+      phase_ms[p] += ms;
+    }
+  b->timed_runs = 0;
   return A4G_OK;
 }
 

@@ -35,11 +35,17 @@ def _iarr(seq):
     return (ctypes.c_int * max(1, len(seq)))(*seq)
 
 
+_LEGACY_DEFAULT_STREAM = 1  # cudaStreamLegacy
+
+
 def _stream(stream) -> ctypes.c_void_p:
+    """None -> the library's own stream; a torch stream object -> that stream
+    (torch's default stream, handle 0, is passed as cudaStreamLegacy so work
+    is ordered with torch's default-stream kernels and events)."""
     if stream is None:
         return ctypes.c_void_p(0)
     if hasattr(stream, "cuda_stream"):
-        return ctypes.c_void_p(stream.cuda_stream)
+        return ctypes.c_void_p(stream.cuda_stream or _LEGACY_DEFAULT_STREAM)
     return ctypes.c_void_p(int(stream))
 
 
@@ -192,6 +198,18 @@ class Batch:
 
     def run_graph(self, stream=None):
         _check(lib().a4g_batch_run_graph(self._h, _stream(stream)), "a4g_batch_run_graph")
+
+    def run_timed(self, stream=None):
+        _check(lib().a4g_batch_run_timed(self._h, _stream(stream)), "a4g_batch_run_timed")
+
+    PHASES = ("zero_fill", "exponents", "split", "gemm", "recombine")
+
+    def timings(self):
+        """Summed ms per phase over the timed runs since the last call."""
+        arr = (ctypes.c_float * 5)()
+        runs = ctypes.c_int(0)
+        _check(lib().a4g_batch_timings(self._h, arr, 5, ctypes.byref(runs)), "a4g_batch_timings")
+        return {"runs": runs.value, **{k: float(arr[i]) for i, k in enumerate(self.PHASES)}}
 
     def info(self):
         pairs, flops, ws = ctypes.c_int64(0), ctypes.c_double(0), ctypes.c_int64(0)

@@ -1,0 +1,382 @@
+"""Benchmark of the ACES4 block-contraction hot path on GB300.
+
+Workload (one "step"): the particle-particle ladder contraction
+    R(a,b,i,j) += sum_{c,d} V(a,b,c,d) T(c,d,i,j)
+at o=64 (4 occupied segments of 16) and v=512 (16 virtual segments of 32),
+for one (a,b) slab: 256 V blocks (32^4), all 4096 T blocks (32*32*16*16),
+16 R blocks -> 4096 block pairs of 1024 x 256 x 1024, 2.2e12 FP64 flops.
+V ~ U[-1,1]/512, T ~ N(0, 1e-2) with 1% of its entries scaled by 1e3
+(seeded, generated on the device; synthetic data).  Inputs are 10.7 GB,
+larger than L2, so no cache flush is needed between steps.
+
+Arms:
+  default           the batched split-precision contraction (BF16 slices on
+                    the tcgen05 tensor cores, FP64 recombination): `value`
+                    is FP64-equivalent TFLOP/s with inputs resident in HBM;
+                    `e2e` is the same through the public API with the inputs
+                    copied from pinned host memory and R copied back per step.
+  --impl reference  the reference's CPU algorithm (permute into temporaries
+                    + BLAS dgemm('T','N'), restated in the oracle) on the host
+                    cores, on a bounded sample of the same block pairs.
+
+Multi-GPU: replicas only (each rank contracts its own (a,b) slab; weak scaling).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+O_SEGS = [16] * 4
+V_SEGS = [32] * 16
+METRIC = "FP64-equiv TFLOP/s per contraction (batched split vs plain FP64, <=1e-10 rel err)"
+WORKLOAD = ("ladder R(a,b,i,j)+=V(a,b,c,d)T(c,d,i,j), o=64 (4x16), v=512 (16x32), one (a,b) slab: "
+            "4096 block pairs of 1024x256x1024 (2.2e12 flop)")
+
+
+def _peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return json.load(f), "measured"
+    except Exception:
+        return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "bf16_tflops_sustained": 1700.0}, "fallback"
+
+
+def _traffic(kernel: str):
+    try:
+        with open(os.path.join(ROOT, "profiles", "traffic_per_launch.json")) as f:
+            return json.load(f).get(kernel)
+    except Exception:
+        return None
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle sampling during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            p = [x.strip() for x in ln.split(",")]
+            if len(p) < 9:
+                continue
+            try:
+                sm.append(float(p[1]))
+                mx = float(p[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, p[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def make_workload(torch, a4, slab: int, seed: int):
+    from aces4_gb300.blocks import BlockArray, ladder_triples
+
+    a0, b0 = slab % 16, (slab // 16) % 16
+    V = BlockArray([[V_SEGS[a0]], [V_SEGS[b0]], V_SEGS, V_SEGS])
+    T = BlockArray([V_SEGS, V_SEGS, O_SEGS, O_SEGS])
+    R = BlockArray([[V_SEGS[a0]], [V_SEGS[b0]], O_SEGS, O_SEGS])
+    g = torch.Generator(device="cuda")
+    g.manual_seed(seed + slab)
+    V.buf.uniform_(-1.0, 1.0, generator=g).div_(512.0)
+    step = 1 << 27
+    for s in range(0, T.buf.numel(), step):
+        t = T.buf[s:s + step]
+        t.normal_(0.0, 0.1, generator=g)
+        m = torch.rand(t.shape, device="cuda", generator=g) < 0.01
+        t[m] *= 1e3
+        del m
+    trip = ladder_triples(R, V, T)
+    return V, T, R, trip
+
+
+def cpu_sample_pairs(V, T, n_pairs: int):
+    """Host copies of the first n_pairs (V, T) block pairs of R(a0,b0,0,0)."""
+    import numpy as np
+
+    out = []
+    for c in range(16):
+        for d in range(16):
+            if len(out) >= n_pairs:
+                return out
+            out.append((V.block((0, 0, c, d)).cpu().numpy().copy(), T.block((c, d, 0, 0)).cpu().numpy().copy()))
+    return out
+
+
+def time_cpu_reference(pairs, ptrn, min_seconds: float = 0.0):
+    """The reference's CPU BLAS path (oracle restatement) over block pairs,
+    summed into one R block like `tmp = V*T; R += tmp`."""
+    import numpy as np
+    from oracle import oracle
+
+    le, re, de = [32, 32, 32, 32], [32, 32, 16, 16], [32, 32, 16, 16]
+    acc = np.zeros(32 * 32 * 16 * 16)
+    n = 0
+    t0 = time.perf_counter()
+    while True:
+        for l, r in pairs:
+            acc += oracle.contract_blas(ptrn, l, le, r, re, de)
+            n += 1
+        if time.perf_counter() - t0 >= min_seconds:
+            break
+    dt = time.perf_counter() - t0
+    flops = n * 2.0 * 1024 * 256 * 1024
+    return flops / dt / 1e12, n, dt, acc
+
+
+def run_reference_arm(args, rank: int):
+    """--impl reference: CPU arm, rank 0 only."""
+    if rank != 0:
+        return
+    import numpy as np
+    from oracle import oracle
+
+    oracle.build()
+    _, ptrn = oracle.get_contraction_ptrn(4, 4, 4, [1, 2, 3, 4, 1, 2, 5, 6, 5, 6, 3, 4])
+    rng = np.random.default_rng(11)
+    n_pairs = args.cpu_pairs
+    pairs = [(rng.uniform(-1, 1, 32 ** 4) / 512.0, rng.normal(0, 0.1, 32 * 32 * 16 * 16)) for _ in range(n_pairs)]
+    for _ in range(args.warmup):
+        time_cpu_reference(pairs[:1], ptrn)
+    vals = []
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        v, n, dt, _ = time_cpu_reference(pairs, ptrn)
+        vals.append(dt)
+    total = time.perf_counter() - t0
+    step_s = total / args.steps
+    flops = n_pairs * 2.0 * 1024 * 256 * 1024
+    value = flops / step_s / 1e12
+    cores = os.cpu_count()
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": "TFLOP/s", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": step_s * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "sample": f"{n_pairs} block pairs per step"},
+        "cpu_baseline": {"value": value, "unit": "TFLOP/s", "cores": cores, "kind": "port",
+                         "sample": f"{n_pairs} of the 4096 block pairs (1024x256x1024) per step; oracle permute "
+                                   f"(OpenMP) + numpy OpenBLAS dgemm, all {cores} host threads"},
+        "e2e": {"value": value, "unit": "TFLOP/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--slices", type=int, default=6)
+    ap.add_argument("--fp64-steps", type=int, default=1)
+    ap.add_argument("--e2e-steps", type=int, default=3)
+    ap.add_argument("--cpu-pairs", type=int, default=16)
+    ap.add_argument("--cpu-seconds", type=float, default=10.0)
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if args.impl == "reference":
+        run_reference_arm(args, rank)
+        return
+
+    import numpy as np
+    import torch
+    import torch.distributed as dist
+
+    import aces4_gb300 as a4
+    from oracle import oracle
+
+    torch.cuda.set_device(local)
+    if world > 1:
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    a4.device.init(local)
+    stream = torch.cuda.current_stream()
+    peaks, peak_kind = _peaks()
+
+    V, T, R, trip = make_workload(torch, a4, slab=rank, seed=1234)
+    _, ptrn = oracle.get_contraction_ptrn(4, 4, 4, [1, 2, 3, 4, 1, 2, 5, 6, 5, 6, 3, 4])
+    split = a4.device.Batch(ptrn, 4, 4, 4, trip, precision=a4.device.PREC_OZAKI_BF16, slices=args.slices)
+    info = split.info()
+    flops = info["flops"]
+    S = args.slices
+
+    def barrier():
+        if world > 1:
+            dist.barrier()
+
+    for _ in range(args.warmup):
+        split.run(stream)
+    torch.cuda.synchronize()
+    split.timings()  # discard
+
+    barrier()
+    torch.cuda.synchronize()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    props = torch.cuda.get_device_properties(local)
+    gpu_id = f"GPU-{props.uuid}" if getattr(props, "uuid", None) else str(local)
+    with ClockSampler(gpu_id) as clk:
+        ev0.record(stream)
+        for _ in range(args.steps):
+            split.run_timed(stream)
+        ev1.record(stream)
+        torch.cuda.synchronize()
+    barrier()
+    ms = ev0.elapsed_time(ev1) / args.steps
+    if world > 1:
+        t = torch.tensor([ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    phases = split.timings()
+    value = world * flops / (ms * 1e-3) / 1e12
+    R_split = R.buf.clone()
+
+    # plain FP64 form of the same step (the denominator of the split target)
+    fp64 = a4.device.Batch(ptrn, 4, 4, 4, trip, precision=a4.device.PREC_FP64)
+    fp64.run(stream)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.fp64_steps):
+        fp64.run(stream)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    fp64_ms = e0.elapsed_time(e1) / args.fp64_steps
+    fp64_value = flops / (fp64_ms * 1e-3) / 1e12
+    R_fp64 = R.buf.clone()
+    blk_err = []
+    for k in R.keys():
+        o, n = R.offsets[k], R.size(k)
+        a, b = R_split[o:o + n], R_fp64[o:o + n]
+        blk_err.append(float(torch.linalg.norm(a - b) / torch.linalg.norm(b)))
+    fp64.close()
+
+    # e2e: the same step through the public API from pinned host memory
+    Vh = torch.empty_like(V.buf, device="cpu").pin_memory()
+    Th = torch.empty_like(T.buf, device="cpu").pin_memory()
+    Rh = torch.empty_like(R.buf, device="cpu").pin_memory()
+    Vh.copy_(V.buf)
+    Th.copy_(T.buf)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    for _ in range(args.e2e_steps):
+        V.buf.copy_(Vh, non_blocking=True)
+        T.buf.copy_(Th, non_blocking=True)
+        split.run(stream)
+        Rh.copy_(R.buf, non_blocking=True)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    e2e_ms = e0.elapsed_time(e1) / args.e2e_steps
+    e2e_value = world * flops / (e2e_ms * 1e-3) / 1e12
+    h2d = (V.buf.numel() + T.buf.numel()) * 8
+    d2h = R.buf.numel() * 8
+    del Vh, Th
+
+    out = None
+    if rank == 0:
+        # FP64 CPU oracle check of one R block (all 256 pairs) and the CPU baseline
+        cpu = None
+        err_oracle = None
+        if not args.no_cpu:
+            oracle.build()
+            pairs = cpu_sample_pairs(V, T, 256)
+            _, n_done, dt, acc = time_cpu_reference(pairs, ptrn)
+            o, n = R.offsets[(0, 0, 0, 0)], R.size((0, 0, 0, 0))
+            got = R_split[o:o + n].cpu().numpy()
+            err_oracle = float(np.linalg.norm(got - acc) / np.linalg.norm(acc))
+            v_cpu, n_s, dt_s, _ = time_cpu_reference(pairs[: args.cpu_pairs], ptrn, min_seconds=args.cpu_seconds)
+            cores = os.cpu_count()
+            cpu = {"value": v_cpu, "unit": "TFLOP/s", "cores": cores, "kind": "port",
+                   "sample": f"{n_s} block pairs (1024x256x1024) of the same slab in {dt_s:.1f} s; oracle permute "
+                             f"(OpenMP) + numpy OpenBLAS dgemm, all {cores} host threads"}
+        runs = max(1, phases["runs"])
+        gemm_ms = phases["gemm"] / runs
+        bf16_flops = S * (S + 1) / 2 * flops
+        achieved = bf16_flops / (gemm_ms * 1e-3) / 1e12
+        peak = peaks.get("bf16_tflops_sustained", 1743.3)
+        n_elem = V.buf.numel() + T.buf.numel()
+        split_bytes = n_elem * (8 + 2 * S)
+        exp_bytes = n_elem * 8
+        ck = clk.summary()
+        out = {
+            "metric": METRIC, "value": value, "unit": "TFLOP/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "bf16", "data": "synthetic",
+            "config": {"workload": WORKLOAD, "slices": S, "digit_bits": 7, "block_pairs": info["pairs"],
+                       "l2": "inputs 10.7 GB > 126 MB L2 (no flush needed)", "parallelism": f"replicas x{world}"},
+            "e2e": {"value": e2e_value, "unit": "TFLOP/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                    "ms_per_step": e2e_ms},
+            "roofline": {"kernel": "oz_gemm_kernel (tcgen05 BF16 slice products)", "bound": "tensor",
+                         "achieved": achieved, "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak,
+                         "peak_kind": f"bf16_tflops_sustained of {peak_kind}",
+                         "algorithmic_per_launch": f"{S * (S + 1) // 2} slice-pair GEMMs x {flops:.3e} flop",
+                         "traffic": _traffic("oz_gemm_kernel")},
+            "fp64_plain": {"value": fp64_value, "unit": "TFLOP/s", "ms_per_step": fp64_ms,
+                           "kernel": "grouped DMMA (mma.sync f64)"},
+            "split_over_fp64": value / world / fp64_value,
+            "rel_err_max_block_vs_fp64_gpu": max(blk_err),
+            "rel_err_block_vs_cpu_oracle": err_oracle,
+            "phases_ms_per_step": {k: phases[k] / runs for k in ("exponents", "split", "gemm", "recombine")},
+            "hbm_phases": {
+                "exponents_gbs": exp_bytes / (phases["exponents"] / runs * 1e-3) / 1e9,
+                "split_gbs": split_bytes / (phases["split"] / runs * 1e-3) / 1e9,
+                "hbm_peak_gbs": peaks.get("hbm_gbs")},
+            "gpu_launches": 6 * args.steps,
+            "cpu_baseline": cpu,
+            "clocks": ck,
+        }
+        print(json.dumps(out), flush=True)
+    split.close()
+    if world > 1:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

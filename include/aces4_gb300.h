@@ -208,6 +208,13 @@ int a4g_batch_create(a4g_batch** out, const int* contr_ptrn, int drank, int lran
 int a4g_batch_run(a4g_batch* b, void* stream);
 /* Capture a4g_batch_run into a CUDA graph once; later runs replay it. */
 int a4g_batch_run_graph(a4g_batch* b, void* stream);
+/* Same as a4g_batch_run, with CUDA events recorded on `stream` between the
+ * pipeline phases; a4g_batch_timings returns the summed milliseconds per phase
+ * over every timed run since the previous call (it synchronises).  Phases:
+ * 0 zero fill, 1 exponents, 2 split, 3 tensor-core GEMM (or the FP64 grouped
+ * kernel), 4 recombine. */
+int a4g_batch_run_timed(a4g_batch* b, void* stream);
+int a4g_batch_timings(a4g_batch* b, float* phase_ms, int nphase, int* runs);
 /* Number of block pairs executed (zero blocks skipped) and FP64 flops. */
 int a4g_batch_info(const a4g_batch* b, int64_t* pairs, double* flops, int64_t* workspace_bytes);
 void a4g_batch_destroy(a4g_batch* b);
