@@ -35,11 +35,21 @@ import time
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
-O_SEGS = [16] * 4
-V_SEGS = [32] * 16
+O_SEG, V_SEG = 16, 32
+O_SEGS = [O_SEG] * 4
+V_SEGS = [V_SEG] * 16
 METRIC = "FP64-equiv TFLOP/s per contraction (batched split vs plain FP64, <=1e-10 rel err)"
-WORKLOAD = ("ladder R(a,b,i,j)+=V(a,b,c,d)T(c,d,i,j), o=64 (4x16), v=512 (16x32), one (a,b) slab: "
-            "4096 block pairs of 1024x256x1024 (2.2e12 flop)")
+
+
+def workload_name(nv: int, no: int) -> str:
+    v, o = V_SEG * nv, O_SEG * no
+    pairs = nv * nv * no * no
+    flop = 2.0 * V_SEG ** 2 * (O_SEG * no) ** 2 * v * v
+    return (f"ladder R(a,b,i,j)+=V(a,b,c,d)T(c,d,i,j), o={o} ({no}x{O_SEG}), v={v} ({nv}x{V_SEG}), "
+            f"one (a,b) slab: {pairs} block pairs of 1024x256x1024 ({flop:.3g} flop)")
+
+
+WORKLOAD = workload_name(16, 4)
 
 
 def _peaks():
@@ -114,13 +124,13 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
-def make_workload(torch, a4, slab: int, seed: int):
+def make_workload(torch, a4, slab: int, seed: int, nv: int = 16, no: int = 4):
     from aces4_gb300.blocks import BlockArray, ladder_triples
 
-    a0, b0 = slab % 16, (slab // 16) % 16
-    V = BlockArray([[V_SEGS[a0]], [V_SEGS[b0]], V_SEGS, V_SEGS])
-    T = BlockArray([V_SEGS, V_SEGS, O_SEGS, O_SEGS])
-    R = BlockArray([[V_SEGS[a0]], [V_SEGS[b0]], O_SEGS, O_SEGS])
+    vs, os_ = [V_SEG] * nv, [O_SEG] * no
+    V = BlockArray([[V_SEG], [V_SEG], vs, vs])
+    T = BlockArray([vs, vs, os_, os_])
+    R = BlockArray([[V_SEG], [V_SEG], os_, os_])
     g = torch.Generator(device="cuda")
     g.manual_seed(seed + slab)
     V.buf.uniform_(-1.0, 1.0, generator=g).div_(512.0)
@@ -218,6 +228,8 @@ def main():
     ap.add_argument("--cpu-pairs", type=int, default=16)
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--nvseg", type=int, default=16, help="virtual segments of 32 (16: v=512)")
+    ap.add_argument("--noseg", type=int, default=4, help="occupied segments of 16 (4: o=64)")
     args = ap.parse_args()
 
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -241,7 +253,8 @@ def main():
     stream = torch.cuda.current_stream()
     peaks, peak_kind = _peaks()
 
-    V, T, R, trip = make_workload(torch, a4, slab=rank, seed=1234)
+    V, T, R, trip = make_workload(torch, a4, slab=rank, seed=1234, nv=args.nvseg, no=args.noseg)
+    workload = workload_name(args.nvseg, args.noseg)
     _, ptrn = oracle.get_contraction_ptrn(4, 4, 4, [1, 2, 3, 4, 1, 2, 5, 6, 5, 6, 3, 4])
     split = a4.device.Batch(ptrn, 4, 4, 4, trip, precision=a4.device.PREC_OZAKI_BF16, slices=args.slices)
     info = split.info()
@@ -278,53 +291,57 @@ def main():
     value = world * flops / (ms * 1e-3) / 1e12
     R_split = R.buf.clone()
 
-    # plain FP64 form of the same step (the denominator of the split target)
-    fp64 = a4.device.Batch(ptrn, 4, 4, 4, trip, precision=a4.device.PREC_FP64)
-    fp64.run(stream)
-    torch.cuda.synchronize()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    e0.record(stream)
-    for _ in range(args.fp64_steps):
-        fp64.run(stream)
-    e1.record(stream)
-    torch.cuda.synchronize()
-    fp64_ms = e0.elapsed_time(e1) / args.fp64_steps
-    fp64_value = flops / (fp64_ms * 1e-3) / 1e12
-    R_fp64 = R.buf.clone()
+    fp64_value = fp64_ms = None
     blk_err = []
-    for k in R.keys():
-        o, n = R.offsets[k], R.size(k)
-        a, b = R_split[o:o + n], R_fp64[o:o + n]
-        blk_err.append(float(torch.linalg.norm(a - b) / torch.linalg.norm(b)))
-    fp64.close()
+    if args.fp64_steps > 0:
+        # plain FP64 form of the same step (the denominator of the split target)
+        fp64 = a4.device.Batch(ptrn, 4, 4, 4, trip, precision=a4.device.PREC_FP64)
+        fp64.run(stream)
+        torch.cuda.synchronize()
+        e0.record(stream)
+        for _ in range(args.fp64_steps):
+            fp64.run(stream)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        fp64_ms = e0.elapsed_time(e1) / args.fp64_steps
+        fp64_value = flops / (fp64_ms * 1e-3) / 1e12
+        R_fp64 = R.buf.clone()
+        for k in R.keys():
+            o, n = R.offsets[k], R.size(k)
+            a, b = R_split[o:o + n], R_fp64[o:o + n]
+            blk_err.append(float(torch.linalg.norm(a - b) / torch.linalg.norm(b)))
+        fp64.close()
 
     # e2e: the same step through the public API from pinned host memory
-    Vh = torch.empty_like(V.buf, device="cpu").pin_memory()
-    Th = torch.empty_like(T.buf, device="cpu").pin_memory()
-    Rh = torch.empty_like(R.buf, device="cpu").pin_memory()
-    Vh.copy_(V.buf)
-    Th.copy_(T.buf)
-    torch.cuda.synchronize()
-    e0.record(stream)
-    for _ in range(args.e2e_steps):
-        V.buf.copy_(Vh, non_blocking=True)
-        T.buf.copy_(Th, non_blocking=True)
-        split.run(stream)
-        Rh.copy_(R.buf, non_blocking=True)
-    e1.record(stream)
-    torch.cuda.synchronize()
-    e2e_ms = e0.elapsed_time(e1) / args.e2e_steps
-    e2e_value = world * flops / (e2e_ms * 1e-3) / 1e12
-    h2d = (V.buf.numel() + T.buf.numel()) * 8
-    d2h = R.buf.numel() * 8
-    del Vh, Th
+    e2e = None
+    if args.e2e_steps > 0:
+        Vh = torch.empty_like(V.buf, device="cpu").pin_memory()
+        Th = torch.empty_like(T.buf, device="cpu").pin_memory()
+        Rh = torch.empty_like(R.buf, device="cpu").pin_memory()
+        Vh.copy_(V.buf)
+        Th.copy_(T.buf)
+        torch.cuda.synchronize()
+        e0.record(stream)
+        for _ in range(args.e2e_steps):
+            V.buf.copy_(Vh, non_blocking=True)
+            T.buf.copy_(Th, non_blocking=True)
+            split.run(stream)
+            Rh.copy_(R.buf, non_blocking=True)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        e2e_ms = e0.elapsed_time(e1) / args.e2e_steps
+        e2e = {"value": world * flops / (e2e_ms * 1e-3) / 1e12, "unit": "TFLOP/s",
+               "h2d_bytes_per_step": (V.buf.numel() + T.buf.numel()) * 8,
+               "d2h_bytes_per_step": R.buf.numel() * 8, "ms_per_step": e2e_ms}
+        del Vh, Th
 
     out = None
     if rank == 0:
         # FP64 CPU oracle check of one R block (all 256 pairs) and the CPU baseline
         cpu = None
         err_oracle = None
-        if not args.no_cpu:
+        if not args.no_cpu and (args.nvseg, args.noseg) == (16, 4):
             oracle.build()
             pairs = cpu_sample_pairs(V, T, 256)
             _, n_done, dt, acc = time_cpu_reference(pairs, ptrn)
@@ -341,7 +358,7 @@ def main():
         bf16_flops = S * (S + 1) / 2 * flops
         achieved = bf16_flops / (gemm_ms * 1e-3) / 1e12
         peak = peaks.get("bf16_tflops_sustained", 1743.3)
-        n_elem = V.buf.numel() + T.buf.numel()
+        n_elem = sum(V.size(k) for k in V.keys()) + sum(T.size(k) for k in T.keys())
         split_bytes = n_elem * (8 + 2 * S)
         exp_bytes = n_elem * 8
         ck = clk.summary()
@@ -349,19 +366,18 @@ def main():
             "metric": METRIC, "value": value, "unit": "TFLOP/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "bf16", "data": "synthetic",
-            "config": {"workload": WORKLOAD, "slices": S, "digit_bits": 7, "block_pairs": info["pairs"],
+            "config": {"workload": workload, "slices": S, "digit_bits": 7, "block_pairs": info["pairs"],
                        "l2": "inputs 10.7 GB > 126 MB L2 (no flush needed)", "parallelism": f"replicas x{world}"},
-            "e2e": {"value": e2e_value, "unit": "TFLOP/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
-                    "ms_per_step": e2e_ms},
+            "e2e": e2e,
             "roofline": {"kernel": "oz_gemm_kernel (tcgen05 BF16 slice products)", "bound": "tensor",
                          "achieved": achieved, "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak,
                          "peak_kind": f"bf16_tflops_sustained of {peak_kind}",
                          "algorithmic_per_launch": f"{S * (S + 1) // 2} slice-pair GEMMs x {flops:.3e} flop",
                          "traffic": _traffic("oz_gemm_kernel")},
-            "fp64_plain": {"value": fp64_value, "unit": "TFLOP/s", "ms_per_step": fp64_ms,
-                           "kernel": "grouped DMMA (mma.sync f64)"},
-            "split_over_fp64": value / world / fp64_value,
-            "rel_err_max_block_vs_fp64_gpu": max(blk_err),
+            "fp64_plain": ({"value": fp64_value, "unit": "TFLOP/s", "ms_per_step": fp64_ms,
+                            "kernel": "grouped DMMA (mma.sync f64)"} if fp64_value else None),
+            "split_over_fp64": (value / world / fp64_value) if fp64_value else None,
+            "rel_err_max_block_vs_fp64_gpu": max(blk_err) if blk_err else None,
             "rel_err_block_vs_cpu_oracle": err_oracle,
             "phases_ms_per_step": {k: phases[k] / runs for k in ("exponents", "split", "gemm", "recombine")},
             "hbm_phases": {
