@@ -39,16 +39,25 @@ struct a4g_batch {
   OzPanel* d_pb = nullptr;
   int* d_exps = nullptr;
   size_t exps_bytes = 0;
-  OzSplitJob *d_jobs_a = nullptr, *d_jobs_b = nullptr;
-  int64_t *d_prefix_a = nullptr, *d_prefix_b = nullptr;
-  int njobs_a = 0, njobs_b = 0;
-  int64_t jtiles_a = 0, jtiles_b = 0;
+  // split jobs grouped by operand side (A: left blocks, B: right blocks) and
+  // source layout; each set has its own CTA prefix sums for both passes
+  struct JobSet {
+    bool left;
+    int layout;
+    OzSplitJob* d_jobs = nullptr;
+    int64_t* d_prefix_exp = nullptr;
+    int64_t* d_prefix_split = nullptr;
+    int njobs = 0;
+    int64_t tiles_exp = 0, tiles_split = 0;
+  };
+  std::vector<JobSet> jobsets;
   OzTile* d_tiles = nullptr;
   int n_tiles = 0;
   OzDBlock* d_dblocks = nullptr;
   float2* d_ws = nullptr;
   OzGemmArgs gemm{};
   int grid = 0;
+  int nsplit = 1;
   cudaGraphExec_t graph = nullptr;
   // phase timing: events[run][6] recorded by a4g_batch_run_timed
   std::vector<std::vector<cudaEvent_t>> events;
@@ -237,11 +246,22 @@ int build_ozaki(a4g_batch* b, const std::vector<DGroup>& groups, const std::vect
   for (auto& p : hpb)
     if (p.kpad > 0x7fffffffLL || int64_t(S) * p.rows_pad > 0x7fffffffLL)
       return fail(A4G_ERR_RANGE, "panel exceeds TMA coordinate range");
-  // split jobs (one per block per panel) and their 64x64 tile prefix sums
-  auto jobs_of = [&](std::vector<PanelBuild>& src, bool left, std::vector<OzSplitJob>& jobs,
-                     std::vector<int64_t>& prefix) {
-    prefix.assign(1, 0);
-    for (size_t pi = 0; pi < src.size(); ++pi) {
+  // split jobs (one per block per panel), grouped by side and source layout
+  auto layout_of = [](const DevPlan* dp, bool left) {
+    const GemmPlan& h = dp->host;
+    const std::vector<int64_t>& orow = left ? h.offLm : h.offRn;
+    const std::vector<int64_t>& ok = left ? h.offLk : h.offRk;
+    const int64_t rows = int64_t(orow.size()), K = int64_t(ok.size());
+    bool rm = true, km = true;
+    for (int64_t r = 0; r < rows && (rm || km); ++r) rm &= orow[r] == r, km &= orow[r] == r * K;
+    for (int64_t k = 0; k < K && (rm || km); ++k) rm &= ok[k] == k * rows, km &= ok[k] == k;
+    return rm ? int(kOzRowsMajor) : km ? int(kOzKMajor) : int(kOzGeneric);
+  };
+  for (int side = 0; side < 2; ++side) {
+    const bool left = side == 0;
+    std::vector<PanelBuild>& src = left ? pa : pb;
+    std::vector<OzSplitJob> jobs[3];
+    for (size_t pi = 0; pi < src.size(); ++pi)
       for (auto& kv : src[pi].koff) {
         const DevPlan* dp = plans[src[pi].plan.at(kv.first)];
         OzSplitJob j{};
@@ -253,17 +273,29 @@ int build_ozaki(a4g_batch* b, const std::vector<DGroup>& groups, const std::vect
         j.kfast = left ? dp->host.a_kfast : dp->host.b_kfast;
         j.panel = int(pi);
         j.koff = kv.second;
-        jobs.push_back(j);
-        prefix.push_back(prefix.back() + ceil_to(j.rows, 64) / 64 * (ceil_to(j.K, 64) / 64));
+        int lay = layout_of(dp, left);
+        if ((reinterpret_cast<uintptr_t>(kv.first) & 15) != 0) lay = kOzGeneric;  // vector loads need 16 B
+        jobs[lay].push_back(j);
       }
+    for (int lay = 0; lay < 3; ++lay) {
+      if (jobs[lay].empty()) continue;
+      a4g_batch::JobSet js;
+      js.left = left;
+      js.layout = lay;
+      std::vector<int64_t> pe(1, 0), ps(1, 0);
+      for (const OzSplitJob& j : jobs[lay]) {
+        pe.push_back(pe.back() + oz_exp_tiles(lay, j.rows, j.K));
+        ps.push_back(ps.back() + oz_split_tiles(lay, j.rows, j.K));
+      }
+      js.njobs = int(jobs[lay].size());
+      js.tiles_exp = pe.back();
+      js.tiles_split = ps.back();
+      if ((rc = upload(b, jobs[lay], &js.d_jobs)) || (rc = upload(b, pe, &js.d_prefix_exp)) ||
+          (rc = upload(b, ps, &js.d_prefix_split)))
+        return rc;
+      b->jobsets.push_back(js);
     }
-  };
-  std::vector<OzSplitJob> ja, jb;
-  std::vector<int64_t> xa, xb;
-  jobs_of(pa, true, ja, xa);
-  jobs_of(pb, false, jb, xb);
-  b->njobs_a = int(ja.size()), b->njobs_b = int(jb.size());
-  b->jtiles_a = xa.back(), b->jtiles_b = xb.back();
+  }
   void *dmaps_a = nullptr, *dmaps_b = nullptr;
   const size_t mbytes_a = maps_a.size() * sizeof(MapBytes), mbytes_b = maps_b.size() * sizeof(MapBytes);
   if ((rc = device_alloc(b, mbytes_a, &dmaps_a, false))) return rc;
@@ -271,22 +303,57 @@ int build_ozaki(a4g_batch* b, const std::vector<DGroup>& groups, const std::vect
   A4G_CUDA(cudaMemcpy(dmaps_a, maps_a.data(), mbytes_a, cudaMemcpyHostToDevice));
   A4G_CUDA(cudaMemcpy(dmaps_b, maps_b.data(), mbytes_b, cudaMemcpyHostToDevice));
   OzTrip* d_trips = nullptr;
-  if ((rc = upload(b, hpa, &b->d_pa)) || (rc = upload(b, hpb, &b->d_pb)) || (rc = upload(b, ja, &b->d_jobs_a)) ||
-      (rc = upload(b, jb, &b->d_jobs_b)) || (rc = upload(b, xa, &b->d_prefix_a)) ||
-      (rc = upload(b, xb, &b->d_prefix_b)) || (rc = upload(b, tiles, &b->d_tiles)) ||
+  if ((rc = upload(b, hpa, &b->d_pa)) || (rc = upload(b, hpb, &b->d_pb)) || (rc = upload(b, tiles, &b->d_tiles)) ||
       (rc = upload(b, trips, &d_trips)) || (rc = upload(b, dblocks, &b->d_dblocks)))
     return rc;
   b->n_tiles = int(tiles.size());
+  // Split-K: the smallest split count that gives every SM the same number of
+  // equal units per level (so the CTAs stay in step through the k panels),
+  // keeping at least 16 k blocks per unit and the workspace below 6 GB.
+  const int P = ctx()->num_sms;
+  int min_kb = 1 << 30;
+  for (const OzTile& t : tiles) min_kb = std::min(min_kb, t.kb_total);
+  int nsplit = 1;
+  double best = -1.0;
+  for (int ns = 1; ns <= 64; ++ns) {
+    if (ns > 1 && min_kb / ns < 16) break;
+    if (double(b->n_tiles) * S * ns * kOzBM * kOzBN * sizeof(float2) > 6.0 * (1u << 30)) break;
+    const int64_t units = int64_t(b->n_tiles) * ns;
+    const double eff = double(units) / double(P * ((units + P - 1) / P));
+    if (eff > best + 1e-9) best = eff, nsplit = ns;
+    if (eff >= 0.999) break;
+  }
+  b->nsplit = nsplit;
+  std::vector<OzUnit> units;
+  for (int lv = 0; lv < S; ++lv)
+    for (int sp = 0; sp < nsplit; ++sp)
+      for (int ti = 0; ti < b->n_tiles; ++ti) {
+        const OzTile& t = tiles[ti];
+        OzUnit u{};
+        u.tile = ti, u.level = lv, u.split = sp;
+        u.kb_begin = int(int64_t(t.kb_total) * sp / nsplit);
+        u.kb_end = int(int64_t(t.kb_total) * (sp + 1) / nsplit);
+        int acc = 0, q = t.trip_begin;
+        while (q < t.trip_end && acc + trips[q].nkb <= u.kb_begin) acc += trips[q].nkb, ++q;
+        u.trip_first = q;
+        u.kb_in_trip = u.kb_begin - acc;
+        units.push_back(u);
+      }
+  OzUnit* d_units = nullptr;
+  if ((rc = upload(b, units, &d_units))) return rc;
   void* ws = nullptr;
-  if ((rc = device_alloc(b, size_t(b->n_tiles) * S * kOzBM * kOzBN * sizeof(float2), &ws, false))) return rc;
+  if ((rc = device_alloc(b, size_t(b->n_tiles) * S * nsplit * kOzBM * kOzBN * sizeof(float2), &ws, false)))
+    return rc;
   b->d_ws = static_cast<float2*>(ws);
   OzGemmArgs& ga = b->gemm;
   ga.maps_a = dmaps_a, ga.maps_b = dmaps_b;
   ga.panels_a = b->d_pa, ga.panels_b = b->d_pb;
   ga.tiles = b->d_tiles, ga.trips = d_trips;
   ga.n_tiles = b->n_tiles;
-  ga.n_units = b->n_tiles * S;
+  ga.units = d_units;
+  ga.n_units = int(units.size());
   ga.slices = S;
+  ga.nsplit = nsplit;
   for (int t = 0; t < kOzMaxSlices; ++t) ga.chunk_kb[t] = t < S ? oz_chunk_kb(t) : 1;
   for (int t = 0; t < S; ++t)
     if (ga.chunk_kb[t] < 1) return fail(A4G_ERR_ARG, "slice count too large for exact accumulation");
@@ -317,20 +384,24 @@ int run(a4g_batch* b, cudaStream_t s, const cudaEvent_t* ev = nullptr) {
   }
   if (b->n_tiles > 0) {
     A4G_CUDA(cudaMemsetAsync(b->d_exps, 0, b->exps_bytes, s));
-    if ((rc = oz_launch_exp(b->d_jobs_a, b->d_prefix_a, b->njobs_a, b->jtiles_a, b->d_pa, s))) return rc;
-    if ((rc = oz_launch_exp(b->d_jobs_b, b->d_prefix_b, b->njobs_b, b->jtiles_b, b->d_pb, s))) return rc;
+    for (const auto& js : b->jobsets)
+      if ((rc = oz_launch_exp(js.layout, js.d_jobs, js.d_prefix_exp, js.njobs, js.tiles_exp,
+                              js.left ? b->d_pa : b->d_pb, s)))
+        return rc;
   }
   if ((rc = mark(2))) return rc;
   if (b->n_tiles > 0) {
-    if ((rc = oz_launch_split(b->d_jobs_a, b->d_prefix_a, b->njobs_a, b->jtiles_a, b->d_pa, b->slices, s))) return rc;
-    if ((rc = oz_launch_split(b->d_jobs_b, b->d_prefix_b, b->njobs_b, b->jtiles_b, b->d_pb, b->slices, s))) return rc;
+    for (const auto& js : b->jobsets)
+      if ((rc = oz_launch_split(js.layout, js.d_jobs, js.d_prefix_split, js.njobs, js.tiles_split,
+                                js.left ? b->d_pa : b->d_pb, b->slices, s)))
+        return rc;
   }
   if ((rc = mark(3))) return rc;
   if (b->n_tiles > 0 && (rc = oz_launch_gemm(b->gemm, b->grid, s))) return rc;
   if ((rc = mark(4))) return rc;
   if (b->n_tiles > 0 &&
       (rc = oz_launch_recombine(b->d_tiles, b->n_tiles, b->d_dblocks, b->d_plans, b->d_pa, b->d_pb, b->d_ws,
-                                b->slices, b->beta, s)))
+                                b->slices, b->nsplit, b->beta, s)))
     return rc;
   return mark(5);
 }

@@ -60,6 +60,12 @@ struct OzSplitJob {
   int64_t koff;  // first k column of this block inside the panel (multiple of 64)
 };
 
+// Memory layout of a split job's source block, detected on the host from the
+// address tables: a plain column-major [rows x K] matrix (rows contiguous), a
+// [K x rows] matrix (k contiguous), or anything else (gathered through the
+// tables).
+enum OzLayout { kOzGeneric = 0, kOzRowsMajor = 1, kOzKMajor = 2 };
+
 // One 128x128 output tile of one destination block.
 struct OzTile {
   int dblock;
@@ -82,6 +88,17 @@ struct OzDBlock {
 
 constexpr int kOzBM = 128, kOzBN = 128, kOzBK = 64, kOzMaxSlices = 8;
 
+// Work unit of the tensor-core kernel: one level of one tile over a range of
+// its k blocks (split-K).  Units are ordered (level, split, tile) so that the
+// CTAs running at the same time stream the same k window of the panels.
+struct OzUnit {
+  int tile, level, split;
+  int kb_begin, kb_end;  // range in the tile's concatenated k-block list
+  int trip_first;        // first trip overlapping kb_begin
+  int kb_in_trip;        // k-block offset inside that trip
+  int pad;
+};
+
 struct OzGemmArgs {
   const void* maps_a;  // CUtensorMap[n_panels_a], 64-byte aligned, device memory
   const void* maps_b;
@@ -89,11 +106,13 @@ struct OzGemmArgs {
   const OzPanel* panels_b;
   const OzTile* tiles;
   const OzTrip* trips;
-  int n_units;  // units = (tile, level), level-major order: unit u -> tile u % n_tiles, level u / n_tiles
+  const OzUnit* units;
+  int n_units;
   int n_tiles;
   int slices;
+  int nsplit;
   int chunk_kb[kOzMaxSlices];  // k blocks per exact flush at each level
-  float2* ws;                  // [tile][level][col 128][row 128] (hi, lo)
+  float2* ws;                  // [tile][level][split][col 128][row 128] (hi, lo)
   int* err_flag;
 };
 

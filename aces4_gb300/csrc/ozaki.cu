@@ -40,7 +40,7 @@ namespace {
 
 constexpr int kDigitBits = 7;
 constexpr int kStages = 6;
-constexpr int kThreadsOz = 192;  // warp 0 TMA, warp 1 MMA, warps 2..5 epilogue
+constexpr int kThreadsOz = 320;  // warp 0 TMA, warp 1 MMA, warps 2..9 epilogue
 constexpr uint32_t kTileBytes = kOzBM * kOzBK * 2;  // 16 KB per operand tile
 constexpr uint32_t kStageBytes = 2 * kTileBytes;
 // TMEM columns: [0,128) and [128,256) are the two FP32 MMA accumulators; [256,384)
@@ -152,6 +152,21 @@ __device__ __forceinline__ uint64_t sw128_desc(const void* tile) {
   d |= uint64_t(2) << 61;            // SWIZZLE_128B
   return d;
 }
+__device__ __forceinline__ void tc_wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
+__device__ __forceinline__ void tc_wait_st() { asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory"); }
+// 32 consecutive TMEM columns of this thread's lane; completes at tc_wait_ld().
+__device__ __forceinline__ void tc_ld32_nowait(uint32_t taddr, uint32_t (&r)[32]) {
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x32.b32 "
+      "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+      "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+        "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]),
+        "=r"(r[14]), "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]),
+        "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]), "=r"(r[25]),
+        "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+      : "r"(taddr));
+}
 __device__ __forceinline__ void tc_ld32(uint32_t taddr, uint32_t (&r)[32]) {
   asm volatile(
       "tcgen05.ld.sync.aligned.32x32b.x32.b32 "
@@ -176,70 +191,85 @@ __device__ __forceinline__ void two_sum_acc(float& hi, float& lo, float x) {
 }
 
 // ------------------------------------------------------------------ roles
+// Walks the k blocks of one unit: calls f(koff_a, koff_b) per 64-wide block.
+template <class F>
+__device__ __forceinline__ void for_unit_kblocks(const OzGemmArgs& a, const OzUnit& un, const OzTile& tl,
+                                                 F&& f) {
+  int kb = un.kb_begin;
+  int q = un.trip_first, j = un.kb_in_trip;
+  while (kb < un.kb_end && q < tl.trip_end) {
+    const OzTrip tr = a.trips[q];
+    for (; j < tr.nkb && kb < un.kb_end; ++j, ++kb)
+      if (!f(int(tr.koff_a) + j * kOzBK, int(tr.koff_b) + j * kOzBK, kb)) return;
+    ++q;
+    j = 0;
+  }
+}
+
 __device__ void producer(const OzGemmArgs& a, OzSmem& sm) {
   uint32_t it = 0;
   for (int u = blockIdx.x; u < a.n_units; u += gridDim.x) {
-    const int tile = u % a.n_tiles, level = u / a.n_tiles;
-    const OzTile tl = a.tiles[tile];
+    const OzUnit un = a.units[u];
+    const OzTile tl = a.tiles[un.tile];
+    const int level = un.level;
     const void* ma = static_cast<const uint8_t*>(a.maps_a) + size_t(tl.panel_a) * 128;
     const void* mb = static_cast<const uint8_t*>(a.maps_b) + size_t(tl.panel_b) * 128;
     const int rpa = a.panels_a[tl.panel_a].rows_pad, rpb = a.panels_b[tl.panel_b].rows_pad;
-    for (int q = tl.trip_begin; q < tl.trip_end; ++q) {
-      const OzTrip tr = a.trips[q];
-      for (int j = 0; j < tr.nkb; ++j) {
-        const int ka = int(tr.koff_a) + j * kOzBK, kb = int(tr.koff_b) + j * kOzBK;
-        for (int i = 0; i <= level; ++i) {
-          const int s = it % kStages;
-          const uint32_t ph = (it / kStages) & 1;
-          if (!mbar_wait(&sm.empty[s], ph ^ 1, sm, a.err_flag, 1)) return;
-          mbar_expect_tx(&sm.full[s], kStageBytes);
-          tma_load_2d(sm.a[s], ma, &sm.full[s], ka, i * rpa + tl.m0);
-          tma_load_2d(sm.b[s], mb, &sm.full[s], kb, (level - i) * rpb + tl.n0);
-          ++it;
-        }
+    bool ok = true;
+    for_unit_kblocks(a, un, tl, [&](int ka, int kb, int) {
+      for (int i = 0; i <= level; ++i) {
+        const int s = it % kStages;
+        const uint32_t ph = (it / kStages) & 1;
+        if (!mbar_wait(&sm.empty[s], ph ^ 1, sm, a.err_flag, 1)) return ok = false;
+        mbar_expect_tx(&sm.full[s], kStageBytes);
+        tma_load_2d(sm.a[s], ma, &sm.full[s], ka, i * rpa + tl.m0);
+        tma_load_2d(sm.b[s], mb, &sm.full[s], kb, (level - i) * rpb + tl.n0);
+        ++it;
       }
-    }
+      return true;
+    });
+    if (!ok) return;
   }
 }
 
 __device__ void mma_issuer(const OzGemmArgs& a, OzSmem& sm, uint32_t tmem) {
   uint32_t it = 0, chunk = 0;
   for (int u = blockIdx.x; u < a.n_units; u += gridDim.x) {
-    const int tile = u % a.n_tiles, level = u / a.n_tiles;
-    const OzTile tl = a.tiles[tile];
+    const OzUnit un = a.units[u];
+    const OzTile tl = a.tiles[un.tile];
+    const int level = un.level;
     const int ckb = a.chunk_kb[level];
-    int kb_done = 0, in_chunk = 0;
+    int in_chunk = 0;
     uint32_t buf = 0;
-    for (int q = tl.trip_begin; q < tl.trip_end; ++q) {
-      const int nkb = a.trips[q].nkb;
-      for (int j = 0; j < nkb; ++j) {
-        if (in_chunk == 0) {
-          buf = chunk & 1;
-          if (!mbar_wait(&sm.acc_empty[buf], ((chunk >> 1) & 1) ^ 1, sm, a.err_flag, 2)) return;
-          tc_fence_after();
-        }
-        const uint32_t d_tmem = tmem + buf * kOzBN;
-        for (int i = 0; i <= level; ++i) {
-          const int s = it % kStages;
-          const uint32_t ph = (it / kStages) & 1;
-          if (!mbar_wait(&sm.full[s], ph, sm, a.err_flag, 3)) return;
-          tc_fence_after();
-          const uint64_t ad = sw128_desc(sm.a[s]), bd = sw128_desc(sm.b[s]);
-#pragma unroll
-          for (int kk = 0; kk < kOzBK / 16; ++kk)
-            tc_mma(d_tmem, ad + 2 * kk, bd + 2 * kk, (in_chunk == 0 && i == 0 && kk == 0) ? 0u : 1u);
-          tc_commit(&sm.empty[s]);
-          ++it;
-        }
-        ++kb_done;
-        ++in_chunk;
-        if (in_chunk == ckb || kb_done == tl.kb_total) {
-          tc_commit(&sm.acc_full[buf]);
-          ++chunk;
-          in_chunk = 0;
-        }
+    bool ok = true;
+    for_unit_kblocks(a, un, tl, [&](int, int, int kb) {
+      if (in_chunk == 0) {
+        buf = chunk & 1;
+        if (!mbar_wait(&sm.acc_empty[buf], ((chunk >> 1) & 1) ^ 1, sm, a.err_flag, 2)) return ok = false;
+        tc_fence_after();
       }
-    }
+      const uint32_t d_tmem = tmem + buf * kOzBN;
+      for (int i = 0; i <= level; ++i) {
+        const int s = it % kStages;
+        const uint32_t ph = (it / kStages) & 1;
+        if (!mbar_wait(&sm.full[s], ph, sm, a.err_flag, 3)) return ok = false;
+        tc_fence_after();
+        const uint64_t ad = sw128_desc(sm.a[s]), bd = sw128_desc(sm.b[s]);
+#pragma unroll
+        for (int kk = 0; kk < kOzBK / 16; ++kk)
+          tc_mma(d_tmem, ad + 2 * kk, bd + 2 * kk, (in_chunk == 0 && i == 0 && kk == 0) ? 0u : 1u);
+        tc_commit(&sm.empty[s]);
+        ++it;
+      }
+      ++in_chunk;
+      if (in_chunk == ckb || kb + 1 == un.kb_end) {
+        tc_commit(&sm.acc_full[buf]);
+        ++chunk;
+        in_chunk = 0;
+      }
+      return true;
+    });
+    if (!ok) return;
   }
 }
 
@@ -256,51 +286,55 @@ __device__ __forceinline__ void tc_st32(uint32_t taddr, const uint32_t (&r)[32])
       : "memory");
 }
 
-// Four warps, one per TMEM lane quadrant; each thread owns one accumulator
-// row and walks its 128 columns in groups of 32.
+// Eight warps, two per TMEM lane quadrant (warp % 4); each thread owns one
+// accumulator row and 64 of its 128 columns, in two groups of 32.  The three
+// TMEM loads of a group (chunk, hi, lo) are issued before one wait.
 __device__ void epilogue(const OzGemmArgs& a, OzSmem& sm, uint32_t tmem, int warp, int lane) {
-  const int q = warp & 3;
+  const int q = warp & 3, h = (warp - 2) >> 2;
   const int row = 32 * q + lane;
-  const uint32_t lane_addr = tmem + (uint32_t(32 * q) << 16);
+  const uint32_t lane_addr = tmem + (uint32_t(32 * q) << 16) + uint32_t(64 * h);
   uint32_t chunk = 0;
   for (int u = blockIdx.x; u < a.n_units; u += gridDim.x) {
-    const int tile = u % a.n_tiles, level = u / a.n_tiles;
-    const int kb_total = a.tiles[tile].kb_total;
-    const int ckb = a.chunk_kb[level];
-    const int nchunks = (kb_total + ckb - 1) / ckb;
-    float2* w = a.ws + (size_t(tile) * a.slices + level) * kOzBN * kOzBM + row;
+    const OzUnit un = a.units[u];
+    const int ckb = a.chunk_kb[un.level];
+    const int nchunks = (un.kb_end - un.kb_begin + ckb - 1) / ckb;
+    float2* w = a.ws + ((size_t(un.tile) * a.slices + un.level) * a.nsplit + un.split) * kOzBN * kOzBM +
+                size_t(64 * h) * kOzBM + row;
     for (int c = 0; c < nchunks; ++c) {
       const uint32_t buf = chunk & 1;
       if (!mbar_wait(&sm.acc_full[buf], (chunk >> 1) & 1, sm, a.err_flag, 4)) return;
       tc_fence_after();
       const bool first = c == 0, last = c == nchunks - 1;
 #pragma unroll 1
-      for (int g = 0; g < kOzBN / 32; ++g) {
+      for (int g = 0; g < 2; ++g) {
         uint32_t x[32], hi[32], lo[32];
-        tc_ld32(lane_addr + buf * kOzBN + 32 * g, x);
+        tc_ld32_nowait(lane_addr + buf * kOzBN + 32 * g, x);
+        if (!first) {
+          tc_ld32_nowait(lane_addr + kTmemHi + 32 * g, hi);
+          tc_ld32_nowait(lane_addr + kTmemLo + 32 * g, lo);
+        }
+        tc_wait_ld();
         if (first) {
 #pragma unroll
           for (int j = 0; j < 32; ++j) hi[j] = x[j], lo[j] = 0u;
         } else {
-          tc_ld32(lane_addr + kTmemHi + 32 * g, hi);
-          tc_ld32(lane_addr + kTmemLo + 32 * g, lo);
 #pragma unroll
           for (int j = 0; j < 32; ++j) {
-            float h = __uint_as_float(hi[j]), l = __uint_as_float(lo[j]);
-            two_sum_acc(h, l, __uint_as_float(x[j]));
-            hi[j] = __float_as_uint(h), lo[j] = __float_as_uint(l);
+            float hv = __uint_as_float(hi[j]), lv = __uint_as_float(lo[j]);
+            two_sum_acc(hv, lv, __uint_as_float(x[j]));
+            hi[j] = __float_as_uint(hv), lo[j] = __float_as_uint(lv);
           }
         }
         if (!last) {
           tc_st32(lane_addr + kTmemHi + 32 * g, hi);
           tc_st32(lane_addr + kTmemLo + 32 * g, lo);
-          asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
         } else {
 #pragma unroll
           for (int j = 0; j < 32; ++j)
             w[size_t(32 * g + j) * kOzBM] = make_float2(__uint_as_float(hi[j]), __uint_as_float(lo[j]));
         }
       }
+      if (!last) tc_wait_st();
       tc_fence_before();
       __syncwarp();
       if (lane == 0) mbar_arrive(&sm.acc_empty[buf]);
@@ -320,7 +354,7 @@ __global__ void __launch_bounds__(kThreadsOz, 1) oz_gemm_kernel(const __grid_con
     }
     for (int b = 0; b < 2; ++b) {
       mbar_init(&sm.acc_full[b], 1);
-      mbar_init(&sm.acc_empty[b], 4);  // one arrive per epilogue warp
+      mbar_init(&sm.acc_empty[b], 8);  // one arrive per epilogue warp
     }
     mbar_init(&sm.drain, 1);
     sm.abort = 0;
@@ -461,35 +495,229 @@ __global__ void __launch_bounds__(256) oz_split_kernel(const OzSplitJob* __restr
   }
 }
 
+// ------------------------------------------------------------------ fast split paths
+// Exact BF16 bits of a digit d in [0, 127] with the sign bit of the source:
+// float(d) is formed exactly as (2^23 + d) - 2^23, two digits are packed by
+// one cvt.rn.bf16x2.f32 (exact, they have at most 7 significant bits), and
+// the signs are applied to the packed bits.
+__device__ __forceinline__ uint32_t digits_bf16x2(uint32_t d0, uint32_t d1, uint32_t neg0, uint32_t neg1) {
+  const float f0 = __fsub_rn(__uint_as_float(0x4B000000u | d0), 8388608.0f);
+  const float f1 = __fsub_rn(__uint_as_float(0x4B000000u | d1), 8388608.0f);
+  __nv_bfloat162 h = __floats2bfloat162_rn(f0, f1);
+  return *reinterpret_cast<uint32_t*>(&h) ^ ((neg0 << 15) | (neg1 << 31));
+}
+
+// Row maxima of a column-major [rows x K] block (rows contiguous): each thread
+// owns two rows (one 16-byte load per k) over a 64-wide k range.
+__global__ void __launch_bounds__(256) oz_exp_rows_kernel(const OzSplitJob* __restrict__ jobs,
+                                                          const int64_t* __restrict__ prefix, int njobs,
+                                                          const OzPanel* __restrict__ panels) {
+  const int j = find_job(prefix, njobs, blockIdx.x);
+  const OzSplitJob jb = jobs[j];
+  const int64_t local = int64_t(blockIdx.x) - prefix[j];
+  const int ktiles = (jb.K + 63) / 64;
+  const int r = int(local / ktiles) * 512 + 2 * threadIdx.x;
+  const int k0 = int(local % ktiles) * 64;
+  if (r >= jb.rows) return;
+  const int k1 = min(jb.K, k0 + 64);
+  const bool pair = r + 1 < jb.rows && (jb.rows & 1) == 0;
+  unsigned long long m0 = 0, m1 = 0;
+  const double* base = jb.src + r;
+  if (pair) {
+#pragma unroll 8
+    for (int k = k0; k < k1; ++k) {
+      const double2 v = __ldg(reinterpret_cast<const double2*>(base + size_t(k) * jb.rows));
+      m0 = max(m0, __double_as_longlong(v.x) & 0x7FF0000000000000ull);
+      m1 = max(m1, __double_as_longlong(v.y) & 0x7FF0000000000000ull);
+    }
+  } else {
+    for (int k = k0; k < k1; ++k) {
+      m0 = max(m0, __double_as_longlong(__ldg(base + size_t(k) * jb.rows)) & 0x7FF0000000000000ull);
+      if (r + 1 < jb.rows)
+        m1 = max(m1, __double_as_longlong(__ldg(base + 1 + size_t(k) * jb.rows)) & 0x7FF0000000000000ull);
+    }
+  }
+  int* e = panels[jb.panel].exps;
+  if (m0) atomicMax(&e[r], int(m0 >> 52));
+  if (m1 && r + 1 < jb.rows) atomicMax(&e[r + 1], int(m1 >> 52));
+}
+
+// Row maxima of a [K x rows] block (k contiguous): one warp per row.
+__global__ void __launch_bounds__(256) oz_exp_kmaj_kernel(const OzSplitJob* __restrict__ jobs,
+                                                          const int64_t* __restrict__ prefix, int njobs,
+                                                          const OzPanel* __restrict__ panels) {
+  const int j = find_job(prefix, njobs, blockIdx.x);
+  const OzSplitJob jb = jobs[j];
+  const int64_t local = int64_t(blockIdx.x) - prefix[j];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  int* e = panels[jb.panel].exps;
+  const bool vec = (jb.K & 1) == 0;
+  for (int rr = 0; rr < 4; ++rr) {
+    const int r = int(local) * 32 + warp * 4 + rr;
+    if (r >= jb.rows) return;
+    const double* row = jb.src + size_t(r) * jb.K;
+    unsigned long long m = 0;
+    if (vec) {
+      const double2* row2 = reinterpret_cast<const double2*>(row);
+#pragma unroll 4
+      for (int k = lane; k < jb.K / 2; k += 32) {
+        const double2 v = __ldg(row2 + k);
+        m = max(m, max(__double_as_longlong(v.x) & 0x7FF0000000000000ull,
+                       __double_as_longlong(v.y) & 0x7FF0000000000000ull));
+      }
+    } else {
+      for (int k = lane; k < jb.K; k += 32)
+        m = max(m, __double_as_longlong(__ldg(row + k)) & 0x7FF0000000000000ull);
+    }
+    for (int o = 16; o > 0; o >>= 1) m = max(m, __shfl_xor_sync(0xffffffffu, m, o));
+    if (lane == 0 && m) atomicMax(&e[r], int(m >> 52));
+  }
+}
+
+// Slices of a [K x rows] block: one warp per row, each lane four consecutive k
+// (two 16-byte loads, one 8-byte store per slice).
+__global__ void __launch_bounds__(256) oz_split_kmaj_kernel(const OzSplitJob* __restrict__ jobs,
+                                                            const int64_t* __restrict__ prefix, int njobs,
+                                                            const OzPanel* __restrict__ panels, int slices) {
+  const int j = find_job(prefix, njobs, blockIdx.x);
+  const OzSplitJob jb = jobs[j];
+  const int64_t local = int64_t(blockIdx.x) - prefix[j];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int r = int(local) * 8 + warp;
+  if (r >= jb.rows) return;
+  const OzPanel pn = panels[jb.panel];
+  const int mx = pn.exps[r];
+  const double* row = jb.src + size_t(r) * jb.K;
+  uint2* dst = reinterpret_cast<uint2*>(pn.base + (size_t(r) * pn.kpad + jb.koff));
+  const size_t slice_stride = size_t(pn.rows_pad) * pn.kpad / 4;  // in uint2 (4 bf16)
+  const bool vec = (jb.K & 3) == 0;
+  for (int k = 4 * lane; k < jb.K; k += 128) {
+    unsigned long long b[4];
+    if (vec) {
+      const double2 v0 = __ldg(reinterpret_cast<const double2*>(row + k));
+      const double2 v1 = __ldg(reinterpret_cast<const double2*>(row + k + 2));
+      b[0] = __double_as_longlong(v0.x), b[1] = __double_as_longlong(v0.y);
+      b[2] = __double_as_longlong(v1.x), b[3] = __double_as_longlong(v1.y);
+    } else {
+#pragma unroll
+      for (int t = 0; t < 4; ++t) b[t] = k + t < jb.K ? __double_as_longlong(__ldg(row + k + t)) : 0ull;
+    }
+    unsigned long long q[4];
+    uint32_t ng[4];
+#pragma unroll
+    for (int t = 0; t < 4; ++t) q[t] = quantize(b[t], mx, slices), ng[t] = uint32_t(b[t] >> 63);
+    for (int i = 0; i < slices; ++i) {
+      const int sh = kDigitBits * (slices - 1 - i);
+      uint2 o;
+      o.x = digits_bf16x2(uint32_t(q[0] >> sh) & 127u, uint32_t(q[1] >> sh) & 127u, ng[0], ng[1]);
+      o.y = digits_bf16x2(uint32_t(q[2] >> sh) & 127u, uint32_t(q[3] >> sh) & 127u, ng[2], ng[3]);
+      dst[i * slice_stride + (k >> 2)] = o;
+    }
+  }
+}
+
+// Slices of a column-major [rows x K] block: 64x64 tiles transposed through
+// shared memory (16-byte loads along rows, 8-byte stores along k).
+__global__ void __launch_bounds__(256) oz_split_rows_kernel(const OzSplitJob* __restrict__ jobs,
+                                                            const int64_t* __restrict__ prefix, int njobs,
+                                                            const OzPanel* __restrict__ panels, int slices) {
+  __shared__ unsigned long long tile[64][65];
+  const int j = find_job(prefix, njobs, blockIdx.x);
+  const OzSplitJob jb = jobs[j];
+  const int64_t local = int64_t(blockIdx.x) - prefix[j];
+  const int ktiles = (jb.K + 63) / 64;
+  const int r0 = int(local / ktiles) * 64, k0 = int(local % ktiles) * 64;
+  const int t = threadIdx.x;
+  // load: thread -> (row pair, k): 32 row pairs x 8 k per pass, 8 passes
+  const bool vec = (jb.rows & 1) == 0;
+#pragma unroll
+  for (int p = 0; p < 8; ++p) {
+    const int rp = t & 31, k = (t >> 5) + 8 * p;
+    const int r = r0 + 2 * rp;
+    unsigned long long x0 = 0, x1 = 0;
+    if (k0 + k < jb.K && r < jb.rows) {
+      const double* src = jb.src + size_t(k0 + k) * jb.rows + r;
+      if (vec) {
+        const double2 v = __ldg(reinterpret_cast<const double2*>(src));
+        x0 = __double_as_longlong(v.x), x1 = __double_as_longlong(v.y);
+      } else {
+        x0 = __double_as_longlong(__ldg(src));
+        if (r + 1 < jb.rows) x1 = __double_as_longlong(__ldg(src + 1));
+      }
+    }
+    tile[2 * rp][k] = x0;
+    tile[2 * rp + 1][k] = x1;
+  }
+  __syncthreads();
+  // store: thread -> (row, 4 consecutive k): 16 k-quads x 16 rows per pass, 4 passes
+  const OzPanel pn = panels[jb.panel];
+  const size_t slice_stride = size_t(pn.rows_pad) * pn.kpad / 4;
+#pragma unroll 1
+  for (int p = 0; p < 4; ++p) {
+    const int kq = t & 15, r = (t >> 4) + 16 * p;
+    if (r0 + r >= jb.rows || k0 + 4 * kq >= jb.K) continue;
+    const int mx = pn.exps[r0 + r];
+    unsigned long long q[4];
+    uint32_t ng[4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      const unsigned long long b = (k0 + 4 * kq + u < jb.K) ? tile[r][4 * kq + u] : 0ull;
+      q[u] = quantize(b, mx, slices), ng[u] = uint32_t(b >> 63);
+    }
+    uint2* dst = reinterpret_cast<uint2*>(pn.base + (size_t(r0 + r) * pn.kpad + jb.koff + k0 + 4 * kq));
+    for (int i = 0; i < slices; ++i) {
+      const int sh = kDigitBits * (slices - 1 - i);
+      uint2 o;
+      o.x = digits_bf16x2(uint32_t(q[0] >> sh) & 127u, uint32_t(q[1] >> sh) & 127u, ng[0], ng[1]);
+      o.y = digits_bf16x2(uint32_t(q[2] >> sh) & 127u, uint32_t(q[3] >> sh) & 127u, ng[2], ng[3]);
+      dst[i * slice_stride] = o;
+    }
+  }
+}
+
 // ------------------------------------------------------------------ recombine
+// One thread per output element (grid: tiles x 64 blocks of 256): sums the
+// split partials of each level exactly in FP64 (integers < 2^53), applies the
+// level's power of two, then the row/column scales.
 __global__ void __launch_bounds__(256) oz_recombine_kernel(const OzTile* __restrict__ tiles,
                                                            const OzDBlock* __restrict__ dblocks,
                                                            const PlanRef* __restrict__ plans,
                                                            const OzPanel* __restrict__ pa,
                                                            const OzPanel* __restrict__ pb,
                                                            const float2* __restrict__ ws, int slices,
-                                                           int beta) {
-  const int tile = blockIdx.x;
+                                                           int nsplit, int beta) {
+  const int tile = blockIdx.x >> 6;
+  const int e = ((blockIdx.x & 63) << 8) + threadIdx.x;
+  const int row = e & (kOzBM - 1), col = e >> 7;
   const OzTile tl = tiles[tile];
   const OzDBlock db = dblocks[tl.dblock];
   const PlanRef pl = plans[db.plan];
+  const int m = tl.m0 + row, n = tl.n0 + col;
+  if (m >= pl.M || n >= pl.N) return;
   const int* ea = pa[tl.panel_a].exps;
   const int* eb = pb[tl.panel_b].exps;
-  for (int e = threadIdx.x; e < kOzBM * kOzBN; e += blockDim.x) {
-    const int row = e & (kOzBM - 1), col = e >> 7;
-    const int m = tl.m0 + row, n = tl.n0 + col;
-    if (m >= pl.M || n >= pl.N) continue;
-    double v = 0.0;
-    for (int lv = slices - 1; lv >= 0; --lv) {
-      const float2 p = ws[((size_t(tile) * slices + lv) * kOzBN + col) * kOzBM + row];
-      const double s = double(p.x) + double(p.y);  // exact: both integers, sum < 2^53
-      v += ldexp(s, -kDigitBits * (lv + 2));
+  double v = 0.0;
+  for (int lv = slices - 1; lv >= 0; --lv) {
+    const float2* p = ws + ((size_t(tile) * slices + lv) * nsplit * kOzBN + col) * kOzBM + row;
+    double s0 = 0.0, s1 = 0.0;
+    int sp = 0;
+#pragma unroll 4
+    for (; sp + 1 < nsplit; sp += 2) {
+      const float2 x = __ldg(p + size_t(sp) * kOzBN * kOzBM);
+      const float2 y = __ldg(p + size_t(sp + 1) * kOzBN * kOzBM);
+      s0 += double(x.x) + double(x.y);
+      s1 += double(y.x) + double(y.y);
     }
-    const int E = (ea[m] ? ea[m] : 1) - 1022, F = (eb[n] ? eb[n] : 1) - 1022;
-    v = ldexp(v, E + F);
-    double* dst = db.d + pl.offDm[m] + pl.offDn[n];
-    *dst = beta ? *dst + v : v;
+    if (sp < nsplit) {
+      const float2 x = __ldg(p + size_t(sp) * kOzBN * kOzBM);
+      s0 += double(x.x) + double(x.y);
+    }
+    v += ldexp(s0 + s1, -kDigitBits * (lv + 2));
   }
+  const int E = (ea[m] ? ea[m] : 1) - 1022, F = (eb[n] ? eb[n] : 1) - 1022;
+  v = ldexp(v, E + F);
+  double* dst = db.d + pl.offDm[m] + pl.offDn[n];
+  *dst = beta ? *dst + v : v;
 }
 
 using EncodeTiled = PFN_cuTensorMapEncodeTiled_v12000;
@@ -532,20 +760,38 @@ int oz_make_tensor_map(void* map128, const void* base, int64_t kpad, int64_t row
   return A4G_OK;
 }
 
-int oz_launch_exp(const OzSplitJob* jobs, const int64_t* prefix, int njobs, int64_t ntiles,
+int64_t oz_exp_tiles(int layout, int rows, int K) {
+  if (layout == kOzRowsMajor) return int64_t((rows + 511) / 512) * ((K + 63) / 64);
+  if (layout == kOzKMajor) return (rows + 31) / 32;
+  return int64_t((rows + 63) / 64) * ((K + 63) / 64);
+}
+
+int64_t oz_split_tiles(int layout, int rows, int K) {
+  if (layout == kOzKMajor) return (rows + 7) / 8;
+  return int64_t((rows + 63) / 64) * ((K + 63) / 64);
+}
+
+int oz_launch_exp(int layout, const OzSplitJob* jobs, const int64_t* prefix, int njobs, int64_t ntiles,
                   const OzPanel* panels, cudaStream_t s) {
   if (ntiles <= 0) return A4G_OK;
   if (ntiles > 0x7fffffffLL) return fail(A4G_ERR_RANGE, "too many split tiles");
-  oz_exp_kernel<<<unsigned(ntiles), 256, 0, s>>>(jobs, prefix, njobs, panels);
+  if (layout == kOzRowsMajor) oz_exp_rows_kernel<<<unsigned(ntiles), 256, 0, s>>>(jobs, prefix, njobs, panels);
+  else if (layout == kOzKMajor) oz_exp_kmaj_kernel<<<unsigned(ntiles), 256, 0, s>>>(jobs, prefix, njobs, panels);
+  else oz_exp_kernel<<<unsigned(ntiles), 256, 0, s>>>(jobs, prefix, njobs, panels);
   A4G_CUDA(cudaGetLastError());
   return A4G_OK;
 }
 
-int oz_launch_split(const OzSplitJob* jobs, const int64_t* prefix, int njobs, int64_t ntiles,
+int oz_launch_split(int layout, const OzSplitJob* jobs, const int64_t* prefix, int njobs, int64_t ntiles,
                     const OzPanel* panels, int slices, cudaStream_t s) {
   if (ntiles <= 0) return A4G_OK;
   if (ntiles > 0x7fffffffLL) return fail(A4G_ERR_RANGE, "too many split tiles");
-  oz_split_kernel<<<unsigned(ntiles), 256, 0, s>>>(jobs, prefix, njobs, panels, slices);
+  if (layout == kOzRowsMajor)
+    oz_split_rows_kernel<<<unsigned(ntiles), 256, 0, s>>>(jobs, prefix, njobs, panels, slices);
+  else if (layout == kOzKMajor)
+    oz_split_kmaj_kernel<<<unsigned(ntiles), 256, 0, s>>>(jobs, prefix, njobs, panels, slices);
+  else
+    oz_split_kernel<<<unsigned(ntiles), 256, 0, s>>>(jobs, prefix, njobs, panels, slices);
   A4G_CUDA(cudaGetLastError());
   return A4G_OK;
 }
@@ -573,10 +819,11 @@ int oz_launch_gemm(const OzGemmArgs& args, int grid, cudaStream_t s) {
 }
 
 int oz_launch_recombine(const OzTile* tiles, int ntiles, const OzDBlock* dblocks, const PlanRef* plans,
-                        const OzPanel* pa, const OzPanel* pb, const float2* ws, int slices, int beta,
-                        cudaStream_t s) {
+                        const OzPanel* pa, const OzPanel* pb, const float2* ws, int slices, int nsplit,
+                        int beta, cudaStream_t s) {
   if (ntiles <= 0) return A4G_OK;
-  oz_recombine_kernel<<<ntiles, 256, 0, s>>>(tiles, dblocks, plans, pa, pb, ws, slices, beta);
+  if (int64_t(ntiles) * 64 > 0x7fffffffLL) return fail(A4G_ERR_RANGE, "too many tiles");
+  oz_recombine_kernel<<<ntiles * 64, 256, 0, s>>>(tiles, dblocks, plans, pa, pb, ws, slices, nsplit, beta);
   A4G_CUDA(cudaGetLastError());
   return A4G_OK;
 }

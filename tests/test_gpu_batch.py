@@ -200,3 +200,16 @@ def test_zero_destination_blocks_are_cleared(a4):
         b = _run(a4, R, trip, labels, prec)
         assert b.info()["pairs"] == 0
         assert all(float(R.block(k).abs().max()) == 0.0 for k in R.keys())
+
+
+def test_split_odd_extents_non_vector_paths(a4):
+    # odd segment sizes: row counts and k lengths that are not multiples of
+    # 2 or 4 exercise the scalar branches of the layout-specialised kernels
+    R, V, T, trip, labels = _make(a4, "ladder", [5, 7, 9], [3, 5], 0.2, 8)
+    ref = _reference(R, trip, labels)
+    _run(a4, R, trip, labels, a4.device.PREC_OZAKI_BF16, slices=6)
+    assert _errors(R, ref).max() <= TOL_SPLIT
+    R2, V2, T2, trip2, labels2 = _make(a4, "ladder", [5, 7, 9], [3, 5], 0.2, 8, integer=True)
+    _run(a4, R2, trip2, labels2, a4.device.PREC_OZAKI_BF16, slices=1)
+    for k, want in _reference(R2, trip2, labels2).items():
+        np.testing.assert_array_equal(R2.block(k).cpu().numpy(), want)
