@@ -63,6 +63,7 @@ SIGNATURES = {
     "a4g_increment": (ctypes.c_int, [c_void_p, ctypes.c_int64, ctypes.c_double, c_void_p]),
     "a4g_add_scaled": (ctypes.c_int, [c_void_p, c_void_p, ctypes.c_int64, ctypes.c_double, c_void_p]),
     "a4g_add_sub": (ctypes.c_int, None),
+    "a4g_add_sub_noalloc": (ctypes.c_int, None),
     "a4g_norm2": (ctypes.c_int, [c_void_p, ctypes.c_int64, c_double_p, c_void_p]),
     "a4g_slice": (ctypes.c_int, None),
     "a4g_insert": (ctypes.c_int, None),

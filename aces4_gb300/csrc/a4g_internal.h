@@ -47,6 +47,7 @@ int check_device_flag(cudaStream_t s);        // syncs s, reads and clears the f
 // Pattern handling restated from tensor_dil_omp.F90 (get_contraction_ptrn
 // :87-142, contr_ptrn_ok :861-896) plus the GEMM view used by the kernels.
 int get_contraction_ptrn(int drank, int lrank, int rrank, const int* aces, int* my);
+bool perm_from_labels(int rank, const int* dst_labels, const int* src_labels, int* o2n);
 bool contr_ptrn_ok(const int* ptrn, int lr, int rr, int dr, const int* lext, const int* rext,
                    const int* dext);
 

@@ -69,19 +69,6 @@ std::mutex g_host_mu;  // host-buffer entries share one arena
 std::map<std::string, std::vector<int>> g_predefined;
 std::mutex g_predef_mu;
 
-// o2n (1-based) from two label lists: source dim j goes to the destination
-// dim i carrying the same label (permute_rhs_to_lhs, interpreter.cpp:2049-2084).
-bool perm_from_labels(int rank, const int* dst_labels, const int* src_labels, int* o2n) {
-  for (int j = 0; j < rank; ++j) o2n[j] = 0;
-  for (int i = 0; i < rank; ++i) {
-    int j = 0;
-    while (j < rank && src_labels[j] != dst_labels[i]) ++j;
-    if (j >= rank || o2n[j] != 0) return false;
-    o2n[j] = i + 1;
-  }
-  return true;
-}
-
 int contract_device(const int* ptrn, const double* l, int lrank, const int* lext, const double* r,
                     int rrank, const int* rext, double* d, int drank, const int* dext, int beta,
                     double* scratch, cudaStream_t s) {

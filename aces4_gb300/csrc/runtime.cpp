@@ -82,6 +82,19 @@ int check_device_flag(cudaStream_t s) {
   return A4G_OK;
 }
 
+// o2n (1-based) from two label lists: source dim j goes to the destination
+// dim i carrying the same label (permute_rhs_to_lhs, interpreter.cpp:2049-2084).
+bool perm_from_labels(int rank, const int* dst_labels, const int* src_labels, int* o2n) {
+  for (int j = 0; j < rank; ++j) o2n[j] = 0;
+  for (int i = 0; i < rank; ++i) {
+    int j = 0;
+    while (j < rank && src_labels[j] != dst_labels[i]) ++j;
+    if (j >= rank || o2n[j] != 0) return false;
+    o2n[j] = i + 1;
+  }
+  return true;
+}
+
 // ------------------------------------------------------------------ planner
 // Stable sort of 1-based item numbers by key; equal keys keep their order, as
 // the reference's merge sort does (merge_sort_key_int_, tensor_dil_omp.F90:1183).

@@ -161,6 +161,20 @@ int a4g_add_scaled(double* t0, const double* t1, int64_t n, double scale, void* 
  * d may alias l (the "+=" form); r is then permuted on the fly, no temp block. */
 int a4g_add_sub(int subtract, int rank, const int* d_labels, const int* r_labels, const int* r_ext,
                 double* d, const double* l, const double* r, void* stream);
+/* Same operation as a4g_add_sub, for callers that cannot allocate device
+ * memory while they run (a fixed pre-reserved device budget, or work issued
+ * inside CUDA stream capture where cudaMalloc is not allowed).  No
+ * counterpart in the reference: it allocates nothing.  When r aliases d in a
+ * different index order, the permuted r is staged in a device array built
+ * into the library: 2^20 doubles (8 MiB), held by every GPU that loads the
+ * library until exit; a larger aliased, permuted operand is rejected with
+ * A4G_ERR_RANGE.  The array's device address is looked up on the first call
+ * per device, so make that first call outside stream capture.  Calls share
+ * the array: calls that overlap on the GPU race.  stream: the caller's
+ * stream, NULL = the CUDA legacy default stream (this entry point never
+ * creates the library's own stream). */
+int a4g_add_sub_noalloc(int subtract, int rank, const int* d_labels, const int* r_labels,
+                        const int* r_ext, double* d, const double* l, const double* r, void* stream);
 /* Sum of squares into *h_result (host), tensor_block_norm2_. Synchronous. */
 int a4g_norm2(const double* t, int64_t n, double* h_result, void* stream);
 /* Slice / insert of a rectangular sub-block (tensor_dil_omp.F90:271-392). */
