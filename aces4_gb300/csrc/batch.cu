@@ -22,7 +22,7 @@ using namespace a4g;
 
 struct a4g_batch {
   int precision = A4G_PREC_FP64;
-  int slices = 6;
+  int slices = 5;
   int beta = 0;
   int64_t pairs = 0;
   double flops = 0.0;
@@ -422,7 +422,7 @@ int a4g_batch_create(a4g_batch** out, const int* ptrn, int drank, int lrank, int
   std::unique_ptr<a4g_batch> b(new a4g_batch());
   if (opts) {
     b->precision = opts->precision;
-    b->slices = opts->slices > 0 ? opts->slices : 6;
+    b->slices = opts->slices > 0 ? opts->slices : 5;
     b->beta = opts->beta ? 1 : 0;
   }
   if (b->precision != A4G_PREC_FP64 && b->precision != A4G_PREC_OZAKI_BF16)

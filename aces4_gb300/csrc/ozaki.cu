@@ -1,11 +1,13 @@
 // Split-precision (Ozaki scheme) block contraction on the tcgen05 tensor cores.
 //
 // Each FP64 operand row (left blocks) / column (right blocks) is scaled by a
-// power of two 2^E with |x| < 2^E over the whole row of the pardo step, then
-// cut into `slices` signed 7-bit digits:
-//     x = sign * sum_i d_i * 2^(E - 7(i+1)) + truncation,   d_i in [0, 127].
-// Digits are exact BF16 values.  The product of two slices is an integer
-// matrix, so   L*R ~= sum_t 2^(E_m + F_n - 7(t+2)) * S_t,   S_t = sum_{i+j=t} A_i B_j
+// power of two with |x| < 2^E over the whole row of the pardo step, rounded to
+// the integer n = round(x * 2^(8*slices - E - 1)) (|n| <= 2^(8*slices-1)) and
+// cut into `slices` balanced base-256 digits:
+//     x ~= sum_i d_i * 2^(E + 1 - 8(i+1)),   d_0 in [-128, 128], d_i in [-128, 127].
+// Digits are exact BF16 values and every digit product is at most 2^14.  The
+// product of two slices is an integer matrix, so
+//     L*R ~= sum_t 2^(E_m + F_n + 2 - 8(t+2)) * S_t,   S_t = sum_{i+j=t} A_i B_j
 // over levels t < slices (triangular truncation).  Each S_t is computed on the
 // tensor cores (kind::f16, BF16 x BF16 -> FP32) in chunks of k short enough
 // that every FP32 partial sum is an integer below 2^24 and therefore exact;
@@ -38,7 +40,7 @@
 namespace a4g {
 namespace {
 
-constexpr int kDigitBits = 7;
+constexpr int kDigitBits = 8;
 constexpr int kStages = 6;
 constexpr int kThreadsOz = 320;  // warp 0 TMA, warp 1 MMA, warps 2..9 epilogue
 constexpr uint32_t kTileBytes = kOzBM * kOzBK * 2;  // 16 KB per operand tile
@@ -446,18 +448,45 @@ __global__ void __launch_bounds__(256) oz_exp_kernel(const OzSplitJob* __restric
   if (part == 0 && r0 + r < jb.rows && m > 0) atomicMax(&panels[jb.panel].exps[r0 + r], m);
 }
 
-// Digits of one double against the row exponent (biased max exponent mx):
-// q = floor(|x| * 2^(7*slices - E)) with E = mx - 1022, so |x| < 2^E and
-// q < 2^(7*slices); digit i is bits [7(slices-1-i), 7(slices-i)) of q.
-__device__ __forceinline__ unsigned long long quantize(unsigned long long bits, int mx, int slices) {
+// Signed fixed-point value of one double against its row exponent (biased
+// max exponent mx, |x| < 2^E with E = mx - 1022):
+//     n = round_half_away(x * 2^(8*slices - E - 1)),   |n| <= 2^(8*slices - 1).
+__device__ __forceinline__ long long quantize(unsigned long long bits, int mx, int slices) {
   const int be = int((bits >> 52) & 0x7FF);
   const unsigned long long frac = bits & ((1ull << 52) - 1);
   const unsigned long long mant = be ? (frac | (1ull << 52)) : frac;
   const int ex = be ? be : 1;
   const int E = (mx ? mx : 1) - 1022;
-  const int sh = ex - 1075 + kDigitBits * slices - E;  // always <= 7*slices - 53 < 0
-  const int rs = -sh;
-  return rs >= 64 ? 0ull : (mant >> rs);
+  const int sh = ex - 1076 + kDigitBits * slices - E;  // |x| * 2^(8s-E-1) = mant * 2^sh
+  unsigned long long m;
+  if (sh >= 0) m = mant << sh;  // only for 7 slices: sh <= 2, mant << 2 < 2^55
+  else if (-sh >= 63) m = 0ull;
+  else m = (mant + (1ull << (-sh - 1))) >> (-sh);
+  return (bits >> 63) ? -static_cast<long long>(m) : static_cast<long long>(m);
+}
+
+// Balanced base-256 digits of n, most significant first: d[0] in [-128, 128],
+// the others in [-128, 127]; sum_i d[i] * 256^(slices-1-i) == n.
+__device__ __forceinline__ void balanced_digits(long long n, int slices, int (&d)[kOzMaxSlices]) {
+#pragma unroll
+  for (int i = kOzMaxSlices - 1; i >= 1; --i) {
+    if (i < slices) {
+      const long long r = ((n + 128) & 255) - 128;
+      d[i] = int(r);
+      n = (n - r) >> 8;
+    }
+  }
+  d[0] = int(n);
+}
+
+// Exact BF16 bits of two digits in [-128, 128]: float(d) is formed exactly as
+// (2^23 + 256 + d) - (2^23 + 256); one cvt.rn.bf16x2.f32 packs the pair (exact,
+// at most 8 significant bits).
+__device__ __forceinline__ uint32_t digits_bf16x2(int d0, int d1) {
+  const float f0 = __fsub_rn(__uint_as_float(0x4B000000u + uint32_t(d0 + 256)), 8388864.0f);
+  const float f1 = __fsub_rn(__uint_as_float(0x4B000000u + uint32_t(d1 + 256)), 8388864.0f);
+  __nv_bfloat162 h = __floats2bfloat162_rn(f0, f1);
+  return *reinterpret_cast<uint32_t*>(&h);
 }
 
 __global__ void __launch_bounds__(256) oz_split_kernel(const OzSplitJob* __restrict__ jobs,
@@ -482,31 +511,18 @@ __global__ void __launch_bounds__(256) oz_split_kernel(const OzSplitJob* __restr
     if (k0 + k >= jb.K) continue;
     const int mx = pn.exps[r0 + r];
     const unsigned long long b0 = tile[r][k], b1 = (k0 + k + 1 < jb.K) ? tile[r][k + 1] : 0ull;
-    const unsigned long long q0 = quantize(b0, mx, slices), q1 = quantize(b1, mx, slices);
-    const float s0 = (b0 >> 63) ? -1.f : 1.f, s1 = (b1 >> 63) ? -1.f : 1.f;
-    __nv_bfloat162* dst = reinterpret_cast<__nv_bfloat162*>(
-        pn.base + (size_t(r0 + r) * pn.kpad + jb.koff + k0 + k));
+    int d0[kOzMaxSlices], d1[kOzMaxSlices];
+    balanced_digits(quantize(b0, mx, slices), slices, d0);
+    balanced_digits(quantize(b1, mx, slices), slices, d1);
+    uint32_t* dst = reinterpret_cast<uint32_t*>(pn.base + (size_t(r0 + r) * pn.kpad + jb.koff + k0 + k));
     const size_t slice_stride = size_t(pn.rows_pad) * pn.kpad / 2;
-    for (int i = 0; i < slices; ++i) {
-      const int sh = kDigitBits * (slices - 1 - i);
-      const float d0 = s0 * float((q0 >> sh) & 127ull), d1 = s1 * float((q1 >> sh) & 127ull);
-      dst[i * slice_stride] = __floats2bfloat162_rn(d0, d1);
-    }
+#pragma unroll
+    for (int i = 0; i < kOzMaxSlices; ++i)
+      if (i < slices) dst[i * slice_stride] = digits_bf16x2(d0[i], d1[i]);
   }
 }
 
 // ------------------------------------------------------------------ fast split paths
-// Exact BF16 bits of a digit d in [0, 127] with the sign bit of the source:
-// float(d) is formed exactly as (2^23 + d) - 2^23, two digits are packed by
-// one cvt.rn.bf16x2.f32 (exact, they have at most 7 significant bits), and
-// the signs are applied to the packed bits.
-__device__ __forceinline__ uint32_t digits_bf16x2(uint32_t d0, uint32_t d1, uint32_t neg0, uint32_t neg1) {
-  const float f0 = __fsub_rn(__uint_as_float(0x4B000000u | d0), 8388608.0f);
-  const float f1 = __fsub_rn(__uint_as_float(0x4B000000u | d1), 8388608.0f);
-  __nv_bfloat162 h = __floats2bfloat162_rn(f0, f1);
-  return *reinterpret_cast<uint32_t*>(&h) ^ ((neg0 << 15) | (neg1 << 31));
-}
-
 // Row maxima of a column-major [rows x K] block (rows contiguous): each thread
 // owns two rows (one 16-byte load per k) over a 64-wide k range.
 __global__ void __launch_bounds__(256) oz_exp_rows_kernel(const OzSplitJob* __restrict__ jobs,
@@ -602,15 +618,15 @@ __global__ void __launch_bounds__(256) oz_split_kmaj_kernel(const OzSplitJob* __
 #pragma unroll
       for (int t = 0; t < 4; ++t) b[t] = k + t < jb.K ? __double_as_longlong(__ldg(row + k + t)) : 0ull;
     }
-    unsigned long long q[4];
-    uint32_t ng[4];
+    int d[4][kOzMaxSlices];
 #pragma unroll
-    for (int t = 0; t < 4; ++t) q[t] = quantize(b[t], mx, slices), ng[t] = uint32_t(b[t] >> 63);
-    for (int i = 0; i < slices; ++i) {
-      const int sh = kDigitBits * (slices - 1 - i);
+    for (int t = 0; t < 4; ++t) balanced_digits(quantize(b[t], mx, slices), slices, d[t]);
+#pragma unroll
+    for (int i = 0; i < kOzMaxSlices; ++i) {
+      if (i >= slices) break;
       uint2 o;
-      o.x = digits_bf16x2(uint32_t(q[0] >> sh) & 127u, uint32_t(q[1] >> sh) & 127u, ng[0], ng[1]);
-      o.y = digits_bf16x2(uint32_t(q[2] >> sh) & 127u, uint32_t(q[3] >> sh) & 127u, ng[2], ng[3]);
+      o.x = digits_bf16x2(d[0][i], d[1][i]);
+      o.y = digits_bf16x2(d[2][i], d[3][i]);
       dst[i * slice_stride + (k >> 2)] = o;
     }
   }
@@ -657,19 +673,19 @@ __global__ void __launch_bounds__(256) oz_split_rows_kernel(const OzSplitJob* __
     const int kq = t & 15, r = (t >> 4) + 16 * p;
     if (r0 + r >= jb.rows || k0 + 4 * kq >= jb.K) continue;
     const int mx = pn.exps[r0 + r];
-    unsigned long long q[4];
-    uint32_t ng[4];
+    int d[4][kOzMaxSlices];
 #pragma unroll
     for (int u = 0; u < 4; ++u) {
       const unsigned long long b = (k0 + 4 * kq + u < jb.K) ? tile[r][4 * kq + u] : 0ull;
-      q[u] = quantize(b, mx, slices), ng[u] = uint32_t(b >> 63);
+      balanced_digits(quantize(b, mx, slices), slices, d[u]);
     }
     uint2* dst = reinterpret_cast<uint2*>(pn.base + (size_t(r0 + r) * pn.kpad + jb.koff + k0 + 4 * kq));
-    for (int i = 0; i < slices; ++i) {
-      const int sh = kDigitBits * (slices - 1 - i);
+#pragma unroll
+    for (int i = 0; i < kOzMaxSlices; ++i) {
+      if (i >= slices) break;
       uint2 o;
-      o.x = digits_bf16x2(uint32_t(q[0] >> sh) & 127u, uint32_t(q[1] >> sh) & 127u, ng[0], ng[1]);
-      o.y = digits_bf16x2(uint32_t(q[2] >> sh) & 127u, uint32_t(q[3] >> sh) & 127u, ng[2], ng[3]);
+      o.x = digits_bf16x2(d[0][i], d[1][i]);
+      o.y = digits_bf16x2(d[2][i], d[3][i]);
       dst[i * slice_stride] = o;
     }
   }
@@ -715,7 +731,7 @@ __global__ void __launch_bounds__(256) oz_recombine_kernel(const OzTile* __restr
     v += ldexp(s0 + s1, -kDigitBits * (lv + 2));
   }
   const int E = (ea[m] ? ea[m] : 1) - 1022, F = (eb[n] ? eb[n] : 1) - 1022;
-  v = ldexp(v, E + F);
+  v = ldexp(v, E + F + 2);
   double* dst = db.d + pl.offDm[m] + pl.offDn[n];
   *dst = beta ? *dst + v : v;
 }
@@ -737,8 +753,9 @@ EncodeTiled get_encoder() {
 }  // namespace
 
 int oz_chunk_kb(int level) {
-  // largest multiple of 64 k such that (level+1) * 127^2 * k < 2^24
-  const long long per = (long long)(level + 1) * 127 * 127;
+  // largest multiple of 64 k such that (level+1) * 128^2 * k < 2^24: every
+  // FP32 partial sum of the chunk is an integer below 2^24, hence exact
+  const long long per = (long long)(level + 1) * 128 * 128;
   const long long k = ((1LL << 24) - 1) / per;
   return int(k / kOzBK);
 }

@@ -179,7 +179,7 @@ class Batch:
     device addresses) and per-block extents.
     """
 
-    def __init__(self, ptrn, drank, lrank, rrank, triples, precision=PREC_FP64, slices=6, beta=0):
+    def __init__(self, ptrn, drank, lrank, rrank, triples, precision=PREC_FP64, slices=5, beta=0):
         tl = list(triples)
         arr = (_Triple * max(1, len(tl)))()
         for i, (d, l, r, de, le, re) in enumerate(tl):

@@ -222,7 +222,7 @@ def main():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--slices", type=int, default=6)
+    ap.add_argument("--slices", type=int, default=5)
     ap.add_argument("--fp64-steps", type=int, default=1)
     ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--cpu-pairs", type=int, default=16)
@@ -366,7 +366,7 @@ def main():
             "metric": METRIC, "value": value, "unit": "TFLOP/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "bf16", "data": "synthetic",
-            "config": {"workload": workload, "slices": S, "digit_bits": 7, "block_pairs": info["pairs"],
+            "config": {"workload": workload, "slices": S, "digits": "balanced base-256 (8-bit)", "block_pairs": info["pairs"],
                        "l2": "inputs 10.7 GB > 126 MB L2 (no flush needed)", "parallelism": f"replicas x{world}"},
             "e2e": e2e,
             "roofline": {"kernel": "oz_gemm_kernel (tcgen05 BF16 slice products)", "bound": "tensor",

@@ -209,7 +209,9 @@ typedef struct a4g_triple {
 
 typedef struct a4g_batch_opts {
   int precision;   /* A4G_PREC_*                                              */
-  int slices;      /* number of BF16 slices per operand (Ozaki), 2..8       */
+  int slices;      /* BF16 digit slices per operand (Ozaki), 1..7; 0 = 5.
+                      Each slice is a balanced base-256 digit; 5 slices keep
+                      the relative error near 1e-11, 6 near 1e-13.          */
   int beta;        /* 0: D = sum of products (overwrite); 1: D += sum        */
   int reserved[5];
 } a4g_batch_opts;

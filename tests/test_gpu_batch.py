@@ -4,7 +4,7 @@ path per destination block.
 
 Tolerances (relative Frobenius error per destination block):
   plain FP64 grouped kernel   1e-12
-  split precision, 6 slices   1e-10   (the stated bound of the split form)
+  split precision, 5 slices   1e-10   (the stated bound of the split form)
   split precision, 1 slice on integer data in [-127, 127]: bit-exact
 """
 import itertools
@@ -105,7 +105,7 @@ def _errors(R, ref):
     return np.array(errs)
 
 
-def _run(a4, R, trip, labels, precision, slices=6, beta=0, graph=False):
+def _run(a4, R, trip, labels, precision, slices=5, beta=0, graph=False):
     import torch
 
     b = a4.device.Batch(_ptrn(labels), 4, 4, 4, trip, precision=precision, slices=slices, beta=beta)
@@ -138,7 +138,7 @@ def test_fp64_uneven_sparse_ring(a4):
 
 
 def test_split_one_slice_integer_exact(a4):
-    # integers in [-127, 127] are exact single 7-bit digits: the tensor-core
+    # integers in [-127, 127] are exact single 8-bit digits: the tensor-core
     # products and the chunked FP32 accumulation must reproduce FP64 exactly
     R, V, T, trip, labels = _make(a4, "ladder", [32, 32], [16, 16], 0.0, 3, integer=True)
     _run(a4, R, trip, labels, a4.device.PREC_OZAKI_BF16, slices=1)
@@ -157,7 +157,7 @@ def test_split_long_k_integer_exact(a4):
         np.testing.assert_array_equal(R.block(k).cpu().numpy(), want)
 
 
-@pytest.mark.parametrize("slices,tol", [(4, 1e-6), (5, 1e-8), (6, TOL_SPLIT), (7, 1e-12)])
+@pytest.mark.parametrize("slices,tol", [(3, 1e-5), (4, 1e-7), (5, TOL_SPLIT), (6, 1e-12), (7, 1e-13)])
 def test_split_ladder_outliers(a4, slices, tol):
     # config-4 distributions (V ~ U[-1,1]/v, T ~ N(0,1e-2) with 1% x1e3) on a
     # smaller ladder: v=64 in 2 segments of 32, o=32 in 2 segments of 16
@@ -172,18 +172,18 @@ def test_split_uneven_sparse_ring_graph_and_beta(a4):
 
     R, V, T, trip, labels = _make(a4, "ring", [12, 16, 24, 32], [5, 8], 0.3, 6)
     ref = _reference(R, trip, labels)
-    _run(a4, R, trip, labels, a4.device.PREC_OZAKI_BF16, slices=6, graph=True)
+    _run(a4, R, trip, labels, a4.device.PREC_OZAKI_BF16, slices=5, graph=True)
     assert _errors(R, ref).max() <= TOL_SPLIT
     first = R.buf.clone()
     # replaying the captured graph gives identical bits
-    b = a4.device.Batch(_ptrn(labels), 4, 4, 4, trip, precision=a4.device.PREC_OZAKI_BF16, slices=6)
+    b = a4.device.Batch(_ptrn(labels), 4, 4, 4, trip, precision=a4.device.PREC_OZAKI_BF16, slices=5)
     b.run_graph()
     b.run_graph()
     a4.device.sync()
     assert torch.equal(first, R.buf)
     # beta = 1 accumulates on top of the existing blocks
     base = R.buf.clone()
-    bb = a4.device.Batch(_ptrn(labels), 4, 4, 4, trip, precision=a4.device.PREC_OZAKI_BF16, slices=6, beta=1)
+    bb = a4.device.Batch(_ptrn(labels), 4, 4, 4, trip, precision=a4.device.PREC_OZAKI_BF16, slices=5, beta=1)
     bb.run()
     a4.device.sync()
     for k, want in ref.items():
@@ -207,7 +207,7 @@ def test_split_odd_extents_non_vector_paths(a4):
     # 2 or 4 exercise the scalar branches of the layout-specialised kernels
     R, V, T, trip, labels = _make(a4, "ladder", [5, 7, 9], [3, 5], 0.2, 8)
     ref = _reference(R, trip, labels)
-    _run(a4, R, trip, labels, a4.device.PREC_OZAKI_BF16, slices=6)
+    _run(a4, R, trip, labels, a4.device.PREC_OZAKI_BF16, slices=5)
     assert _errors(R, ref).max() <= TOL_SPLIT
     R2, V2, T2, trip2, labels2 = _make(a4, "ladder", [5, 7, 9], [3, 5], 0.2, 8, integer=True)
     _run(a4, R2, trip2, labels2, a4.device.PREC_OZAKI_BF16, slices=1)
