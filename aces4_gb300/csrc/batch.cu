@@ -54,7 +54,7 @@ struct a4g_batch {
   OzTile* d_tiles = nullptr;
   int n_tiles = 0;
   OzDBlock* d_dblocks = nullptr;
-  float2* d_ws = nullptr;
+  int* d_ws = nullptr;
   OzGemmArgs gemm{};
   int grid = 0;
   int nsplit = 1;
@@ -307,17 +307,21 @@ int build_ozaki(a4g_batch* b, const std::vector<DGroup>& groups, const std::vect
       (rc = upload(b, trips, &d_trips)) || (rc = upload(b, dblocks, &b->d_dblocks)))
     return rc;
   b->n_tiles = int(tiles.size());
-  // Split-K: the smallest split count that gives every SM the same number of
-  // equal units per level (so the CTAs stay in step through the k panels),
-  // keeping at least 16 k blocks per unit and the workspace below 6 GB.
+  // Split-K: units short enough that a level sum of one unit stays below 2^31
+  // (slices * 128^2 * K_unit < 2^31, written as int32), then the smallest split
+  // count that gives every SM the same number of equal units per level (the
+  // CTAs then stay in step through the k panels), keeping at least 16 k
+  // blocks per unit and the workspace below 6 GB.
   const int P = ctx()->num_sms;
-  int min_kb = 1 << 30;
-  for (const OzTile& t : tiles) min_kb = std::min(min_kb, t.kb_total);
-  int nsplit = 1;
+  const int max_unit_kb = int(((1LL << 31) - 1) / (int64_t(S) * 128 * 128 * kOzBK));
+  int min_kb = 1 << 30, max_kb = 0;
+  for (const OzTile& t : tiles) min_kb = std::min(min_kb, t.kb_total), max_kb = std::max(max_kb, t.kb_total);
+  const int ns_min = std::max(1, (max_kb + max_unit_kb - 1) / max_unit_kb);
+  int nsplit = ns_min;
   double best = -1.0;
-  for (int ns = 1; ns <= 64; ++ns) {
-    if (ns > 1 && min_kb / ns < 16) break;
-    if (double(b->n_tiles) * S * ns * kOzBM * kOzBN * sizeof(float2) > 6.0 * (1u << 30)) break;
+  for (int ns = ns_min; ns <= std::max(64, ns_min); ++ns) {
+    if (ns > ns_min && min_kb / ns < 16) break;
+    if (ns > ns_min && double(b->n_tiles) * S * ns * kOzBM * kOzBN * sizeof(int) > 6.0 * (1u << 30)) break;
     const int64_t units = int64_t(b->n_tiles) * ns;
     const double eff = double(units) / double(P * ((units + P - 1) / P));
     if (eff > best + 1e-9) best = eff, nsplit = ns;
@@ -342,9 +346,9 @@ int build_ozaki(a4g_batch* b, const std::vector<DGroup>& groups, const std::vect
   OzUnit* d_units = nullptr;
   if ((rc = upload(b, units, &d_units))) return rc;
   void* ws = nullptr;
-  if ((rc = device_alloc(b, size_t(b->n_tiles) * S * nsplit * kOzBM * kOzBN * sizeof(float2), &ws, false)))
+  if ((rc = device_alloc(b, size_t(b->n_tiles) * S * nsplit * kOzBM * kOzBN * sizeof(int), &ws, false)))
     return rc;
-  b->d_ws = static_cast<float2*>(ws);
+  b->d_ws = static_cast<int*>(ws);
   OzGemmArgs& ga = b->gemm;
   ga.maps_a = dmaps_a, ga.maps_b = dmaps_b;
   ga.panels_a = b->d_pa, ga.panels_b = b->d_pb;

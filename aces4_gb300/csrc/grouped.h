@@ -112,7 +112,7 @@ struct OzGemmArgs {
   int slices;
   int nsplit;
   int chunk_kb[kOzMaxSlices];  // k blocks per exact flush at each level
-  float2* ws;                  // [tile][level][split][col 128][row 128] (hi, lo)
+  int* ws;                     // [tile][level][split][col 128][row 128] exact integer level sums
   int* err_flag;
 };
 

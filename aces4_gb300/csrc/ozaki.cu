@@ -33,6 +33,8 @@
 #include <cuda_bf16.h>
 #include <cudaTypedefs.h>
 
+#include <type_traits>
+
 #include "a4g_internal.h"
 #include "grouped.h"
 #include "ozaki.h"
@@ -300,8 +302,13 @@ __device__ void epilogue(const OzGemmArgs& a, OzSmem& sm, uint32_t tmem, int war
     const OzUnit un = a.units[u];
     const int ckb = a.chunk_kb[un.level];
     const int nchunks = (un.kb_end - un.kb_begin + ckb - 1) / ckb;
-    float2* w = a.ws + ((size_t(un.tile) * a.slices + un.level) * a.nsplit + un.split) * kOzBN * kOzBM +
-                size_t(64 * h) * kOzBM + row;
+    int* w = a.ws + ((size_t(un.tile) * a.slices + un.level) * a.nsplit + un.split) * kOzBN * kOzBM +
+             size_t(64 * h) * kOzBM + row;
+    if (nchunks == 0) {  // empty k range: its partial sum is zero
+#pragma unroll 8
+      for (int j = 0; j < 64; ++j) w[size_t(j) * kOzBM] = 0;
+      continue;
+    }
     for (int c = 0; c < nchunks; ++c) {
       const uint32_t buf = chunk & 1;
       if (!mbar_wait(&sm.acc_full[buf], (chunk >> 1) & 1, sm, a.err_flag, 4)) return;
@@ -331,9 +338,12 @@ __device__ void epilogue(const OzGemmArgs& a, OzSmem& sm, uint32_t tmem, int war
           tc_st32(lane_addr + kTmemHi + 32 * g, hi);
           tc_st32(lane_addr + kTmemLo + 32 * g, lo);
         } else {
+          // hi + lo is the unit's exact level sum, an integer below 2^31 (the
+          // host sizes units for that), stored as int32
 #pragma unroll
           for (int j = 0; j < 32; ++j)
-            w[size_t(32 * g + j) * kOzBM] = make_float2(__uint_as_float(hi[j]), __uint_as_float(lo[j]));
+            w[size_t(32 * g + j) * kOzBM] =
+                int(static_cast<long long>(__uint_as_float(hi[j])) + static_cast<long long>(__uint_as_float(lo[j])));
         }
       }
       if (!last) tc_wait_st();
@@ -466,17 +476,40 @@ __device__ __forceinline__ long long quantize(unsigned long long bits, int mx, i
 }
 
 // Balanced base-256 digits of n, most significant first: d[0] in [-128, 128],
-// the others in [-128, 127]; sum_i d[i] * 256^(slices-1-i) == n.
-__device__ __forceinline__ void balanced_digits(long long n, int slices, int (&d)[kOzMaxSlices]) {
+// the others in [-128, 127]; sum_i d[i] * 256^(S-1-i) == n.  The low 24 bits
+// give up to three digits with 32-bit arithmetic; the rest (|n| < 2^47 for up
+// to 6 slices) also stays in 32 bits, only 7 slices need 64-bit steps.  S is
+// a compile-time constant so every digit lives in a register.
+template <int S>
+__device__ __forceinline__ void balanced_digits(long long n, int (&d)[S]) {
+  constexpr int K = S - 1 < 3 ? S - 1 : 3;  // digits taken from the low 24 bits
+  int x = int(n & 0xFFFFFF);
+  const long long hi = n >> 24;  // arithmetic shift: n == hi * 2^24 + x
 #pragma unroll
-  for (int i = kOzMaxSlices - 1; i >= 1; --i) {
-    if (i < slices) {
-      const long long r = ((n + 128) & 255) - 128;
-      d[i] = int(r);
-      n = (n - r) >> 8;
-    }
+  for (int t = 0; t < K; ++t) {
+    const int r = ((x + 128) & 255) - 128;
+    d[S - 1 - t] = r;
+    x = (x - r) >> 8;
   }
-  d[0] = int(n);
+  if constexpr (S <= 6) {
+    int rem = int(hi << (24 - 8 * K)) + x;
+#pragma unroll
+    for (int t = K; t < S - 1; ++t) {
+      const int r = ((rem + 128) & 255) - 128;
+      d[S - 1 - t] = r;
+      rem = (rem - r) >> 8;
+    }
+    d[0] = rem;
+  } else {
+    long long rem = (hi << (24 - 8 * K)) + x;
+#pragma unroll
+    for (int t = K; t < S - 1; ++t) {
+      const long long r = ((rem + 128) & 255) - 128;
+      d[S - 1 - t] = int(r);
+      rem = (rem - r) >> 8;
+    }
+    d[0] = int(rem);
+  }
 }
 
 // Exact BF16 bits of two digits in [-128, 128]: float(d) is formed exactly as
@@ -489,9 +522,11 @@ __device__ __forceinline__ uint32_t digits_bf16x2(int d0, int d1) {
   return *reinterpret_cast<uint32_t*>(&h);
 }
 
+template <int S>
 __global__ void __launch_bounds__(256) oz_split_kernel(const OzSplitJob* __restrict__ jobs,
                                                        const int64_t* __restrict__ prefix, int njobs,
-                                                       const OzPanel* __restrict__ panels, int slices) {
+                                                       const OzPanel* __restrict__ panels) {
+  constexpr int slices = S;
   __shared__ unsigned long long tile[kSplitT][kSplitT + 1];
   const int64_t t = blockIdx.x;
   const int j = find_job(prefix, njobs, t);
@@ -511,14 +546,13 @@ __global__ void __launch_bounds__(256) oz_split_kernel(const OzSplitJob* __restr
     if (k0 + k >= jb.K) continue;
     const int mx = pn.exps[r0 + r];
     const unsigned long long b0 = tile[r][k], b1 = (k0 + k + 1 < jb.K) ? tile[r][k + 1] : 0ull;
-    int d0[kOzMaxSlices], d1[kOzMaxSlices];
-    balanced_digits(quantize(b0, mx, slices), slices, d0);
-    balanced_digits(quantize(b1, mx, slices), slices, d1);
+    int d0[S], d1[S];
+    balanced_digits<S>(quantize(b0, mx, S), d0);
+    balanced_digits<S>(quantize(b1, mx, S), d1);
     uint32_t* dst = reinterpret_cast<uint32_t*>(pn.base + (size_t(r0 + r) * pn.kpad + jb.koff + k0 + k));
     const size_t slice_stride = size_t(pn.rows_pad) * pn.kpad / 2;
 #pragma unroll
-    for (int i = 0; i < kOzMaxSlices; ++i)
-      if (i < slices) dst[i * slice_stride] = digits_bf16x2(d0[i], d1[i]);
+    for (int i = 0; i < S; ++i) dst[i * slice_stride] = digits_bf16x2(d0[i], d1[i]);
   }
 }
 
@@ -592,9 +626,10 @@ __global__ void __launch_bounds__(256) oz_exp_kmaj_kernel(const OzSplitJob* __re
 
 // Slices of a [K x rows] block: one warp per row, each lane four consecutive k
 // (two 16-byte loads, one 8-byte store per slice).
+template <int S>
 __global__ void __launch_bounds__(256) oz_split_kmaj_kernel(const OzSplitJob* __restrict__ jobs,
                                                             const int64_t* __restrict__ prefix, int njobs,
-                                                            const OzPanel* __restrict__ panels, int slices) {
+                                                            const OzPanel* __restrict__ panels) {
   const int j = find_job(prefix, njobs, blockIdx.x);
   const OzSplitJob jb = jobs[j];
   const int64_t local = int64_t(blockIdx.x) - prefix[j];
@@ -618,12 +653,11 @@ __global__ void __launch_bounds__(256) oz_split_kmaj_kernel(const OzSplitJob* __
 #pragma unroll
       for (int t = 0; t < 4; ++t) b[t] = k + t < jb.K ? __double_as_longlong(__ldg(row + k + t)) : 0ull;
     }
-    int d[4][kOzMaxSlices];
+    int d[4][S];
 #pragma unroll
-    for (int t = 0; t < 4; ++t) balanced_digits(quantize(b[t], mx, slices), slices, d[t]);
+    for (int t = 0; t < 4; ++t) balanced_digits<S>(quantize(b[t], mx, S), d[t]);
 #pragma unroll
-    for (int i = 0; i < kOzMaxSlices; ++i) {
-      if (i >= slices) break;
+    for (int i = 0; i < S; ++i) {
       uint2 o;
       o.x = digits_bf16x2(d[0][i], d[1][i]);
       o.y = digits_bf16x2(d[2][i], d[3][i]);
@@ -634,9 +668,10 @@ __global__ void __launch_bounds__(256) oz_split_kmaj_kernel(const OzSplitJob* __
 
 // Slices of a column-major [rows x K] block: 64x64 tiles transposed through
 // shared memory (16-byte loads along rows, 8-byte stores along k).
+template <int S>
 __global__ void __launch_bounds__(256) oz_split_rows_kernel(const OzSplitJob* __restrict__ jobs,
                                                             const int64_t* __restrict__ prefix, int njobs,
-                                                            const OzPanel* __restrict__ panels, int slices) {
+                                                            const OzPanel* __restrict__ panels) {
   __shared__ unsigned long long tile[64][65];
   const int j = find_job(prefix, njobs, blockIdx.x);
   const OzSplitJob jb = jobs[j];
@@ -673,16 +708,15 @@ __global__ void __launch_bounds__(256) oz_split_rows_kernel(const OzSplitJob* __
     const int kq = t & 15, r = (t >> 4) + 16 * p;
     if (r0 + r >= jb.rows || k0 + 4 * kq >= jb.K) continue;
     const int mx = pn.exps[r0 + r];
-    int d[4][kOzMaxSlices];
+    int d[4][S];
 #pragma unroll
     for (int u = 0; u < 4; ++u) {
       const unsigned long long b = (k0 + 4 * kq + u < jb.K) ? tile[r][4 * kq + u] : 0ull;
-      balanced_digits(quantize(b, mx, slices), slices, d[u]);
+      balanced_digits<S>(quantize(b, mx, S), d[u]);
     }
     uint2* dst = reinterpret_cast<uint2*>(pn.base + (size_t(r0 + r) * pn.kpad + jb.koff + k0 + 4 * kq));
 #pragma unroll
-    for (int i = 0; i < kOzMaxSlices; ++i) {
-      if (i >= slices) break;
+    for (int i = 0; i < S; ++i) {
       uint2 o;
       o.x = digits_bf16x2(d[0][i], d[1][i]);
       o.y = digits_bf16x2(d[2][i], d[3][i]);
@@ -700,7 +734,7 @@ __global__ void __launch_bounds__(256) oz_recombine_kernel(const OzTile* __restr
                                                            const PlanRef* __restrict__ plans,
                                                            const OzPanel* __restrict__ pa,
                                                            const OzPanel* __restrict__ pb,
-                                                           const float2* __restrict__ ws, int slices,
+                                                           const int* __restrict__ ws, int slices,
                                                            int nsplit, int beta) {
   const int tile = blockIdx.x >> 6;
   const int e = ((blockIdx.x & 63) << 8) + threadIdx.x;
@@ -714,21 +748,16 @@ __global__ void __launch_bounds__(256) oz_recombine_kernel(const OzTile* __restr
   const int* eb = pb[tl.panel_b].exps;
   double v = 0.0;
   for (int lv = slices - 1; lv >= 0; --lv) {
-    const float2* p = ws + ((size_t(tile) * slices + lv) * nsplit * kOzBN + col) * kOzBM + row;
-    double s0 = 0.0, s1 = 0.0;
+    const int* p = ws + ((size_t(tile) * slices + lv) * nsplit * kOzBN + col) * kOzBM + row;
+    long long s0 = 0, s1 = 0;  // exact
     int sp = 0;
 #pragma unroll 4
     for (; sp + 1 < nsplit; sp += 2) {
-      const float2 x = __ldg(p + size_t(sp) * kOzBN * kOzBM);
-      const float2 y = __ldg(p + size_t(sp + 1) * kOzBN * kOzBM);
-      s0 += double(x.x) + double(x.y);
-      s1 += double(y.x) + double(y.y);
+      s0 += __ldg(p + size_t(sp) * kOzBN * kOzBM);
+      s1 += __ldg(p + size_t(sp + 1) * kOzBN * kOzBM);
     }
-    if (sp < nsplit) {
-      const float2 x = __ldg(p + size_t(sp) * kOzBN * kOzBM);
-      s0 += double(x.x) + double(x.y);
-    }
-    v += ldexp(s0 + s1, -kDigitBits * (lv + 2));
+    if (sp < nsplit) s0 += __ldg(p + size_t(sp) * kOzBN * kOzBM);
+    v += ldexp(double(s0 + s1), -kDigitBits * (lv + 2));  // exact: |sum| < 2^53
   }
   const int E = (ea[m] ? ea[m] : 1) - 1022, F = (eb[n] ? eb[n] : 1) - 1022;
   v = ldexp(v, E + F + 2);
@@ -803,12 +832,22 @@ int oz_launch_split(int layout, const OzSplitJob* jobs, const int64_t* prefix, i
                     const OzPanel* panels, int slices, cudaStream_t s) {
   if (ntiles <= 0) return A4G_OK;
   if (ntiles > 0x7fffffffLL) return fail(A4G_ERR_RANGE, "too many split tiles");
-  if (layout == kOzRowsMajor)
-    oz_split_rows_kernel<<<unsigned(ntiles), 256, 0, s>>>(jobs, prefix, njobs, panels, slices);
-  else if (layout == kOzKMajor)
-    oz_split_kmaj_kernel<<<unsigned(ntiles), 256, 0, s>>>(jobs, prefix, njobs, panels, slices);
-  else
-    oz_split_kernel<<<unsigned(ntiles), 256, 0, s>>>(jobs, prefix, njobs, panels, slices);
+  auto go = [&](auto sc) {
+    constexpr int S = decltype(sc)::value;
+    if (layout == kOzRowsMajor) oz_split_rows_kernel<S><<<unsigned(ntiles), 256, 0, s>>>(jobs, prefix, njobs, panels);
+    else if (layout == kOzKMajor) oz_split_kmaj_kernel<S><<<unsigned(ntiles), 256, 0, s>>>(jobs, prefix, njobs, panels);
+    else oz_split_kernel<S><<<unsigned(ntiles), 256, 0, s>>>(jobs, prefix, njobs, panels);
+  };
+  switch (slices) {
+    case 1: go(std::integral_constant<int, 1>()); break;
+    case 2: go(std::integral_constant<int, 2>()); break;
+    case 3: go(std::integral_constant<int, 3>()); break;
+    case 4: go(std::integral_constant<int, 4>()); break;
+    case 5: go(std::integral_constant<int, 5>()); break;
+    case 6: go(std::integral_constant<int, 6>()); break;
+    case 7: go(std::integral_constant<int, 7>()); break;
+    default: return fail(A4G_ERR_ARG, "slices must be 1..7");
+  }
   A4G_CUDA(cudaGetLastError());
   return A4G_OK;
 }
@@ -836,7 +875,7 @@ int oz_launch_gemm(const OzGemmArgs& args, int grid, cudaStream_t s) {
 }
 
 int oz_launch_recombine(const OzTile* tiles, int ntiles, const OzDBlock* dblocks, const PlanRef* plans,
-                        const OzPanel* pa, const OzPanel* pb, const float2* ws, int slices, int nsplit,
+                        const OzPanel* pa, const OzPanel* pb, const int* ws, int slices, int nsplit,
                         int beta, cudaStream_t s) {
   if (ntiles <= 0) return A4G_OK;
   if (int64_t(ntiles) * 64 > 0x7fffffffLL) return fail(A4G_ERR_RANGE, "too many tiles");

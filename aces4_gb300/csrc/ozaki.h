@@ -19,7 +19,7 @@ int oz_launch_split(int layout, const OzSplitJob* jobs, const int64_t* prefix, i
                     const OzPanel* panels, int slices, cudaStream_t s);
 int oz_launch_gemm(const OzGemmArgs& args, int grid, cudaStream_t s);
 int oz_launch_recombine(const OzTile* tiles, int ntiles, const OzDBlock* dblocks, const PlanRef* plans,
-                        const OzPanel* pa, const OzPanel* pb, const float2* ws, int slices, int nsplit,
+                        const OzPanel* pa, const OzPanel* pb, const int* ws, int slices, int nsplit,
                         int beta, cudaStream_t s);
 
 }  // namespace a4g
