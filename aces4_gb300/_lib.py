@@ -74,6 +74,7 @@ SIGNATURES = {
     "a4g_batch_run_timed": (ctypes.c_int, [c_void_p, c_void_p]),
     "a4g_batch_timings": (ctypes.c_int, None),
     "a4g_batch_info": (ctypes.c_int, None),
+    "a4g_batch_form": (ctypes.c_int, None),
     "a4g_batch_destroy": (None, [c_void_p]),
 }
 

@@ -24,6 +24,7 @@ struct a4g_batch {
   int precision = A4G_PREC_FP64;
   int slices = 5;
   int beta = 0;
+  int variant = 0;  // tensor-core GEMM form: 0 autotuned, 1 one SM per tile, 2 CTA pair per tile
   int64_t pairs = 0;
   double flops = 0.0;
   int64_t device_bytes = 0;
@@ -51,13 +52,22 @@ struct a4g_batch {
     int64_t tiles_exp = 0, tiles_split = 0;
   };
   std::vector<JobSet> jobsets;
-  OzTile* d_tiles = nullptr;
-  int n_tiles = 0;
   OzDBlock* d_dblocks = nullptr;
+  // Tensor-core GEMM forms: [0] 1-SM 128x128 tiles, [1] CTA-pair 256x128 tiles.
+  struct GemmForm {
+    bool pair = false;
+    bool built = false;
+    int tile_rows = 128;
+    OzTile* d_tiles = nullptr;
+    int n_tiles = 0;
+    int nsplit = 1;
+    int grid = 0;
+    OzGemmArgs args{};
+    float tuned_ms = -1.f;
+  };
+  GemmForm forms[2];
+  int form = 0;  // the form run() uses (chosen by the autotuner or the caller)
   int* d_ws = nullptr;
-  OzGemmArgs gemm{};
-  int grid = 0;
-  int nsplit = 1;
   cudaGraphExec_t graph = nullptr;
   // phase timing: events[run][6] recorded by a4g_batch_run_timed
   std::vector<std::vector<cudaEvent_t>> events;
@@ -181,7 +191,7 @@ int build_ozaki(a4g_batch* b, const std::vector<DGroup>& groups, const std::vect
   std::vector<PanelBuild> pa, pb;
   std::map<std::vector<const double*>, int> ia, ib;
   std::vector<OzDBlock> dblocks;
-  std::vector<OzTile> tiles;
+  std::vector<OzTile> dinfo;  // one per destination block: m0 = M, n0 = N (tiles are cut per form)
   std::vector<OzTrip> trips;
   for (const DGroup& g : groups) {
     const GemmPlan& h = plans[g.plan]->host;
@@ -199,18 +209,16 @@ int build_ozaki(a4g_batch* b, const std::vector<DGroup>& groups, const std::vect
       kb_total += nkb;
     }
     const int te = int(trips.size());
-    for (int64_t n0 = 0; n0 < h.N; n0 += kOzBN)
-      for (int64_t m0 = 0; m0 < h.M; m0 += kOzBM)
-        tiles.push_back({db, int(m0), int(n0), a, c, tb, te, kb_total});
+    dinfo.push_back({db, int(h.M), int(h.N), a, c, tb, te, kb_total});
   }
   const int S = b->slices;
   int rc0 = oz_prepare();
   if (rc0) return rc0;
   // panels: slices (BF16, zero padded), exponents, tensor maps
   std::vector<OzPanel> hpa, hpb;
-  std::vector<MapBytes> maps_a(pa.size()), maps_b(pb.size());
+  std::vector<MapBytes> maps_a(pa.size()), maps_b(pb.size()), maps_b2(pb.size());
   size_t exps_total = 0;
-  for (auto& p : pa) exps_total += ceil_to(p.rows, kOzBM);
+  for (auto& p : pa) exps_total += ceil_to(p.rows, 2 * kOzBM);
   for (auto& p : pb) exps_total += ceil_to(p.rows, kOzBN);
   void* exps = nullptr;
   int rc = device_alloc(b, exps_total * sizeof(int), &exps, true);
@@ -218,8 +226,10 @@ int build_ozaki(a4g_batch* b, const std::vector<DGroup>& groups, const std::vect
   b->d_exps = static_cast<int*>(exps);
   b->exps_bytes = exps_total * sizeof(int);
   size_t eoff = 0;
+  // A panels are padded to 256 rows (either tile form), B panels to 128; B
+  // panels get a second descriptor with 64-row boxes for the CTA-pair form.
   auto make_panels = [&](std::vector<PanelBuild>& src, std::vector<OzPanel>& dst, std::vector<MapBytes>& maps,
-                         int rows_tile) -> int {
+                         std::vector<MapBytes>* maps2, int rows_tile) -> int {
     for (size_t i = 0; i < src.size(); ++i) {
       OzPanel p{};
       p.rows = src[i].rows;
@@ -232,14 +242,16 @@ int build_ozaki(a4g_batch* b, const std::vector<DGroup>& groups, const std::vect
       p.base = static_cast<__nv_bfloat16*>(mem);
       p.exps = b->d_exps + eoff;
       eoff += p.rows_pad;
-      r = oz_make_tensor_map(maps[i].b, mem, p.kpad, int64_t(S) * p.rows_pad);
+      r = oz_make_tensor_map(maps[i].b, mem, p.kpad, int64_t(S) * p.rows_pad, kOzBM);
       if (r) return r;
+      if (maps2 && (r = oz_make_tensor_map((*maps2)[i].b, mem, p.kpad, int64_t(S) * p.rows_pad, kOzBN / 2)))
+        return r;
       dst.push_back(p);
     }
     return A4G_OK;
   };
-  if ((rc = make_panels(pa, hpa, maps_a, kOzBM))) return rc;
-  if ((rc = make_panels(pb, hpb, maps_b, kOzBN))) return rc;
+  if ((rc = make_panels(pa, hpa, maps_a, nullptr, 2 * kOzBM))) return rc;
+  if ((rc = make_panels(pb, hpb, maps_b, &maps_b2, kOzBN))) return rc;
   for (auto& p : hpa)
     if (p.kpad > 0x7fffffffLL || int64_t(S) * p.rows_pad > 0x7fffffffLL)
       return fail(A4G_ERR_RANGE, "panel exceeds TMA coordinate range");
@@ -296,74 +308,119 @@ int build_ozaki(a4g_batch* b, const std::vector<DGroup>& groups, const std::vect
       b->jobsets.push_back(js);
     }
   }
-  void *dmaps_a = nullptr, *dmaps_b = nullptr;
+  void *dmaps_a = nullptr, *dmaps_b = nullptr, *dmaps_b2 = nullptr;
   const size_t mbytes_a = maps_a.size() * sizeof(MapBytes), mbytes_b = maps_b.size() * sizeof(MapBytes);
   if ((rc = device_alloc(b, mbytes_a, &dmaps_a, false))) return rc;
   if ((rc = device_alloc(b, mbytes_b, &dmaps_b, false))) return rc;
+  if ((rc = device_alloc(b, mbytes_b, &dmaps_b2, false))) return rc;
   A4G_CUDA(cudaMemcpy(dmaps_a, maps_a.data(), mbytes_a, cudaMemcpyHostToDevice));
   A4G_CUDA(cudaMemcpy(dmaps_b, maps_b.data(), mbytes_b, cudaMemcpyHostToDevice));
+  A4G_CUDA(cudaMemcpy(dmaps_b2, maps_b2.data(), mbytes_b, cudaMemcpyHostToDevice));
   OzTrip* d_trips = nullptr;
-  if ((rc = upload(b, hpa, &b->d_pa)) || (rc = upload(b, hpb, &b->d_pb)) || (rc = upload(b, tiles, &b->d_tiles)) ||
-      (rc = upload(b, trips, &d_trips)) || (rc = upload(b, dblocks, &b->d_dblocks)))
+  if ((rc = upload(b, hpa, &b->d_pa)) || (rc = upload(b, hpb, &b->d_pb)) || (rc = upload(b, trips, &d_trips)) ||
+      (rc = upload(b, dblocks, &b->d_dblocks)))
     return rc;
-  b->n_tiles = int(tiles.size());
-  // Split-K: units short enough that a level sum of one unit stays below 2^31
-  // (slices * 128^2 * K_unit < 2^31, written as int32), then the smallest split
-  // count that gives every SM the same number of equal units per level (the
-  // CTAs then stay in step through the k panels), keeping at least 16 k
-  // blocks per unit and the workspace below 6 GB.
-  const int P = ctx()->num_sms;
-  const int max_unit_kb = int(((1LL << 31) - 1) / (int64_t(S) * 128 * 128 * kOzBK));
-  int min_kb = 1 << 30, max_kb = 0;
-  for (const OzTile& t : tiles) min_kb = std::min(min_kb, t.kb_total), max_kb = std::max(max_kb, t.kb_total);
-  const int ns_min = std::max(1, (max_kb + max_unit_kb - 1) / max_unit_kb);
-  int nsplit = ns_min;
-  double best = -1.0;
-  for (int ns = ns_min; ns <= std::max(64, ns_min); ++ns) {
-    if (ns > ns_min && min_kb / ns < 16) break;
-    if (ns > ns_min && double(b->n_tiles) * S * ns * kOzBM * kOzBN * sizeof(int) > 6.0 * (1u << 30)) break;
-    const int64_t units = int64_t(b->n_tiles) * ns;
-    const double eff = double(units) / double(P * ((units + P - 1) / P));
-    if (eff > best + 1e-9) best = eff, nsplit = ns;
-    if (eff >= 0.999) break;
-  }
-  b->nsplit = nsplit;
-  std::vector<OzUnit> units;
-  for (int lv = 0; lv < S; ++lv)
-    for (int sp = 0; sp < nsplit; ++sp)
-      for (int ti = 0; ti < b->n_tiles; ++ti) {
-        const OzTile& t = tiles[ti];
-        OzUnit u{};
-        u.tile = ti, u.level = lv, u.split = sp;
-        u.kb_begin = int(int64_t(t.kb_total) * sp / nsplit);
-        u.kb_end = int(int64_t(t.kb_total) * (sp + 1) / nsplit);
-        int acc = 0, q = t.trip_begin;
-        while (q < t.trip_end && acc + trips[q].nkb <= u.kb_begin) acc += trips[q].nkb, ++q;
-        u.trip_first = q;
-        u.kb_in_trip = u.kb_begin - acc;
-        units.push_back(u);
-      }
-  OzUnit* d_units = nullptr;
-  if ((rc = upload(b, units, &d_units))) return rc;
-  void* ws = nullptr;
-  if ((rc = device_alloc(b, size_t(b->n_tiles) * S * nsplit * kOzBM * kOzBN * sizeof(int), &ws, false)))
-    return rc;
-  b->d_ws = static_cast<int*>(ws);
-  OzGemmArgs& ga = b->gemm;
-  ga.maps_a = dmaps_a, ga.maps_b = dmaps_b;
-  ga.panels_a = b->d_pa, ga.panels_b = b->d_pb;
-  ga.tiles = b->d_tiles, ga.trips = d_trips;
-  ga.n_tiles = b->n_tiles;
-  ga.units = d_units;
-  ga.n_units = int(units.size());
-  ga.slices = S;
-  ga.nsplit = nsplit;
-  for (int t = 0; t < kOzMaxSlices; ++t) ga.chunk_kb[t] = t < S ? oz_chunk_kb(t) : 1;
   for (int t = 0; t < S; ++t)
-    if (ga.chunk_kb[t] < 1) return fail(A4G_ERR_ARG, "slice count too large for exact accumulation");
-  ga.ws = b->d_ws;
-  ga.err_flag = ctx()->d_error_flag;
-  b->grid = std::min(ga.n_units, ctx()->num_sms);
+    if (oz_chunk_kb(t) < 1) return fail(A4G_ERR_ARG, "slice count too large for exact accumulation");
+  int pairs = 0;
+  if ((rc = oz_max_pairs(&pairs))) return rc;
+  size_t ws_elems = 0;
+  std::vector<std::vector<OzTile>> form_tiles(2);
+  std::vector<std::vector<OzUnit>> form_units(2);
+  for (int f = 0; f < 2; ++f) {
+    a4g_batch::GemmForm& gf = b->forms[f];
+    gf.pair = f == 1;
+    gf.tile_rows = gf.pair ? 2 * kOzBM : kOzBM;
+    const int P = gf.pair ? pairs : ctx()->num_sms;  // concurrent workers (CTAs or CTA pairs)
+    if (P < 1 || (b->variant && b->variant != f + 1)) continue;
+    std::vector<OzTile>& tiles = form_tiles[f];
+    for (const OzTile& di : dinfo)
+      for (int64_t n0 = 0; n0 < di.n0; n0 += kOzBN)
+        for (int64_t m0 = 0; m0 < di.m0; m0 += gf.tile_rows)
+          tiles.push_back({di.dblock, int(m0), int(n0), di.panel_a, di.panel_b, di.trip_begin, di.trip_end,
+                           di.kb_total});
+    gf.n_tiles = int(tiles.size());
+    // Split-K: units short enough that a level sum of one unit stays below
+    // 2^31 (slices * 128^2 * K_unit < 2^31, written as int32), then the
+    // smallest split count that gives every worker the same number of equal
+    // units per level (the workers then stay in step through the k panels),
+    // keeping at least 16 k blocks per unit and the workspace below 6 GB.
+    const int max_unit_kb = int(((1LL << 31) - 1) / (int64_t(S) * 128 * 128 * kOzBK));
+    int min_kb = 1 << 30, max_kb = 0;
+    for (const OzTile& t : tiles) min_kb = std::min(min_kb, t.kb_total), max_kb = std::max(max_kb, t.kb_total);
+    const int ns_min = std::max(1, (max_kb + max_unit_kb - 1) / max_unit_kb);
+    const double tile_bytes = double(gf.tile_rows) * kOzBN * sizeof(int);
+    int nsplit = ns_min;
+    double best = -1.0;
+    for (int ns = ns_min; ns <= std::max(64, ns_min); ++ns) {
+      if (ns > ns_min && min_kb / ns < 16) break;
+      if (ns > ns_min && double(gf.n_tiles) * S * ns * tile_bytes > 6.0 * (1u << 30)) break;
+      const int64_t units = int64_t(gf.n_tiles) * ns;
+      const double eff = double(units) / double(P * ((units + P - 1) / P));
+      if (eff > best + 1e-9) best = eff, nsplit = ns;
+      if (eff >= 0.999) break;
+    }
+    gf.nsplit = nsplit;
+    std::vector<OzUnit>& units = form_units[f];
+    for (int lv = 0; lv < S; ++lv)
+      for (int sp = 0; sp < nsplit; ++sp)
+        for (int ti = 0; ti < gf.n_tiles; ++ti) {
+          const OzTile& t = tiles[ti];
+          OzUnit u{};
+          u.tile = ti, u.level = lv, u.split = sp;
+          u.kb_begin = int(int64_t(t.kb_total) * sp / nsplit);
+          u.kb_end = int(int64_t(t.kb_total) * (sp + 1) / nsplit);
+          int acc = 0, q = t.trip_begin;
+          while (q < t.trip_end && acc + trips[q].nkb <= u.kb_begin) acc += trips[q].nkb, ++q;
+          u.trip_first = q;
+          u.kb_in_trip = u.kb_begin - acc;
+          units.push_back(u);
+        }
+    ws_elems = std::max(ws_elems, size_t(gf.n_tiles) * S * nsplit * gf.tile_rows * kOzBN);
+    OzUnit* d_units = nullptr;
+    if ((rc = upload(b, tiles, &gf.d_tiles)) || (rc = upload(b, units, &d_units))) return rc;
+    OzGemmArgs& ga = gf.args;
+    ga.maps_a = dmaps_a, ga.maps_b = gf.pair ? dmaps_b2 : dmaps_b;
+    ga.panels_a = b->d_pa, ga.panels_b = b->d_pb;
+    ga.tiles = gf.d_tiles, ga.trips = d_trips;
+    ga.n_tiles = gf.n_tiles;
+    ga.units = d_units;
+    ga.n_units = int(units.size());
+    ga.slices = S;
+    ga.nsplit = nsplit;
+    for (int t = 0; t < kOzMaxSlices; ++t) ga.chunk_kb[t] = t < S ? oz_chunk_kb(t) : 1;
+    ga.err_flag = ctx()->d_error_flag;
+    gf.grid = gf.pair ? 2 * std::min(ga.n_units, pairs) : std::min(ga.n_units, ctx()->num_sms);
+    gf.built = true;
+  }
+  void* ws = nullptr;
+  if ((rc = device_alloc(b, ws_elems * sizeof(int), &ws, false))) return rc;
+  b->d_ws = static_cast<int*>(ws);
+  for (auto& gf : b->forms) gf.args.ws = b->d_ws;
+  b->form = b->forms[1].built && b->variant == 2 ? 1 : 0;
+  if (!b->forms[b->form].built) b->form = b->forms[0].built ? 0 : 1;
+  if (!b->variant && b->forms[0].built && b->forms[1].built) {
+    // autotune: time each form's GEMM once (after one untimed run) on this
+    // batch's panels and keep the faster
+    cudaStream_t s = ctx()->stream;
+    cudaEvent_t e0, e1;
+    A4G_CUDA(cudaEventCreate(&e0));
+    A4G_CUDA(cudaEventCreate(&e1));
+    for (int f = 0; f < 2; ++f) {
+      a4g_batch::GemmForm& gf = b->forms[f];
+      if ((rc = oz_launch_gemm(gf.args, gf.grid, gf.pair, s))) break;
+      A4G_CUDA(cudaEventRecord(e0, s));
+      if ((rc = oz_launch_gemm(gf.args, gf.grid, gf.pair, s))) break;
+      A4G_CUDA(cudaEventRecord(e1, s));
+      A4G_CUDA(cudaEventSynchronize(e1));
+      A4G_CUDA(cudaEventElapsedTime(&gf.tuned_ms, e0, e1));
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (rc) return rc;
+    if ((rc = check_device_flag(s))) return rc;
+    b->form = b->forms[1].tuned_ms < b->forms[0].tuned_ms ? 1 : 0;
+  }
   return A4G_OK;
 }
 
@@ -386,7 +443,8 @@ int run(a4g_batch* b, cudaStream_t s, const cudaEvent_t* ev = nullptr) {
     if ((rc = mark(4)) || (rc = mark(5))) return rc;
     return A4G_OK;
   }
-  if (b->n_tiles > 0) {
+  const a4g_batch::GemmForm& gf = b->forms[b->form];
+  if (gf.n_tiles > 0) {
     A4G_CUDA(cudaMemsetAsync(b->d_exps, 0, b->exps_bytes, s));
     for (const auto& js : b->jobsets)
       if ((rc = oz_launch_exp(js.layout, js.d_jobs, js.d_prefix_exp, js.njobs, js.tiles_exp,
@@ -394,18 +452,18 @@ int run(a4g_batch* b, cudaStream_t s, const cudaEvent_t* ev = nullptr) {
         return rc;
   }
   if ((rc = mark(2))) return rc;
-  if (b->n_tiles > 0) {
+  if (gf.n_tiles > 0) {
     for (const auto& js : b->jobsets)
       if ((rc = oz_launch_split(js.layout, js.d_jobs, js.d_prefix_split, js.njobs, js.tiles_split,
                                 js.left ? b->d_pa : b->d_pb, b->slices, s)))
         return rc;
   }
   if ((rc = mark(3))) return rc;
-  if (b->n_tiles > 0 && (rc = oz_launch_gemm(b->gemm, b->grid, s))) return rc;
+  if (gf.n_tiles > 0 && (rc = oz_launch_gemm(gf.args, gf.grid, gf.pair, s))) return rc;
   if ((rc = mark(4))) return rc;
-  if (b->n_tiles > 0 &&
-      (rc = oz_launch_recombine(b->d_tiles, b->n_tiles, b->d_dblocks, b->d_plans, b->d_pa, b->d_pb, b->d_ws,
-                                b->slices, b->nsplit, b->beta, s)))
+  if (gf.n_tiles > 0 &&
+      (rc = oz_launch_recombine(gf.d_tiles, gf.n_tiles, gf.tile_rows, b->d_dblocks, b->d_plans, b->d_pa, b->d_pb,
+                                b->d_ws, b->slices, gf.nsplit, b->beta, s)))
     return rc;
   return mark(5);
 }
@@ -428,7 +486,9 @@ int a4g_batch_create(a4g_batch** out, const int* ptrn, int drank, int lrank, int
     b->precision = opts->precision;
     b->slices = opts->slices > 0 ? opts->slices : 5;
     b->beta = opts->beta ? 1 : 0;
+    b->variant = opts->variant;
   }
+  if (b->variant < 0 || b->variant > 2) return fail(A4G_ERR_ARG, "unknown GEMM variant");
   if (b->precision != A4G_PREC_FP64 && b->precision != A4G_PREC_OZAKI_BF16)
     return fail(A4G_ERR_ARG, "unknown precision mode");
   if (b->slices < 1 || b->slices > kOzMaxUsableSlices) return fail(A4G_ERR_ARG, "slices must be 1..7");
@@ -543,6 +603,14 @@ int a4g_batch_info(const a4g_batch* b, int64_t* pairs, double* flops, int64_t* w
   if (pairs) *pairs = b->pairs;
   if (flops) *flops = b->flops;
   if (workspace_bytes) *workspace_bytes = b->device_bytes;
+  return A4G_OK;
+}
+
+int a4g_batch_form(const a4g_batch* b, int* form, float* ms_one_sm, float* ms_pair) {
+  if (!b) return fail(A4G_ERR_ARG, "null batch");
+  if (form) *form = b->precision == A4G_PREC_FP64 ? 0 : b->form + 1;
+  if (ms_one_sm) *ms_one_sm = b->forms[0].tuned_ms;
+  if (ms_pair) *ms_pair = b->forms[1].tuned_ms;
   return A4G_OK;
 }
 

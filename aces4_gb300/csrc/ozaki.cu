@@ -43,10 +43,8 @@ namespace a4g {
 namespace {
 
 constexpr int kDigitBits = 8;
-constexpr int kStages = 6;
 constexpr int kThreadsOz = 320;  // warp 0 TMA, warp 1 MMA, warps 2..9 epilogue
 constexpr uint32_t kTileBytes = kOzBM * kOzBK * 2;  // 16 KB per operand tile
-constexpr uint32_t kStageBytes = 2 * kTileBytes;
 // TMEM columns: [0,128) and [128,256) are the two FP32 MMA accumulators; [256,384)
 // and [384,512) hold the running exact (hi, lo) sums of the current level.
 constexpr uint32_t kTmemCols = 512;
@@ -59,10 +57,17 @@ constexpr unsigned long long kWaitLimitNs = 20ull * 1000 * 1000 * 1000;  // 20 s
 constexpr uint32_t kIdesc = (1u << 4) | (1u << 7) | (1u << 10) | (uint32_t(kOzBN >> 3) << 17) |
                             (uint32_t(kOzBM >> 4) << 24);
 
-struct __align__(1024) OzSmem {
-  uint8_t a[kStages][kTileBytes];
-  uint8_t b[kStages][kTileBytes];
-  uint64_t full[kStages], empty[kStages];
+// Shared memory of the tensor-core kernel.  1-SM form: 6 stages of a 128x64
+// A tile and a 128x64 B tile (32 KB).  2-SM form (cta_group::2, a CTA pair
+// computes a 256x128 tile): each CTA stages its 128 rows of A and 64 rows of
+// B (24 KB), 9 stages.
+template <bool PAIR>
+struct __align__(1024) OzSmemT {
+  static constexpr int kSt = PAIR ? 9 : 6;
+  static constexpr uint32_t kBBytes = PAIR ? kTileBytes / 2 : kTileBytes;
+  uint8_t a[kSt][kTileBytes];
+  uint8_t b[kSt][kBBytes];
+  uint64_t full[kSt], empty[kSt];
   uint64_t acc_full[2], acc_empty[2];
   uint64_t drain;
   uint32_t tmem_base;
@@ -103,8 +108,8 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
   return ok != 0;
 }
 // Bounded wait: gives up after kWaitLimitNs or when another role aborted.
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, OzSmem& sm, int* err,
-                                          int code) {
+template <class SM>
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, SM& sm, int* err, int code) {
   if (mbar_try_wait(bar, parity)) return true;
   const unsigned long long t0 = now_ns();
 #pragma unroll 1
@@ -145,6 +150,57 @@ __device__ __forceinline__ void tc_mma(uint32_t d_tmem, uint64_t adesc, uint64_t
       "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(d_tmem),
       "l"(adesc), "l"(bdesc), "r"(kIdesc), "r"(accum));
 }
+// --- CTA-pair (cta_group::2) forms
+constexpr uint32_t kIdescPair = (1u << 4) | (1u << 7) | (1u << 10) | (uint32_t(kOzBN >> 3) << 17) |
+                                (uint32_t(256 >> 4) << 24);
+__device__ __forceinline__ uint32_t cluster_rank() {
+  uint32_t r;
+  asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
+  return r;
+}
+// shared::cluster address of the same shared variable in CTA `rank` of the cluster
+__device__ __forceinline__ uint32_t mapa_shared(const void* p, uint32_t rank) {
+  uint32_t out;
+  asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(out) : "r"(smem_u32(p)), "r"(rank));
+  return out;
+}
+__device__ __forceinline__ void cluster_sync() {
+  asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;" ::: "memory");
+}
+__device__ __forceinline__ void mbar_arrive_cluster(uint32_t bar_cluster) {
+  asm volatile("mbarrier.arrive.shared::cluster.b64 _, [%0];" ::"r"(bar_cluster) : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx_cluster(uint32_t bar_cluster, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cluster.b64 _, [%0], %1;" ::"r"(bar_cluster), "r"(bytes)
+               : "memory");
+}
+// TMA load into this CTA's shared memory that signals an mbarrier which may
+// live in either CTA of the pair
+__device__ __forceinline__ void tma_load_2d_pair(void* dst, const void* map, uint32_t bar_cluster, int c0,
+                                                 int c1) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes.cta_group::2 [%0], [%1, {%3, %4}], [%2];" ::"r"(
+          smem_u32(dst)),
+      "l"(map), "r"(bar_cluster), "r"(c0), "r"(c1)
+      : "memory");
+}
+__device__ __forceinline__ void tc_mma_pair(uint32_t d_tmem, uint64_t adesc, uint64_t bdesc, uint32_t accum) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "setp.ne.b32 p, %4, 0;\n\t"
+      "tcgen05.mma.cta_group::2.kind::f16 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(d_tmem),
+      "l"(adesc), "l"(bdesc), "r"(kIdescPair), "r"(accum));
+}
+// arrive on the mbarrier at the same offset in both CTAs of the pair once
+// this thread's tcgen05 operations complete
+__device__ __forceinline__ void tc_commit_pair(uint64_t* bar) {
+  asm volatile(
+      "tcgen05.commit.cta_group::2.mbarrier::arrive::one.shared::cluster.multicast::cluster.b64 [%0], %1;" ::"r"(
+          smem_u32(bar)),
+      "h"(uint16_t(3))
+      : "memory");
+}
+
 // Shared-memory matrix descriptor: K-major, 128-byte swizzle, rows of 128 B,
 // 8-row core groups 1024 B apart (SBO), descriptor version 1 (bits 46-48).
 __device__ __forceinline__ uint64_t sw128_desc(const void* tile) {
@@ -195,7 +251,7 @@ __device__ __forceinline__ void two_sum_acc(float& hi, float& lo, float x) {
 }
 
 // ------------------------------------------------------------------ roles
-// Walks the k blocks of one unit: calls f(koff_a, koff_b) per 64-wide block.
+// Walks the k blocks of one unit: calls f(koff_a, koff_b, kb) per 64-wide block.
 template <class F>
 __device__ __forceinline__ void for_unit_kblocks(const OzGemmArgs& a, const OzUnit& un, const OzTile& tl,
                                                  F&& f) {
@@ -210,24 +266,43 @@ __device__ __forceinline__ void for_unit_kblocks(const OzGemmArgs& a, const OzUn
   }
 }
 
-__device__ void producer(const OzGemmArgs& a, OzSmem& sm) {
+// Units are distributed over CTAs (1-SM form) or over CTA pairs (2-SM form:
+// both CTAs of a pair walk the same units).
+template <bool PAIR>
+__device__ __forceinline__ int unit_first() { return PAIR ? int(blockIdx.x >> 1) : int(blockIdx.x); }
+template <bool PAIR>
+__device__ __forceinline__ int unit_stride() { return PAIR ? int(gridDim.x >> 1) : int(gridDim.x); }
+
+template <bool PAIR>
+__device__ void producer(const OzGemmArgs& a, OzSmemT<PAIR>& sm, uint32_t rank) {
+  using SM = OzSmemT<PAIR>;
+  constexpr uint32_t kBytes = kTileBytes + SM::kBBytes;
   uint32_t it = 0;
-  for (int u = blockIdx.x; u < a.n_units; u += gridDim.x) {
+  for (int u = unit_first<PAIR>(); u < a.n_units; u += unit_stride<PAIR>()) {
     const OzUnit un = a.units[u];
     const OzTile tl = a.tiles[un.tile];
     const int level = un.level;
     const void* ma = static_cast<const uint8_t*>(a.maps_a) + size_t(tl.panel_a) * 128;
     const void* mb = static_cast<const uint8_t*>(a.maps_b) + size_t(tl.panel_b) * 128;
     const int rpa = a.panels_a[tl.panel_a].rows_pad, rpb = a.panels_b[tl.panel_b].rows_pad;
+    const int arow = tl.m0 + int(rank) * kOzBM;          // this CTA's 128 rows of A
+    const int brow = tl.n0 + int(rank) * (kOzBN / 2);    // this CTA's half of B (pair form)
     bool ok = true;
     for_unit_kblocks(a, un, tl, [&](int ka, int kb, int) {
       for (int i = 0; i <= level; ++i) {
-        const int s = it % kStages;
-        const uint32_t ph = (it / kStages) & 1;
+        const int s = it % SM::kSt;
+        const uint32_t ph = (it / SM::kSt) & 1;
         if (!mbar_wait(&sm.empty[s], ph ^ 1, sm, a.err_flag, 1)) return ok = false;
-        mbar_expect_tx(&sm.full[s], kStageBytes);
-        tma_load_2d(sm.a[s], ma, &sm.full[s], ka, i * rpa + tl.m0);
-        tma_load_2d(sm.b[s], mb, &sm.full[s], kb, (level - i) * rpb + tl.n0);
+        if constexpr (PAIR) {
+          const uint32_t fb = mapa_shared(&sm.full[s], 0);  // the leader CTA's barrier
+          mbar_expect_tx_cluster(fb, kBytes);
+          tma_load_2d_pair(sm.a[s], ma, fb, ka, i * rpa + arow);
+          tma_load_2d_pair(sm.b[s], mb, fb, kb, (level - i) * rpb + brow);
+        } else {
+          mbar_expect_tx(&sm.full[s], kBytes);
+          tma_load_2d(sm.a[s], ma, &sm.full[s], ka, i * rpa + arow);
+          tma_load_2d(sm.b[s], mb, &sm.full[s], kb, (level - i) * rpb + tl.n0);
+        }
         ++it;
       }
       return true;
@@ -236,9 +311,12 @@ __device__ void producer(const OzGemmArgs& a, OzSmem& sm) {
   }
 }
 
-__device__ void mma_issuer(const OzGemmArgs& a, OzSmem& sm, uint32_t tmem) {
+// One thread issues every MMA (the leader CTA's in the pair form).
+template <bool PAIR>
+__device__ void mma_issuer(const OzGemmArgs& a, OzSmemT<PAIR>& sm, uint32_t tmem) {
+  using SM = OzSmemT<PAIR>;
   uint32_t it = 0, chunk = 0;
-  for (int u = blockIdx.x; u < a.n_units; u += gridDim.x) {
+  for (int u = unit_first<PAIR>(); u < a.n_units; u += unit_stride<PAIR>()) {
     const OzUnit un = a.units[u];
     const OzTile tl = a.tiles[un.tile];
     const int level = un.level;
@@ -254,20 +332,25 @@ __device__ void mma_issuer(const OzGemmArgs& a, OzSmem& sm, uint32_t tmem) {
       }
       const uint32_t d_tmem = tmem + buf * kOzBN;
       for (int i = 0; i <= level; ++i) {
-        const int s = it % kStages;
-        const uint32_t ph = (it / kStages) & 1;
+        const int s = it % SM::kSt;
+        const uint32_t ph = (it / SM::kSt) & 1;
         if (!mbar_wait(&sm.full[s], ph, sm, a.err_flag, 3)) return ok = false;
         tc_fence_after();
         const uint64_t ad = sw128_desc(sm.a[s]), bd = sw128_desc(sm.b[s]);
 #pragma unroll
-        for (int kk = 0; kk < kOzBK / 16; ++kk)
-          tc_mma(d_tmem, ad + 2 * kk, bd + 2 * kk, (in_chunk == 0 && i == 0 && kk == 0) ? 0u : 1u);
-        tc_commit(&sm.empty[s]);
+        for (int kk = 0; kk < kOzBK / 16; ++kk) {
+          const uint32_t acc = (in_chunk == 0 && i == 0 && kk == 0) ? 0u : 1u;
+          if constexpr (PAIR) tc_mma_pair(d_tmem, ad + 2 * kk, bd + 2 * kk, acc);
+          else tc_mma(d_tmem, ad + 2 * kk, bd + 2 * kk, acc);
+        }
+        if constexpr (PAIR) tc_commit_pair(&sm.empty[s]);
+        else tc_commit(&sm.empty[s]);
         ++it;
       }
       ++in_chunk;
       if (in_chunk == ckb || kb + 1 == un.kb_end) {
-        tc_commit(&sm.acc_full[buf]);
+        if constexpr (PAIR) tc_commit_pair(&sm.acc_full[buf]);
+        else tc_commit(&sm.acc_full[buf]);
         ++chunk;
         in_chunk = 0;
       }
@@ -292,21 +375,27 @@ __device__ __forceinline__ void tc_st32(uint32_t taddr, const uint32_t (&r)[32])
 
 // Eight warps, two per TMEM lane quadrant (warp % 4); each thread owns one
 // accumulator row and 64 of its 128 columns, in two groups of 32.  The three
-// TMEM loads of a group (chunk, hi, lo) are issued before one wait.
-__device__ void epilogue(const OzGemmArgs& a, OzSmem& sm, uint32_t tmem, int warp, int lane) {
+// TMEM loads of a group (chunk, hi, lo) are issued before one wait.  In the
+// pair form each CTA drains its own 128 rows and signals the leader.
+template <bool PAIR>
+__device__ void epilogue(const OzGemmArgs& a, OzSmemT<PAIR>& sm, uint32_t tmem, int warp, int lane,
+                         uint32_t rank) {
+  constexpr int kRows = PAIR ? 2 * kOzBM : kOzBM;  // rows of a tile
   const int q = warp & 3, h = (warp - 2) >> 2;
-  const int row = 32 * q + lane;
+  const int row = int(rank) * kOzBM + 32 * q + lane;
   const uint32_t lane_addr = tmem + (uint32_t(32 * q) << 16) + uint32_t(64 * h);
+  uint32_t empty_bar[2];
+  for (int b = 0; b < 2; ++b) empty_bar[b] = PAIR ? mapa_shared(&sm.acc_empty[b], 0) : smem_u32(&sm.acc_empty[b]);
   uint32_t chunk = 0;
-  for (int u = blockIdx.x; u < a.n_units; u += gridDim.x) {
+  for (int u = unit_first<PAIR>(); u < a.n_units; u += unit_stride<PAIR>()) {
     const OzUnit un = a.units[u];
     const int ckb = a.chunk_kb[un.level];
     const int nchunks = (un.kb_end - un.kb_begin + ckb - 1) / ckb;
-    int* w = a.ws + ((size_t(un.tile) * a.slices + un.level) * a.nsplit + un.split) * kOzBN * kOzBM +
-             size_t(64 * h) * kOzBM + row;
+    int* w = a.ws + ((size_t(un.tile) * a.slices + un.level) * a.nsplit + un.split) * kOzBN * kRows +
+             size_t(64 * h) * kRows + row;
     if (nchunks == 0) {  // empty k range: its partial sum is zero
 #pragma unroll 8
-      for (int j = 0; j < 64; ++j) w[size_t(j) * kOzBM] = 0;
+      for (int j = 0; j < 64; ++j) w[size_t(j) * kRows] = 0;
       continue;
     }
     for (int c = 0; c < nchunks; ++c) {
@@ -342,64 +431,83 @@ __device__ void epilogue(const OzGemmArgs& a, OzSmem& sm, uint32_t tmem, int war
           // host sizes units for that), stored as int32
 #pragma unroll
           for (int j = 0; j < 32; ++j)
-            w[size_t(32 * g + j) * kOzBM] =
+            w[size_t(32 * g + j) * kRows] =
                 int(static_cast<long long>(__uint_as_float(hi[j])) + static_cast<long long>(__uint_as_float(lo[j])));
         }
       }
       if (!last) tc_wait_st();
       tc_fence_before();
       __syncwarp();
-      if (lane == 0) mbar_arrive(&sm.acc_empty[buf]);
+      if (lane == 0) {
+        if constexpr (PAIR) mbar_arrive_cluster(empty_bar[buf]);
+        else mbar_arrive(&sm.acc_empty[buf]);
+      }
       ++chunk;
     }
   }
 }
 
+template <bool PAIR>
 __global__ void __launch_bounds__(kThreadsOz, 1) oz_gemm_kernel(const __grid_constant__ OzGemmArgs a) {
+  using SM = OzSmemT<PAIR>;
   extern __shared__ uint8_t smem_raw[];
-  OzSmem& sm = *reinterpret_cast<OzSmem*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+  SM& sm = *reinterpret_cast<SM*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const uint32_t rank = PAIR ? cluster_rank() : 0u;
   if (threadIdx.x == 0) {
-    for (int s = 0; s < kStages; ++s) {
-      mbar_init(&sm.full[s], 1);
+    for (int s = 0; s < SM::kSt; ++s) {
+      mbar_init(&sm.full[s], PAIR ? 2 : 1);  // pair form: one expect_tx arrive from each CTA
       mbar_init(&sm.empty[s], 1);
     }
     for (int b = 0; b < 2; ++b) {
       mbar_init(&sm.acc_full[b], 1);
-      mbar_init(&sm.acc_empty[b], 8);  // one arrive per epilogue warp
+      mbar_init(&sm.acc_empty[b], PAIR ? 16 : 8);  // one arrive per epilogue warp (of both CTAs)
     }
     mbar_init(&sm.drain, 1);
     sm.abort = 0;
     fence_mbar_init();
   }
   if (warp == 1) {
-    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
-                     smem_u32(&sm.tmem_base)),
-                 "r"(kTmemCols));
-    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+    if constexpr (PAIR) {
+      asm volatile("tcgen05.alloc.cta_group::2.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                       smem_u32(&sm.tmem_base)),
+                   "r"(kTmemCols));
+      asm volatile("tcgen05.relinquish_alloc_permit.cta_group::2.sync.aligned;");
+    } else {
+      asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                       smem_u32(&sm.tmem_base)),
+                   "r"(kTmemCols));
+      asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+    }
   }
   tc_fence_before();
   __syncthreads();
+  if constexpr (PAIR) cluster_sync();  // the peer's barriers exist before anyone signals them
   tc_fence_after();
   const uint32_t tmem = sm.tmem_base;
 
   if (warp == 0) {
-    if (lane == 0) producer(a, sm);
+    if (lane == 0) producer<PAIR>(a, sm, rank);
   } else if (warp == 1) {
-    if (lane == 0) {
-      mma_issuer(a, sm, tmem);
+    if (lane == 0 && rank == 0) {
+      mma_issuer<PAIR>(a, sm, tmem);
       // all MMAs this thread issued have completed before TMEM is released
-      tc_commit(&sm.drain);
+      if constexpr (PAIR) tc_commit_pair(&sm.drain);
+      else tc_commit(&sm.drain);
       mbar_wait(&sm.drain, 0, sm, a.err_flag, 5);
     }
   } else {
-    epilogue(a, sm, tmem, warp, lane);
+    epilogue<PAIR>(a, sm, tmem, warp, lane, rank);
   }
   tc_fence_before();
   __syncthreads();
+  if constexpr (PAIR) cluster_sync();  // the leader's MMAs have read this CTA's smem and TMEM
   if (warp == 1) {
     tc_fence_after();
-    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kTmemCols));
+    if constexpr (PAIR)
+      asm volatile("tcgen05.dealloc.cta_group::2.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kTmemCols));
+    else
+      asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kTmemCols));
   }
 }
 
@@ -729,6 +837,7 @@ __global__ void __launch_bounds__(256) oz_split_rows_kernel(const OzSplitJob* __
 // One thread per output element (grid: tiles x 64 blocks of 256): sums the
 // split partials of each level exactly in FP64 (integers < 2^53), applies the
 // level's power of two, then the row/column scales.
+template <int ROWS>
 __global__ void __launch_bounds__(256) oz_recombine_kernel(const OzTile* __restrict__ tiles,
                                                            const OzDBlock* __restrict__ dblocks,
                                                            const PlanRef* __restrict__ plans,
@@ -736,9 +845,10 @@ __global__ void __launch_bounds__(256) oz_recombine_kernel(const OzTile* __restr
                                                            const OzPanel* __restrict__ pb,
                                                            const int* __restrict__ ws, int slices,
                                                            int nsplit, int beta) {
-  const int tile = blockIdx.x >> 6;
-  const int e = ((blockIdx.x & 63) << 8) + threadIdx.x;
-  const int row = e & (kOzBM - 1), col = e >> 7;
+  constexpr int kBlocksPerTile = ROWS * kOzBN / 256;
+  const int tile = blockIdx.x / kBlocksPerTile;
+  const int e = (blockIdx.x % kBlocksPerTile) * 256 + threadIdx.x;
+  const int row = e % ROWS, col = e / ROWS;
   const OzTile tl = tiles[tile];
   const OzDBlock db = dblocks[tl.dblock];
   const PlanRef pl = plans[db.plan];
@@ -748,15 +858,15 @@ __global__ void __launch_bounds__(256) oz_recombine_kernel(const OzTile* __restr
   const int* eb = pb[tl.panel_b].exps;
   double v = 0.0;
   for (int lv = slices - 1; lv >= 0; --lv) {
-    const int* p = ws + ((size_t(tile) * slices + lv) * nsplit * kOzBN + col) * kOzBM + row;
+    const int* p = ws + ((size_t(tile) * slices + lv) * nsplit * kOzBN + col) * ROWS + row;
     long long s0 = 0, s1 = 0;  // exact
     int sp = 0;
 #pragma unroll 4
     for (; sp + 1 < nsplit; sp += 2) {
-      s0 += __ldg(p + size_t(sp) * kOzBN * kOzBM);
-      s1 += __ldg(p + size_t(sp + 1) * kOzBN * kOzBM);
+      s0 += __ldg(p + size_t(sp) * kOzBN * ROWS);
+      s1 += __ldg(p + size_t(sp + 1) * kOzBN * ROWS);
     }
-    if (sp < nsplit) s0 += __ldg(p + size_t(sp) * kOzBN * kOzBM);
+    if (sp < nsplit) s0 += __ldg(p + size_t(sp) * kOzBN * ROWS);
     v += ldexp(double(s0 + s1), -kDigitBits * (lv + 2));  // exact: |sum| < 2^53
   }
   const int E = (ea[m] ? ea[m] : 1) - 1022, F = (eb[n] ? eb[n] : 1) - 1022;
@@ -789,14 +899,14 @@ int oz_chunk_kb(int level) {
   return int(k / kOzBK);
 }
 
-int oz_make_tensor_map(void* map128, const void* base, int64_t kpad, int64_t rows_total) {
+int oz_make_tensor_map(void* map128, const void* base, int64_t kpad, int64_t rows_total, int box_rows) {
   EncodeTiled enc = get_encoder();
   if (!enc) return fail(A4G_ERR_CUDA, "cuTensorMapEncodeTiled unavailable");
   if (kpad % kOzBK != 0 || (reinterpret_cast<uintptr_t>(base) & 15) != 0)
     return fail(A4G_ERR_ARG, "panel not aligned for TMA");
   cuuint64_t dims[2] = {cuuint64_t(kpad), cuuint64_t(rows_total)};
   cuuint64_t strides[1] = {cuuint64_t(kpad) * 2};
-  cuuint32_t box[2] = {kOzBK, kOzBM};
+  cuuint32_t box[2] = {kOzBK, cuuint32_t(box_rows)};
   cuuint32_t estr[2] = {1, 1};
   CUresult r = enc(reinterpret_cast<CUtensorMap*>(map128), CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2,
                    const_cast<void*>(base), dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
@@ -855,31 +965,68 @@ int oz_launch_split(int layout, const OzSplitJob* jobs, const int64_t* prefix, i
 int oz_prepare() {
   static bool done = false;
   if (!done) {
-    A4G_CUDA(cudaFuncSetAttribute(oz_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                  int(sizeof(OzSmem)) + 1024));
+    A4G_CUDA(cudaFuncSetAttribute(oz_gemm_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  int(sizeof(OzSmemT<false>)) + 1024));
+    A4G_CUDA(cudaFuncSetAttribute(oz_gemm_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  int(sizeof(OzSmemT<true>)) + 1024));
     done = true;
   }
   return A4G_OK;
 }
 
-int oz_launch_gemm(const OzGemmArgs& args, int grid, cudaStream_t s) {
-  if (args.slices > kOzMaxUsableSlices) return fail(A4G_ERR_ARG, "at most 7 slices");
-  const int smem = int(sizeof(OzSmem)) + 1024;
+int oz_max_pairs(int* pairs) {
   int rc = oz_prepare();
   if (rc) return rc;
-  if (args.slices < 1 || args.slices > kOzMaxSlices) return fail(A4G_ERR_ARG, "slices out of range");
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(2 * 76, 1, 1);
+  cfg.blockDim = dim3(kThreadsOz, 1, 1);
+  cfg.dynamicSmemBytes = sizeof(OzSmemT<true>) + 1024;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeClusterDimension;
+  attr[0].val.clusterDim.x = 2, attr[0].val.clusterDim.y = 1, attr[0].val.clusterDim.z = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  int n = 0;
+  A4G_CUDA(cudaOccupancyMaxActiveClusters(&n, oz_gemm_kernel<true>, &cfg));
+  *pairs = n;
+  return A4G_OK;
+}
+
+int oz_launch_gemm(const OzGemmArgs& args, int grid, bool pair, cudaStream_t s) {
+  if (args.slices > kOzMaxUsableSlices) return fail(A4G_ERR_ARG, "at most 7 slices");
+  int rc = oz_prepare();
+  if (rc) return rc;
   if (args.n_units <= 0) return A4G_OK;
-  oz_gemm_kernel<<<grid, kThreadsOz, smem, s>>>(args);
+  if (!pair) {
+    oz_gemm_kernel<false><<<grid, kThreadsOz, sizeof(OzSmemT<false>) + 1024, s>>>(args);
+  } else {
+    if (grid % 2) return fail(A4G_ERR_ARG, "CTA-pair grid must be even");
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(grid, 1, 1);
+    cfg.blockDim = dim3(kThreadsOz, 1, 1);
+    cfg.dynamicSmemBytes = sizeof(OzSmemT<true>) + 1024;
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = 2, attr[0].val.clusterDim.y = 1, attr[0].val.clusterDim.z = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    A4G_CUDA(cudaLaunchKernelEx(&cfg, oz_gemm_kernel<true>, args));
+  }
   A4G_CUDA(cudaGetLastError());
   return A4G_OK;
 }
 
-int oz_launch_recombine(const OzTile* tiles, int ntiles, const OzDBlock* dblocks, const PlanRef* plans,
-                        const OzPanel* pa, const OzPanel* pb, const int* ws, int slices, int nsplit,
-                        int beta, cudaStream_t s) {
+int oz_launch_recombine(const OzTile* tiles, int ntiles, int tile_rows, const OzDBlock* dblocks,
+                        const PlanRef* plans, const OzPanel* pa, const OzPanel* pb, const int* ws, int slices,
+                        int nsplit, int beta, cudaStream_t s) {
   if (ntiles <= 0) return A4G_OK;
-  if (int64_t(ntiles) * 64 > 0x7fffffffLL) return fail(A4G_ERR_RANGE, "too many tiles");
-  oz_recombine_kernel<<<ntiles * 64, 256, 0, s>>>(tiles, dblocks, plans, pa, pb, ws, slices, nsplit, beta);
+  const int per = tile_rows * kOzBN / 256;
+  if (int64_t(ntiles) * per > 0x7fffffffLL) return fail(A4G_ERR_RANGE, "too many tiles");
+  if (tile_rows == 2 * kOzBM)
+    oz_recombine_kernel<2 * kOzBM><<<ntiles * per, 256, 0, s>>>(tiles, dblocks, plans, pa, pb, ws, slices, nsplit, beta);
+  else
+    oz_recombine_kernel<kOzBM><<<ntiles * per, 256, 0, s>>>(tiles, dblocks, plans, pa, pb, ws, slices, nsplit, beta);
   A4G_CUDA(cudaGetLastError());
   return A4G_OK;
 }

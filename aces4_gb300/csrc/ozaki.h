@@ -9,7 +9,8 @@ constexpr int kOzMaxUsableSlices = 7;  // 7 digits x 7 bits = 49 bits <= the 53-
 
 int oz_prepare();  // one-time kernel attributes (call outside stream capture)
 int oz_chunk_kb(int level);  // 64-wide k blocks per exact FP32 flush at a level
-int oz_make_tensor_map(void* map128, const void* base, int64_t kpad, int64_t rows_total);
+int oz_make_tensor_map(void* map128, const void* base, int64_t kpad, int64_t rows_total, int box_rows);
+int oz_max_pairs(int* pairs);  // CTA pairs of the 2-SM kernel that fit on the GPU at once
 // CTA counts of the exponent / split kernels for one job of a given layout.
 int64_t oz_exp_tiles(int layout, int rows, int K);
 int64_t oz_split_tiles(int layout, int rows, int K);
@@ -17,9 +18,11 @@ int oz_launch_exp(int layout, const OzSplitJob* jobs, const int64_t* prefix, int
                   const OzPanel* panels, cudaStream_t s);
 int oz_launch_split(int layout, const OzSplitJob* jobs, const int64_t* prefix, int njobs, int64_t ntiles,
                     const OzPanel* panels, int slices, cudaStream_t s);
-int oz_launch_gemm(const OzGemmArgs& args, int grid, cudaStream_t s);
-int oz_launch_recombine(const OzTile* tiles, int ntiles, const OzDBlock* dblocks, const PlanRef* plans,
-                        const OzPanel* pa, const OzPanel* pb, const int* ws, int slices, int nsplit,
-                        int beta, cudaStream_t s);
+// pair = false: 1-SM kernel, 128x128 tiles; pair = true: CTA-pair kernel
+// (cluster of 2, cta_group::2), 256x128 tiles, grid even.
+int oz_launch_gemm(const OzGemmArgs& args, int grid, bool pair, cudaStream_t s);
+int oz_launch_recombine(const OzTile* tiles, int ntiles, int tile_rows, const OzDBlock* dblocks,
+                        const PlanRef* plans, const OzPanel* pa, const OzPanel* pb, const int* ws, int slices,
+                        int nsplit, int beta, cudaStream_t s);
 
 }  // namespace a4g

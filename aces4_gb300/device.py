@@ -162,7 +162,7 @@ class _Triple(ctypes.Structure):
 
 class _Opts(ctypes.Structure):
     _fields_ = [("precision", ctypes.c_int), ("slices", ctypes.c_int), ("beta", ctypes.c_int),
-                ("reserved", ctypes.c_int * 5)]
+                ("variant", ctypes.c_int), ("reserved", ctypes.c_int * 4)]
 
 
 def _ext6(e):
@@ -179,13 +179,13 @@ class Batch:
     device addresses) and per-block extents.
     """
 
-    def __init__(self, ptrn, drank, lrank, rrank, triples, precision=PREC_FP64, slices=5, beta=0):
+    def __init__(self, ptrn, drank, lrank, rrank, triples, precision=PREC_FP64, slices=5, beta=0, variant=0):
         tl = list(triples)
         arr = (_Triple * max(1, len(tl)))()
         for i, (d, l, r, de, le, re) in enumerate(tl):
             arr[i].d, arr[i].l, arr[i].r = _ptr(d), _ptr(l), _ptr(r)
             arr[i].dext, arr[i].lext, arr[i].rext = _ext6(de), _ext6(le), _ext6(re)
-        opts = _Opts(precision, slices, beta)
+        opts = _Opts(precision, slices, beta, variant)
         h = ctypes.c_void_p(0)
         rc = lib().a4g_batch_create(ctypes.byref(h), _iarr(ptrn), _i(drank), _i(lrank), _i(rrank), arr,
                                     ctypes.c_int64(len(tl)), ctypes.byref(opts))
@@ -216,6 +216,12 @@ class Batch:
         _check(lib().a4g_batch_info(self._h, ctypes.byref(pairs), ctypes.byref(flops), ctypes.byref(ws)),
                "a4g_batch_info")
         return {"pairs": pairs.value, "flops": flops.value, "device_bytes": ws.value}
+
+    def form(self):
+        """(form, autotune ms of the 1-SM form, of the CTA-pair form)."""
+        f, a, b = ctypes.c_int(0), ctypes.c_float(-1), ctypes.c_float(-1)
+        _check(lib().a4g_batch_form(self._h, ctypes.byref(f), ctypes.byref(a), ctypes.byref(b)), "a4g_batch_form")
+        return {"form": f.value, "tuned_ms_one_sm": a.value, "tuned_ms_pair": b.value}
 
     def close(self):
         if getattr(self, "_h", None) and self._h.value:

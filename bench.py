@@ -228,6 +228,7 @@ def main():
     ap.add_argument("--cpu-pairs", type=int, default=16)
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--variant", type=int, default=0, help="tensor-core GEMM form: 0 autotuned, 1 one SM, 2 CTA pair")
     ap.add_argument("--nvseg", type=int, default=16, help="virtual segments of 32 (16: v=512)")
     ap.add_argument("--noseg", type=int, default=4, help="occupied segments of 16 (4: o=64)")
     args = ap.parse_args()
@@ -256,8 +257,10 @@ def main():
     V, T, R, trip = make_workload(torch, a4, slab=rank, seed=1234, nv=args.nvseg, no=args.noseg)
     workload = workload_name(args.nvseg, args.noseg)
     _, ptrn = oracle.get_contraction_ptrn(4, 4, 4, [1, 2, 3, 4, 1, 2, 5, 6, 5, 6, 3, 4])
-    split = a4.device.Batch(ptrn, 4, 4, 4, trip, precision=a4.device.PREC_OZAKI_BF16, slices=args.slices)
+    split = a4.device.Batch(ptrn, 4, 4, 4, trip, precision=a4.device.PREC_OZAKI_BF16, slices=args.slices,
+                            variant=args.variant)
     info = split.info()
+    form = split.form()
     flops = info["flops"]
     S = args.slices
 
@@ -380,6 +383,8 @@ def main():
             "rel_err_max_block_vs_fp64_gpu": max(blk_err) if blk_err else None,
             "rel_err_block_vs_cpu_oracle": err_oracle,
             "phases_ms_per_step": {k: phases[k] / runs for k in ("exponents", "split", "gemm", "recombine")},
+            "gemm_form": {"chosen": {1: "one SM per 128x128 tile", 2: "CTA pair per 256x128 tile"}.get(form["form"]),
+                          "autotune_ms": {"one_sm": form["tuned_ms_one_sm"], "cta_pair": form["tuned_ms_pair"]}},
             "hbm_phases": {
                 "exponents_gbs": exp_bytes / (phases["exponents"] / runs * 1e-3) / 1e9,
                 "split_gbs": split_bytes / (phases["split"] / runs * 1e-3) / 1e9,

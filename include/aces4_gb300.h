@@ -213,7 +213,11 @@ typedef struct a4g_batch_opts {
                       Each slice is a balanced base-256 digit; 5 slices keep
                       the relative error near 1e-11, 6 near 1e-13.          */
   int beta;        /* 0: D = sum of products (overwrite); 1: D += sum        */
-  int reserved[5];
+  int variant;     /* split precision, tensor-core GEMM form: 0 autotuned at
+                      creation (each form timed once, the faster kept),
+                      1: one SM per 128x128 tile, 2: a CTA pair per 256x128
+                      tile (cta_group::2)                                    */
+  int reserved[4];
 } a4g_batch_opts;
 
 /* Opaque handle of a planned pardo step: pattern + triple list + workspace. */
@@ -233,6 +237,9 @@ int a4g_batch_run_timed(a4g_batch* b, void* stream);
 int a4g_batch_timings(a4g_batch* b, float* phase_ms, int nphase, int* runs);
 /* Number of block pairs executed (zero blocks skipped) and FP64 flops. */
 int a4g_batch_info(const a4g_batch* b, int64_t* pairs, double* flops, int64_t* workspace_bytes);
+/* The tensor-core GEMM form in use (1: one SM per tile, 2: CTA pair; 0 for
+ * FP64 batches) and the autotuner's timings of both forms (ms, -1 if not run). */
+int a4g_batch_form(const a4g_batch* b, int* form, float* ms_one_sm, float* ms_pair);
 void a4g_batch_destroy(a4g_batch* b);
 
 #ifdef __cplusplus

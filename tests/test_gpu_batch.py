@@ -105,10 +105,11 @@ def _errors(R, ref):
     return np.array(errs)
 
 
-def _run(a4, R, trip, labels, precision, slices=5, beta=0, graph=False):
+def _run(a4, R, trip, labels, precision, slices=5, beta=0, graph=False, variant=0):
     import torch
 
-    b = a4.device.Batch(_ptrn(labels), 4, 4, 4, trip, precision=precision, slices=slices, beta=beta)
+    b = a4.device.Batch(_ptrn(labels), 4, 4, 4, trip, precision=precision, slices=slices, beta=beta,
+                        variant=variant)
     if graph:
         b.run_graph()
     else:
@@ -137,21 +138,25 @@ def test_fp64_uneven_sparse_ring(a4):
     assert errs.max() <= TOL_FP64
 
 
-def test_split_one_slice_integer_exact(a4):
+@pytest.mark.parametrize("variant", [1, 2])
+def test_split_one_slice_integer_exact(a4, variant):
     # integers in [-127, 127] are exact single 8-bit digits: the tensor-core
-    # products and the chunked FP32 accumulation must reproduce FP64 exactly
+    # products and the chunked FP32 accumulation must reproduce FP64 exactly,
+    # in both GEMM forms (one SM per 128x128 tile, CTA pair per 256x128 tile)
     R, V, T, trip, labels = _make(a4, "ladder", [32, 32], [16, 16], 0.0, 3, integer=True)
-    _run(a4, R, trip, labels, a4.device.PREC_OZAKI_BF16, slices=1)
+    b = _run(a4, R, trip, labels, a4.device.PREC_OZAKI_BF16, slices=1, variant=variant)
+    assert b.form()["form"] == variant
     ref = _reference(R, trip, labels)
     for k, want in ref.items():
         np.testing.assert_array_equal(R.block(k).cpu().numpy(), want)
 
 
-def test_split_long_k_integer_exact(a4):
+@pytest.mark.parametrize("variant", [1, 2])
+def test_split_long_k_integer_exact(a4, variant):
     # K per destination row = 16 * 48^2 = 36864 (several exact flush chunks,
     # several levels' chunk sizes) with 2 slices on integer data
     R, V, T, trip, labels = _make(a4, "ladder", [48] * 4, [8], 0.0, 4, integer=True)
-    _run(a4, R, trip, labels, a4.device.PREC_OZAKI_BF16, slices=2)
+    _run(a4, R, trip, labels, a4.device.PREC_OZAKI_BF16, slices=2, variant=variant)
     ref = _reference(R, trip, labels)
     for k, want in ref.items():
         np.testing.assert_array_equal(R.block(k).cpu().numpy(), want)
@@ -162,7 +167,7 @@ def test_split_ladder_outliers(a4, slices, tol):
     # config-4 distributions (V ~ U[-1,1]/v, T ~ N(0,1e-2) with 1% x1e3) on a
     # smaller ladder: v=64 in 2 segments of 32, o=32 in 2 segments of 16
     R, V, T, trip, labels = _make(a4, "ladder", [32, 32], [16, 16], 0.0, 5, outliers=True)
-    _run(a4, R, trip, labels, a4.device.PREC_OZAKI_BF16, slices=slices)
+    _run(a4, R, trip, labels, a4.device.PREC_OZAKI_BF16, slices=slices, variant=2 if slices % 2 else 1)
     errs = _errors(R, _reference(R, trip, labels))
     assert errs.max() <= tol, (slices, errs.max())
 
@@ -172,7 +177,7 @@ def test_split_uneven_sparse_ring_graph_and_beta(a4):
 
     R, V, T, trip, labels = _make(a4, "ring", [12, 16, 24, 32], [5, 8], 0.3, 6)
     ref = _reference(R, trip, labels)
-    _run(a4, R, trip, labels, a4.device.PREC_OZAKI_BF16, slices=5, graph=True)
+    _run(a4, R, trip, labels, a4.device.PREC_OZAKI_BF16, slices=5, graph=True, variant=2)
     assert _errors(R, ref).max() <= TOL_SPLIT
     first = R.buf.clone()
     # replaying the captured graph gives identical bits
