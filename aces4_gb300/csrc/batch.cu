@@ -24,7 +24,7 @@ struct a4g_batch {
   int precision = A4G_PREC_FP64;
   int slices = 5;
   int beta = 0;
-  int variant = 0;  // tensor-core GEMM form: 0 autotuned, 1 one SM per tile, 2 CTA pair per tile
+  int variant = 0;  // tensor-core GEMM form: 0 autotuned, else 1 + index into forms
   int64_t pairs = 0;
   double flops = 0.0;
   int64_t device_bytes = 0;
@@ -53,11 +53,14 @@ struct a4g_batch {
   };
   std::vector<JobSet> jobsets;
   OzDBlock* d_dblocks = nullptr;
-  // Tensor-core GEMM forms: [0] 1-SM 128x128 tiles, [1] CTA-pair 256x128 tiles.
+  // Tensor-core GEMM forms: [0] 1-SM 128x128 tiles, [1] CTA-pair 256x128,
+  // [2] 1-SM 128x256, [3] CTA-pair 256x256.
+  static constexpr int kForms = 4;
   struct GemmForm {
     bool pair = false;
     bool built = false;
     int tile_rows = 128;
+    int tile_cols = 128;
     OzTile* d_tiles = nullptr;
     int n_tiles = 0;
     int nsplit = 1;
@@ -65,7 +68,7 @@ struct a4g_batch {
     OzGemmArgs args{};
     float tuned_ms = -1.f;
   };
-  GemmForm forms[2];
+  GemmForm forms[kForms];
   int form = 0;  // the form run() uses (chosen by the autotuner or the caller)
   int* d_ws = nullptr;
   cudaGraphExec_t graph = nullptr;
@@ -216,20 +219,21 @@ int build_ozaki(a4g_batch* b, const std::vector<DGroup>& groups, const std::vect
   if (rc0) return rc0;
   // panels: slices (BF16, zero padded), exponents, tensor maps
   std::vector<OzPanel> hpa, hpb;
-  std::vector<MapBytes> maps_a(pa.size()), maps_b(pb.size()), maps_b2(pb.size());
+  // one A descriptor (128-row boxes); B descriptors with 64-, 128- and
+  // 256-row boxes for the forms' B halves / tiles
+  std::vector<MapBytes> maps_a(pa.size()), maps_b64(pb.size()), maps_b128(pb.size()), maps_b256(pb.size());
   size_t exps_total = 0;
   for (auto& p : pa) exps_total += ceil_to(p.rows, 2 * kOzBM);
-  for (auto& p : pb) exps_total += ceil_to(p.rows, kOzBN);
+  for (auto& p : pb) exps_total += ceil_to(p.rows, 2 * kOzBN);
   void* exps = nullptr;
   int rc = device_alloc(b, exps_total * sizeof(int), &exps, true);
   if (rc) return rc;
   b->d_exps = static_cast<int*>(exps);
   b->exps_bytes = exps_total * sizeof(int);
   size_t eoff = 0;
-  // A panels are padded to 256 rows (either tile form), B panels to 128; B
-  // panels get a second descriptor with 64-row boxes for the CTA-pair form.
+  // A and B panels are padded to 256 rows (every tile form fits).
   auto make_panels = [&](std::vector<PanelBuild>& src, std::vector<OzPanel>& dst, std::vector<MapBytes>& maps,
-                         std::vector<MapBytes>* maps2, int rows_tile) -> int {
+                         std::vector<MapBytes>* maps2, std::vector<MapBytes>* maps3, int rows_tile) -> int {
     for (size_t i = 0; i < src.size(); ++i) {
       OzPanel p{};
       p.rows = src[i].rows;
@@ -244,14 +248,14 @@ int build_ozaki(a4g_batch* b, const std::vector<DGroup>& groups, const std::vect
       eoff += p.rows_pad;
       r = oz_make_tensor_map(maps[i].b, mem, p.kpad, int64_t(S) * p.rows_pad, kOzBM);
       if (r) return r;
-      if (maps2 && (r = oz_make_tensor_map((*maps2)[i].b, mem, p.kpad, int64_t(S) * p.rows_pad, kOzBN / 2)))
-        return r;
+      if (maps2 && (r = oz_make_tensor_map((*maps2)[i].b, mem, p.kpad, int64_t(S) * p.rows_pad, 64))) return r;
+      if (maps3 && (r = oz_make_tensor_map((*maps3)[i].b, mem, p.kpad, int64_t(S) * p.rows_pad, 256))) return r;
       dst.push_back(p);
     }
     return A4G_OK;
   };
-  if ((rc = make_panels(pa, hpa, maps_a, nullptr, 2 * kOzBM))) return rc;
-  if ((rc = make_panels(pb, hpb, maps_b, &maps_b2, kOzBN))) return rc;
+  if ((rc = make_panels(pa, hpa, maps_a, nullptr, nullptr, 2 * kOzBM))) return rc;
+  if ((rc = make_panels(pb, hpb, maps_b128, &maps_b64, &maps_b256, 2 * kOzBN))) return rc;
   for (auto& p : hpa)
     if (p.kpad > 0x7fffffffLL || int64_t(S) * p.rows_pad > 0x7fffffffLL)
       return fail(A4G_ERR_RANGE, "panel exceeds TMA coordinate range");
@@ -308,14 +312,16 @@ int build_ozaki(a4g_batch* b, const std::vector<DGroup>& groups, const std::vect
       b->jobsets.push_back(js);
     }
   }
-  void *dmaps_a = nullptr, *dmaps_b = nullptr, *dmaps_b2 = nullptr;
-  const size_t mbytes_a = maps_a.size() * sizeof(MapBytes), mbytes_b = maps_b.size() * sizeof(MapBytes);
+  void *dmaps_a = nullptr, *dmaps_b64 = nullptr, *dmaps_b128 = nullptr, *dmaps_b256 = nullptr;
+  const size_t mbytes_a = maps_a.size() * sizeof(MapBytes), mbytes_b = maps_b128.size() * sizeof(MapBytes);
   if ((rc = device_alloc(b, mbytes_a, &dmaps_a, false))) return rc;
-  if ((rc = device_alloc(b, mbytes_b, &dmaps_b, false))) return rc;
-  if ((rc = device_alloc(b, mbytes_b, &dmaps_b2, false))) return rc;
+  if ((rc = device_alloc(b, mbytes_b, &dmaps_b64, false))) return rc;
+  if ((rc = device_alloc(b, mbytes_b, &dmaps_b128, false))) return rc;
+  if ((rc = device_alloc(b, mbytes_b, &dmaps_b256, false))) return rc;
   A4G_CUDA(cudaMemcpy(dmaps_a, maps_a.data(), mbytes_a, cudaMemcpyHostToDevice));
-  A4G_CUDA(cudaMemcpy(dmaps_b, maps_b.data(), mbytes_b, cudaMemcpyHostToDevice));
-  A4G_CUDA(cudaMemcpy(dmaps_b2, maps_b2.data(), mbytes_b, cudaMemcpyHostToDevice));
+  A4G_CUDA(cudaMemcpy(dmaps_b64, maps_b64.data(), mbytes_b, cudaMemcpyHostToDevice));
+  A4G_CUDA(cudaMemcpy(dmaps_b128, maps_b128.data(), mbytes_b, cudaMemcpyHostToDevice));
+  A4G_CUDA(cudaMemcpy(dmaps_b256, maps_b256.data(), mbytes_b, cudaMemcpyHostToDevice));
   OzTrip* d_trips = nullptr;
   if ((rc = upload(b, hpa, &b->d_pa)) || (rc = upload(b, hpb, &b->d_pb)) || (rc = upload(b, trips, &d_trips)) ||
       (rc = upload(b, dblocks, &b->d_dblocks)))
@@ -325,17 +331,18 @@ int build_ozaki(a4g_batch* b, const std::vector<DGroup>& groups, const std::vect
   int pairs = 0;
   if ((rc = oz_max_pairs(&pairs))) return rc;
   size_t ws_elems = 0;
-  std::vector<std::vector<OzTile>> form_tiles(2);
-  std::vector<std::vector<OzUnit>> form_units(2);
-  for (int f = 0; f < 2; ++f) {
+  std::vector<std::vector<OzTile>> form_tiles(a4g_batch::kForms);
+  std::vector<std::vector<OzUnit>> form_units(a4g_batch::kForms);
+  for (int f = 0; f < a4g_batch::kForms; ++f) {
     a4g_batch::GemmForm& gf = b->forms[f];
-    gf.pair = f == 1;
+    gf.pair = f & 1;
     gf.tile_rows = gf.pair ? 2 * kOzBM : kOzBM;
+    gf.tile_cols = f >= 2 ? 2 * kOzBN : kOzBN;
     const int P = gf.pair ? pairs : ctx()->num_sms;  // concurrent workers (CTAs or CTA pairs)
     if (P < 1 || (b->variant && b->variant != f + 1)) continue;
     std::vector<OzTile>& tiles = form_tiles[f];
     for (const OzTile& di : dinfo)
-      for (int64_t n0 = 0; n0 < di.n0; n0 += kOzBN)
+      for (int64_t n0 = 0; n0 < di.n0; n0 += gf.tile_cols)
         for (int64_t m0 = 0; m0 < di.m0; m0 += gf.tile_rows)
           tiles.push_back({di.dblock, int(m0), int(n0), di.panel_a, di.panel_b, di.trip_begin, di.trip_end,
                            di.kb_total});
@@ -349,7 +356,7 @@ int build_ozaki(a4g_batch* b, const std::vector<DGroup>& groups, const std::vect
     int min_kb = 1 << 30, max_kb = 0;
     for (const OzTile& t : tiles) min_kb = std::min(min_kb, t.kb_total), max_kb = std::max(max_kb, t.kb_total);
     const int ns_min = std::max(1, (max_kb + max_unit_kb - 1) / max_unit_kb);
-    const double tile_bytes = double(gf.tile_rows) * kOzBN * sizeof(int);
+    const double tile_bytes = double(gf.tile_rows) * gf.tile_cols * sizeof(int);
     int nsplit = ns_min;
     double best = -1.0;
     for (int ns = ns_min; ns <= std::max(64, ns_min); ++ns) {
@@ -376,11 +383,12 @@ int build_ozaki(a4g_batch* b, const std::vector<DGroup>& groups, const std::vect
           u.kb_in_trip = u.kb_begin - acc;
           units.push_back(u);
         }
-    ws_elems = std::max(ws_elems, size_t(gf.n_tiles) * S * nsplit * gf.tile_rows * kOzBN);
+    ws_elems = std::max(ws_elems, size_t(gf.n_tiles) * S * nsplit * gf.tile_rows * gf.tile_cols);
     OzUnit* d_units = nullptr;
     if ((rc = upload(b, tiles, &gf.d_tiles)) || (rc = upload(b, units, &d_units))) return rc;
     OzGemmArgs& ga = gf.args;
-    ga.maps_a = dmaps_a, ga.maps_b = gf.pair ? dmaps_b2 : dmaps_b;
+    const int bbox = gf.pair ? gf.tile_cols / 2 : gf.tile_cols;  // B rows one CTA loads
+    ga.maps_a = dmaps_a, ga.maps_b = bbox == 64 ? dmaps_b64 : bbox == 128 ? dmaps_b128 : dmaps_b256;
     ga.panels_a = b->d_pa, ga.panels_b = b->d_pb;
     ga.tiles = gf.d_tiles, ga.trips = d_trips;
     ga.n_tiles = gf.n_tiles;
@@ -397,29 +405,33 @@ int build_ozaki(a4g_batch* b, const std::vector<DGroup>& groups, const std::vect
   if ((rc = device_alloc(b, ws_elems * sizeof(int), &ws, false))) return rc;
   b->d_ws = static_cast<int*>(ws);
   for (auto& gf : b->forms) gf.args.ws = b->d_ws;
-  b->form = b->forms[1].built && b->variant == 2 ? 1 : 0;
-  if (!b->forms[b->form].built) b->form = b->forms[0].built ? 0 : 1;
-  if (!b->variant && b->forms[0].built && b->forms[1].built) {
+  b->form = -1;
+  for (int f = 0; f < a4g_batch::kForms; ++f)
+    if (b->forms[f].built && (b->form < 0 || b->variant == f + 1)) b->form = f;
+  if (b->form < 0) return fail(A4G_ERR_UNSUPPORTED, "no tensor-core GEMM form fits this GPU");
+  if (!b->variant) {
     // autotune: time each form's GEMM once (after one untimed run) on this
-    // batch's panels and keep the faster
+    // batch's panels and keep the fastest
     cudaStream_t s = ctx()->stream;
     cudaEvent_t e0, e1;
     A4G_CUDA(cudaEventCreate(&e0));
     A4G_CUDA(cudaEventCreate(&e1));
-    for (int f = 0; f < 2; ++f) {
+    float best_ms = 0.f;
+    for (int f = 0; f < a4g_batch::kForms && !rc; ++f) {
       a4g_batch::GemmForm& gf = b->forms[f];
-      if ((rc = oz_launch_gemm(gf.args, gf.grid, gf.pair, s))) break;
+      if (!gf.built) continue;
+      if ((rc = oz_launch_gemm(gf.args, gf.grid, gf.pair, gf.tile_cols, s))) break;
       A4G_CUDA(cudaEventRecord(e0, s));
-      if ((rc = oz_launch_gemm(gf.args, gf.grid, gf.pair, s))) break;
+      if ((rc = oz_launch_gemm(gf.args, gf.grid, gf.pair, gf.tile_cols, s))) break;
       A4G_CUDA(cudaEventRecord(e1, s));
       A4G_CUDA(cudaEventSynchronize(e1));
       A4G_CUDA(cudaEventElapsedTime(&gf.tuned_ms, e0, e1));
+      if (best_ms == 0.f || gf.tuned_ms < best_ms) best_ms = gf.tuned_ms, b->form = f;
     }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     if (rc) return rc;
     if ((rc = check_device_flag(s))) return rc;
-    b->form = b->forms[1].tuned_ms < b->forms[0].tuned_ms ? 1 : 0;
   }
   return A4G_OK;
 }
@@ -459,11 +471,11 @@ int run(a4g_batch* b, cudaStream_t s, const cudaEvent_t* ev = nullptr) {
         return rc;
   }
   if ((rc = mark(3))) return rc;
-  if (gf.n_tiles > 0 && (rc = oz_launch_gemm(gf.args, gf.grid, gf.pair, s))) return rc;
+  if (gf.n_tiles > 0 && (rc = oz_launch_gemm(gf.args, gf.grid, gf.pair, gf.tile_cols, s))) return rc;
   if ((rc = mark(4))) return rc;
   if (gf.n_tiles > 0 &&
-      (rc = oz_launch_recombine(gf.d_tiles, gf.n_tiles, gf.tile_rows, b->d_dblocks, b->d_plans, b->d_pa, b->d_pb,
-                                b->d_ws, b->slices, gf.nsplit, b->beta, s)))
+      (rc = oz_launch_recombine(gf.d_tiles, gf.n_tiles, gf.tile_rows, gf.tile_cols, b->d_dblocks, b->d_plans,
+                                b->d_pa, b->d_pb, b->d_ws, b->slices, gf.nsplit, b->beta, s)))
     return rc;
   return mark(5);
 }
@@ -488,7 +500,7 @@ int a4g_batch_create(a4g_batch** out, const int* ptrn, int drank, int lrank, int
     b->beta = opts->beta ? 1 : 0;
     b->variant = opts->variant;
   }
-  if (b->variant < 0 || b->variant > 2) return fail(A4G_ERR_ARG, "unknown GEMM variant");
+  if (b->variant < 0 || b->variant > a4g_batch::kForms) return fail(A4G_ERR_ARG, "unknown GEMM variant");
   if (b->precision != A4G_PREC_FP64 && b->precision != A4G_PREC_OZAKI_BF16)
     return fail(A4G_ERR_ARG, "unknown precision mode");
   if (b->slices < 1 || b->slices > kOzMaxUsableSlices) return fail(A4G_ERR_ARG, "slices must be 1..7");
@@ -606,11 +618,10 @@ int a4g_batch_info(const a4g_batch* b, int64_t* pairs, double* flops, int64_t* w
   return A4G_OK;
 }
 
-int a4g_batch_form(const a4g_batch* b, int* form, float* ms_one_sm, float* ms_pair) {
+int a4g_batch_form(const a4g_batch* b, int* form, float* tuned_ms, int n) {
   if (!b) return fail(A4G_ERR_ARG, "null batch");
   if (form) *form = b->precision == A4G_PREC_FP64 ? 0 : b->form + 1;
-  if (ms_one_sm) *ms_one_sm = b->forms[0].tuned_ms;
-  if (ms_pair) *ms_pair = b->forms[1].tuned_ms;
+  for (int f = 0; f < n && tuned_ms; ++f) tuned_ms[f] = f < a4g_batch::kForms ? b->forms[f].tuned_ms : -1.f;
   return A4G_OK;
 }
 

@@ -33,6 +33,7 @@
 #include <cuda_bf16.h>
 #include <cudaTypedefs.h>
 
+#include <algorithm>
 #include <type_traits>
 
 #include "a4g_internal.h"
@@ -54,17 +55,21 @@ constexpr unsigned long long kWaitLimitNs = 20ull * 1000 * 1000 * 1000;  // 20 s
 // tcgen05 instruction descriptor, kind::f16: D F32 (bits 4-5 = 1), A BF16
 // (bits 7-9 = 1), B BF16 (bits 10-12 = 1), both K-major (bits 15/16 = 0),
 // N>>3 at bits 17-22, M>>4 at bits 24-28.
-constexpr uint32_t kIdesc = (1u << 4) | (1u << 7) | (1u << 10) | (uint32_t(kOzBN >> 3) << 17) |
-                            (uint32_t(kOzBM >> 4) << 24);
+template <int M, int N>
+constexpr uint32_t idesc_bf16() {
+  return (1u << 4) | (1u << 7) | (1u << 10) | (uint32_t(N >> 3) << 17) | (uint32_t(M >> 4) << 24);
+}
 
-// Shared memory of the tensor-core kernel.  1-SM form: 6 stages of a 128x64
-// A tile and a 128x64 B tile (32 KB).  2-SM form (cta_group::2, a CTA pair
-// computes a 256x128 tile): each CTA stages its 128 rows of A and 64 rows of
-// B (24 KB), 9 stages.
-template <bool PAIR>
+// Shared memory of the tensor-core kernel, per form (PAIR: a CTA pair computes
+// one tile with cta_group::2; BN: tile columns).  Each CTA stages its 128 rows
+// of A and its BN (1-SM) or BN/2 (pair) rows of B per 64-wide k block:
+//   1-SM BN=128: 32 KB x 6 stages   pair BN=128: 24 KB x 9
+//   1-SM BN=256: 48 KB x 4 stages   pair BN=256: 32 KB x 6
+template <bool PAIR, int BN>
 struct __align__(1024) OzSmemT {
-  static constexpr int kSt = PAIR ? 9 : 6;
-  static constexpr uint32_t kBBytes = PAIR ? kTileBytes / 2 : kTileBytes;
+  static constexpr uint32_t kBBytes = uint32_t(PAIR ? BN / 2 : BN) * kOzBK * 2;
+  static constexpr int kSt = int((216u * 1024u) / (kTileBytes + kBBytes)) > 9 ? 9
+                                                                               : int((216u * 1024u) / (kTileBytes + kBBytes));
   uint8_t a[kSt][kTileBytes];
   uint8_t b[kSt][kBBytes];
   uint64_t full[kSt], empty[kSt];
@@ -143,16 +148,15 @@ __device__ __forceinline__ void tc_commit(uint64_t* bar) {
                    smem_u32(bar))
                : "memory");
 }
+template <int N>
 __device__ __forceinline__ void tc_mma(uint32_t d_tmem, uint64_t adesc, uint64_t bdesc, uint32_t accum) {
   asm volatile(
       "{\n\t.reg .pred p;\n\t"
       "setp.ne.b32 p, %4, 0;\n\t"
       "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(d_tmem),
-      "l"(adesc), "l"(bdesc), "r"(kIdesc), "r"(accum));
+      "l"(adesc), "l"(bdesc), "r"(idesc_bf16<128, N>()), "r"(accum));
 }
 // --- CTA-pair (cta_group::2) forms
-constexpr uint32_t kIdescPair = (1u << 4) | (1u << 7) | (1u << 10) | (uint32_t(kOzBN >> 3) << 17) |
-                                (uint32_t(256 >> 4) << 24);
 __device__ __forceinline__ uint32_t cluster_rank() {
   uint32_t r;
   asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
@@ -184,12 +188,13 @@ __device__ __forceinline__ void tma_load_2d_pair(void* dst, const void* map, uin
       "l"(map), "r"(bar_cluster), "r"(c0), "r"(c1)
       : "memory");
 }
+template <int N>
 __device__ __forceinline__ void tc_mma_pair(uint32_t d_tmem, uint64_t adesc, uint64_t bdesc, uint32_t accum) {
   asm volatile(
       "{\n\t.reg .pred p;\n\t"
       "setp.ne.b32 p, %4, 0;\n\t"
       "tcgen05.mma.cta_group::2.kind::f16 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(d_tmem),
-      "l"(adesc), "l"(bdesc), "r"(kIdescPair), "r"(accum));
+      "l"(adesc), "l"(bdesc), "r"(idesc_bf16<256, N>()), "r"(accum));
 }
 // arrive on the mbarrier at the same offset in both CTAs of the pair once
 // this thread's tcgen05 operations complete
@@ -225,6 +230,15 @@ __device__ __forceinline__ void tc_ld32_nowait(uint32_t taddr, uint32_t (&r)[32]
         "=r"(r[14]), "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]),
         "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]), "=r"(r[25]),
         "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+      : "r"(taddr));
+}
+__device__ __forceinline__ void tc_ld16_nowait(uint32_t taddr, uint32_t (&r)[16]) {
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 "
+      "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+        "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]),
+        "=r"(r[14]), "=r"(r[15])
       : "r"(taddr));
 }
 __device__ __forceinline__ void tc_ld32(uint32_t taddr, uint32_t (&r)[32]) {
@@ -273,9 +287,9 @@ __device__ __forceinline__ int unit_first() { return PAIR ? int(blockIdx.x >> 1)
 template <bool PAIR>
 __device__ __forceinline__ int unit_stride() { return PAIR ? int(gridDim.x >> 1) : int(gridDim.x); }
 
-template <bool PAIR>
-__device__ void producer(const OzGemmArgs& a, OzSmemT<PAIR>& sm, uint32_t rank) {
-  using SM = OzSmemT<PAIR>;
+template <bool PAIR, int BN>
+__device__ void producer(const OzGemmArgs& a, OzSmemT<PAIR, BN>& sm, uint32_t rank) {
+  using SM = OzSmemT<PAIR, BN>;
   constexpr uint32_t kBytes = kTileBytes + SM::kBBytes;
   uint32_t it = 0;
   for (int u = unit_first<PAIR>(); u < a.n_units; u += unit_stride<PAIR>()) {
@@ -286,7 +300,7 @@ __device__ void producer(const OzGemmArgs& a, OzSmemT<PAIR>& sm, uint32_t rank) 
     const void* mb = static_cast<const uint8_t*>(a.maps_b) + size_t(tl.panel_b) * 128;
     const int rpa = a.panels_a[tl.panel_a].rows_pad, rpb = a.panels_b[tl.panel_b].rows_pad;
     const int arow = tl.m0 + int(rank) * kOzBM;          // this CTA's 128 rows of A
-    const int brow = tl.n0 + int(rank) * (kOzBN / 2);    // this CTA's half of B (pair form)
+    const int brow = tl.n0 + int(rank) * (BN / 2);       // this CTA's half of B (pair form)
     bool ok = true;
     for_unit_kblocks(a, un, tl, [&](int ka, int kb, int) {
       for (int i = 0; i <= level; ++i) {
@@ -312,9 +326,9 @@ __device__ void producer(const OzGemmArgs& a, OzSmemT<PAIR>& sm, uint32_t rank) 
 }
 
 // One thread issues every MMA (the leader CTA's in the pair form).
-template <bool PAIR>
-__device__ void mma_issuer(const OzGemmArgs& a, OzSmemT<PAIR>& sm, uint32_t tmem) {
-  using SM = OzSmemT<PAIR>;
+template <bool PAIR, int BN>
+__device__ void mma_issuer(const OzGemmArgs& a, OzSmemT<PAIR, BN>& sm, uint32_t tmem) {
+  using SM = OzSmemT<PAIR, BN>;
   uint32_t it = 0, chunk = 0;
   for (int u = unit_first<PAIR>(); u < a.n_units; u += unit_stride<PAIR>()) {
     const OzUnit un = a.units[u];
@@ -330,7 +344,7 @@ __device__ void mma_issuer(const OzGemmArgs& a, OzSmemT<PAIR>& sm, uint32_t tmem
         if (!mbar_wait(&sm.acc_empty[buf], ((chunk >> 1) & 1) ^ 1, sm, a.err_flag, 2)) return ok = false;
         tc_fence_after();
       }
-      const uint32_t d_tmem = tmem + buf * kOzBN;
+      const uint32_t d_tmem = tmem + buf * BN;
       for (int i = 0; i <= level; ++i) {
         const int s = it % SM::kSt;
         const uint32_t ph = (it / SM::kSt) & 1;
@@ -340,8 +354,8 @@ __device__ void mma_issuer(const OzGemmArgs& a, OzSmemT<PAIR>& sm, uint32_t tmem
 #pragma unroll
         for (int kk = 0; kk < kOzBK / 16; ++kk) {
           const uint32_t acc = (in_chunk == 0 && i == 0 && kk == 0) ? 0u : 1u;
-          if constexpr (PAIR) tc_mma_pair(d_tmem, ad + 2 * kk, bd + 2 * kk, acc);
-          else tc_mma(d_tmem, ad + 2 * kk, bd + 2 * kk, acc);
+          if constexpr (PAIR) tc_mma_pair<BN>(d_tmem, ad + 2 * kk, bd + 2 * kk, acc);
+          else tc_mma<BN>(d_tmem, ad + 2 * kk, bd + 2 * kk, acc);
         }
         if constexpr (PAIR) tc_commit_pair(&sm.empty[s]);
         else tc_commit(&sm.empty[s]);
@@ -378,7 +392,7 @@ __device__ __forceinline__ void tc_st32(uint32_t taddr, const uint32_t (&r)[32])
 // TMEM loads of a group (chunk, hi, lo) are issued before one wait.  In the
 // pair form each CTA drains its own 128 rows and signals the leader.
 template <bool PAIR>
-__device__ void epilogue(const OzGemmArgs& a, OzSmemT<PAIR>& sm, uint32_t tmem, int warp, int lane,
+__device__ void epilogue(const OzGemmArgs& a, OzSmemT<PAIR, 128>& sm, uint32_t tmem, int warp, int lane,
                          uint32_t rank) {
   constexpr int kRows = PAIR ? 2 * kOzBM : kOzBM;  // rows of a tile
   const int q = warp & 3, h = (warp - 2) >> 2;
@@ -447,9 +461,59 @@ __device__ void epilogue(const OzGemmArgs& a, OzSmemT<PAIR>& sm, uint32_t tmem, 
   }
 }
 
+// 256-column tiles: the two FP32 accumulators use all 512 TMEM columns, so the
+// exact running level sum of a unit lives in registers as int32 (a unit's
+// level sum is an integer below 2^31 and every chunk value below 2^24, so the
+// conversion and the additions are exact).  Eight warps, two per lane
+// quadrant; each thread owns one row and 128 columns, read 16 at a time.
 template <bool PAIR>
+__device__ void epilogue_int(const OzGemmArgs& a, OzSmemT<PAIR, 256>& sm, uint32_t tmem, int warp, int lane,
+                             uint32_t rank) {
+  constexpr int BN = 256;
+  constexpr int kRows = PAIR ? 2 * kOzBM : kOzBM;
+  const int q = warp & 3, h = (warp - 2) >> 2;
+  const int row = int(rank) * kOzBM + 32 * q + lane;
+  const uint32_t lane_addr = tmem + (uint32_t(32 * q) << 16) + uint32_t(128 * h);
+  uint32_t empty_bar[2];
+  for (int b = 0; b < 2; ++b) empty_bar[b] = PAIR ? mapa_shared(&sm.acc_empty[b], 0) : smem_u32(&sm.acc_empty[b]);
+  uint32_t chunk = 0;
+  for (int u = unit_first<PAIR>(); u < a.n_units; u += unit_stride<PAIR>()) {
+    const OzUnit un = a.units[u];
+    const int ckb = a.chunk_kb[un.level];
+    const int nchunks = (un.kb_end - un.kb_begin + ckb - 1) / ckb;
+    int* w = a.ws + ((size_t(un.tile) * a.slices + un.level) * a.nsplit + un.split) * BN * kRows +
+             size_t(128 * h) * kRows + row;
+    int sum[128];
+#pragma unroll
+    for (int j = 0; j < 128; ++j) sum[j] = 0;
+    for (int c = 0; c < nchunks; ++c) {
+      const uint32_t buf = chunk & 1;
+      if (!mbar_wait(&sm.acc_full[buf], (chunk >> 1) & 1, sm, a.err_flag, 4)) return;
+      tc_fence_after();
+#pragma unroll
+      for (int g = 0; g < 8; ++g) {
+        uint32_t x[16];
+        tc_ld16_nowait(lane_addr + buf * BN + 16 * g, x);
+        tc_wait_ld();
+#pragma unroll
+        for (int j = 0; j < 16; ++j) sum[16 * g + j] += __float2int_rz(__uint_as_float(x[j]));
+      }
+      tc_fence_before();
+      __syncwarp();
+      if (lane == 0) {
+        if constexpr (PAIR) mbar_arrive_cluster(empty_bar[buf]);
+        else mbar_arrive(&sm.acc_empty[buf]);
+      }
+      ++chunk;
+    }
+#pragma unroll
+    for (int j = 0; j < 128; ++j) w[size_t(j) * kRows] = sum[j];
+  }
+}
+
+template <bool PAIR, int BN>
 __global__ void __launch_bounds__(kThreadsOz, 1) oz_gemm_kernel(const __grid_constant__ OzGemmArgs a) {
-  using SM = OzSmemT<PAIR>;
+  using SM = OzSmemT<PAIR, BN>;
   extern __shared__ uint8_t smem_raw[];
   SM& sm = *reinterpret_cast<SM*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -487,17 +551,18 @@ __global__ void __launch_bounds__(kThreadsOz, 1) oz_gemm_kernel(const __grid_con
   const uint32_t tmem = sm.tmem_base;
 
   if (warp == 0) {
-    if (lane == 0) producer<PAIR>(a, sm, rank);
+    if (lane == 0) producer<PAIR, BN>(a, sm, rank);
   } else if (warp == 1) {
     if (lane == 0 && rank == 0) {
-      mma_issuer<PAIR>(a, sm, tmem);
+      mma_issuer<PAIR, BN>(a, sm, tmem);
       // all MMAs this thread issued have completed before TMEM is released
       if constexpr (PAIR) tc_commit_pair(&sm.drain);
       else tc_commit(&sm.drain);
       mbar_wait(&sm.drain, 0, sm, a.err_flag, 5);
     }
   } else {
-    epilogue<PAIR>(a, sm, tmem, warp, lane, rank);
+    if constexpr (BN == 256) epilogue_int<PAIR>(a, sm, tmem, warp, lane, rank);
+    else epilogue<PAIR>(a, sm, tmem, warp, lane, rank);
   }
   tc_fence_before();
   __syncthreads();
@@ -837,7 +902,7 @@ __global__ void __launch_bounds__(256) oz_split_rows_kernel(const OzSplitJob* __
 // One thread per output element (grid: tiles x 64 blocks of 256): sums the
 // split partials of each level exactly in FP64 (integers < 2^53), applies the
 // level's power of two, then the row/column scales.
-template <int ROWS>
+template <int ROWS, int COLS>
 __global__ void __launch_bounds__(256) oz_recombine_kernel(const OzTile* __restrict__ tiles,
                                                            const OzDBlock* __restrict__ dblocks,
                                                            const PlanRef* __restrict__ plans,
@@ -845,7 +910,7 @@ __global__ void __launch_bounds__(256) oz_recombine_kernel(const OzTile* __restr
                                                            const OzPanel* __restrict__ pb,
                                                            const int* __restrict__ ws, int slices,
                                                            int nsplit, int beta) {
-  constexpr int kBlocksPerTile = ROWS * kOzBN / 256;
+  constexpr int kBlocksPerTile = ROWS * COLS / 256;
   const int tile = blockIdx.x / kBlocksPerTile;
   const int e = (blockIdx.x % kBlocksPerTile) * 256 + threadIdx.x;
   const int row = e % ROWS, col = e / ROWS;
@@ -858,15 +923,15 @@ __global__ void __launch_bounds__(256) oz_recombine_kernel(const OzTile* __restr
   const int* eb = pb[tl.panel_b].exps;
   double v = 0.0;
   for (int lv = slices - 1; lv >= 0; --lv) {
-    const int* p = ws + ((size_t(tile) * slices + lv) * nsplit * kOzBN + col) * ROWS + row;
+    const int* p = ws + ((size_t(tile) * slices + lv) * nsplit * COLS + col) * ROWS + row;
     long long s0 = 0, s1 = 0;  // exact
     int sp = 0;
 #pragma unroll 4
     for (; sp + 1 < nsplit; sp += 2) {
-      s0 += __ldg(p + size_t(sp) * kOzBN * ROWS);
-      s1 += __ldg(p + size_t(sp + 1) * kOzBN * ROWS);
+      s0 += __ldg(p + size_t(sp) * COLS * ROWS);
+      s1 += __ldg(p + size_t(sp + 1) * COLS * ROWS);
     }
-    if (sp < nsplit) s0 += __ldg(p + size_t(sp) * kOzBN * ROWS);
+    if (sp < nsplit) s0 += __ldg(p + size_t(sp) * COLS * ROWS);
     v += ldexp(double(s0 + s1), -kDigitBits * (lv + 2));  // exact: |sum| < 2^53
   }
   const int E = (ea[m] ? ea[m] : 1) - 1022, F = (eb[n] ? eb[n] : 1) - 1022;
@@ -962,13 +1027,20 @@ int oz_launch_split(int layout, const OzSplitJob* jobs, const int64_t* prefix, i
   return A4G_OK;
 }
 
+template <bool PAIR, int BN>
+int set_smem_attr() {
+  A4G_CUDA(cudaFuncSetAttribute(oz_gemm_kernel<PAIR, BN>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                int(sizeof(OzSmemT<PAIR, BN>)) + 1024));
+  return A4G_OK;
+}
+
 int oz_prepare() {
   static bool done = false;
   if (!done) {
-    A4G_CUDA(cudaFuncSetAttribute(oz_gemm_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                  int(sizeof(OzSmemT<false>)) + 1024));
-    A4G_CUDA(cudaFuncSetAttribute(oz_gemm_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                  int(sizeof(OzSmemT<true>)) + 1024));
+    int rc;
+    if ((rc = set_smem_attr<false, 128>()) || (rc = set_smem_attr<true, 128>()) ||
+        (rc = set_smem_attr<false, 256>()) || (rc = set_smem_attr<true, 256>()))
+      return rc;
     done = true;
   }
   return A4G_OK;
@@ -980,53 +1052,67 @@ int oz_max_pairs(int* pairs) {
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3(2 * 76, 1, 1);
   cfg.blockDim = dim3(kThreadsOz, 1, 1);
-  cfg.dynamicSmemBytes = sizeof(OzSmemT<true>) + 1024;
+  cfg.dynamicSmemBytes = sizeof(OzSmemT<true, 128>) + 1024;
   cudaLaunchAttribute attr[1];
   attr[0].id = cudaLaunchAttributeClusterDimension;
   attr[0].val.clusterDim.x = 2, attr[0].val.clusterDim.y = 1, attr[0].val.clusterDim.z = 1;
   cfg.attrs = attr;
   cfg.numAttrs = 1;
-  int n = 0;
-  A4G_CUDA(cudaOccupancyMaxActiveClusters(&n, oz_gemm_kernel<true>, &cfg));
-  *pairs = n;
+  int n = 0, n2 = 0;
+  A4G_CUDA(cudaOccupancyMaxActiveClusters(&n, oz_gemm_kernel<true, 128>, &cfg));
+  cfg.dynamicSmemBytes = sizeof(OzSmemT<true, 256>) + 1024;
+  A4G_CUDA(cudaOccupancyMaxActiveClusters(&n2, oz_gemm_kernel<true, 256>, &cfg));
+  *pairs = std::min(n, n2);
   return A4G_OK;
 }
 
-int oz_launch_gemm(const OzGemmArgs& args, int grid, bool pair, cudaStream_t s) {
-  if (args.slices > kOzMaxUsableSlices) return fail(A4G_ERR_ARG, "at most 7 slices");
-  int rc = oz_prepare();
-  if (rc) return rc;
-  if (args.n_units <= 0) return A4G_OK;
-  if (!pair) {
-    oz_gemm_kernel<false><<<grid, kThreadsOz, sizeof(OzSmemT<false>) + 1024, s>>>(args);
+template <bool PAIR, int BN>
+int launch_form(const OzGemmArgs& args, int grid, cudaStream_t s) {
+  const size_t smem = sizeof(OzSmemT<PAIR, BN>) + 1024;
+  if constexpr (!PAIR) {
+    oz_gemm_kernel<false, BN><<<grid, kThreadsOz, smem, s>>>(args);
   } else {
     if (grid % 2) return fail(A4G_ERR_ARG, "CTA-pair grid must be even");
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3(grid, 1, 1);
     cfg.blockDim = dim3(kThreadsOz, 1, 1);
-    cfg.dynamicSmemBytes = sizeof(OzSmemT<true>) + 1024;
+    cfg.dynamicSmemBytes = smem;
     cfg.stream = s;
     cudaLaunchAttribute attr[1];
     attr[0].id = cudaLaunchAttributeClusterDimension;
     attr[0].val.clusterDim.x = 2, attr[0].val.clusterDim.y = 1, attr[0].val.clusterDim.z = 1;
     cfg.attrs = attr;
     cfg.numAttrs = 1;
-    A4G_CUDA(cudaLaunchKernelEx(&cfg, oz_gemm_kernel<true>, args));
+    A4G_CUDA(cudaLaunchKernelEx(&cfg, oz_gemm_kernel<true, BN>, args));
   }
   A4G_CUDA(cudaGetLastError());
   return A4G_OK;
 }
 
-int oz_launch_recombine(const OzTile* tiles, int ntiles, int tile_rows, const OzDBlock* dblocks,
+int oz_launch_gemm(const OzGemmArgs& args, int grid, bool pair, int tile_cols, cudaStream_t s) {
+  if (args.slices > kOzMaxUsableSlices) return fail(A4G_ERR_ARG, "at most 7 slices");
+  int rc = oz_prepare();
+  if (rc) return rc;
+  if (args.n_units <= 0) return A4G_OK;
+  if (tile_cols == 256) return pair ? launch_form<true, 256>(args, grid, s) : launch_form<false, 256>(args, grid, s);
+  return pair ? launch_form<true, 128>(args, grid, s) : launch_form<false, 128>(args, grid, s);
+}
+
+int oz_launch_recombine(const OzTile* tiles, int ntiles, int tile_rows, int tile_cols, const OzDBlock* dblocks,
                         const PlanRef* plans, const OzPanel* pa, const OzPanel* pb, const int* ws, int slices,
                         int nsplit, int beta, cudaStream_t s) {
   if (ntiles <= 0) return A4G_OK;
-  const int per = tile_rows * kOzBN / 256;
+  const int per = tile_rows * tile_cols / 256;
   if (int64_t(ntiles) * per > 0x7fffffffLL) return fail(A4G_ERR_RANGE, "too many tiles");
-  if (tile_rows == 2 * kOzBM)
-    oz_recombine_kernel<2 * kOzBM><<<ntiles * per, 256, 0, s>>>(tiles, dblocks, plans, pa, pb, ws, slices, nsplit, beta);
+  const unsigned g = unsigned(ntiles * per);
+  if (tile_rows == 256 && tile_cols == 256)
+    oz_recombine_kernel<256, 256><<<g, 256, 0, s>>>(tiles, dblocks, plans, pa, pb, ws, slices, nsplit, beta);
+  else if (tile_rows == 256)
+    oz_recombine_kernel<256, 128><<<g, 256, 0, s>>>(tiles, dblocks, plans, pa, pb, ws, slices, nsplit, beta);
+  else if (tile_cols == 256)
+    oz_recombine_kernel<128, 256><<<g, 256, 0, s>>>(tiles, dblocks, plans, pa, pb, ws, slices, nsplit, beta);
   else
-    oz_recombine_kernel<kOzBM><<<ntiles * per, 256, 0, s>>>(tiles, dblocks, plans, pa, pb, ws, slices, nsplit, beta);
+    oz_recombine_kernel<128, 128><<<g, 256, 0, s>>>(tiles, dblocks, plans, pa, pb, ws, slices, nsplit, beta);
   A4G_CUDA(cudaGetLastError());
   return A4G_OK;
 }

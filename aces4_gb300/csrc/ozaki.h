@@ -18,10 +18,11 @@ int oz_launch_exp(int layout, const OzSplitJob* jobs, const int64_t* prefix, int
                   const OzPanel* panels, cudaStream_t s);
 int oz_launch_split(int layout, const OzSplitJob* jobs, const int64_t* prefix, int njobs, int64_t ntiles,
                     const OzPanel* panels, int slices, cudaStream_t s);
-// pair = false: 1-SM kernel, 128x128 tiles; pair = true: CTA-pair kernel
-// (cluster of 2, cta_group::2), 256x128 tiles, grid even.
-int oz_launch_gemm(const OzGemmArgs& args, int grid, bool pair, cudaStream_t s);
-int oz_launch_recombine(const OzTile* tiles, int ntiles, int tile_rows, const OzDBlock* dblocks,
+// pair = false: 1-SM kernel, 128 x tile_cols tiles; pair = true: CTA-pair
+// kernel (cluster of 2, cta_group::2), 256 x tile_cols tiles, grid even.
+// tile_cols: 128 (exact sums kept in TMEM) or 256 (exact sums in registers).
+int oz_launch_gemm(const OzGemmArgs& args, int grid, bool pair, int tile_cols, cudaStream_t s);
+int oz_launch_recombine(const OzTile* tiles, int ntiles, int tile_rows, int tile_cols, const OzDBlock* dblocks,
                         const PlanRef* plans, const OzPanel* pa, const OzPanel* pb, const int* ws, int slices,
                         int nsplit, int beta, cudaStream_t s);
 

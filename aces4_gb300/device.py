@@ -217,11 +217,16 @@ class Batch:
                "a4g_batch_info")
         return {"pairs": pairs.value, "flops": flops.value, "device_bytes": ws.value}
 
+    FORMS = {1: "one SM per 128x128 tile", 2: "CTA pair per 256x128 tile", 3: "one SM per 128x256 tile",
+             4: "CTA pair per 256x256 tile"}
+
     def form(self):
-        """(form, autotune ms of the 1-SM form, of the CTA-pair form)."""
-        f, a, b = ctypes.c_int(0), ctypes.c_float(-1), ctypes.c_float(-1)
-        _check(lib().a4g_batch_form(self._h, ctypes.byref(f), ctypes.byref(a), ctypes.byref(b)), "a4g_batch_form")
-        return {"form": f.value, "tuned_ms_one_sm": a.value, "tuned_ms_pair": b.value}
+        """The tensor-core GEMM form in use and the autotuner's ms per form."""
+        f = ctypes.c_int(0)
+        ms = (ctypes.c_float * 4)()
+        _check(lib().a4g_batch_form(self._h, ctypes.byref(f), ms, 4), "a4g_batch_form")
+        return {"form": f.value, "name": self.FORMS.get(f.value),
+                "tuned_ms": {self.FORMS[i + 1]: float(ms[i]) for i in range(4) if ms[i] >= 0}}
 
     def close(self):
         if getattr(self, "_h", None) and self._h.value:

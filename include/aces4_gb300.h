@@ -214,9 +214,10 @@ typedef struct a4g_batch_opts {
                       the relative error near 1e-11, 6 near 1e-13.          */
   int beta;        /* 0: D = sum of products (overwrite); 1: D += sum        */
   int variant;     /* split precision, tensor-core GEMM form: 0 autotuned at
-                      creation (each form timed once, the faster kept),
+                      creation (each form timed once, the fastest kept),
                       1: one SM per 128x128 tile, 2: a CTA pair per 256x128
-                      tile (cta_group::2)                                    */
+                      tile (cta_group::2), 3: one SM per 128x256 tile,
+                      4: a CTA pair per 256x256 tile                          */
   int reserved[4];
 } a4g_batch_opts;
 
@@ -237,9 +238,9 @@ int a4g_batch_run_timed(a4g_batch* b, void* stream);
 int a4g_batch_timings(a4g_batch* b, float* phase_ms, int nphase, int* runs);
 /* Number of block pairs executed (zero blocks skipped) and FP64 flops. */
 int a4g_batch_info(const a4g_batch* b, int64_t* pairs, double* flops, int64_t* workspace_bytes);
-/* The tensor-core GEMM form in use (1: one SM per tile, 2: CTA pair; 0 for
- * FP64 batches) and the autotuner's timings of both forms (ms, -1 if not run). */
-int a4g_batch_form(const a4g_batch* b, int* form, float* ms_one_sm, float* ms_pair);
+/* The tensor-core GEMM form in use (the `variant` numbering; 0 for FP64
+ * batches) and the autotuner's timing of each form in ms (-1: not run). */
+int a4g_batch_form(const a4g_batch* b, int* form, float* tuned_ms, int n);
 void a4g_batch_destroy(a4g_batch* b);
 
 #ifdef __cplusplus

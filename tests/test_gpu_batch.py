@@ -138,7 +138,7 @@ def test_fp64_uneven_sparse_ring(a4):
     assert errs.max() <= TOL_FP64
 
 
-@pytest.mark.parametrize("variant", [1, 2])
+@pytest.mark.parametrize("variant", [1, 2, 3, 4])
 def test_split_one_slice_integer_exact(a4, variant):
     # integers in [-127, 127] are exact single 8-bit digits: the tensor-core
     # products and the chunked FP32 accumulation must reproduce FP64 exactly,
@@ -151,7 +151,7 @@ def test_split_one_slice_integer_exact(a4, variant):
         np.testing.assert_array_equal(R.block(k).cpu().numpy(), want)
 
 
-@pytest.mark.parametrize("variant", [1, 2])
+@pytest.mark.parametrize("variant", [1, 2, 3, 4])
 def test_split_long_k_integer_exact(a4, variant):
     # K per destination row = 16 * 48^2 = 36864 (several exact flush chunks,
     # several levels' chunk sizes) with 2 slices on integer data
@@ -167,7 +167,7 @@ def test_split_ladder_outliers(a4, slices, tol):
     # config-4 distributions (V ~ U[-1,1]/v, T ~ N(0,1e-2) with 1% x1e3) on a
     # smaller ladder: v=64 in 2 segments of 32, o=32 in 2 segments of 16
     R, V, T, trip, labels = _make(a4, "ladder", [32, 32], [16, 16], 0.0, 5, outliers=True)
-    _run(a4, R, trip, labels, a4.device.PREC_OZAKI_BF16, slices=slices, variant=2 if slices % 2 else 1)
+    _run(a4, R, trip, labels, a4.device.PREC_OZAKI_BF16, slices=slices, variant=1 + slices % 4)
     errs = _errors(R, _reference(R, trip, labels))
     assert errs.max() <= tol, (slices, errs.max())
 
