@@ -92,3 +92,30 @@ def ring_triples(R: BlockArray, V: BlockArray, T: BlockArray):
             rk, vk, tk = (a, i, b, j), (a, k, c, i), (c, b, k, j)
             out.append((R.block(rk), V.block(vk), T.block(tk), R.ext(rk), V.ext(vk), T.ext(tk)))
     return out
+
+
+def segments_uniform(total: int, lo: int, hi: int, seed: int):
+    """Segment sizes drawn uniformly from [lo, hi] (seeded) until they cover
+    `total`; the last segment absorbs the remainder."""
+    rng = np.random.default_rng(seed)
+    segs, acc = [], 0
+    while total - acc > hi:
+        s = int(rng.integers(lo, hi + 1))
+        segs.append(s)
+        acc += s
+    if total - acc > 0:
+        segs.append(total - acc)
+    return segs
+
+
+def segments_choice(total: int, choices, seed: int):
+    """Segment sizes drawn from `choices` (seeded) summing exactly to `total`."""
+    rng = np.random.default_rng(seed)
+    choices = sorted(choices)
+    segs, acc = [], 0
+    while acc < total:
+        fit = [c for c in choices if acc + c <= total and (total - acc - c == 0 or total - acc - c >= choices[0])]
+        s = int(rng.choice(fit))
+        segs.append(s)
+        acc += s
+    return segs

@@ -11,8 +11,10 @@
 // over levels t < slices (triangular truncation).  Each S_t is computed on the
 // tensor cores (kind::f16, BF16 x BF16 -> FP32) in chunks of k short enough
 // that every FP32 partial sum is an integer below 2^24 and therefore exact;
-// the epilogue warps fold each chunk into an exact FP32 (hi, lo) pair with
-// TwoSum.  A final FP64 kernel applies the powers of two and writes D.
+// the epilogue warps fold each chunk into an exact running sum (an FP32 (hi,
+// lo) TwoSum pair kept in TMEM for 128-column tiles, int32 registers for
+// 256-column tiles).  A final FP64 kernel applies the powers of two and
+// writes D.
 //
 // Published method: Ozaki, Ogita, Oishi, Rump, "Error-free transformations of
 // matrix multiplication by using fast routines of matrix multiplication and
@@ -21,14 +23,18 @@
 // Versions", ISC 2020 (slices on tensor cores with exact FP32 accumulation).
 //
 // Kernels:
-//   oz_exp_kernel       max exponent per panel row          (HBM: 8 B/elem read)
-//   oz_split_kernel     FP64 -> BF16 digit slices, K-major   (HBM: 8 B read + 2*slices B write)
+//   oz_exp_*_kernel     max exponent per panel row          (HBM: 8 B/elem read)
+//   oz_split_*_kernel   FP64 -> BF16 digit slices, K-major   (HBM: 8 B read + 2*slices B write)
 //                       with the block's index permute folded into the gather
-//   oz_gemm_kernel      persistent warp-specialised tcgen05 GEMM: TMA (SW128)
-//                       -> 6-stage smem ring -> tcgen05.mma into TMEM (2 buffers)
-//                       -> epilogue warps fold each chunk into (hi, lo) sums
-//                       that also live in TMEM (tcgen05.ld / tcgen05.st)
-//   oz_recombine_kernel FP64 combination of the levels, scaled store into D
+//   oz_gemm_kernel<PAIR, BN>
+//                       persistent warp-specialised tcgen05 GEMM: TMA (SW128)
+//                       -> smem ring -> tcgen05.mma into TMEM (2 accumulators)
+//                       -> epilogue warps fold each exact chunk into the level
+//                       sum.  Four forms: one SM or a CTA pair (cta_group::2)
+//                       per tile, 128 or 256 columns per MMA; the batch
+//                       autotunes among them.
+//   oz_recombine_kernel int64 sum over split-K units, FP64 combination of the
+//                       levels, scaled store into D
 #include <cuda.h>
 #include <cuda_bf16.h>
 #include <cudaTypedefs.h>
@@ -46,8 +52,10 @@ namespace {
 constexpr int kDigitBits = 8;
 constexpr int kThreadsOz = 320;  // warp 0 TMA, warp 1 MMA, warps 2..9 epilogue
 constexpr uint32_t kTileBytes = kOzBM * kOzBK * 2;  // 16 KB per operand tile
-// TMEM columns: [0,128) and [128,256) are the two FP32 MMA accumulators; [256,384)
-// and [384,512) hold the running exact (hi, lo) sums of the current level.
+// TMEM columns, 128-column forms: [0,128) and [128,256) are the two FP32 MMA
+// accumulators; [256,384) and [384,512) hold the running exact (hi, lo) sums of
+// the current level.  256-column forms: [0,256) and [256,512) are the two
+// accumulators; the level sums live in the epilogue threads' registers.
 constexpr uint32_t kTmemCols = 512;
 constexpr uint32_t kTmemHi = 256, kTmemLo = 384;
 constexpr unsigned long long kWaitLimitNs = 20ull * 1000 * 1000 * 1000;  // 20 s

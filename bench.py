@@ -237,7 +237,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--slices", type=int, default=5)
     ap.add_argument("--fp64-steps", type=int, default=1)
-    ap.add_argument("--e2e-steps", type=int, default=4)
+    ap.add_argument("--e2e-steps", type=int, default=10)
     ap.add_argument("--cpu-pairs", type=int, default=16)
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--no-cpu", action="store_true")
@@ -411,7 +411,8 @@ def main():
             "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "bf16", "data": "synthetic",
             "config": {"workload": workload, "slices": S, "digits": "balanced base-256 (8-bit)", "block_pairs": info["pairs"],
-                       "l2": "inputs 10.7 GB > 126 MB L2 (no flush needed)", "parallelism": f"replicas x{world}"},
+                       "l2": f"inputs {n_elem * 8 / 1e9:.2f} GB > 126 MB L2 (no flush needed)",
+                       "parallelism": f"replicas x{world}"},
             "e2e": e2e,
             "roofline": {"kernel": "oz_gemm_kernel (tcgen05 BF16 slice products)", "bound": "tensor",
                          "achieved": achieved, "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak,
