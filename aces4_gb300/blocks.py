@@ -119,3 +119,39 @@ def segments_choice(total: int, choices, seed: int):
         segs.append(s)
         acc += s
     return segs
+
+
+# (T)-type connected triples, W(a,i,b,j,c,k) = sum_d V1(b,c,d,k) T(a,d,i,j)
+#                                            - sum_l V2(l,c,j,k) T(a,b,i,l)
+# labels: a=1 i=2 b=3 j=4 c=5 k=6 d=7 l=8; W is stored in the denominator's
+# index order (virtual, occupied, virtual, occupied, virtual, occupied), the
+# order energy_denominator_rhf's rank-6 form expects (rccsdpt_aaa.sialx:2163-2172).
+TRIPLES_TERM1_LABELS = ([1, 2, 3, 4, 5, 6], [3, 5, 7, 6], [1, 7, 2, 4])
+TRIPLES_TERM2_LABELS = ([1, 2, 3, 4, 5, 6], [8, 5, 4, 6], [1, 3, 2, 8])
+
+
+def triples_step(W: BlockArray, V1: BlockArray, V2: BlockArray, T: BlockArray, a: int, b: int):
+    """Block triples of one pardo step of the triples energy: the fixed
+    virtual segments (a, b), every c and every occupied (i, j, k).  Returns
+    (term-1 triples, term-2 triples); the second term is run with negate=1
+    and beta=1 into the same W blocks."""
+    nv, no = len(T.segs[0]), len(T.segs[2])
+    t1, t2 = [], []
+    for c in range(nv):
+        for i, j, k in itertools.product(range(no), repeat=3):
+            wk = (a, i, b, j, c, k)
+            wb, we = W.block(wk), W.ext(wk)
+            for d in range(nv):
+                lk, rk = (b, c, d, k), (a, d, i, j)
+                t1.append((wb, V1.block(lk), T.block(rk), we, V1.ext(lk), T.ext(rk)))
+            for l in range(no):
+                lk, rk = (l, c, j, k), (a, b, i, l)
+                t2.append((wb, V2.block(lk), T.block(rk), we, V2.ext(lk), T.ext(rk)))
+    return t1, t2
+
+
+def triples_index_values(key, n_occ_segs: int):
+    """1-based global segment numbers of W block `key` (occupied segments
+    first, then virtual, as moa_seg_ranges lists them)."""
+    a, i, b, j, c, k = key
+    return [n_occ_segs + a + 1, i + 1, n_occ_segs + b + 1, j + 1, n_occ_segs + c + 1, k + 1]

@@ -93,6 +93,9 @@ int launch_dot(const double* a, const double* b, const int64_t* offA, const int6
                int64_t n, double* d_out, double* d_scratch, int64_t scratch_len, cudaStream_t s);
 int launch_slice_insert(int insert, int rank, double* tens, const int* tens_ext, double* slice,
                         const int* slice_ext, const int* ext_beg, cudaStream_t s);
+int launch_energy_contract(int rank0, const int* off, const int* ext0, const int* pos, const double* w,
+                           int rank1, int ld1, const double* e_or_fock, double efact, double* esum,
+                           double* d_scratch, int scratch_len, cudaStream_t s);
 int launch_denominator(int rank0, const int* off, const int* ext0, double* data, int rank1,
                        int ld1, const double* e_or_fock, cudaStream_t s);
 int launch_dot_beta(const double* a, const double* b, const int64_t* offA, const int64_t* offB,

@@ -598,4 +598,30 @@ int a4g_energy_denominator(int rank0, const int* iv, const int* ext0, double* da
   return launch_denominator(rank0, off, ext0, data0, rank1, ext1[0], e, pick(stream));
 }
 
+int a4g_energy_contract(int rank0, const int* iv, const int* ext0, const double* data0, const int* den_order,
+                        int rank1, const int* ext1, const double* e, int nsegs, const int* segs, double efact,
+                        double* esum, void* stream) {
+  int rc = ensure_init();
+  if (rc) return rc;
+  if (!iv || !ext0 || !data0 || !ext1 || !e || !esum || (nsegs > 0 && !segs))
+    return fail(A4G_ERR_ARG, "energy contraction: null argument");
+  if (!((rank0 == 2 || rank0 == 4) && (rank1 == 1 || rank1 == 2)) && !(rank0 == 6 && rank1 == 2))
+    return fail(A4G_ERR_UNSUPPORTED, "energy contraction: unsupported rank combination");
+  int pos[6];
+  bool seen[6] = {false, false, false, false, false, false};
+  for (int q = 0; q < rank0; ++q) {
+    pos[q] = den_order ? den_order[q] : q;
+    if (pos[q] < 0 || pos[q] >= rank0 || seen[pos[q]])
+      return fail(A4G_ERR_ARG, "energy contraction: den_order is not a permutation");
+    seen[pos[q]] = true;
+  }
+  int off[6];
+  rc = denominator_offsets(rank0, iv, ext0, rank1, ext1, std::vector<int>(segs, segs + std::max(nsegs, 0)), off);
+  if (rc) return rc;
+  double* scratch = reduction_scratch();
+  if (!scratch) return fail(A4G_ERR_NOMEM, "reduction scratch");
+  return launch_energy_contract(rank0, off, ext0, pos, data0, rank1, ext1[0], e, efact, esum, scratch,
+                                dot_scratch_len(), pick(stream));
+}
+
 }  // extern "C"

@@ -24,6 +24,9 @@ struct a4g_batch {
   int precision = A4G_PREC_FP64;
   int slices = 5;
   int beta = 0;
+  int negate = 0;
+  // store mode of the writing kernels: bit 0 accumulate into D, bit 1 negate
+  int store_mode() const { return beta | (negate << 1); }
   int variant = 0;  // tensor-core GEMM form: 0 autotuned, else 1 + index into forms
   int64_t pairs = 0;
   double flops = 0.0;
@@ -207,8 +210,10 @@ int build_ozaki(a4g_batch* b, const std::vector<DGroup>& groups, const std::vect
     const int tb = int(trips.size());
     int kb_total = 0;
     for (const Pair& p : g.pairs) {
-      const int nkb = int(ceil_to(plans[p.plan]->host.K, kOzBK) / kOzBK);
-      trips.push_back({pa[a].koff.at(p.l), pb[c].koff.at(p.r), nkb, 0});
+      const int64_t K = plans[p.plan]->host.K;
+      const int nkb = int(ceil_to(K, kOzBK) / kOzBK);
+      const int k16_last = K > 0 ? int(((K - 1) % kOzBK) / 16 + 1) : 4;
+      trips.push_back({pa[a].koff.at(p.l), pb[c].koff.at(p.r), nkb, k16_last});
       kb_total += nkb;
     }
     const int te = int(trips.size());
@@ -450,7 +455,7 @@ int run(a4g_batch* b, cudaStream_t s, const cudaEvent_t* ev = nullptr) {
   if ((rc = mark(1))) return rc;
   if (b->precision == A4G_PREC_FP64) {
     if ((rc = mark(2)) || (rc = mark(3))) return rc;
-    rc = launch_grouped_f64(b->d_f64_tiles, b->n_f64_tiles, b->d_f64_pairs, b->d_plans, b->beta, s);
+    rc = launch_grouped_f64(b->d_f64_tiles, b->n_f64_tiles, b->d_f64_pairs, b->d_plans, b->store_mode(), s);
     if (rc) return rc;
     if ((rc = mark(4)) || (rc = mark(5))) return rc;
     return A4G_OK;
@@ -475,7 +480,7 @@ int run(a4g_batch* b, cudaStream_t s, const cudaEvent_t* ev = nullptr) {
   if ((rc = mark(4))) return rc;
   if (gf.n_tiles > 0 &&
       (rc = oz_launch_recombine(gf.d_tiles, gf.n_tiles, gf.tile_rows, gf.tile_cols, b->d_dblocks, b->d_plans,
-                                b->d_pa, b->d_pb, b->d_ws, b->slices, gf.nsplit, b->beta, s)))
+                                b->d_pa, b->d_pb, b->d_ws, b->slices, gf.nsplit, b->store_mode(), s)))
     return rc;
   return mark(5);
 }
@@ -498,6 +503,7 @@ int a4g_batch_create(a4g_batch** out, const int* ptrn, int drank, int lrank, int
     b->precision = opts->precision;
     b->slices = opts->slices > 0 ? opts->slices : 5;
     b->beta = opts->beta ? 1 : 0;
+    b->negate = opts->negate ? 1 : 0;
     b->variant = opts->variant;
   }
   if (b->variant < 0 || b->variant > a4g_batch::kForms) return fail(A4G_ERR_ARG, "unknown GEMM variant");

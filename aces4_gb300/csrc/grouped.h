@@ -29,7 +29,7 @@ struct GroupedF64Tile {
   int pad;
 };
 int launch_grouped_f64(const GroupedF64Tile* tiles, int ntiles, const GroupedPair* pairs,
-                       const PlanRef* plans, int beta, cudaStream_t s);
+                       const PlanRef* plans, int mode, cudaStream_t s);  // mode: bit 0 accumulate, bit 1 negate
 int grouped_f64_tile_m();
 int grouped_f64_tile_n();
 
@@ -78,7 +78,7 @@ struct OzTile {
 struct OzTrip {
   int64_t koff_a, koff_b;
   int nkb;
-  int pad;
+  int k16_last;  // K16 MMA steps that reach live k in the last k block (1..4)
 };
 struct OzDBlock {
   double* d;

@@ -287,12 +287,40 @@ __global__ void __launch_bounds__(kThreads) slice_insert_kernel(SliceParams p, i
 // ---------------------------------------------------------------- denominator
 struct DenParams {
   int rank0, rank1, ld1;
-  int ext[6];
-  int off[6];
+  int ext[6];  // extents in storage order
+  int off[6];  // first orbital of each storage dimension's segment
+  int pos[6];  // storage dimension holding denominator position q
 };
 
 __device__ __forceinline__ double eps_at(const DenParams& p, const double* e, int orb) {
   return p.rank1 == 2 ? e[int64_t(orb) + int64_t(orb) * p.ld1] : e[orb];
+}
+
+// Denominator of the element with storage coordinates x, in the reference's
+// order of additions (energy_denominator_rhf.F do_rhf_den2/4/6): positions
+// 0, 2, 4 are virtual (subtracted), 1, 3, 5 occupied (added).
+__device__ __forceinline__ double den_eps(const DenParams& p, const double* e, const int (&x)[6]) {
+  const double ea = eps_at(p, e, x[p.pos[0]] + p.off[p.pos[0]]);
+  const double eb = eps_at(p, e, x[p.pos[1]] + p.off[p.pos[1]]);
+  if (p.rank0 == 2) return __dsub_rn(eb, ea);  // epsb - epsa
+  const double ec = eps_at(p, e, x[p.pos[2]] + p.off[p.pos[2]]);
+  const double ed = eps_at(p, e, x[p.pos[3]] + p.off[p.pos[3]]);
+  if (p.rank0 == 4) return __dsub_rn(__dsub_rn(__dadd_rn(eb, ed), ea), ec);  // epsb + epsd - epsa - epsc
+  const double e5 = eps_at(p, e, x[p.pos[4]] + p.off[p.pos[4]]);
+  const double e6 = eps_at(p, e, x[p.pos[5]] + p.off[p.pos[5]]);
+  return __dsub_rn(__dsub_rn(__dsub_rn(__dadd_rn(__dadd_rn(eb, ed), e6), ea), ec), e5);
+}
+
+__device__ __forceinline__ void den_coords(const DenParams& p, int64_t i, int (&x)[6]) {
+#pragma unroll
+  for (int q = 0; q < 6; ++q) {
+    if (q < p.rank0) {
+      x[q] = int(i % p.ext[q]);
+      i /= p.ext[q];
+    } else {
+      x[q] = 0;
+    }
+  }
 }
 
 __global__ void __launch_bounds__(kThreads) denominator_kernel(DenParams p, double* data,
@@ -300,30 +328,50 @@ __global__ void __launch_bounds__(kThreads) denominator_kernel(DenParams p, doub
                                                                int64_t n) {
   const int64_t stride = int64_t(gridDim.x) * blockDim.x;
   for (int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += stride) {
-    int64_t rem = i;
     int x[6];
-    for (int q = 0; q < p.rank0; ++q) {
-      x[q] = int(rem % p.ext[q]);
-      rem /= p.ext[q];
-    }
-    const double ea = eps_at(p, e, x[0] + p.off[0]);
-    const double eb = eps_at(p, e, x[1] + p.off[1]);
-    double eps;
-    if (p.rank0 == 2) {
-      eps = __dsub_rn(eb, ea);  // do_rhf_den2: epsb - epsa
-    } else if (p.rank0 == 4) {
-      const double ec = eps_at(p, e, x[2] + p.off[2]);
-      const double ed = eps_at(p, e, x[3] + p.off[3]);
-      eps = __dsub_rn(__dsub_rn(__dadd_rn(eb, ed), ea), ec);  // epsb + epsd - epsa - epsc
-    } else {
-      const double ec = eps_at(p, e, x[2] + p.off[2]);
-      const double ed = eps_at(p, e, x[3] + p.off[3]);
-      const double e5 = eps_at(p, e, x[4] + p.off[4]);
-      const double e6 = eps_at(p, e, x[5] + p.off[5]);
-      eps = __dsub_rn(__dsub_rn(__dsub_rn(__dadd_rn(__dadd_rn(eb, ed), e6), ea), ec), e5);
-    }
-    data[i] = __ddiv_rn(data[i], eps);
+    den_coords(p, i, x);
+    data[i] = __ddiv_rn(data[i], den_eps(p, e, x));
   }
+}
+
+// Fused (T)-energy pass: partial[block] = sum over this block's elements of
+// w * (w / eps), the product of the divided and the undivided element as the
+// reference forms it (rccsdpt_aaa.sialx:2163-2172).  Fixed grid and fixed
+// order: deterministic for a given GPU.
+__global__ void __launch_bounds__(kThreads) energy_partial_kernel(DenParams p, const double* __restrict__ w,
+                                                                  const double* __restrict__ e, int64_t n,
+                                                                  double* partial) {
+  double acc = 0.0;
+  const int64_t stride = int64_t(gridDim.x) * blockDim.x;
+  for (int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += stride) {
+    int x[6];
+    den_coords(p, i, x);
+    const double v = w[i];
+    acc = __dadd_rn(acc, __dmul_rn(__ddiv_rn(v, den_eps(p, e, x)), v));
+  }
+  __shared__ double red[kThreads / 32];
+  for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = acc;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double s = 0.0;
+    for (int q = 0; q < kThreads / 32; ++q) s += red[q];
+    partial[blockIdx.x] = s;
+  }
+}
+
+// *esum += efact * (fixed-order sum of the partials)
+__global__ void energy_final_kernel(const double* partial, int np, double efact, double* esum) {
+  __shared__ double red[kThreads];
+  double acc = 0.0;
+  for (int i = threadIdx.x; i < np; i += blockDim.x) acc += partial[i];
+  red[threadIdx.x] = acc;
+  __syncthreads();
+  for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+    if (threadIdx.x < s) red[threadIdx.x] += red[threadIdx.x + s];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) *esum = __dadd_rn(*esum, __dmul_rn(red[0], efact));
 }
 
 // ---------------------------------------------------------------- scalar cases
@@ -474,19 +522,39 @@ int launch_slice_insert(int insert, int rank, double* tens, const int* tens_ext,
   return A4G_OK;
 }
 
-int launch_denominator(int rank0, const int* off, const int* ext0, double* data, int rank1,
-                       int ld1, const double* e_or_fock, cudaStream_t s) {
+static DenParams den_params(int rank0, const int* off, const int* ext0, const int* pos, int rank1, int ld1,
+                            int64_t* n) {
   DenParams p{};
   p.rank0 = rank0;
   p.rank1 = rank1;
   p.ld1 = ld1;
-  int64_t n = 1;
+  *n = 1;
   for (int q = 0; q < rank0; ++q) {
     p.ext[q] = ext0[q];
     p.off[q] = off[q];
-    n *= ext0[q];
+    p.pos[q] = pos ? pos[q] : q;
+    *n *= ext0[q];
   }
+  return p;
+}
+
+int launch_denominator(int rank0, const int* off, const int* ext0, double* data, int rank1,
+                       int ld1, const double* e_or_fock, cudaStream_t s) {
+  int64_t n = 0;
+  const DenParams p = den_params(rank0, off, ext0, nullptr, rank1, ld1, &n);
   denominator_kernel<<<grid_for(n), kThreads, 0, s>>>(p, data, e_or_fock, n);
+  A4G_CUDA(cudaGetLastError());
+  return A4G_OK;
+}
+
+int launch_energy_contract(int rank0, const int* off, const int* ext0, const int* pos, const double* w,
+                           int rank1, int ld1, const double* e_or_fock, double efact, double* esum,
+                           double* d_scratch, int scratch_len, cudaStream_t s) {
+  int64_t n = 0;
+  const DenParams p = den_params(rank0, off, ext0, pos, rank1, ld1, &n);
+  const int g = std::max(1, std::min(grid_for(n), scratch_len));
+  energy_partial_kernel<<<g, kThreads, 0, s>>>(p, w, e_or_fock, n, d_scratch);
+  energy_final_kernel<<<1, kThreads, 0, s>>>(d_scratch, g, efact, esum);
   A4G_CUDA(cudaGetLastError());
   return A4G_OK;
 }

@@ -109,9 +109,10 @@ __device__ void accumulate_pair(Smem& sm, double (&acc)[4][4][2], const double* 
   }
 }
 
+// mode bit 0: accumulate into D (beta = 1), bit 1: store the negated sum.
 __device__ void write_tile(const double (&acc)[4][4][2], double* __restrict__ D,
                            const int64_t* __restrict__ offDm, const int64_t* __restrict__ offDn,
-                           int M, int N, int m0, int n0, int beta) {
+                           int M, int N, int m0, int n0, int mode) {
   const int t = threadIdx.x, warp = t >> 5, lane = t & 31;
   const int g = lane >> 2, tig = lane & 3;
   const int wm = (warp & 1) * 32, wn = (warp >> 1) * 32;
@@ -127,7 +128,8 @@ __device__ void write_tile(const double (&acc)[4][4][2], double* __restrict__ D,
         const int n = n0 + wn + j * 8 + 2 * tig + h;
         if (n >= N) continue;
         double* p = &D[om + offDn[n]];
-        *p = beta ? *p + acc[i][j][h] : acc[i][j][h];
+        const double v = (mode & 2) ? -acc[i][j][h] : acc[i][j][h];
+        *p = (mode & 1) ? *p + v : v;
       }
     }
   }
@@ -138,7 +140,7 @@ __global__ void __launch_bounds__(kThreadsF64) contract_f64_kernel(
     const int64_t* __restrict__ offLm, const int64_t* __restrict__ offLk,
     const int64_t* __restrict__ offRk, const int64_t* __restrict__ offRn,
     const int64_t* __restrict__ offDm, const int64_t* __restrict__ offDn, int M, int N, int K,
-    int tiles_m, int beta, int a_kfast, int b_kfast) {
+    int tiles_m, int mode, int a_kfast, int b_kfast) {
   __shared__ __align__(16) Smem sm;
   const int tm = blockIdx.x % tiles_m, tn = blockIdx.x / tiles_m;
   const int m0 = tm * BM, n0 = tn * BN;
@@ -148,14 +150,14 @@ __global__ void __launch_bounds__(kThreadsF64) contract_f64_kernel(
 #pragma unroll
     for (int j = 0; j < 4; ++j) acc[i][j][0] = acc[i][j][1] = 0.0;
   accumulate_pair(sm, acc, L, R, offLm, offLk, offRk, offRn, M, N, K, m0, n0, a_kfast, b_kfast);
-  write_tile(acc, D, offDm, offDn, M, N, m0, n0, beta);
+  write_tile(acc, D, offDm, offDn, M, N, m0, n0, mode);
 }
 
 // One CTA per (destination block, 64x64 tile); the block's pairs are summed.
 __global__ void __launch_bounds__(kThreadsF64) grouped_f64_kernel(const GroupedF64Tile* __restrict__ tiles,
                                                                   const GroupedPair* __restrict__ pairs,
                                                                   const PlanRef* __restrict__ plans,
-                                                                  int beta) {
+                                                                  int mode) {
   __shared__ __align__(16) Smem sm;
   const GroupedF64Tile tl = tiles[blockIdx.x];
   double acc[4][4][2];
@@ -170,12 +172,12 @@ __global__ void __launch_bounds__(kThreadsF64) grouped_f64_kernel(const GroupedF
                     tl.m0, tl.n0, pl.a_kfast, pl.b_kfast);
   }
   const PlanRef dp = plans[tl.dplan];
-  write_tile(acc, tl.d, dp.offDm, dp.offDn, dp.M, dp.N, tl.m0, tl.n0, beta);
+  write_tile(acc, tl.d, dp.offDm, dp.offDn, dp.M, dp.N, tl.m0, tl.n0, mode);
 }
 
 }  // namespace
 
-int launch_contract_f64(const DevPlan* p, const double* L, const double* R, double* D, int beta,
+int launch_contract_f64(const DevPlan* p, const double* L, const double* R, double* D, int mode,
                         cudaStream_t s) {
   const GemmPlan& h = p->host;
   if (h.M > 0x7fffffff || h.N > 0x7fffffff || h.K > 0x7fffffff)
@@ -186,15 +188,15 @@ int launch_contract_f64(const DevPlan* p, const double* L, const double* R, doub
   if (grid > 0x7fffffffLL) return fail(A4G_ERR_RANGE, "contraction grid too large");
   contract_f64_kernel<<<unsigned(grid), kThreadsF64, 0, s>>>(L, R, D, p->offLm, p->offLk, p->offRk,
                                                             p->offRn, p->offDm, p->offDn, M, N, K,
-                                                            int(tiles_m), beta, h.a_kfast, h.b_kfast);
+                                                            int(tiles_m), mode, h.a_kfast, h.b_kfast);
   A4G_CUDA(cudaGetLastError());
   return A4G_OK;
 }
 
 int launch_grouped_f64(const GroupedF64Tile* tiles, int ntiles, const GroupedPair* pairs,
-                       const PlanRef* plans, int beta, cudaStream_t s) {
+                       const PlanRef* plans, int mode, cudaStream_t s) {
   if (ntiles <= 0) return A4G_OK;
-  grouped_f64_kernel<<<ntiles, kThreadsF64, 0, s>>>(tiles, pairs, plans, beta);
+  grouped_f64_kernel<<<ntiles, kThreadsF64, 0, s>>>(tiles, pairs, plans, mode);
   A4G_CUDA(cudaGetLastError());
   return A4G_OK;
 }

@@ -273,7 +273,10 @@ __device__ __forceinline__ void two_sum_acc(float& hi, float& lo, float x) {
 }
 
 // ------------------------------------------------------------------ roles
-// Walks the k blocks of one unit: calls f(koff_a, koff_b, kb) per 64-wide block.
+// Walks the k blocks of one unit: calls f(koff_a, koff_b, kb, k16) per 64-wide
+// block; k16 = the K16 MMA steps that reach live k (fewer than 4 only in the
+// last block of a pair whose K is not a multiple of 64: the panel's zero
+// padding beyond K need not be multiplied).
 template <class F>
 __device__ __forceinline__ void for_unit_kblocks(const OzGemmArgs& a, const OzUnit& un, const OzTile& tl,
                                                  F&& f) {
@@ -282,7 +285,8 @@ __device__ __forceinline__ void for_unit_kblocks(const OzGemmArgs& a, const OzUn
   while (kb < un.kb_end && q < tl.trip_end) {
     const OzTrip tr = a.trips[q];
     for (; j < tr.nkb && kb < un.kb_end; ++j, ++kb)
-      if (!f(int(tr.koff_a) + j * kOzBK, int(tr.koff_b) + j * kOzBK, kb)) return;
+      if (!f(int(tr.koff_a) + j * kOzBK, int(tr.koff_b) + j * kOzBK, kb, j + 1 == tr.nkb ? tr.k16_last : 4))
+        return;
     ++q;
     j = 0;
   }
@@ -310,7 +314,7 @@ __device__ void producer(const OzGemmArgs& a, OzSmemT<PAIR, BN>& sm, uint32_t ra
     const int arow = tl.m0 + int(rank) * kOzBM;          // this CTA's 128 rows of A
     const int brow = tl.n0 + int(rank) * (BN / 2);       // this CTA's half of B (pair form)
     bool ok = true;
-    for_unit_kblocks(a, un, tl, [&](int ka, int kb, int) {
+    for_unit_kblocks(a, un, tl, [&](int ka, int kb, int, int) {
       for (int i = 0; i <= level; ++i) {
         const int s = it % SM::kSt;
         const uint32_t ph = (it / SM::kSt) & 1;
@@ -346,7 +350,7 @@ __device__ void mma_issuer(const OzGemmArgs& a, OzSmemT<PAIR, BN>& sm, uint32_t 
     int in_chunk = 0;
     uint32_t buf = 0;
     bool ok = true;
-    for_unit_kblocks(a, un, tl, [&](int, int, int kb) {
+    for_unit_kblocks(a, un, tl, [&](int, int, int kb, int k16) {
       if (in_chunk == 0) {
         buf = chunk & 1;
         if (!mbar_wait(&sm.acc_empty[buf], ((chunk >> 1) & 1) ^ 1, sm, a.err_flag, 2)) return ok = false;
@@ -361,6 +365,7 @@ __device__ void mma_issuer(const OzGemmArgs& a, OzSmemT<PAIR, BN>& sm, uint32_t 
         const uint64_t ad = sw128_desc(sm.a[s]), bd = sw128_desc(sm.b[s]);
 #pragma unroll
         for (int kk = 0; kk < kOzBK / 16; ++kk) {
+          if (kk >= k16) break;
           const uint32_t acc = (in_chunk == 0 && i == 0 && kk == 0) ? 0u : 1u;
           if constexpr (PAIR) tc_mma_pair<BN>(d_tmem, ad + 2 * kk, bd + 2 * kk, acc);
           else tc_mma<BN>(d_tmem, ad + 2 * kk, bd + 2 * kk, acc);
@@ -917,7 +922,7 @@ __global__ void __launch_bounds__(256) oz_recombine_kernel(const OzTile* __restr
                                                            const OzPanel* __restrict__ pa,
                                                            const OzPanel* __restrict__ pb,
                                                            const int* __restrict__ ws, int slices,
-                                                           int nsplit, int beta) {
+                                                           int nsplit, int mode) {
   constexpr int kBlocksPerTile = ROWS * COLS / 256;
   const int tile = blockIdx.x / kBlocksPerTile;
   const int e = (blockIdx.x % kBlocksPerTile) * 256 + threadIdx.x;
@@ -944,8 +949,9 @@ __global__ void __launch_bounds__(256) oz_recombine_kernel(const OzTile* __restr
   }
   const int E = (ea[m] ? ea[m] : 1) - 1022, F = (eb[n] ? eb[n] : 1) - 1022;
   v = ldexp(v, E + F + 2);
+  if (mode & 2) v = -v;  // negated term
   double* dst = db.d + pl.offDm[m] + pl.offDn[n];
-  *dst = beta ? *dst + v : v;
+  *dst = (mode & 1) ? *dst + v : v;
 }
 
 using EncodeTiled = PFN_cuTensorMapEncodeTiled_v12000;
@@ -1108,19 +1114,19 @@ int oz_launch_gemm(const OzGemmArgs& args, int grid, bool pair, int tile_cols, c
 
 int oz_launch_recombine(const OzTile* tiles, int ntiles, int tile_rows, int tile_cols, const OzDBlock* dblocks,
                         const PlanRef* plans, const OzPanel* pa, const OzPanel* pb, const int* ws, int slices,
-                        int nsplit, int beta, cudaStream_t s) {
+                        int nsplit, int mode, cudaStream_t s) {
   if (ntiles <= 0) return A4G_OK;
   const int per = tile_rows * tile_cols / 256;
   if (int64_t(ntiles) * per > 0x7fffffffLL) return fail(A4G_ERR_RANGE, "too many tiles");
   const unsigned g = unsigned(ntiles * per);
   if (tile_rows == 256 && tile_cols == 256)
-    oz_recombine_kernel<256, 256><<<g, 256, 0, s>>>(tiles, dblocks, plans, pa, pb, ws, slices, nsplit, beta);
+    oz_recombine_kernel<256, 256><<<g, 256, 0, s>>>(tiles, dblocks, plans, pa, pb, ws, slices, nsplit, mode);
   else if (tile_rows == 256)
-    oz_recombine_kernel<256, 128><<<g, 256, 0, s>>>(tiles, dblocks, plans, pa, pb, ws, slices, nsplit, beta);
+    oz_recombine_kernel<256, 128><<<g, 256, 0, s>>>(tiles, dblocks, plans, pa, pb, ws, slices, nsplit, mode);
   else if (tile_cols == 256)
-    oz_recombine_kernel<128, 256><<<g, 256, 0, s>>>(tiles, dblocks, plans, pa, pb, ws, slices, nsplit, beta);
+    oz_recombine_kernel<128, 256><<<g, 256, 0, s>>>(tiles, dblocks, plans, pa, pb, ws, slices, nsplit, mode);
   else
-    oz_recombine_kernel<128, 128><<<g, 256, 0, s>>>(tiles, dblocks, plans, pa, pb, ws, slices, nsplit, beta);
+    oz_recombine_kernel<128, 128><<<g, 256, 0, s>>>(tiles, dblocks, plans, pa, pb, ws, slices, nsplit, mode);
   A4G_CUDA(cudaGetLastError());
   return A4G_OK;
 }

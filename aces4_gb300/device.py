@@ -138,6 +138,18 @@ def energy_denominator(index_values, ext0, data0, ext1, e_or_fock, seg_sizes, st
     _check(rc, "a4g_energy_denominator")
 
 
+def energy_contract(index_values, ext0, data0, ext1, e_or_fock, seg_sizes, efact, esum, den_order=None,
+                    stream=None):
+    """esum (1-element CUDA float64 tensor) += efact * sum w * (w / eps): the
+    fused (T)-energy pass of one block (a4g_energy_contract)."""
+    order = _iarr(den_order) if den_order is not None else None
+    rc = lib().a4g_energy_contract(_i(len(ext0)), _iarr(index_values), _iarr(ext0), ctypes.c_void_p(_ptr(data0)),
+                                   order, _i(len(ext1)), _iarr(ext1), ctypes.c_void_p(_ptr(e_or_fock)),
+                                   _i(len(seg_sizes)), _iarr(seg_sizes), ctypes.c_double(efact),
+                                   ctypes.c_void_p(_ptr(esum)), _stream(stream))
+    _check(rc, "a4g_energy_contract")
+
+
 # ------------------------------------------------ legacy GPU API (synchronous)
 def gpu_contract(y, ydims, yinds, x1, x1dims, x1inds, x2, x2dims, x2inds):
     lib()._gpu_contract(ctypes.c_void_p(_ptr(y)), _i(len(ydims)), _iarr(ydims), _iarr(yinds),
@@ -162,7 +174,7 @@ class _Triple(ctypes.Structure):
 
 class _Opts(ctypes.Structure):
     _fields_ = [("precision", ctypes.c_int), ("slices", ctypes.c_int), ("beta", ctypes.c_int),
-                ("variant", ctypes.c_int), ("reserved", ctypes.c_int * 4)]
+                ("variant", ctypes.c_int), ("negate", ctypes.c_int), ("reserved", ctypes.c_int * 3)]
 
 
 def _ext6(e):
@@ -179,13 +191,14 @@ class Batch:
     device addresses) and per-block extents.
     """
 
-    def __init__(self, ptrn, drank, lrank, rrank, triples, precision=PREC_FP64, slices=5, beta=0, variant=0):
+    def __init__(self, ptrn, drank, lrank, rrank, triples, precision=PREC_FP64, slices=5, beta=0, variant=0,
+                 negate=False):
         tl = list(triples)
         arr = (_Triple * max(1, len(tl)))()
         for i, (d, l, r, de, le, re) in enumerate(tl):
             arr[i].d, arr[i].l, arr[i].r = _ptr(d), _ptr(l), _ptr(r)
             arr[i].dext, arr[i].lext, arr[i].rext = _ext6(de), _ext6(le), _ext6(re)
-        opts = _Opts(precision, slices, beta, variant)
+        opts = _Opts(precision, slices, beta, variant, int(bool(negate)))
         h = ctypes.c_void_p(0)
         rc = lib().a4g_batch_create(ctypes.byref(h), _iarr(ptrn), _i(drank), _i(lrank), _i(rrank), arr,
                                     ctypes.c_int64(len(tl)), ctypes.byref(opts))

@@ -187,6 +187,21 @@ int a4g_insert(int rank, double* tens, const int* tens_ext, const double* slice,
 int a4g_energy_denominator(int rank0, const int* index_values0, const int* ext0, double* data0,
                            int rank1, const int* ext1, const double* e_or_fock, int nsegs,
                            const int* seg_sizes, void* stream);
+/* Energy contribution of one block, the (T) pattern of
+ * src/sialx/qm/cc/rccsdpt_aaa.sialx:2163-2172 (permute to the denominator's
+ * index order, energy_denominator_rhf, full contraction of the divided block
+ * with the undivided one, times efact, added to esum) fused into one read of
+ * data0 that leaves data0 unchanged:
+ *     *esum += efact * sum_x data0[x] * (data0[x] / eps(x))
+ * with eps(x) formed exactly as a4g_energy_denominator forms it.
+ * index_values0 / ext0 follow data0's storage order; den_order[q] names the
+ * dimension of data0 at position q of the denominator's order (virtual,
+ * occupied, virtual, occupied, ...), NULL when data0 is stored in that order.
+ * esum is a device double.  The sum is deterministic on a given GPU; calls
+ * share the library's reduction scratch, so keep them on one stream. */
+int a4g_energy_contract(int rank0, const int* index_values0, const int* ext0, const double* data0,
+                        const int* den_order, int rank1, const int* ext1, const double* e_or_fock,
+                        int nsegs, const int* seg_sizes, double efact, double* esum, void* stream);
 
 /* ----------------------------------------------------------------------------
  * Batched contraction of one pardo step (one call, many block triples).
@@ -218,7 +233,10 @@ typedef struct a4g_batch_opts {
                       1: one SM per 128x128 tile, 2: a CTA pair per 256x128
                       tile (cta_group::2), 3: one SM per 128x256 tile,
                       4: a CTA pair per 256x256 tile                          */
-  int reserved[4];
+  int negate;      /* 1: subtract the products: D = -sum (beta 0) or
+                      D -= sum (beta 1), e.g. the second term of
+                      W = A*B - C*E run as a second batch on the same D      */
+  int reserved[3];
 } a4g_batch_opts;
 
 /* Opaque handle of a planned pardo step: pattern + triple list + workspace. */

@@ -209,3 +209,34 @@ def contract_blas(ptrn, l, lext, r, rext, dext, threads: int | None = None) -> n
         return dtp
     mext = [dext[p - 1] for p in do2n]
     return tensor_block_copy(mext, do2n, dtp)[1]
+
+
+def energy_contract(index_values, ext0, w, ext1, fock, seg_sizes, efact, den_order=None) -> float:
+    """The (T) energy pattern of one block, rccsdpt_aaa.sialx:2163-2172, as
+    the reference's operations: permute the block into the denominator's index
+    order (tensor_block_copy_), divide a copy by the orbital-energy
+    denominators (energy_denominator_rhf), contract the divided block with the
+    undivided one to a scalar (tensor_block_contract_ with drank 0, i.e.
+    tensor_block_fcontract), multiply by efact.  Returns the contribution
+    added to esum."""
+    w = np.ascontiguousarray(w, dtype=np.float64).reshape(-1)
+    r = len(ext0)
+    order = list(den_order) if den_order is not None else list(range(r))
+    if order != list(range(r)):
+        o2n = [0] * r
+        for q, dim in enumerate(order):
+            o2n[dim] = q + 1
+        ierr, wp = tensor_block_copy(ext0, o2n, w)
+        assert ierr == 0
+    else:
+        wp = w.copy()
+    ext_p = [ext0[d] for d in order]
+    iv_p = [index_values[d] for d in order]
+    wd = wp.copy()
+    assert energy_denominator_rhf(iv_p, ext_p, wd, ext1, np.ascontiguousarray(fock, dtype=np.float64), seg_sizes) == 0
+    labels = list(range(1, r + 1))
+    ierr, ptrn = get_contraction_ptrn(0, r, r, labels + labels)
+    assert ierr == 0
+    etemp = np.zeros(1)
+    assert tensor_block_contract(ptrn, wd, ext_p, wp, ext_p, etemp, []) == 0
+    return float(etemp[0] * efact)

@@ -256,3 +256,35 @@ def test_energy_denominator(rank0, rank1):
             den = ev[1] + ev[3] + ev[5] - ev[0] - ev[2] - ev[4]
         ref[idx] = blk[idx] / den
     np.testing.assert_array_equal(out, ref.ravel(order="F"))
+
+
+@pytest.mark.parametrize("rank0,rank1,permuted", [(6, 2, False), (6, 2, True), (4, 1, True), (2, 2, False)])
+def test_energy_contract_oracle_against_loops(rank0, rank1, permuted):
+    """The oracle's (T) energy pattern (permute, divide, contract to scalar,
+    scale) against a plain loop over the block."""
+    rng = np.random.default_rng(100 + rank0 * 10 + rank1 + permuted)
+    segs = [2, 3, 3]
+    norb = sum(segs)
+    e = np.concatenate([rng.uniform(-2, -0.5, 2), rng.uniform(0.2, 5, 6)])
+    f1 = np.diag(e).ravel(order="F") if rank1 == 2 else e.copy()
+    ext1 = [norb, norb] if rank1 == 2 else [norb]
+    # denominator order: virtual, occupied, virtual, ...
+    iv_d = [[2, 3][q // 2 % 2] if q % 2 == 0 else 1 for q in range(rank0)]
+    ext_d = [segs[v - 1] for v in iv_d]
+    store = list(range(rank0))
+    if permuted:
+        store = [q for q in range(0, rank0, 2)] + [q for q in range(1, rank0, 2)]  # (v.., o..)
+    ext_s = [ext_d[p] for p in store]
+    iv_s = [iv_d[p] for p in store]
+    den_order = [store.index(q) for q in range(rank0)]
+    w = rng.standard_normal(kat.size(ext_s))
+    got = oracle.energy_contract(iv_s, ext_s, w, ext1, f1, segs, 0.75, den_order=den_order)
+    W = w.reshape(ext_s, order="F")
+    offs = [sum(segs[: v - 1]) for v in iv_s]
+    ref = 0.0
+    for idx in np.ndindex(*ext_s):
+        ev = {store[s]: e[idx[s] + offs[s]] for s in range(rank0)}
+        occ = sum(ev[q] for q in range(1, rank0, 2))
+        vir = sum(ev[q] for q in range(0, rank0, 2))
+        ref += W[idx] * (W[idx] / (occ - vir))
+    assert abs(got - 0.75 * ref) <= 1e-13 * abs(ref)
