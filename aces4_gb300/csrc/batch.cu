@@ -11,6 +11,7 @@
 #include <algorithm>
 #include <cstring>
 #include <map>
+#include <set>
 #include <memory>
 #include <vector>
 
@@ -140,18 +141,37 @@ struct alignas(64) MapBytes {  // host image of one CUtensorMap (128 bytes, 64-b
 };
 
 // Panel of one operand side: the distinct blocks feeding a set of destination
-// rows (A) or columns (B), each with its k offset inside the panel.
+// rows (A) or columns (B), each with its k offset inside the panel.  Blocks
+// are packed at a 16-column granularity (32-byte aligned TMA coordinates,
+// zero padded to it), so pairs that sit back to back in both panels run as
+// one stretch of k.  In the A panel every stretch starts on a 64-column
+// boundary and its last block is zero padded to the next one, so the last
+// 64-wide k block of a stretch multiplies A's zeros beyond it.
 struct PanelBuild {
-  std::vector<const double*> key;  // sorted block pointers
+  std::vector<const double*> key;    // sorted block pointers
+  std::vector<const double*> order;  // blocks in panel order
   std::map<const double*, int64_t> koff;
   std::map<const double*, int> plan;
+  std::set<const double*> pad_before, pad_after;  // stretch starts / ends (A panels)
   int rows = 0;
   int64_t kpad = 0;
 };
 
+// (Re)assign the k offsets of a panel's blocks in panel order.
+void layout_panel(PanelBuild& pb, const std::vector<DevPlan const*>& plans) {
+  pb.kpad = 0;
+  for (const double* blk : pb.order) {
+    if (pb.pad_before.count(blk)) pb.kpad = ceil_to(pb.kpad, kOzBK);
+    pb.koff[blk] = pb.kpad;
+    pb.kpad += ceil_to(plans[pb.plan.at(blk)]->host.K, kOzK16);
+    if (pb.pad_after.count(blk)) pb.kpad = ceil_to(pb.kpad, kOzBK);
+  }
+  pb.kpad = ceil_to(pb.kpad, kOzBK);  // whole 64-column boxes
+}
+
 int find_or_add_panel(std::vector<PanelBuild>& panels, std::map<std::vector<const double*>, int>& index,
                       const std::vector<std::pair<const double*, int>>& blocks, int rows,
-                      const std::vector<DevPlan const*>& plans, bool left) {
+                      const std::vector<DevPlan const*>& plans) {
   std::vector<const double*> key;
   for (auto& b : blocks) key.push_back(b.first);
   std::sort(key.begin(), key.end());
@@ -162,15 +182,36 @@ int find_or_add_panel(std::vector<PanelBuild>& panels, std::map<std::vector<cons
   pb.key = key;
   pb.rows = rows;
   for (auto& b : blocks) {
-    if (pb.koff.count(b.first)) continue;
-    pb.koff[b.first] = pb.kpad;
+    if (pb.plan.count(b.first)) continue;
+    pb.order.push_back(b.first);
     pb.plan[b.first] = b.second;
-    pb.kpad += ceil_to(plans[b.second]->host.K, kOzBK);
   }
-  (void)left;
+  layout_panel(pb, plans);
   panels.push_back(pb);
   index[key] = int(panels.size()) - 1;
   return int(panels.size()) - 1;
+}
+
+// Stretches of a destination block's pairs: maximal runs of consecutive
+// pairs whose blocks sit back to back in both panels.  f(first, last) per
+// stretch (pair indices, inclusive).
+template <class F>
+void for_stretches(const DGroup& g, const PanelBuild& pa, const PanelBuild& pb,
+                   const std::vector<DevPlan const*>& plans, F&& f) {
+  int first = -1;
+  int64_t ka = 0, kb = 0, kk = 0;
+  for (int q = 0; q < int(g.pairs.size()); ++q) {
+    const Pair& p = g.pairs[q];
+    const int64_t K = ceil_to(plans[p.plan]->host.K, kOzK16);
+    const int64_t a = pa.koff.at(p.l), b = pb.koff.at(p.r);
+    if (first >= 0 && a == ka + kk && b == kb + kk) {
+      kk += K;
+      continue;
+    }
+    if (first >= 0) f(first, q - 1, ka, kb, kk);
+    first = q, ka = a, kb = b, kk = K;
+  }
+  if (first >= 0) f(first, int(g.pairs.size()) - 1, ka, kb, kk);
 }
 
 int build_f64(a4g_batch* b, const std::vector<DGroup>& groups, const std::vector<const DevPlan*>& plans) {
@@ -199,23 +240,44 @@ int build_ozaki(a4g_batch* b, const std::vector<DGroup>& groups, const std::vect
   std::vector<OzDBlock> dblocks;
   std::vector<OzTile> dinfo;  // one per destination block: m0 = M, n0 = N (tiles are cut per form)
   std::vector<OzTrip> trips;
-  for (const DGroup& g : groups) {
+  std::vector<int> ga(groups.size()), gb(groups.size());
+  for (size_t gi = 0; gi < groups.size(); ++gi) {
+    const DGroup& g = groups[gi];
     const GemmPlan& h = plans[g.plan]->host;
     std::vector<std::pair<const double*, int>> ls, rs;
     for (const Pair& p : g.pairs) ls.push_back({p.l, p.plan}), rs.push_back({p.r, p.plan});
-    const int a = find_or_add_panel(pa, ia, ls, int(h.M), plans, true);
-    const int c = find_or_add_panel(pb, ib, rs, int(h.N), plans, false);
+    ga[gi] = find_or_add_panel(pa, ia, ls, int(h.M), plans);
+    gb[gi] = find_or_add_panel(pb, ib, rs, int(h.N), plans);
+  }
+  // In the A panels, align the first block of every stretch to 64 columns and
+  // pad after its last block; padding only splits stretches, so repeat until
+  // every stretch starts and ends on marked blocks (marks only grow).
+  for (bool changed = true; changed;) {
+    changed = false;
+    for (size_t gi = 0; gi < groups.size(); ++gi) {
+      PanelBuild& A = pa[ga[gi]];
+      for_stretches(groups[gi], A, pb[gb[gi]], plans, [&](int first, int last, int64_t, int64_t, int64_t) {
+        changed |= A.pad_before.insert(groups[gi].pairs[first].l).second;
+        changed |= A.pad_after.insert(groups[gi].pairs[last].l).second;
+      });
+    }
+    if (changed)
+      for (auto& p : pa) layout_panel(p, plans);
+  }
+  for (size_t gi = 0; gi < groups.size(); ++gi) {
+    const DGroup& g = groups[gi];
+    const GemmPlan& h = plans[g.plan]->host;
+    const int a = ga[gi], c = gb[gi];
     const int db = int(dblocks.size());
-    dblocks.push_back({g.d, g.plan, a, c});
+    const bool col_fast = h.N > 1 && h.offDn[1] - h.offDn[0] == 1 && !(h.M > 1 && h.offDm[1] - h.offDm[0] == 1);
+    dblocks.push_back({g.d, g.plan, a, c, col_fast ? 1 : 0});
     const int tb = int(trips.size());
     int kb_total = 0;
-    for (const Pair& p : g.pairs) {
-      const int64_t K = plans[p.plan]->host.K;
-      const int nkb = int(ceil_to(K, kOzBK) / kOzBK);
-      const int k16_last = K > 0 ? int(((K - 1) % kOzBK) / 16 + 1) : 4;
-      trips.push_back({pa[a].koff.at(p.l), pb[c].koff.at(p.r), nkb, k16_last});
+    for_stretches(g, pa[a], pb[c], plans, [&](int, int, int64_t ka, int64_t kbo, int64_t kk) {
+      const int nkb = int(ceil_to(kk, kOzBK) / kOzBK);
+      trips.push_back({ka, kbo, nkb, 0});
       kb_total += nkb;
-    }
+    });
     const int te = int(trips.size());
     dinfo.push_back({db, int(h.M), int(h.N), a, c, tb, te, kb_total});
   }

@@ -57,7 +57,7 @@ struct OzSplitJob {
   int rows, K;
   int kfast;  // src is unit-stride along k
   int panel;
-  int64_t koff;  // first k column of this block inside the panel (multiple of 64)
+  int64_t koff;  // first k column of this block inside the panel (multiple of 16)
 };
 
 // Memory layout of a split job's source block, detected on the host from the
@@ -74,19 +74,21 @@ struct OzTile {
   int trip_begin, trip_end;  // range of OzTrip (one per block pair feeding the tile)
   int kb_total;              // sum of the pairs' 64-wide k blocks
 };
-// k position of one block pair inside the A and B panels.
+// k position of one stretch of block pairs (back to back in both panels)
+// inside the A and B panels.
 struct OzTrip {
   int64_t koff_a, koff_b;
   int nkb;
-  int k16_last;  // K16 MMA steps that reach live k in the last k block (1..4)
+  int pad;
 };
 struct OzDBlock {
   double* d;
   int plan;  // PlanRef index for offDm/offDn and M, N
   int panel_a, panel_b;
+  int col_fast;  // D is unit-stride along n, not along m: store by columns
 };
 
-constexpr int kOzBM = 128, kOzBN = 128, kOzBK = 64, kOzMaxSlices = 8;
+constexpr int kOzBM = 128, kOzBN = 128, kOzBK = 64, kOzK16 = 16, kOzMaxSlices = 8;
 
 // Work unit of the tensor-core kernel: one level of one tile over a range of
 // its k blocks (split-K).  Units are ordered (level, split, tile) so that the

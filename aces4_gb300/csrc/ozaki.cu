@@ -273,10 +273,9 @@ __device__ __forceinline__ void two_sum_acc(float& hi, float& lo, float x) {
 }
 
 // ------------------------------------------------------------------ roles
-// Walks the k blocks of one unit: calls f(koff_a, koff_b, kb, k16) per 64-wide
-// block; k16 = the K16 MMA steps that reach live k (fewer than 4 only in the
-// last block of a pair whose K is not a multiple of 64: the panel's zero
-// padding beyond K need not be multiplied).
+// Walks the k blocks of one unit: calls f(koff_a, koff_b, kb) per 64-wide
+// block (the panels are zero beyond the end of every stretch of pairs up to
+// the next 64-column boundary, so whole blocks are always multiplied).
 template <class F>
 __device__ __forceinline__ void for_unit_kblocks(const OzGemmArgs& a, const OzUnit& un, const OzTile& tl,
                                                  F&& f) {
@@ -285,8 +284,7 @@ __device__ __forceinline__ void for_unit_kblocks(const OzGemmArgs& a, const OzUn
   while (kb < un.kb_end && q < tl.trip_end) {
     const OzTrip tr = a.trips[q];
     for (; j < tr.nkb && kb < un.kb_end; ++j, ++kb)
-      if (!f(int(tr.koff_a) + j * kOzBK, int(tr.koff_b) + j * kOzBK, kb, j + 1 == tr.nkb ? tr.k16_last : 4))
-        return;
+      if (!f(int(tr.koff_a) + j * kOzBK, int(tr.koff_b) + j * kOzBK, kb)) return;
     ++q;
     j = 0;
   }
@@ -314,7 +312,7 @@ __device__ void producer(const OzGemmArgs& a, OzSmemT<PAIR, BN>& sm, uint32_t ra
     const int arow = tl.m0 + int(rank) * kOzBM;          // this CTA's 128 rows of A
     const int brow = tl.n0 + int(rank) * (BN / 2);       // this CTA's half of B (pair form)
     bool ok = true;
-    for_unit_kblocks(a, un, tl, [&](int ka, int kb, int, int) {
+    for_unit_kblocks(a, un, tl, [&](int ka, int kb, int) {
       for (int i = 0; i <= level; ++i) {
         const int s = it % SM::kSt;
         const uint32_t ph = (it / SM::kSt) & 1;
@@ -350,7 +348,7 @@ __device__ void mma_issuer(const OzGemmArgs& a, OzSmemT<PAIR, BN>& sm, uint32_t 
     int in_chunk = 0;
     uint32_t buf = 0;
     bool ok = true;
-    for_unit_kblocks(a, un, tl, [&](int, int, int kb, int k16) {
+    for_unit_kblocks(a, un, tl, [&](int, int, int kb) {
       if (in_chunk == 0) {
         buf = chunk & 1;
         if (!mbar_wait(&sm.acc_empty[buf], ((chunk >> 1) & 1) ^ 1, sm, a.err_flag, 2)) return ok = false;
@@ -365,7 +363,6 @@ __device__ void mma_issuer(const OzGemmArgs& a, OzSmemT<PAIR, BN>& sm, uint32_t 
         const uint64_t ad = sw128_desc(sm.a[s]), bd = sw128_desc(sm.b[s]);
 #pragma unroll
         for (int kk = 0; kk < kOzBK / 16; ++kk) {
-          if (kk >= k16) break;
           const uint32_t acc = (in_chunk == 0 && i == 0 && kk == 0) ? 0u : 1u;
           if constexpr (PAIR) tc_mma_pair<BN>(d_tmem, ad + 2 * kk, bd + 2 * kk, acc);
           else tc_mma<BN>(d_tmem, ad + 2 * kk, bd + 2 * kk, acc);
@@ -912,46 +909,146 @@ __global__ void __launch_bounds__(256) oz_split_rows_kernel(const OzSplitJob* __
 }
 
 // ------------------------------------------------------------------ recombine
-// One thread per output element (grid: tiles x 64 blocks of 256): sums the
-// split partials of each level exactly in FP64 (integers < 2^53), applies the
-// level's power of two, then the row/column scales.
-template <int ROWS, int COLS>
+// The double nearest (ties to even) to u * 2^e2 with sign `neg`, u an
+// unsigned 64-bit magnitude, built with integer operations only (FP64
+// arithmetic is scarce on this GPU).  Results outside the normal range take
+// an FP64 path.
+__device__ __forceinline__ double u64_scaled_to_double(unsigned long long u, bool neg, int e2) {
+  if (u == 0) return 0.0;
+  const int nbits = 64 - __clzll((long long)u);
+  unsigned long long mant;
+  int e = e2;
+  if (nbits <= 53) {
+    mant = u << (53 - nbits);
+    e -= 53 - nbits;
+  } else {
+    const int sh = nbits - 53;
+    mant = u >> sh;
+    const unsigned long long rem = u & ((1ull << sh) - 1), half = 1ull << (sh - 1);
+    if (rem > half || (rem == half && (mant & 1ull))) ++mant;
+    e += sh;
+    if (mant == (1ull << 53)) mant >>= 1, ++e;
+  }
+  const int field = e + 52 + 1023;  // value = mant * 2^e, mant in [2^52, 2^53)
+  if (field >= 1 && field <= 2046)
+    return __longlong_as_double((long long)((neg ? (1ull << 63) : 0ull) | ((unsigned long long)field << 52) |
+                                            (mant & ((1ull << 52) - 1))));
+  const double v = ldexp(double(mant), e);
+  return neg ? -v : v;
+}
+
+// The same for a two's-complement 128-bit integer N.
+__device__ __forceinline__ double i128_scaled_to_double(__int128 N, int e2) {
+  const bool neg = N < 0;
+  const unsigned __int128 u = neg ? (unsigned __int128)(-N) : (unsigned __int128)N;
+  const unsigned long long hi = (unsigned long long)(u >> 64);
+  if (hi == 0) return u64_scaled_to_double((unsigned long long)u, neg, e2);
+  // keep the top 63 bits and fold the rest into a sticky bit below them (the
+  // rounding position lies above it, so the rounding is exact)
+  const int sh = 65 - __clzll((long long)hi);  // u >> sh has 63 bits
+  const unsigned long long top = (unsigned long long)(u >> sh);
+  const bool sticky = (u & ((((unsigned __int128)1) << sh) - 1)) != 0;
+  return u64_scaled_to_double((top << 1) | (sticky ? 1ull : 0ull), neg, e2 + sh - 1);
+}
+
+// One block of 256 threads per 32-column strip of a tile, walked as 32x32
+// pieces (four elements per thread): every level's split partials of a piece
+// are loaded before any is used (20 loads in flight per thread at 5 slices),
+// summed exactly (int64), the levels combined exactly (64-bit when the top
+// level allows it, else 128-bit) and rounded once to FP64 with the row/column
+// scales.  Reads run along rows (the workspace order); strips whose D is
+// unit-stride along n transpose through shared memory so the stores run
+// along n.
+template <int S>
 __global__ void __launch_bounds__(256) oz_recombine_kernel(const OzTile* __restrict__ tiles,
                                                            const OzDBlock* __restrict__ dblocks,
                                                            const PlanRef* __restrict__ plans,
                                                            const OzPanel* __restrict__ pa,
                                                            const OzPanel* __restrict__ pb,
-                                                           const int* __restrict__ ws, int slices,
+                                                           const int* __restrict__ ws, int log_rows, int log_cols,
                                                            int nsplit, int mode) {
-  constexpr int kBlocksPerTile = ROWS * COLS / 256;
-  const int tile = blockIdx.x / kBlocksPerTile;
-  const int e = (blockIdx.x % kBlocksPerTile) * 256 + threadIdx.x;
-  const int row = e % ROWS, col = e / ROWS;
+  constexpr int kSub = 32, kPer = kSub * kSub / 256;
+  __shared__ double sm[kSub][kSub + 1];
+  const int strips_log = log_cols - 5;
+  const int tile = blockIdx.x >> strips_log;
+  const int sc = (blockIdx.x & ((1 << strips_log) - 1)) * kSub;
   const OzTile tl = tiles[tile];
   const OzDBlock db = dblocks[tl.dblock];
   const PlanRef pl = plans[db.plan];
-  const int m = tl.m0 + row, n = tl.n0 + col;
-  if (m >= pl.M || n >= pl.N) return;
   const int* ea = pa[tl.panel_a].exps;
   const int* eb = pb[tl.panel_b].exps;
-  double v = 0.0;
-  for (int lv = slices - 1; lv >= 0; --lv) {
-    const int* p = ws + ((size_t(tile) * slices + lv) * nsplit * COLS + col) * ROWS + row;
-    long long s0 = 0, s1 = 0;  // exact
-    int sp = 0;
-#pragma unroll 4
-    for (; sp + 1 < nsplit; sp += 2) {
-      s0 += __ldg(p + size_t(sp) * COLS * ROWS);
-      s1 += __ldg(p + size_t(sp + 1) * COLS * ROWS);
+  const size_t plane = size_t(1) << (log_rows + log_cols);     // one split's [cols][rows]
+  const int* wtile = ws + size_t(tile) * S * nsplit * plane;
+  const int rows_here = min(1 << log_rows, pl.M - tl.m0);
+  for (int sr = 0; sr < rows_here; sr += kSub) {
+    long long lev[kPer][S];
+#pragma unroll
+    for (int p = 0; p < kPer; ++p)
+#pragma unroll
+      for (int lv = 0; lv < S; ++lv) lev[p][lv] = 0;
+    for (int sp = 0; sp < nsplit; ++sp) {
+      int raw[kPer][S];
+#pragma unroll
+      for (int p = 0; p < kPer; ++p) {
+        const int e = p * 256 + threadIdx.x;
+        const int row = sr + (e & (kSub - 1)), col = sc + (e >> 5);
+        const int* q = wtile + (size_t(sp) << (log_rows + log_cols)) + (size_t(col) << log_rows) + row;
+#pragma unroll
+        for (int lv = 0; lv < S; ++lv) raw[p][lv] = __ldg(q + size_t(lv) * nsplit * plane);
+      }
+#pragma unroll
+      for (int p = 0; p < kPer; ++p)
+#pragma unroll
+        for (int lv = 0; lv < S; ++lv) lev[p][lv] += raw[p][lv];
     }
-    if (sp < nsplit) s0 += __ldg(p + size_t(sp) * COLS * ROWS);
-    v += ldexp(double(s0 + s1), -kDigitBits * (lv + 2));  // exact: |sum| < 2^53
+#pragma unroll
+    for (int p = 0; p < kPer; ++p) {
+      const int e = p * 256 + threadIdx.x;
+      const int row = sr + (e & (kSub - 1)), col = sc + (e >> 5);
+      const int m = tl.m0 + row, n = tl.n0 + col;
+      double v = 0.0;
+      const bool live = m < pl.M && n < pl.N;
+      if (live) {
+        // value = sum_t lev[t] 2^(8(S-1-t)) * 2^(E + F + 2 - 8(S+1))
+        const int E = (ea[m] ? ea[m] : 1) - 1022, F = (eb[n] ? eb[n] : 1) - 1022;
+        const int e2 = E + F + 2 - kDigitBits * (S + 1);
+        const long long top = lev[p][0] < 0 ? -lev[p][0] : lev[p][0];
+        if (top < (1ll << (62 - kDigitBits * (S - 1)))) {  // the 64-bit sum cannot overflow
+          long long acc = 0;
+#pragma unroll
+          for (int lv = 0; lv < S; ++lv) acc += lev[p][lv] * (1ll << (kDigitBits * (S - 1 - lv)));
+          v = u64_scaled_to_double(acc < 0 ? (unsigned long long)(-acc) : (unsigned long long)acc, acc < 0, e2);
+        } else {
+          unsigned __int128 acc = 0;  // two's complement, wrapping (exact: |sum| < 2^101)
+#pragma unroll
+          for (int lv = 0; lv < S; ++lv)
+            acc += (unsigned __int128)(__int128)lev[p][lv] << (kDigitBits * (S - 1 - lv));
+          v = i128_scaled_to_double((__int128)acc, e2);
+        }
+        if (mode & 2) v = -v;  // negated term
+      }
+      if (db.col_fast) {
+        sm[e & (kSub - 1)][e >> 5] = v;
+      } else if (live) {
+        double* dst = db.d + pl.offDm[m] + pl.offDn[n];
+        *dst = (mode & 1) ? *dst + v : v;
+      }
+    }
+    if (!db.col_fast) continue;
+    __syncthreads();
+#pragma unroll
+    for (int p = 0; p < kPer; ++p) {
+      const int e = p * 256 + threadIdx.x;
+      const int col = sc + (e & (kSub - 1)), row = sr + (e >> 5);
+      const int m = tl.m0 + row, n = tl.n0 + col;
+      if (m < pl.M && n < pl.N) {
+        const double v = sm[e >> 5][e & (kSub - 1)];
+        double* dst = db.d + pl.offDm[m] + pl.offDn[n];
+        *dst = (mode & 1) ? *dst + v : v;
+      }
+    }
+    __syncthreads();
   }
-  const int E = (ea[m] ? ea[m] : 1) - 1022, F = (eb[n] ? eb[n] : 1) - 1022;
-  v = ldexp(v, E + F + 2);
-  if (mode & 2) v = -v;  // negated term
-  double* dst = db.d + pl.offDm[m] + pl.offDn[n];
-  *dst = (mode & 1) ? *dst + v : v;
 }
 
 using EncodeTiled = PFN_cuTensorMapEncodeTiled_v12000;
@@ -1116,17 +1213,20 @@ int oz_launch_recombine(const OzTile* tiles, int ntiles, int tile_rows, int tile
                         const PlanRef* plans, const OzPanel* pa, const OzPanel* pb, const int* ws, int slices,
                         int nsplit, int mode, cudaStream_t s) {
   if (ntiles <= 0) return A4G_OK;
-  const int per = tile_rows * tile_cols / 256;
+  if ((tile_rows != 128 && tile_rows != 256) || (tile_cols != 128 && tile_cols != 256))
+    return fail(A4G_ERR_ARG, "recombine: unsupported tile shape");
+  const int lr = tile_rows == 256 ? 8 : 7, lc = tile_cols == 256 ? 8 : 7;
+  const int per = tile_cols / 32;  // 32-column strips per tile
   if (int64_t(ntiles) * per > 0x7fffffffLL) return fail(A4G_ERR_RANGE, "too many tiles");
   const unsigned g = unsigned(ntiles * per);
-  if (tile_rows == 256 && tile_cols == 256)
-    oz_recombine_kernel<256, 256><<<g, 256, 0, s>>>(tiles, dblocks, plans, pa, pb, ws, slices, nsplit, mode);
-  else if (tile_rows == 256)
-    oz_recombine_kernel<256, 128><<<g, 256, 0, s>>>(tiles, dblocks, plans, pa, pb, ws, slices, nsplit, mode);
-  else if (tile_cols == 256)
-    oz_recombine_kernel<128, 256><<<g, 256, 0, s>>>(tiles, dblocks, plans, pa, pb, ws, slices, nsplit, mode);
-  else
-    oz_recombine_kernel<128, 128><<<g, 256, 0, s>>>(tiles, dblocks, plans, pa, pb, ws, slices, nsplit, mode);
+  switch (slices) {
+#define A4G_RECOMBINE(SL) \
+  case SL: oz_recombine_kernel<SL><<<g, 256, 0, s>>>(tiles, dblocks, plans, pa, pb, ws, lr, lc, nsplit, mode); break;
+    A4G_RECOMBINE(1) A4G_RECOMBINE(2) A4G_RECOMBINE(3) A4G_RECOMBINE(4) A4G_RECOMBINE(5) A4G_RECOMBINE(6)
+    A4G_RECOMBINE(7)
+#undef A4G_RECOMBINE
+    default: return fail(A4G_ERR_ARG, "recombine: slices must be 1..7");
+  }
   A4G_CUDA(cudaGetLastError());
   return A4G_OK;
 }

@@ -229,6 +229,148 @@ def run_reference_arm(args, rank: int):
     print(json.dumps(line), flush=True)
 
 
+TRIPLES_METRIC = "FP64-equiv TFLOP/s per triples step (W = V1*T - V2*T, E = sum W^2/D; split vs plain FP64)"
+
+
+def run_triples(args, world, rank, local):
+    """Triples energy step, by default at o=24 (1 x 24), v=240 (10 x 24):
+    fixed virtual segments (a, b), every c: 10 W blocks of 24^6 (1.53 GB
+    each), 100 + 10 block pairs, 1.01e12 flop, then the fused denominator +
+    contraction pass over the 1.9e9 W elements.  V1, V2 ~ U[-1,1]/v,
+    T ~ N(0, 1e-2), e_occ ~ U[-2,-0.5], e_virt ~ U[0.2,5] (seeded,
+    synthetic)."""
+    import numpy as np
+    import torch
+    import torch.distributed as dist
+
+    import aces4_gb300 as a4
+    from aces4_gb300.blocks import (TRIPLES_TERM1_LABELS, TRIPLES_TERM2_LABELS, BlockArray,
+                                    triples_index_values, triples_step)
+    from oracle import oracle
+
+    torch.cuda.set_device(local)
+    if world > 1:
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    a4.device.init(local)
+    stream = torch.cuda.current_stream()
+    seg, nv = args.tseg, args.tnv
+    o_segs, v_segs = [seg], [seg] * nv
+    o, v = seg, seg * nv
+    a, b = rank % nv, (rank + 1) % nv
+    V1 = BlockArray([v_segs, v_segs, v_segs, o_segs])
+    V2 = BlockArray([o_segs, v_segs, o_segs, o_segs])
+    T = BlockArray([v_segs, v_segs, o_segs, o_segs])
+    g = torch.Generator(device="cuda")
+    g.manual_seed(77 + rank)
+    V1.buf.uniform_(-1.0, 1.0, generator=g).div_(v)
+    V2.buf.uniform_(-1.0, 1.0, generator=g).div_(v)
+    T.buf.normal_(0.0, 0.1, generator=g)
+    rng = np.random.default_rng(77 + rank)  # orbital energies
+    e = np.concatenate([rng.uniform(-2.0, -0.5, o), rng.uniform(0.2, 5.0, v)])
+    fock = torch.tensor(np.diag(e).ravel(order="F"), device="cuda")
+    W = BlockArray([v_segs, o_segs, v_segs, o_segs, v_segs, o_segs], present=lambda k: k[0] == a and k[2] == b)
+    t1, t2 = triples_step(W, V1, V2, T, a, b)
+    p1 = oracle.get_contraction_ptrn(6, 4, 4, sum(TRIPLES_TERM1_LABELS, []))[1]
+    p2 = oracle.get_contraction_ptrn(6, 4, 4, sum(TRIPLES_TERM2_LABELS, []))[1]
+    segs = o_segs + v_segs
+    norb = sum(segs)
+    esum = torch.zeros(1, dtype=torch.float64, device="cuda")
+    ivs = [(triples_index_values(k, 1), W.ext(k), W.block(k)) for k in W.keys()]
+
+    def energy():
+        for iv, ext, blk in ivs:
+            a4.device.energy_contract(iv, ext, blk, [norb, norb], fock, segs, 1.0, esum, stream=stream)
+
+    def batches(prec):
+        kw = dict(precision=prec, slices=args.slices)
+        return (a4.device.Batch(p1, 6, 4, 4, t1, variant=args.variant if prec else 0, **kw),
+                a4.device.Batch(p2, 6, 4, 4, t2, beta=1, negate=True, variant=args.variant if prec else 0, **kw))
+
+    b1, b2 = batches(a4.device.PREC_OZAKI_BF16)
+    flops = b1.info()["flops"] + b2.info()["flops"]
+    for _ in range(args.warmup):
+        b1.run(stream)
+        b2.run(stream)
+        energy()
+    torch.cuda.synchronize()
+    b1.timings(), b2.timings()
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
+    t_terms = t_energy = 0.0
+    if world > 1:
+        dist.barrier()
+    torch.cuda.synchronize()
+    props = torch.cuda.get_device_properties(local)
+    gpu_id = f"GPU-{props.uuid}" if getattr(props, "uuid", None) else str(local)
+    with ClockSampler(gpu_id) as clk:
+        ev[0].record(stream)
+        for _ in range(args.steps):
+            ev[1].record(stream)
+            b1.run_timed(stream)
+            b2.run_timed(stream)
+            ev[2].record(stream)
+            energy()
+            ev[3].record(stream)
+            torch.cuda.synchronize()
+            t_terms += ev[1].elapsed_time(ev[2])
+            t_energy += ev[2].elapsed_time(ev[3])
+        ev[3].record(stream)
+        torch.cuda.synchronize()
+    ms = max_over_ranks(ev[0].elapsed_time(ev[3]) / args.steps)
+    ph1, ph2 = b1.timings(), b2.timings()
+    esum.zero_()
+    b1.run(stream)
+    b2.run(stream)
+    energy()
+    E_split = float(esum.item())
+    W_split = W.buf.clone()
+    form = b1.form()
+    b1.close()
+    b2.close()
+    f1, f2 = batches(a4.device.PREC_FP64)
+    torch.cuda.synchronize()
+    ev[0].record(stream)
+    f1.run(stream)
+    f2.run(stream)
+    ev[1].record(stream)
+    esum.zero_()
+    energy()
+    torch.cuda.synchronize()
+    fp64_ms = ev[0].elapsed_time(ev[1])
+    E64 = float(esum.item())
+    werr = max(float(torch.linalg.norm(W_split[W.offsets[k]:W.offsets[k] + W.size(k)] -
+                                       W.buf[W.offsets[k]:W.offsets[k] + W.size(k)]) /
+                     torch.linalg.norm(W.buf[W.offsets[k]:W.offsets[k] + W.size(k)])) for k in W.keys())
+    f1.close()
+    f2.close()
+    if rank == 0:
+        runs = max(1, ph1["runs"])
+        n_w = sum(W.size(k) for k in W.keys())
+        e_ms = t_energy / args.steps
+        line = {
+            "metric": TRIPLES_METRIC, "value": world * flops / (ms * 1e-3) / 1e12, "unit": "TFLOP/s",
+            "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "bf16", "data": "synthetic",
+            "config": {"workload": f"triples o={o} (1x{seg}), v={v} ({nv}x{seg}), one (a,b) step: "
+                                   f"{len(W.keys())} W blocks of {seg}^6, {len(t1)}+{len(t2)} block pairs "
+                                   f"({flops:.3g} flop)", "slices": args.slices},
+            "phases_ms_per_step": {
+                "term1": {k: ph1[k] / runs for k in ("zero_fill", "exponents", "split", "gemm", "recombine")},
+                "term2": {k: ph2[k] / runs for k in ("zero_fill", "exponents", "split", "gemm", "recombine")},
+                "terms_total": t_terms / args.steps, "energy": e_ms},
+            "energy_pass": {"elements": n_w, "ms": e_ms, "gelem_per_s": n_w / (e_ms * 1e-3) / 1e9,
+                            "hbm_gbs": n_w * 8 / (e_ms * 1e-3) / 1e9},
+            "gemm_form": {"chosen": form["name"], "autotune_ms": form["tuned_ms"]},
+            "fp64_plain": {"value": flops / (fp64_ms * 1e-3) / 1e12, "unit": "TFLOP/s",
+                           "ms_per_step_terms": fp64_ms},
+            "energy": {"split": E_split, "fp64": E64, "rel_diff": abs(E_split - E64) / abs(E64)},
+            "rel_err_max_w_block_vs_fp64_gpu": werr,
+            "clocks": clk.summary(),
+        }
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        dist.destroy_process_group()
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -245,6 +387,10 @@ def main():
                     help="tensor-core GEMM form: 0 autotuned, 1/2 one SM / CTA pair x 128 columns, 3/4 x 256 columns")
     ap.add_argument("--nvseg", type=int, default=16, help="virtual segments of 32 (16: v=512)")
     ap.add_argument("--noseg", type=int, default=4, help="occupied segments of 16 (4: o=64)")
+    ap.add_argument("--tseg", type=int, default=24, help="triples: segment size (occupied: one segment)")
+    ap.add_argument("--tnv", type=int, default=10, help="triples: virtual segments")
+    ap.add_argument("--workload", default="ladder", choices=["ladder", "triples"],
+                    help="ladder: the o=64/v=512 ladder slab (the headline metric); triples: one triples energy step")
     args = ap.parse_args()
 
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -252,6 +398,9 @@ def main():
     local = int(os.environ.get("LOCAL_RANK", "0"))
     if args.impl == "reference":
         run_reference_arm(args, rank)
+        return
+    if args.workload == "triples":
+        run_triples(args, world, rank, local)
         return
 
     import numpy as np

@@ -218,3 +218,28 @@ def test_split_odd_extents_non_vector_paths(a4):
     _run(a4, R2, trip2, labels2, a4.device.PREC_OZAKI_BF16, slices=1)
     for k, want in _reference(R2, trip2, labels2).items():
         np.testing.assert_array_equal(R2.block(k).cpu().numpy(), want)
+
+
+@pytest.mark.parametrize("variant", [1, 4])
+def test_split_shared_panels_in_different_pair_orders(a4, variant):
+    """Destination blocks that use the same operand blocks in different orders
+    share a panel whose k layout cannot be contiguous for all of them: the
+    stretches break up and every stretch must still multiply zeros past its
+    end.  Uneven small K (5 and 7 wide segments, K = 25 .. 49) makes most
+    stretch ends ragged.  Integer data with one slice: bit-exact."""
+    import random
+
+    R, V, T, trip, labels = _make(a4, "ladder", [5, 7, 6], [3, 4], 0.0, 12, integer=True)
+    by_d = {}
+    for t in trip:
+        by_d.setdefault(t[0].data_ptr(), []).append(t)
+    rnd = random.Random(5)
+    shuffled = []
+    for i, (dp, ts) in enumerate(sorted(by_d.items())):
+        ts = list(ts)
+        if i % 2:
+            rnd.shuffle(ts)
+        shuffled += ts
+    _run(a4, R, shuffled, labels, a4.device.PREC_OZAKI_BF16, slices=1, variant=variant)
+    for k, want in _reference(R, trip, labels).items():
+        np.testing.assert_array_equal(R.block(k).cpu().numpy(), want)
