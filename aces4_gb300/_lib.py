@@ -69,6 +69,7 @@ SIGNATURES = {
     "a4g_insert": (ctypes.c_int, None),
     "a4g_energy_denominator": (ctypes.c_int, None),
     "a4g_energy_contract": (ctypes.c_int, None),
+    "a4g_batch_launches": (ctypes.c_int, None),
     "a4g_batch_create": (ctypes.c_int, None),
     "a4g_batch_run": (ctypes.c_int, [c_void_p, c_void_p]),
     "a4g_batch_run_graph": (ctypes.c_int, [c_void_p, c_void_p]),

@@ -29,6 +29,7 @@ struct a4g_batch {
   // store mode of the writing kernels: bit 0 accumulate into D, bit 1 negate
   int store_mode() const { return beta | (negate << 1); }
   int variant = 0;  // tensor-core GEMM form: 0 autotuned, else 1 + index into forms
+  int pipeline = 0;  // requested GEMM parts (0/1: one launch)
   int64_t pairs = 0;
   double flops = 0.0;
   int64_t device_bytes = 0;
@@ -49,6 +50,7 @@ struct a4g_batch {
   struct JobSet {
     bool left;
     int layout;
+    int group = 0;  // split pipeline group: 0 before the GEMM, g > 0 with GEMM part g-1
     OzSplitJob* d_jobs = nullptr;
     int64_t* d_prefix_exp = nullptr;
     int64_t* d_prefix_split = nullptr;
@@ -74,6 +76,14 @@ struct a4g_batch {
   };
   GemmForm forms[kForms];
   int form = 0;  // the form run() uses (chosen by the autotuner or the caller)
+  // Split/GEMM pipeline of the chosen form: the GEMM runs as `parts` launches
+  // over consecutive split-K ranges; the right-operand split jobs that only
+  // later parts read run on `side` while earlier parts multiply.
+  int parts = 1;
+  std::vector<OzGemmArgs> part_args;
+  std::vector<int> part_grid;
+  cudaStream_t side = nullptr;
+  std::vector<cudaEvent_t> part_ev;  // [0]: fork after split group 0; [g]: split group g done
   int* d_ws = nullptr;
   cudaGraphExec_t graph = nullptr;
   // phase timing: events[run][6] recorded by a4g_batch_run_timed
@@ -83,6 +93,8 @@ struct a4g_batch {
   ~a4g_batch() {
     for (auto& ev : events)
       for (cudaEvent_t e : ev) cudaEventDestroy(e);
+    for (cudaEvent_t e : part_ev) cudaEventDestroy(e);
+    if (side) cudaStreamDestroy(side);
     if (graph) cudaGraphExecDestroy(graph);
     for (void* p : allocs) cudaFree(p);
   }
@@ -340,10 +352,10 @@ int build_ozaki(a4g_batch* b, const std::vector<DGroup>& groups, const std::vect
     for (int64_t k = 0; k < K && (rm || km); ++k) rm &= ok[k] == k * rows, km &= ok[k] == k;
     return rm ? int(kOzRowsMajor) : km ? int(kOzKMajor) : int(kOzGeneric);
   };
+  std::vector<OzSplitJob> host_jobs[2][3];  // [side][layout]
   for (int side = 0; side < 2; ++side) {
     const bool left = side == 0;
     std::vector<PanelBuild>& src = left ? pa : pb;
-    std::vector<OzSplitJob> jobs[3];
     for (size_t pi = 0; pi < src.size(); ++pi)
       for (auto& kv : src[pi].koff) {
         const DevPlan* dp = plans[src[pi].plan.at(kv.first)];
@@ -358,27 +370,30 @@ int build_ozaki(a4g_batch* b, const std::vector<DGroup>& groups, const std::vect
         j.koff = kv.second;
         int lay = layout_of(dp, left);
         if ((reinterpret_cast<uintptr_t>(kv.first) & 15) != 0) lay = kOzGeneric;  // vector loads need 16 B
-        jobs[lay].push_back(j);
+        host_jobs[side][lay].push_back(j);
       }
-    for (int lay = 0; lay < 3; ++lay) {
-      if (jobs[lay].empty()) continue;
-      a4g_batch::JobSet js;
-      js.left = left;
-      js.layout = lay;
-      std::vector<int64_t> pe(1, 0), ps(1, 0);
-      for (const OzSplitJob& j : jobs[lay]) {
-        pe.push_back(pe.back() + oz_exp_tiles(lay, j.rows, j.K));
-        ps.push_back(ps.back() + oz_split_tiles(lay, j.rows, j.K));
-      }
-      js.njobs = int(jobs[lay].size());
-      js.tiles_exp = pe.back();
-      js.tiles_split = ps.back();
-      if ((rc = upload(b, jobs[lay], &js.d_jobs)) || (rc = upload(b, pe, &js.d_prefix_exp)) ||
-          (rc = upload(b, ps, &js.d_prefix_split)))
-        return rc;
-      b->jobsets.push_back(js);
-    }
   }
+  auto add_jobset = [&](bool left, int lay, int group, const std::vector<OzSplitJob>& jobs) -> int {
+    if (jobs.empty()) return A4G_OK;
+    a4g_batch::JobSet js;
+    js.left = left;
+    js.layout = lay;
+    js.group = group;
+    std::vector<int64_t> pe(1, 0), ps(1, 0);
+    for (const OzSplitJob& j : jobs) {
+      pe.push_back(pe.back() + oz_exp_tiles(lay, j.rows, j.K));
+      ps.push_back(ps.back() + oz_split_tiles(lay, j.rows, j.K));
+    }
+    js.njobs = int(jobs.size());
+    js.tiles_exp = pe.back();
+    js.tiles_split = ps.back();
+    int r;
+    if ((r = upload(b, jobs, &js.d_jobs)) || (r = upload(b, pe, &js.d_prefix_exp)) ||
+        (r = upload(b, ps, &js.d_prefix_split)))
+      return r;
+    b->jobsets.push_back(js);
+    return A4G_OK;
+  };
   void *dmaps_a = nullptr, *dmaps_b64 = nullptr, *dmaps_b128 = nullptr, *dmaps_b256 = nullptr;
   const size_t mbytes_a = maps_a.size() * sizeof(MapBytes), mbytes_b = maps_b128.size() * sizeof(MapBytes);
   if ((rc = device_alloc(b, mbytes_a, &dmaps_a, false))) return rc;
@@ -500,6 +515,85 @@ int build_ozaki(a4g_batch* b, const std::vector<DGroup>& groups, const std::vect
     if (rc) return rc;
     if ((rc = check_device_flag(s))) return rc;
   }
+  // Pipeline of the chosen form (when the caller asks for one): GEMM parts
+  // over consecutive split-K ranges; each k-major right-operand split job
+  // joins the group of the first part that reads its columns.  (Those jobs
+  // need no shared memory and few registers, so they run beside the
+  // persistent GEMM's CTAs; the other split kernels run before the GEMM.)
+  const a4g_batch::GemmForm& gf = b->forms[b->form];
+  const int ns = gf.nsplit;
+  std::vector<OzSplitJob>& kmaj = host_jobs[1][kOzKMajor];
+  int P = std::min(std::min(b->pipeline, kOzMaxPipelineParts), ns);
+  std::vector<int> job_group(kmaj.size(), 0);
+  if (P > 1 && !kmaj.empty()) {
+    std::vector<int> part_of_split(ns);
+    for (int p = 0; p < P; ++p)
+      for (int sp = ns * p / P; sp < ns * (p + 1) / P; ++sp) part_of_split[sp] = p;
+    std::vector<std::vector<int>> need(pb.size());
+    for (size_t i = 0; i < pb.size(); ++i) need[i].assign(size_t(pb[i].kpad / kOzK16), P);
+    const std::vector<OzTile>& tiles = form_tiles[b->form];
+    for (const OzUnit& u : form_units[b->form]) {
+      if (u.level != 0) continue;  // every level reads the same columns
+      const int part = part_of_split[u.split];
+      const OzTile& t = tiles[u.tile];
+      std::vector<int>& nd = need[t.panel_b];
+      int q = u.trip_first, j = u.kb_in_trip;
+      for (int kb = u.kb_begin; kb < u.kb_end && q < t.trip_end; ++kb) {
+        const int64_t c0 = (trips[q].koff_b + int64_t(j) * kOzBK) / kOzK16;
+        for (int64_t c = c0; c < c0 + kOzBK / kOzK16 && c < int64_t(nd.size()); ++c) nd[c] = std::min(nd[c], part);
+        if (++j == trips[q].nkb) ++q, j = 0;
+      }
+    }
+    bool any_late = false;
+    for (size_t i = 0; i < kmaj.size(); ++i) {
+      const std::vector<int>& nd = need[kmaj[i].panel];
+      int g = P;
+      for (int64_t c = kmaj[i].koff / kOzK16; c <= (kmaj[i].koff + kmaj[i].K - 1) / kOzK16; ++c) g = std::min(g, nd[c]);
+      job_group[i] = g >= P ? 0 : g;
+      any_late |= job_group[i] > 0;
+    }
+    if (!any_late) P = 1;
+  } else {
+    P = 1;
+  }
+  for (int side = 0; side < 2; ++side)
+    for (int lay = 0; lay < 3; ++lay) {
+      if (side == 1 && lay == kOzKMajor) continue;
+      if ((rc = add_jobset(side == 0, lay, 0, host_jobs[side][lay]))) return rc;
+    }
+  for (int g = 0; g < P; ++g) {
+    std::vector<OzSplitJob> grp;
+    for (size_t i = 0; i < kmaj.size(); ++i)
+      if (job_group[i] == g) grp.push_back(kmaj[i]);
+    if ((rc = add_jobset(false, kOzKMajor, g, grp))) return rc;
+  }
+  b->parts = P;
+  if (P > 1) {
+    // units of part p: levels from the most expensive down (the launch's
+    // tail then holds the cheapest units), its splits, every tile
+    const std::vector<OzUnit>& all = form_units[b->form];
+    std::vector<OzUnit> units;
+    std::vector<size_t> start;
+    for (int p = 0; p < P; ++p) {
+      start.push_back(units.size());
+      for (int lv = S - 1; lv >= 0; --lv)
+        for (int sp = ns * p / P; sp < ns * (p + 1) / P; ++sp)
+          for (int ti = 0; ti < gf.n_tiles; ++ti) units.push_back(all[(size_t(lv) * ns + sp) * gf.n_tiles + ti]);
+    }
+    start.push_back(units.size());
+    OzUnit* d_units = nullptr;
+    if ((rc = upload(b, units, &d_units))) return rc;
+    for (int p = 0; p < P; ++p) {
+      OzGemmArgs ga = gf.args;
+      ga.units = d_units + start[p];
+      ga.n_units = int(start[p + 1] - start[p]);
+      b->part_args.push_back(ga);
+      b->part_grid.push_back(gf.pair ? 2 * std::min(ga.n_units, pairs) : std::min(ga.n_units, ctx()->num_sms));
+    }
+    A4G_CUDA(cudaStreamCreateWithFlags(&b->side, cudaStreamNonBlocking));
+    b->part_ev.resize(P);
+    for (auto& e : b->part_ev) A4G_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+  }
   return A4G_OK;
 }
 
@@ -531,14 +625,36 @@ int run(a4g_batch* b, cudaStream_t s, const cudaEvent_t* ev = nullptr) {
         return rc;
   }
   if ((rc = mark(2))) return rc;
-  if (gf.n_tiles > 0) {
+  auto split_group = [&](int g, cudaStream_t st) -> int {
     for (const auto& js : b->jobsets)
-      if ((rc = oz_launch_split(js.layout, js.d_jobs, js.d_prefix_split, js.njobs, js.tiles_split,
-                                js.left ? b->d_pa : b->d_pb, b->slices, s)))
-        return rc;
+      if (js.group == g) {
+        const int r = oz_launch_split(js.layout, js.d_jobs, js.d_prefix_split, js.njobs, js.tiles_split,
+                                      js.left ? b->d_pa : b->d_pb, b->slices, st);
+        if (r) return r;
+      }
+    return A4G_OK;
+  };
+  if (gf.n_tiles > 0 && (rc = split_group(0, s))) return rc;
+  if (gf.n_tiles > 0 && b->parts > 1) {
+    // groups 1.. on the side stream, overlapping the GEMM parts before them
+    A4G_CUDA(cudaEventRecord(b->part_ev[0], s));
+    A4G_CUDA(cudaStreamWaitEvent(b->side, b->part_ev[0], 0));
+    for (int g = 1; g < b->parts; ++g) {
+      if ((rc = split_group(g, b->side))) return rc;
+      A4G_CUDA(cudaEventRecord(b->part_ev[g], b->side));
+    }
   }
   if ((rc = mark(3))) return rc;
-  if (gf.n_tiles > 0 && (rc = oz_launch_gemm(gf.args, gf.grid, gf.pair, gf.tile_cols, s))) return rc;
+  if (gf.n_tiles > 0) {
+    if (b->parts > 1) {
+      for (int p = 0; p < b->parts; ++p) {
+        if (p > 0) A4G_CUDA(cudaStreamWaitEvent(s, b->part_ev[p], 0));
+        if ((rc = oz_launch_gemm(b->part_args[p], b->part_grid[p], gf.pair, gf.tile_cols, s))) return rc;
+      }
+    } else if ((rc = oz_launch_gemm(gf.args, gf.grid, gf.pair, gf.tile_cols, s))) {
+      return rc;
+    }
+  }
   if ((rc = mark(4))) return rc;
   if (gf.n_tiles > 0 &&
       (rc = oz_launch_recombine(gf.d_tiles, gf.n_tiles, gf.tile_rows, gf.tile_cols, b->d_dblocks, b->d_plans,
@@ -566,6 +682,7 @@ int a4g_batch_create(a4g_batch** out, const int* ptrn, int drank, int lrank, int
     b->slices = opts->slices > 0 ? opts->slices : 5;
     b->beta = opts->beta ? 1 : 0;
     b->negate = opts->negate ? 1 : 0;
+    b->pipeline = opts->pipeline;
     b->variant = opts->variant;
   }
   if (b->variant < 0 || b->variant > a4g_batch::kForms) return fail(A4G_ERR_ARG, "unknown GEMM variant");
@@ -683,6 +800,21 @@ int a4g_batch_info(const a4g_batch* b, int64_t* pairs, double* flops, int64_t* w
   if (pairs) *pairs = b->pairs;
   if (flops) *flops = b->flops;
   if (workspace_bytes) *workspace_bytes = b->device_bytes;
+  return A4G_OK;
+}
+
+int a4g_batch_launches(const a4g_batch* b, int* kernels_per_run, int* gemm_parts) {
+  if (!b) return fail(A4G_ERR_ARG, "null batch");
+  int k = b->beta == 0 ? int(b->zero_blocks.size()) : 0;
+  int parts = 1;
+  if (b->precision == A4G_PREC_FP64) {
+    k += b->n_f64_tiles > 0 ? 1 : 0;
+  } else if (b->forms[b->form].n_tiles > 0) {
+    parts = b->parts;
+    k += 2 * int(b->jobsets.size()) + parts + 1;  // exponents + splits, GEMM parts, recombine
+  }
+  if (kernels_per_run) *kernels_per_run = k;
+  if (gemm_parts) *gemm_parts = parts;
   return A4G_OK;
 }
 

@@ -89,6 +89,7 @@ struct OzDBlock {
 };
 
 constexpr int kOzBM = 128, kOzBN = 128, kOzBK = 64, kOzK16 = 16, kOzMaxSlices = 8;
+constexpr int kOzMaxPipelineParts = 8;  // GEMM launches per pardo step when the right split pipelines
 
 // Work unit of the tensor-core kernel: one level of one tile over a range of
 // its k blocks (split-K).  Units are ordered (level, split, tile) so that the

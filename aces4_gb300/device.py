@@ -174,7 +174,8 @@ class _Triple(ctypes.Structure):
 
 class _Opts(ctypes.Structure):
     _fields_ = [("precision", ctypes.c_int), ("slices", ctypes.c_int), ("beta", ctypes.c_int),
-                ("variant", ctypes.c_int), ("negate", ctypes.c_int), ("reserved", ctypes.c_int * 3)]
+                ("variant", ctypes.c_int), ("negate", ctypes.c_int), ("pipeline", ctypes.c_int),
+                ("reserved", ctypes.c_int * 2)]
 
 
 def _ext6(e):
@@ -192,13 +193,13 @@ class Batch:
     """
 
     def __init__(self, ptrn, drank, lrank, rrank, triples, precision=PREC_FP64, slices=5, beta=0, variant=0,
-                 negate=False):
+                 negate=False, pipeline=0):
         tl = list(triples)
         arr = (_Triple * max(1, len(tl)))()
         for i, (d, l, r, de, le, re) in enumerate(tl):
             arr[i].d, arr[i].l, arr[i].r = _ptr(d), _ptr(l), _ptr(r)
             arr[i].dext, arr[i].lext, arr[i].rext = _ext6(de), _ext6(le), _ext6(re)
-        opts = _Opts(precision, slices, beta, variant, int(bool(negate)))
+        opts = _Opts(precision, slices, beta, variant, int(bool(negate)), int(pipeline))
         h = ctypes.c_void_p(0)
         rc = lib().a4g_batch_create(ctypes.byref(h), _iarr(ptrn), _i(drank), _i(lrank), _i(rrank), arr,
                                     ctypes.c_int64(len(tl)), ctypes.byref(opts))
@@ -229,6 +230,12 @@ class Batch:
         _check(lib().a4g_batch_info(self._h, ctypes.byref(pairs), ctypes.byref(flops), ctypes.byref(ws)),
                "a4g_batch_info")
         return {"pairs": pairs.value, "flops": flops.value, "device_bytes": ws.value}
+
+    def launches(self):
+        """Library kernels per run and the GEMM launches among them."""
+        k, p = ctypes.c_int(0), ctypes.c_int(0)
+        _check(lib().a4g_batch_launches(self._h, ctypes.byref(k), ctypes.byref(p)), "a4g_batch_launches")
+        return {"kernels_per_run": k.value, "gemm_parts": p.value}
 
     FORMS = {1: "one SM per 128x128 tile", 2: "CTA pair per 256x128 tile", 3: "one SM per 128x256 tile",
              4: "CTA pair per 256x256 tile"}

@@ -503,6 +503,15 @@ def main():
                 tb.copy_(Th, non_blocking=True)
                 loaded[i % 2].record(copy)
 
+        # the host link alone: one step's inputs, host -> device, timed on the copy stream
+        h0, h1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        with torch.cuda.stream(copy):
+            h0.record(copy)
+            V2.buf.copy_(Vh, non_blocking=True)
+            T2.buf.copy_(Th, non_blocking=True)
+            h1.record(copy)
+        torch.cuda.synchronize()
+        h2d_gbs = (Vh.numel() + Th.numel()) * 8 / (h0.elapsed_time(h1) * 1e-3) / 1e9
         for ev in freed:
             ev.record(stream)
         e0.record(stream)
@@ -520,7 +529,7 @@ def main():
         e2e_ms = e0.elapsed_time(e1) / args.e2e_steps
         e2e = {"value": world * flops / (e2e_ms * 1e-3) / 1e12, "unit": "TFLOP/s",
                "h2d_bytes_per_step": (V.buf.numel() + T.buf.numel()) * 8,
-               "d2h_bytes_per_step": R.buf.numel() * 8, "ms_per_step": e2e_ms,
+               "d2h_bytes_per_step": R.buf.numel() * 8, "ms_per_step": e2e_ms, "h2d_gbs_alone": h2d_gbs,
                "pipelining": "double-buffered inputs: next step's H2D overlaps this step's compute"}
         split2.close()
         del Vh, Th, V2, T2, R2, trip2, split2
@@ -577,9 +586,12 @@ def main():
             "gemm_form": {"chosen": form["name"], "autotune_ms": form["tuned_ms"]},
             "hbm_phases": {
                 "exponents_gbs": exp_bytes / (phases["exponents"] / runs * 1e-3) / 1e9,
-                "split_gbs": split_bytes / (phases["split"] / runs * 1e-3) / 1e9,
+                # with GEMM parts, "split" is only the exposed share (the rest runs beside the GEMM)
+                "split_gbs": (split_bytes / (phases["split"] / runs * 1e-3) / 1e9
+                              if split.launches()["gemm_parts"] == 1 else None),
                 "hbm_peak_gbs": peaks.get("hbm_gbs")},
-            "gpu_launches": 6 * args.steps,
+            "gpu_launches": split.launches()["kernels_per_run"] * args.steps,
+            "gemm_parts": split.launches()["gemm_parts"],
             "cpu_baseline": cpu,
             "clocks": ck,
         }

@@ -238,7 +238,12 @@ typedef struct a4g_batch_opts {
   int negate;      /* 1: subtract the products: D = -sum (beta 0) or
                       D -= sum (beta 1), e.g. the second term of
                       W = A*B - C*E run as a second batch on the same D      */
-  int reserved[3];
+  int pipeline;    /* split precision: 0/1 off; p > 1 runs the GEMM as up to
+                      p launches over split-K ranges and slices the right
+                      operand's later ranges on a second stream beside them.
+                      Off by default: on a power-capped GB300 the overlap
+                      lowered the clock and the step gained nothing.         */
+  int reserved[2];
 } a4g_batch_opts;
 
 /* Opaque handle of a planned pardo step: pattern + triple list + workspace. */
@@ -258,6 +263,10 @@ int a4g_batch_run_timed(a4g_batch* b, void* stream);
 int a4g_batch_timings(a4g_batch* b, float* phase_ms, int nphase, int* runs);
 /* Number of block pairs executed (zero blocks skipped) and FP64 flops. */
 int a4g_batch_info(const a4g_batch* b, int64_t* pairs, double* flops, int64_t* workspace_bytes);
+/* Library kernels one run launches, and the number of tensor-core GEMM
+ * launches among them (more than one when the right operand's split runs
+ * beside the GEMM on a second stream). */
+int a4g_batch_launches(const a4g_batch* b, int* kernels_per_run, int* gemm_parts);
 /* The tensor-core GEMM form in use (the `variant` numbering; 0 for FP64
  * batches) and the autotuner's timing of each form in ms (-1: not run). */
 int a4g_batch_form(const a4g_batch* b, int* form, float* tuned_ms, int n);

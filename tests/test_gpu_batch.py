@@ -243,3 +243,24 @@ def test_split_shared_panels_in_different_pair_orders(a4, variant):
     _run(a4, R, shuffled, labels, a4.device.PREC_OZAKI_BF16, slices=1, variant=variant)
     for k, want in _reference(R, trip, labels).items():
         np.testing.assert_array_equal(R.block(k).cpu().numpy(), want)
+
+
+@pytest.mark.parametrize("variant", [1, 4])
+def test_split_pipelined_right_operand(a4, variant):
+    """pipeline=4: the GEMM runs as several launches over split-K ranges while
+    a second stream slices the right operand's later ranges; eager and
+    graph-captured runs are bit-exact on integer data."""
+    import torch
+
+    R, V, T, trip, labels = _make(a4, "ladder", [48] * 4, [8], 0.0, 4, integer=True)
+    ref = _reference(R, trip, labels)
+    b = a4.device.Batch(_ptrn(labels), 4, 4, 4, trip, precision=a4.device.PREC_OZAKI_BF16, slices=2,
+                        variant=variant, pipeline=4)
+    assert b.launches()["gemm_parts"] > 1
+    for graph in (False, True):
+        R.buf.fill_(float("nan"))
+        b.run_graph() if graph else b.run()
+        a4.device.sync()
+        torch.cuda.synchronize()
+        for k, want in ref.items():
+            np.testing.assert_array_equal(R.block(k).cpu().numpy(), want)
