@@ -93,6 +93,10 @@ int launch_dot(const double* a, const double* b, const int64_t* offA, const int6
                int64_t n, double* d_out, double* d_scratch, int64_t scratch_len, cudaStream_t s);
 int launch_slice_insert(int insert, int rank, double* tens, const int* tens_ext, double* slice,
                         const int* slice_ext, const int* ext_beg, cudaStream_t s);
+int launch_update_t2(const int* off, const int* ext, const double* t2new, const double* t2new_pair,
+                     const double* t2old, const double* t2old_pair, double* err, double* next, int rank1, int ld1,
+                     const double* e_or_fock, double* norm2, double* d_scratch, int64_t scratch_len,
+                     cudaStream_t s);
 int launch_energy_contract(int rank0, const int* off, const int* ext0, const int* pos, const double* w,
                            int rank1, int ld1, const double* e_or_fock, double efact, double* esum,
                            double* d_scratch, int scratch_len, cudaStream_t s);

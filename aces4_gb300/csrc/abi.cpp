@@ -95,6 +95,7 @@ extern "C" {
 const char* a4g_version(void) { return "aces4_gb300 0.1 (sm_103a)"; }
 
 const char* a4g_last_error(void) { return last_error_text(); }
+void a4g_clear_error(void) { clear_error(); }
 
 // ============================================================ drop-in (host)
 long long tensor_size_by_shape_(int* num_dim, int* dims, int* ierr) {
@@ -596,6 +597,31 @@ int a4g_energy_denominator(int rank0, const int* iv, const int* ext0, double* da
   rc = denominator_offsets(rank0, iv, ext0, rank1, ext1, std::vector<int>(segs, segs + nsegs), off);
   if (rc) return rc;
   return launch_denominator(rank0, off, ext0, data0, rank1, ext1[0], e, pick(stream));
+}
+
+int a4g_update_t2(const int* iv, const int* ext, const double* t2new, const double* t2new_pair,
+                  const double* t2old, const double* t2old_pair, double* diis_err, double* t2old_next, int rank1,
+                  const int* ext1, const double* e_or_fock, int nsegs, const int* segs, double* norm2,
+                  void* stream) {
+  int rc = ensure_init();
+  if (rc) return rc;
+  if (!iv || !ext || !t2new || !t2new_pair || !t2old || !t2old_pair || !t2old_next || !ext1 || !e_or_fock ||
+      (nsegs > 0 && !segs))
+    return fail(A4G_ERR_ARG, "amplitude update: null argument");
+  if (rank1 != 1 && rank1 != 2) return fail(A4G_ERR_UNSUPPORTED, "amplitude update: energies must be rank 1 or 2");
+  const int64_t n = int64_t(ext[0]) * ext[1] * ext[2] * ext[3];
+  auto overlaps = [n](const double* x, const double* y) { return x && y && x < y + n && y < x + n; };
+  for (const double* in : {t2new, t2new_pair, t2old, t2old_pair})
+    if (overlaps(in, t2old_next) || overlaps(in, diis_err))
+      return fail(A4G_ERR_ARG, "amplitude update: outputs must not overlap the inputs");
+  if (overlaps(diis_err, t2old_next)) return fail(A4G_ERR_ARG, "amplitude update: outputs overlap");
+  int off[6];
+  rc = denominator_offsets(4, iv, ext, rank1, ext1, std::vector<int>(segs, segs + std::max(nsegs, 0)), off);
+  if (rc) return rc;
+  double* scratch = reduction_scratch();
+  if (!scratch) return fail(A4G_ERR_NOMEM, "reduction scratch");
+  return launch_update_t2(off, ext, t2new, t2new_pair, t2old, t2old_pair, diis_err, t2old_next, rank1, ext1[0],
+                          e_or_fock, norm2, scratch, dot_scratch_len(), pick(stream));
 }
 
 int a4g_energy_contract(int rank0, const int* iv, const int* ext0, const double* data0, const int* den_order,

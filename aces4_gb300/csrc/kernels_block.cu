@@ -495,6 +495,95 @@ __global__ void __launch_bounds__(1024) energy_partial_kernel(DenParams p, const
   }
 }
 
+// ---------------------------------------------------------------- amplitude update
+// updatet2 of rlccd_rhf.sialx:557-600 for one block (a,i,b,j), both pardo
+// passes fused into one read of the four input blocks:
+//   t  = T2new[b,j,a,i] + T2new[a,i,b,j]        (the partner block in its own storage)
+//   t1 = T2old[b,j,a,i] + T2old[a,i,b,j]
+//   E(a,i,b,j)      = -0.5 * (t1 - t / eps)      (DIIS error vector)
+//   T2old'(a,i,b,j) = (0.5 * t) / eps            (next amplitudes, a separate buffer:
+//                                                 the partner block still reads T2old)
+//   partial[block] = sum of E^2                  (its residual norm, deterministic)
+// eps = ((e_i + e_j) - e_a) - e_b, energy_denominator_rhf's rank-4 order.  Each
+// CTA handles a 32x32 (a,b) tile at fixed (i,j); the partner tiles are read
+// along b and transposed through shared memory so all loads coalesce.
+// (0.5 t)/eps is formed as 0.5 (t/eps): both are t/(2 eps) correctly rounded
+// while the quotient is a normal number; below that the division is redone.
+struct UpdParams {
+  int ea, ei, eb, ej;   // extents
+  int oa, oi, ob, oj;   // first orbitals
+  int rank1, ld1;
+};
+
+__device__ __forceinline__ double eps_at_upd(const UpdParams& p, const double* e, int orb) {
+  return p.rank1 == 2 ? e[int64_t(orb) + int64_t(orb) * p.ld1] : e[orb];
+}
+
+__global__ void __launch_bounds__(256) update_t2_kernel(UpdParams p, const double* __restrict__ xn,
+                                                        const double* __restrict__ xnp,
+                                                        const double* __restrict__ xo,
+                                                        const double* __restrict__ xop, double* __restrict__ err,
+                                                        double* __restrict__ next, const double* __restrict__ e,
+                                                        double* partial) {
+  __shared__ double pn[32][33], po[32][33];  // [a][b] of the partner tiles
+  const int tiles_a = (p.ea + 31) / 32;
+  const int ta = blockIdx.x % tiles_a, tb = blockIdx.x / tiles_a;
+  const int i = blockIdx.y % p.ei, j = blockIdx.y / p.ei;
+  const int a0 = ta * 32, b0 = tb * 32;
+  const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+  // partner block (b,j,a,i): element (b, j, a, i) at b + eb*(j + ej*(a + ea*i))
+  for (int k = ty; k < 32; k += 8) {
+    const int b = b0 + tx, a = a0 + k;
+    double vn = 0.0, vo = 0.0;
+    if (a < p.ea && b < p.eb) {
+      const int64_t q = b + int64_t(p.eb) * (j + int64_t(p.ej) * (a + int64_t(p.ea) * i));
+      vn = __ldg(xnp + q);
+      vo = __ldg(xop + q);
+    }
+    pn[k][tx] = vn;
+    po[k][tx] = vo;
+  }
+  __syncthreads();
+  const double eij = __dadd_rn(eps_at_upd(p, e, p.oi + i), eps_at_upd(p, e, p.oj + j));
+  double acc = 0.0;
+  for (int k = ty; k < 32; k += 8) {
+    const int a = a0 + tx, b = b0 + k;
+    if (a >= p.ea || b >= p.eb) continue;
+    const int64_t q = a + int64_t(p.ea) * (i + int64_t(p.ei) * (b + int64_t(p.eb) * j));
+    const double t = __dadd_rn(pn[tx][k], __ldg(xn + q));
+    const double t1 = __dadd_rn(po[tx][k], __ldg(xo + q));
+    const double eps = __dsub_rn(__dsub_rn(eij, eps_at_upd(p, e, p.oa + a)), eps_at_upd(p, e, p.ob + b));
+    const double td = __ddiv_rn(t, eps);
+    const double ev = __dmul_rn(__dsub_rn(t1, td), -0.5);
+    if (err) err[q] = ev;
+    next[q] = fabs(td) >= 0x1p-1021 ? __dmul_rn(td, 0.5) : __ddiv_rn(__dmul_rn(t, 0.5), eps);
+    acc = fma(ev, ev, acc);
+  }
+  __shared__ double red[8];
+  for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = acc;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double sum = 0.0;
+    for (int q = 0; q < 8; ++q) sum += red[q];
+    partial[int64_t(blockIdx.y) * gridDim.x + blockIdx.x] = sum;
+  }
+}
+
+// *out += fixed-order sum of the partials (out may be null: nothing)
+__global__ void sum_partials_kernel(const double* partial, int64_t np, double* out) {
+  __shared__ double red[kThreads];
+  double acc = 0.0;
+  for (int64_t q = threadIdx.x; q < np; q += blockDim.x) acc += partial[q];
+  red[threadIdx.x] = acc;
+  __syncthreads();
+  for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+    if (threadIdx.x < s) red[threadIdx.x] += red[threadIdx.x + s];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0 && out) *out = __dadd_rn(*out, red[0]);
+}
+
 // *esum += efact * (fixed-order sum of the partials)
 __global__ void energy_final_kernel(const double* partial, int np, double efact, double* esum) {
   __shared__ double red[kThreads];
@@ -678,6 +767,31 @@ int launch_denominator(int rank0, const int* off, const int* ext0, double* data,
   int64_t n = 0;
   const DenParams p = den_params(rank0, off, ext0, nullptr, rank1, ld1, &n);
   denominator_kernel<<<grid_for(n), kThreads, 0, s>>>(p, data, e_or_fock, n);
+  A4G_CUDA(cudaGetLastError());
+  return A4G_OK;
+}
+
+int launch_update_t2(const int* off, const int* ext, const double* t2new, const double* t2new_pair,
+                     const double* t2old, const double* t2old_pair, double* err, double* next, int rank1, int ld1,
+                     const double* e_or_fock, double* norm2, double* d_scratch, int64_t scratch_len,
+                     cudaStream_t s) {
+  UpdParams p{};
+  p.ea = ext[0], p.ei = ext[1], p.eb = ext[2], p.ej = ext[3];
+  p.oa = off[0], p.oi = off[1], p.ob = off[2], p.oj = off[3];
+  p.rank1 = rank1, p.ld1 = ld1;
+  const int64_t gx = int64_t((p.ea + 31) / 32) * ((p.eb + 31) / 32), gy = int64_t(p.ei) * p.ej;
+  if (gx * gy == 0) return A4G_OK;
+  if (gx > 0x7fffffffLL || gy > 65535) return fail(A4G_ERR_RANGE, "amplitude update: block too large");
+  double* partial = d_scratch;
+  bool own = false;
+  if (gx * gy > scratch_len) {  // more CTAs than the reduction scratch holds
+    A4G_CUDA(cudaMallocAsync(reinterpret_cast<void**>(&partial), size_t(gx * gy) * sizeof(double), s));
+    own = true;
+  }
+  update_t2_kernel<<<dim3(unsigned(gx), unsigned(gy)), 256, 0, s>>>(p, t2new, t2new_pair, t2old, t2old_pair, err,
+                                                                     next, e_or_fock, partial);
+  sum_partials_kernel<<<1, kThreads, 0, s>>>(partial, gx * gy, norm2);
+  if (own) A4G_CUDA(cudaFreeAsync(partial, s));
   A4G_CUDA(cudaGetLastError());
   return A4G_OK;
 }

@@ -138,6 +138,17 @@ def energy_denominator(index_values, ext0, data0, ext1, e_or_fock, seg_sizes, st
     _check(rc, "a4g_energy_denominator")
 
 
+def update_t2(index_values, ext, t2new, t2new_pair, t2old, t2old_pair, diis_err, t2old_next, ext1, e_or_fock,
+              seg_sizes, norm2=None, stream=None):
+    """updatet2 for one (a,i,b,j) block (a4g_update_t2): writes the DIIS error
+    block and the next T2old block, adds sum(err^2) to norm2 (CUDA float64)."""
+    p = lambda x: ctypes.c_void_p(_ptr(x)) if x is not None else None
+    rc = lib().a4g_update_t2(_iarr(index_values), _iarr(ext), p(t2new), p(t2new_pair), p(t2old), p(t2old_pair),
+                             p(diis_err), p(t2old_next), _i(len(ext1)), _iarr(ext1), p(e_or_fock),
+                             _i(len(seg_sizes)), _iarr(seg_sizes), p(norm2), _stream(stream))
+    _check(rc, "a4g_update_t2")
+
+
 def energy_contract(index_values, ext0, data0, ext1, e_or_fock, seg_sizes, efact, esum, den_order=None,
                     stream=None):
     """esum (1-element CUDA float64 tensor) += efact * sum w * (w / eps): the

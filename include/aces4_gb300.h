@@ -47,6 +47,9 @@ extern "C" {
 
 /* Text of the last error on the calling thread ("" when none). */
 const char* a4g_last_error(void);
+/* Forget the recorded error (the legacy _gpu_* calls record failures and
+ * never clear them, so a host checks a sequence of calls with one read). */
+void a4g_clear_error(void);
 /* Library version string. */
 const char* a4g_version(void);
 
@@ -187,6 +190,24 @@ int a4g_insert(int rank, double* tens, const int* tens_ext, const double* slice,
 int a4g_energy_denominator(int rank0, const int* index_values0, const int* ext0, double* data0,
                            int rank1, const int* ext1, const double* e_or_fock, int nsegs,
                            const int* seg_sizes, void* stream);
+/* Amplitude update of one block (a,i,b,j): procedure updatet2 of
+ * src/sialx/qm/cc/rlccd_rhf.sialx:557-600, both of its pardo passes fused
+ * into one read of the inputs:
+ *   t  = T2new[b,j,a,i] + T2new[a,i,b,j];   t1 = T2old[b,j,a,i] + T2old[a,i,b,j]
+ *   diis_err   = -0.5 * (t1 - t / eps)      (Eaibj, the DIIS error block; NULL: not stored)
+ *   t2old_next = (0.5 * t) / eps            (the next T2old block)
+ *   *norm2    += sum diis_err^2             (device double; NULL: not formed)
+ * eps as energy_denominator_rhf forms it (index_values / ext: the segments and
+ * extents of (a,i,b,j)).  *_pair are the (b,j,a,i) blocks of the same arrays,
+ * stored with extents (ext[2], ext[3], ext[0], ext[1]); a diagonal block is
+ * its own pair.  The outputs must not overlap any input: the partner block
+ * still reads T2old, so the next T2old goes to another buffer (the reference
+ * separates the passes with a server barrier).  Elements are bit-identical
+ * to the reference's sequence; norm2 is a deterministic sum. */
+int a4g_update_t2(const int* index_values, const int* ext, const double* t2new, const double* t2new_pair,
+                  const double* t2old, const double* t2old_pair, double* diis_err, double* t2old_next,
+                  int rank1, const int* ext1, const double* e_or_fock, int nsegs, const int* seg_sizes,
+                  double* norm2, void* stream);
 /* Energy contribution of one block, the (T) pattern of
  * src/sialx/qm/cc/rccsdpt_aaa.sialx:2163-2172 (permute to the denominator's
  * index order, energy_denominator_rhf, full contraction of the divided block

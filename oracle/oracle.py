@@ -240,3 +240,42 @@ def energy_contract(index_values, ext0, w, ext1, fock, seg_sizes, efact, den_ord
     etemp = np.zeros(1)
     assert tensor_block_contract(ptrn, wd, ext_p, wp, ext_p, etemp, []) == 0
     return float(etemp[0] * efact)
+
+
+def update_t2(index_values, ext, t2new, t2new_pair, t2old, t2old_pair, ext1, fock, seg_sizes):
+    """Procedure updatet2 of rlccd_rhf.sialx:557-600 for one block (a,i,b,j),
+    as the reference's block operations: permuted copies of the (b,j,a,i)
+    partner blocks (tensor_block_copy_), in-place block adds/subtracts
+    (handle_block_add/subtract), energy_denominator_rhf, Block::scale; the
+    error block's squared norm by tensor_block_norm2_.  Returns (E, next
+    T2old block, norm2)."""
+    ea, ei, eb, ej = ext
+    pair_ext = [eb, ej, ea, ei]
+    o2n = [3, 4, 1, 2]  # (b,j,a,i) -> (a,i,b,j)
+    ids = [1, 2, 3, 4]
+    f = np.ascontiguousarray(fock, dtype=np.float64)
+
+    def perm(x):
+        ierr, out = tensor_block_copy(pair_ext, o2n, np.ascontiguousarray(x, dtype=np.float64))
+        assert ierr == 0
+        return out
+
+    t2new = np.ascontiguousarray(t2new, dtype=np.float64)
+    t2old = np.ascontiguousarray(t2old, dtype=np.float64)
+    # first pass
+    taibj = perm(t2new_pair)
+    assert block_add_sub(0, ids, ids, ids, ext, 1, taibj, taibj.copy(), t2new) == 0
+    t1 = perm(t2old_pair)
+    assert block_add_sub(0, ids, ids, ids, ext, 1, t1, t1.copy(), t2old) == 0
+    assert energy_denominator_rhf(index_values, ext, taibj, ext1, f, seg_sizes) == 0
+    assert block_add_sub(1, ids, ids, ids, ext, 1, t1, t1.copy(), taibj) == 0
+    assert tensor_block_scale(t1, ext, -0.5) == 0
+    err = t1
+    # second pass
+    t2 = perm(t2new_pair)
+    assert block_add_sub(0, ids, ids, ids, ext, 1, t2, t2.copy(), t2new) == 0
+    assert tensor_block_scale(t2, ext, 0.5) == 0
+    assert energy_denominator_rhf(index_values, ext, t2, ext1, f, seg_sizes) == 0
+    nrm, ierr = tensor_block_norm2(err, ext)
+    assert ierr == 0
+    return err, t2, nrm

@@ -261,6 +261,7 @@ def test_legacy_gpu_api(lib):
     import torch
 
     L = lib.lib()
+    L.a4g_clear_error()  # errors recorded by earlier tests' rejected calls
     rng = np.random.default_rng(9)
     # y(a,i,b,j) = x1(a,k,c,i) * x2(c,b,k,j) with labels
     ext = dict(a=6, i=4, b=5, j=3, k=7, c=8)

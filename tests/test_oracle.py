@@ -288,3 +288,35 @@ def test_energy_contract_oracle_against_loops(rank0, rank1, permuted):
         vir = sum(ev[q] for q in range(0, rank0, 2))
         ref += W[idx] * (W[idx] / (occ - vir))
     assert abs(got - 0.75 * ref) <= 1e-13 * abs(ref)
+
+
+@pytest.mark.parametrize("diagonal", [False, True])
+def test_update_t2_oracle_against_loops(diagonal):
+    """The oracle's updatet2 (reference block operations) against a plain loop
+    of the procedure's arithmetic, bit for bit."""
+    rng = np.random.default_rng(31 + diagonal)
+    segs = [4, 5, 6]
+    norb = sum(segs)
+    e = np.concatenate([rng.uniform(-2, -0.5, 4), rng.uniform(0.2, 5, 11)])
+    fock = np.diag(e).ravel(order="F")
+    iv = [2, 1, 2, 1] if diagonal else [2, 1, 3, 1]
+    ext = [segs[v - 1] for v in iv]
+    n = kat.size(ext)
+    xn, xo = rng.standard_normal(n) * 0.1, rng.standard_normal(n) * 0.1
+    xnp = xn if diagonal else rng.standard_normal(n) * 0.1
+    xop = xo if diagonal else rng.standard_normal(n) * 0.1
+    err, nxt, nrm = oracle.update_t2(iv, ext, xn, xnp, xo, xop, [norb, norb], fock, segs)
+    offs = [sum(segs[: v - 1]) for v in iv]
+    pe = [ext[2], ext[3], ext[0], ext[1]]
+    Xn, Xo = xn.reshape(ext, order="F"), xo.reshape(ext, order="F")
+    Pn, Po = xnp.reshape(pe, order="F"), xop.reshape(pe, order="F")
+    er, nr = np.empty(ext), np.empty(ext)
+    for a, i, b, j in np.ndindex(*ext):
+        eps = ((e[i + offs[1]] + e[j + offs[3]]) - e[a + offs[0]]) - e[b + offs[2]]
+        t = Pn[b, j, a, i] + Xn[a, i, b, j]
+        t1 = Po[b, j, a, i] + Xo[a, i, b, j]
+        er[a, i, b, j] = (t1 - t / eps) * -0.5
+        nr[a, i, b, j] = (t * 0.5) / eps
+    np.testing.assert_array_equal(err, er.ravel(order="F"))
+    np.testing.assert_array_equal(nxt, nr.ravel(order="F"))
+    assert abs(nrm - (er ** 2).sum()) <= 1e-13 * nrm
