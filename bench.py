@@ -371,6 +371,108 @@ def run_triples(args, world, rank, local):
         dist.destroy_process_group()
 
 
+CONFIG_METRIC = "FP64-equiv TFLOP/s per pardo step (batched split vs plain FP64)"
+
+
+def build_config(torch, name: str, seed: int):
+    """Block arrays and triples of the ring (config 2) and of a batched sparse
+    ladder step (config 3), and of the small ladder (config 1)."""
+    import numpy as np
+
+    from aces4_gb300.blocks import (LADDER_LABELS, RING_LABELS, BlockArray, ladder_triples, ring_triples,
+                                    segments_choice, segments_uniform)
+
+    g = torch.Generator(device="cuda")
+    g.manual_seed(seed)
+    if name == "ladder-small":  # o=10 as 2x5, v=48 as 4x12, all blocks dense
+        vs, os_ = [12] * 4, [5, 5]
+        V = BlockArray([vs] * 4)
+        T = BlockArray([vs, vs, os_, os_])
+        R = BlockArray([vs, vs, os_, os_])
+        V.buf.uniform_(-1.0, 1.0, generator=g).div_(48.0)
+        T.buf.normal_(0.0, 0.1, generator=g)
+        return R, ladder_triples(R, V, T), LADDER_LABELS, "ladder o=10 (2x5), v=48 (4x12), all blocks"
+    if name == "ring":  # o=40 as 2x20, v=300 in seeded segments of 24..40
+        vs, os_ = segments_uniform(300, 24, 40, seed=2), [20, 20]
+        V = BlockArray([vs, os_, vs, os_])
+        T = BlockArray([vs, vs, os_, os_])
+        R = BlockArray([vs, os_, vs, os_])
+        V.buf.uniform_(-1.0, 1.0, generator=g).div_(float(np.sqrt(40 * 300)))
+        T.buf.normal_(0.0, 0.1, generator=g)
+        return (R, ring_triples(R, V, T), RING_LABELS,
+                f"ring R(a,i,b,j)+=V(a,k,c,i)T(c,b,k,j), o=40 (2x20), v=300 ({len(vs)} segments {vs})")
+    # sparse: ladder o=48 as 2x24, v=400 in seeded segments from {12,16,24,32,48},
+    # 30% of V blocks zero, four (a,b) segment pairs x all (c,d,i,j)
+    vs, os_ = segments_choice(400, [12, 16, 24, 32, 48], seed=3), [24, 24]
+    rng = np.random.default_rng(3)
+    zero = {}
+
+    def present(k):
+        zero.setdefault(k, rng.random() < 0.3)
+        return not zero[k]
+
+    V = BlockArray([vs[:2], vs[:2], vs, vs], present=present)
+    T = BlockArray([vs, vs, os_, os_])
+    R = BlockArray([vs[:2], vs[:2], os_, os_])
+    V.buf.uniform_(-1.0, 1.0, generator=g).div_(400.0)
+    T.buf.normal_(0.0, 0.1, generator=g)
+    return (R, ladder_triples(R, V, T), LADDER_LABELS,
+            f"sparse ladder step o=48 (2x24), v=400 ({len(vs)} segments {vs}), 30% of V blocks zero, "
+            f"(a,b) in 2x2 segments")
+
+
+def run_config(args, world, rank, local):
+    """One pardo step of configs 1-3 as a graph, split precision and plain
+    FP64, per-block error of the split result against the FP64 one."""
+    import torch
+
+    import aces4_gb300 as a4
+    from oracle import oracle
+
+    torch.cuda.set_device(local)
+    a4.device.init(local)
+    stream = torch.cuda.Stream()  # graphs are captured on a created stream, not the legacy default one
+    R, trip, labels, desc = build_config(torch, args.workload, 11 + rank)
+    torch.cuda.synchronize()
+    d, l, r = labels
+    ptrn = oracle.get_contraction_ptrn(len(d), len(l), len(r), d + l + r)[1]
+    res = {}
+    for prec in (a4.device.PREC_OZAKI_BF16, a4.device.PREC_FP64):
+        b = a4.device.Batch(ptrn, 4, 4, 4, trip, precision=prec, slices=args.slices)
+        for _ in range(args.warmup):
+            b.run_graph(stream)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        steps = args.steps if prec else max(1, min(args.steps, args.fp64_steps or 1))
+        e0.record(stream)
+        for _ in range(steps):
+            b.run_graph(stream)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        res[prec] = {"ms": e0.elapsed_time(e1) / steps, "out": R.buf.clone(), "info": b.info(),
+                     "form": b.form() if prec else None, "launches": b.launches()}
+        b.close()
+    sp, fp = res[a4.device.PREC_OZAKI_BF16], res[a4.device.PREC_FP64]
+    errs = []
+    for k in R.keys():
+        o, n = R.offsets[k], R.size(k)
+        a, ref = sp["out"][o:o + n], fp["out"][o:o + n]
+        errs.append(float(torch.linalg.norm(a - ref) / torch.linalg.norm(ref)))
+    flops = sp["info"]["flops"]
+    if rank == 0:
+        print(json.dumps({
+            "metric": CONFIG_METRIC, "value": world * flops / (sp["ms"] * 1e-3) / 1e12, "unit": "TFLOP/s",
+            "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": sp["ms"],
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "bf16", "data": "synthetic",
+            "config": {"workload": desc, "block_pairs": sp["info"]["pairs"], "flop": flops, "slices": args.slices,
+                       "graph": True},
+            "fp64_plain": {"value": flops / (fp["ms"] * 1e-3) / 1e12, "unit": "TFLOP/s", "ms_per_step": fp["ms"]},
+            "split_over_fp64": fp["ms"] / sp["ms"], "rel_err_max_block_vs_fp64_gpu": max(errs),
+            "gemm_form": {"chosen": sp["form"]["name"], "autotune_ms": sp["form"]["tuned_ms"]},
+            "gpu_launches": sp["launches"]["kernels_per_run"] * args.steps,
+        }), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -389,8 +491,10 @@ def main():
     ap.add_argument("--noseg", type=int, default=4, help="occupied segments of 16 (4: o=64)")
     ap.add_argument("--tseg", type=int, default=24, help="triples: segment size (occupied: one segment)")
     ap.add_argument("--tnv", type=int, default=10, help="triples: virtual segments")
-    ap.add_argument("--workload", default="ladder", choices=["ladder", "triples"],
-                    help="ladder: the o=64/v=512 ladder slab (the headline metric); triples: one triples energy step")
+    ap.add_argument("--workload", default="ladder", choices=["ladder", "triples", "ladder-small", "ring", "sparse"],
+                    help="ladder: the o=64/v=512 ladder slab (the headline metric); triples: one triples energy "
+                         "step; ladder-small / ring / sparse: one pardo step of the o=10/v=48 ladder, the "
+                         "o=40/v=300 ring, the o=48/v=400 sparse ladder")
     args = ap.parse_args()
 
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -401,6 +505,9 @@ def main():
         return
     if args.workload == "triples":
         run_triples(args, world, rank, local)
+        return
+    if args.workload in ("ladder-small", "ring", "sparse"):
+        run_config(args, world, rank, local)
         return
 
     import numpy as np
@@ -454,7 +561,7 @@ def main():
     R_split = R.buf.clone()
 
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    fp64_value = fp64_ms = None
+    fp64_value = fp64_ms = dgemm_tflops = None
     blk_err = []
     if args.fp64_steps > 0:
         # plain FP64 form of the same step (the denominator of the split target)
@@ -468,6 +575,19 @@ def main():
         torch.cuda.synchronize()
         fp64_ms = e0.elapsed_time(e1) / args.fp64_steps
         fp64_value = flops / (fp64_ms * 1e-3) / 1e12
+        # the FP64 pipe's reference rate on this GPU: cuBLAS DGEMM, 4096^3, timed here
+        ga = torch.randn(4096, 4096, dtype=torch.float64, device="cuda")
+        gb = torch.randn(4096, 4096, dtype=torch.float64, device="cuda")
+        for _ in range(2):
+            torch.matmul(ga, gb)
+        torch.cuda.synchronize()
+        e0.record(stream)
+        for _ in range(3):
+            torch.matmul(ga, gb)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        dgemm_tflops = 3 * 2 * 4096 ** 3 / (e0.elapsed_time(e1) * 1e-3) / 1e12
+        del ga, gb
         R_fp64 = R.buf.clone()
         for k in R.keys():
             o, n = R.offsets[k], R.size(k)
@@ -578,7 +698,10 @@ def main():
                          "algorithmic_per_launch": f"{S * (S + 1) // 2} slice-pair GEMMs x {flops:.3e} flop",
                          "traffic": _traffic("oz_gemm_kernel")},
             "fp64_plain": ({"value": fp64_value, "unit": "TFLOP/s", "ms_per_step": fp64_ms,
-                            "kernel": "grouped DMMA (mma.sync f64)"} if fp64_value else None),
+                            "kernel": "grouped DMMA (mma.sync f64)",
+                            "roofline": {"bound": "fp64 pipe", "peak": dgemm_tflops,
+                                         "peak_kind": "cuBLAS DGEMM 4096^3 measured in this run",
+                                         "frac": fp64_value / dgemm_tflops}} if fp64_value else None),
             "split_over_fp64": (value / world / fp64_value) if fp64_value else None,
             "rel_err_max_block_vs_fp64_gpu": max(blk_err) if blk_err else None,
             "rel_err_block_vs_cpu_oracle": err_oracle,
