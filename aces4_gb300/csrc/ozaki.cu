@@ -1051,6 +1051,134 @@ __global__ void __launch_bounds__(256) oz_recombine_kernel(const OzTile* __restr
   }
 }
 
+// Single-split form of the recombine (every level sum already complete, e.g.
+// the short-k triples): a persistent CTA per SM walks pieces of 4096 elements
+// (16 KB per level: one whole column run of the tile's int32 plane per
+// level, 16 or 32 columns; 1024 threads, four elements each), each level's
+// piece fetched by one bulk async copy
+// into a double-buffered shared-memory stage, so the next piece streams in
+// while this one is combined and stored.  Waits are bounded (error flag, then
+// a bounded drain of the copy still in flight).
+constexpr int kRecPiece = 4096;  // int32 elements per level per piece (16 KB)
+
+template <int S>
+struct __align__(128) RecSmem {
+  int lev[2][S][kRecPiece];
+  double val[kRecPiece + 64];  // [col][rows + 1] transpose buffer
+  uint64_t full[2];
+};
+
+__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                   smem_u32(dst)),
+               "l"(src), "r"(bytes), "r"(smem_u32(bar))
+               : "memory");
+}
+
+__device__ __forceinline__ bool wait_bounded(uint64_t* bar, uint32_t parity) {
+  if (mbar_try_wait(bar, parity)) return true;
+  const unsigned long long t0 = now_ns();
+#pragma unroll 1
+  for (uint32_t it = 1;; ++it) {
+    if (mbar_try_wait(bar, parity)) return true;
+    if ((it & 255) == 0 && now_ns() - t0 > kWaitLimitNs) return false;
+  }
+}
+
+template <int S>
+__global__ void __launch_bounds__(1024, 1) oz_recombine_bulk_kernel(const OzTile* __restrict__ tiles,
+                                                                  const OzDBlock* __restrict__ dblocks,
+                                                                  const PlanRef* __restrict__ plans,
+                                                                  const OzPanel* __restrict__ pa,
+                                                                  const OzPanel* __restrict__ pb,
+                                                                  const int* __restrict__ ws, int log_rows,
+                                                                  int log_cols, int n_tiles, int mode, int* err) {
+  extern __shared__ __align__(128) unsigned char rec_smem_raw[];
+  RecSmem<S>& sm = *reinterpret_cast<RecSmem<S>*>(rec_smem_raw);
+  const int rows = 1 << log_rows;
+  const int cols_pp = kRecPiece >> log_rows;                    // columns per piece
+  const int pieces_per_tile = 1 << (log_rows + log_cols - 12);  // 4096 = 2^12
+  const int npieces = n_tiles * pieces_per_tile;
+  const size_t plane = size_t(1) << (log_rows + log_cols);
+  if (threadIdx.x == 0) {
+    mbar_init(&sm.full[0], 1);
+    mbar_init(&sm.full[1], 1);
+    fence_mbar_init();
+  }
+  __syncthreads();
+  auto issue = [&](int q, int st) {
+    const int tile = q / pieces_per_tile, pc = q % pieces_per_tile;
+    mbar_expect_tx(&sm.full[st], uint32_t(S) * kRecPiece * 4);
+#pragma unroll
+    for (int lv = 0; lv < S; ++lv)
+      bulk_g2s(sm.lev[st][lv], ws + (size_t(tile) * S + lv) * plane + size_t(pc) * kRecPiece, kRecPiece * 4,
+               &sm.full[st]);
+  };
+  int q = blockIdx.x;
+  if (threadIdx.x == 0 && q < npieces) issue(q, 0);
+  for (int it = 0; q < npieces; q += gridDim.x, ++it) {
+    const int st = it & 1;
+    if (threadIdx.x == 0 && q + int(gridDim.x) < npieces) issue(q + gridDim.x, st ^ 1);
+    if (!wait_bounded(&sm.full[st], uint32_t(it >> 1) & 1u)) {
+      atomicExch(err, 5);
+      // drain the next piece's copies (if issued) before this CTA's memory is released
+      if (threadIdx.x == 0 && q + int(gridDim.x) < npieces) wait_bounded(&sm.full[st ^ 1], uint32_t((it + 1) >> 1) & 1u);
+      return;
+    }
+    const int tile = q / pieces_per_tile, pc = q % pieces_per_tile;
+    const OzTile tl = tiles[tile];
+    const OzDBlock db = dblocks[tl.dblock];
+    const PlanRef pl = plans[db.plan];
+    const int* ea = pa[tl.panel_a].exps;
+    const int* eb = pb[tl.panel_b].exps;
+    const int sc = pc * cols_pp;
+#pragma unroll
+    for (int p = 0; p < kRecPiece / 1024; ++p) {
+      const int e = p * 1024 + threadIdx.x;
+      const int row = e & (rows - 1), cl = e >> log_rows;
+      const int m = tl.m0 + row, n = tl.n0 + sc + cl;
+      double v = 0.0;
+      const bool live = m < pl.M && n < pl.N;
+      if (live) {
+        const int E = (ea[m] ? ea[m] : 1) - 1022, F = (eb[n] ? eb[n] : 1) - 1022;
+        const int e2 = E + F + 2 - kDigitBits * (S + 1);
+        long long acc = 0;  // a unit's level-t sum is below (t+1) 2^31 / S: the 64-bit sum is exact
+#pragma unroll
+        for (int lv = 0; lv < S; ++lv) acc += (long long)sm.lev[st][lv][e] * (1ll << (kDigitBits * (S - 1 - lv)));
+        v = u64_scaled_to_double(acc < 0 ? (unsigned long long)(-acc) : (unsigned long long)acc, acc < 0, e2);
+        if (mode & 2) v = -v;
+      }
+      if (db.col_fast) {
+        sm.val[cl * (rows + 1) + row] = v;
+      } else if (live) {
+        double* dst = db.d + pl.offDm[m] + pl.offDn[n];
+        *dst = (mode & 1) ? *dst + v : v;
+      }
+    }
+    if (db.col_fast) {
+      __syncthreads();
+      constexpr int kPer = kRecPiece / 1024;
+      double* dst[kPer];
+      double old[kPer];
+#pragma unroll
+      for (int p = 0; p < kPer; ++p) {  // addresses and (beta) the old values first: loads in flight together
+        const int e = p * 1024 + threadIdx.x;
+        const int cl = e % cols_pp, row = e / cols_pp;
+        const int m = tl.m0 + row, n = tl.n0 + sc + cl;
+        dst[p] = (m < pl.M && n < pl.N) ? db.d + pl.offDm[m] + pl.offDn[n] : nullptr;
+        old[p] = (dst[p] && (mode & 1)) ? *dst[p] : 0.0;
+      }
+#pragma unroll
+      for (int p = 0; p < kPer; ++p) {
+        const int e = p * 1024 + threadIdx.x;
+        const int cl = e % cols_pp, row = e / cols_pp;
+        if (dst[p]) *dst[p] = (mode & 1) ? old[p] + sm.val[cl * (rows + 1) + row] : sm.val[cl * (rows + 1) + row];
+      }
+    }
+    __syncthreads();  // stage st and the transpose buffer are free again
+  }
+}
+
 using EncodeTiled = PFN_cuTensorMapEncodeTiled_v12000;
 EncodeTiled get_encoder() {
   static EncodeTiled fn = nullptr;
@@ -1216,6 +1344,30 @@ int oz_launch_recombine(const OzTile* tiles, int ntiles, int tile_rows, int tile
   if ((tile_rows != 128 && tile_rows != 256) || (tile_cols != 128 && tile_cols != 256))
     return fail(A4G_ERR_ARG, "recombine: unsupported tile shape");
   const int lr = tile_rows == 256 ? 8 : 7, lc = tile_cols == 256 ? 8 : 7;
+  if (nsplit == 1 && slices <= 5) {
+    // single split: the bulk-copy pipelined form (one CTA per SM)
+    const int npieces = ntiles * (tile_rows * tile_cols / kRecPiece);
+    const int grid = std::min(npieces, ctx()->num_sms > 0 ? ctx()->num_sms : 152);
+    int* err = ctx()->d_error_flag;
+    switch (slices) {
+#define A4G_RECOMBINE_BULK(SL)                                                                                   \
+  case SL: {                                                                                                     \
+    static bool attr = false;                                                                                    \
+    if (!attr) {                                                                                                 \
+      A4G_CUDA(cudaFuncSetAttribute(oz_recombine_bulk_kernel<SL>, cudaFuncAttributeMaxDynamicSharedMemorySize,  \
+                                    int(sizeof(RecSmem<SL>))));                                                 \
+      attr = true;                                                                                               \
+    }                                                                                                            \
+    oz_recombine_bulk_kernel<SL><<<grid, 1024, sizeof(RecSmem<SL>), s>>>(tiles, dblocks, plans, pa, pb, ws, lr, lc, \
+                                                                       ntiles, mode, err);                       \
+    break;                                                                                                       \
+  }
+      A4G_RECOMBINE_BULK(1) A4G_RECOMBINE_BULK(2) A4G_RECOMBINE_BULK(3) A4G_RECOMBINE_BULK(4) A4G_RECOMBINE_BULK(5)
+#undef A4G_RECOMBINE_BULK
+    }
+    A4G_CUDA(cudaGetLastError());
+    return A4G_OK;
+  }
   const int per = tile_cols / 32;  // 32-column strips per tile
   if (int64_t(ntiles) * per > 0x7fffffffLL) return fail(A4G_ERR_RANGE, "too many tiles");
   const unsigned g = unsigned(ntiles * per);
