@@ -249,20 +249,6 @@ __device__ __forceinline__ void tc_ld16_nowait(uint32_t taddr, uint32_t (&r)[16]
         "=r"(r[14]), "=r"(r[15])
       : "r"(taddr));
 }
-__device__ __forceinline__ void tc_ld32(uint32_t taddr, uint32_t (&r)[32]) {
-  asm volatile(
-      "tcgen05.ld.sync.aligned.32x32b.x32.b32 "
-      "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
-      "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
-      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
-        "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]),
-        "=r"(r[14]), "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]),
-        "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]), "=r"(r[25]),
-        "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
-      : "r"(taddr));
-  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-}
-
 // Exact accumulation of an integer-valued float x (|x| < 2^24) into hi + lo.
 __device__ __forceinline__ void two_sum_acc(float& hi, float& lo, float x) {
   const float s = __fadd_rn(hi, x);
@@ -709,7 +695,6 @@ template <int S>
 __global__ void __launch_bounds__(256) oz_split_kernel(const OzSplitJob* __restrict__ jobs,
                                                        const int64_t* __restrict__ prefix, int njobs,
                                                        const OzPanel* __restrict__ panels) {
-  constexpr int slices = S;
   __shared__ unsigned long long tile[kSplitT][kSplitT + 1];
   const int64_t t = blockIdx.x;
   const int j = find_job(prefix, njobs, t);
