@@ -86,6 +86,7 @@ struct a4g_batch {
   std::vector<cudaEvent_t> part_ev;  // [0]: fork after split group 0; [g]: split group g done
   int* d_ws = nullptr;
   cudaGraphExec_t graph = nullptr;
+  cudaStream_t capture = nullptr;  // private stream the graph is captured on (any caller stream may replay it)
   // phase timing: events[run][6] recorded by a4g_batch_run_timed
   std::vector<std::vector<cudaEvent_t>> events;
   int timed_runs = 0;
@@ -95,6 +96,7 @@ struct a4g_batch {
       for (cudaEvent_t e : ev) cudaEventDestroy(e);
     for (cudaEvent_t e : part_ev) cudaEventDestroy(e);
     if (side) cudaStreamDestroy(side);
+    if (capture) cudaStreamDestroy(capture);
     if (graph) cudaGraphExecDestroy(graph);
     for (void* p : allocs) cudaFree(p);
   }
@@ -751,10 +753,13 @@ int a4g_batch_run_graph(a4g_batch* b, void* stream) {
   if (!b) return fail(A4G_ERR_ARG, "null batch");
   cudaStream_t s = pick(stream);
   if (!b->graph) {
+    // capture on a private stream: the caller's may be the legacy default
+    // stream, which cannot be captured; capturing records work, runs none
+    if (!b->capture) A4G_CUDA(cudaStreamCreateWithFlags(&b->capture, cudaStreamNonBlocking));
     cudaGraph_t g = nullptr;
-    A4G_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
-    const int rc = run(b, s);
-    cudaError_t e = cudaStreamEndCapture(s, &g);
+    A4G_CUDA(cudaStreamBeginCapture(b->capture, cudaStreamCaptureModeThreadLocal));
+    const int rc = run(b, b->capture);
+    cudaError_t e = cudaStreamEndCapture(b->capture, &g);
     if (rc) {
       if (g) cudaGraphDestroy(g);
       return rc;

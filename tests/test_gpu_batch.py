@@ -264,3 +264,48 @@ def test_split_pipelined_right_operand(a4, variant):
         torch.cuda.synchronize()
         for k, want in ref.items():
             np.testing.assert_array_equal(R.block(k).cpu().numpy(), want)
+
+
+def test_graph_replay_on_the_legacy_default_stream(a4):
+    """run_graph with the caller's legacy default stream (handle 0): the graph
+    is captured on the batch's own stream and replayed on the caller's."""
+    import torch
+
+    R, V, T, trip, labels = _make(a4, "ladder", [12, 12], [5], 0.0, 21, integer=True)
+    ref = _reference(R, trip, labels)
+    b = a4.device.Batch(_ptrn(labels), 4, 4, 4, trip, precision=a4.device.PREC_OZAKI_BF16, slices=1)
+    for _ in range(2):
+        R.buf.fill_(float("nan"))
+        b.run_graph(torch.cuda.default_stream())
+        torch.cuda.synchronize()
+        for k, want in ref.items():
+            np.testing.assert_array_equal(R.block(k).cpu().numpy(), want)
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+def test_batch_matrix_and_outer_product_patterns(a4, precision):
+    """Rank-2 blocks (a plain matrix product per pair) and an outer product
+    (no contracted index, K = 1) through the batch, both precisions, against
+    the oracle."""
+    import torch
+
+    rng = np.random.default_rng(41)
+    cases = [
+        ([1, 2], [1, 3], [3, 2], [37, 29], [37, 45], [45, 29]),  # D(i,j) = L(i,k) R(k,j)
+        ([1, 2, 3], [1, 2], [3], [7, 6, 9], [7, 6], [9]),      # D(a,b,c) = L(a,b) R(c)
+    ]
+    for dl, ll, rl, de, le, re in cases:
+        ierr, p = oracle.get_contraction_ptrn(len(dl), len(ll), len(rl), dl + ll + rl)
+        assert ierr == 0
+        pairs = 3
+        Ls = [rng.integers(-60, 61, int(np.prod(le))).astype(np.float64) for _ in range(pairs)]
+        Rs = [rng.integers(-60, 61, int(np.prod(re))).astype(np.float64) for _ in range(pairs)]
+        D = torch.full((int(np.prod(de)),), float("nan"), dtype=torch.float64, device="cuda")
+        tl = [torch.tensor(x, device="cuda") for x in Ls]
+        tr = [torch.tensor(x, device="cuda") for x in Rs]
+        trip = [(D, tl[q], tr[q], de, le, re) for q in range(pairs)]
+        b = a4.device.Batch(p, len(dl), len(ll), len(rl), trip, precision=precision, slices=2)
+        b.run()
+        a4.device.sync()
+        want = sum(oracle.contract_blas(p, Ls[q], le, Rs[q], re, de) for q in range(pairs))
+        np.testing.assert_array_equal(D.cpu().numpy(), want)
