@@ -53,3 +53,19 @@ def test_host_only_entries_without_gpu(so):
 def test_library_has_no_oracle_dependency(so):
     # the product never links the CPU oracle
     assert not hasattr(so, "a4o_tensor_block_contract")
+
+
+def test_interpreter_style_caller_compiles_and_links(tmp_path):
+    """A C++ caller that declares the drop-ins exactly as the reference's
+    tensor_ops_c_prototypes.h does (scalars by reference) builds and links
+    against the library (it runs in the GPU suite)."""
+    import shutil
+
+    if not shutil.which("g++"):
+        pytest.skip("no g++")
+    from tests import c_abi_helper
+
+    exe = c_abi_helper.build(str(tmp_path))
+    assert os.path.exists(exe)
+    c_abi_helper.write_cases(str(tmp_path / "cases.txt"))
+    assert (tmp_path / "cases.txt").stat().st_size > 0
