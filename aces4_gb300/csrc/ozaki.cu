@@ -40,6 +40,7 @@
 #include <cudaTypedefs.h>
 
 #include <algorithm>
+#include <atomic>
 #include <type_traits>
 
 #include "a4g_internal.h"
@@ -1258,14 +1259,24 @@ int set_smem_attr() {
   return A4G_OK;
 }
 
+// Function attributes are set once per device (they belong to the device's
+// instance of the kernel).
+bool first_on_device(std::atomic<unsigned long long>& mask) {
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return true;
+  const unsigned long long bit = 1ull << dev;
+  return (mask.fetch_or(bit) & bit) == 0;
+}
+
 int oz_prepare() {
-  static bool done = false;
-  if (!done) {
+  static std::atomic<unsigned long long> done{0};
+  if (first_on_device(done)) {
     int rc;
     if ((rc = set_smem_attr<false, 128>()) || (rc = set_smem_attr<true, 128>()) ||
-        (rc = set_smem_attr<false, 256>()) || (rc = set_smem_attr<true, 256>()))
+        (rc = set_smem_attr<false, 256>()) || (rc = set_smem_attr<true, 256>())) {
+      done.store(0);
       return rc;
-    done = true;
+    }
   }
   return A4G_OK;
 }
@@ -1337,12 +1348,10 @@ int oz_launch_recombine(const OzTile* tiles, int ntiles, int tile_rows, int tile
     switch (slices) {
 #define A4G_RECOMBINE_BULK(SL)                                                                                   \
   case SL: {                                                                                                     \
-    static bool attr = false;                                                                                    \
-    if (!attr) {                                                                                                 \
+    static std::atomic<unsigned long long> attr{0};                                                             \
+    if (first_on_device(attr))                                                                                   \
       A4G_CUDA(cudaFuncSetAttribute(oz_recombine_bulk_kernel<SL>, cudaFuncAttributeMaxDynamicSharedMemorySize,  \
                                     int(sizeof(RecSmem<SL>))));                                                 \
-      attr = true;                                                                                               \
-    }                                                                                                            \
     oz_recombine_bulk_kernel<SL><<<grid, 1024, sizeof(RecSmem<SL>), s>>>(tiles, dblocks, plans, pa, pb, ws, lr, lc, \
                                                                        ntiles, mode, err);                       \
     break;                                                                                                       \
