@@ -10,6 +10,7 @@
 #include <vector>
 
 #include "a4g_internal.h"
+#include "ozaki.h"
 
 using namespace a4g;
 
@@ -622,6 +623,15 @@ int a4g_update_t2(const int* iv, const int* ext, const double* t2new, const doub
   if (!scratch) return fail(A4G_ERR_NOMEM, "reduction scratch");
   return launch_update_t2(off, ext, t2new, t2new_pair, t2old, t2old_pair, diis_err, t2old_next, rank1, ext1[0],
                           e_or_fock, norm2, scratch, dot_scratch_len(), pick(stream));
+}
+
+int a4g_selftest_wait_timeout(int limit_ms, int* waited_ms, void* stream) {
+  int rc = ensure_init();
+  if (rc) return rc;
+  if (limit_ms < 1 || limit_ms > 5000 || !waited_ms) return fail(A4G_ERR_ARG, "wait self-test: limit 1..5000 ms");
+  cudaStream_t s = pick(stream);
+  if ((rc = oz_wait_timeout_selftest(limit_ms, waited_ms, s))) return rc;
+  return check_device_flag(s);  // A4G_ERR_TIMEOUT when the wait gave up, as intended
 }
 
 int a4g_energy_contract(int rank0, const int* iv, const int* ext0, const double* data0, const int* den_order,

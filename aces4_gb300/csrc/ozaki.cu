@@ -1165,6 +1165,25 @@ __global__ void __launch_bounds__(1024, 1) oz_recombine_bulk_kernel(const OzTile
   }
 }
 
+// Self-test of the bounded-wait path every pipeline wait uses: one thread
+// waits on an mbarrier that nothing arrives at, gives up after limit_ns, and
+// reports through the device error flag exactly as a stalled pipeline would.
+__global__ void wait_timeout_selftest_kernel(unsigned long long limit_ns, int* err, int* waited_ms) {
+  __shared__ uint64_t bar;
+  if (threadIdx.x != 0) return;
+  mbar_init(&bar, 1);
+  fence_mbar_init();
+  const unsigned long long t0 = now_ns();
+  bool done = mbar_try_wait(&bar, 0);
+#pragma unroll 1
+  for (uint32_t it = 1; !done; ++it) {
+    done = mbar_try_wait(&bar, 0);
+    if (!done && (it & 255) == 0 && now_ns() - t0 > limit_ns) break;
+  }
+  *waited_ms = int((now_ns() - t0) / 1000000ull);
+  if (!done) atomicExch(err, 6);
+}
+
 using EncodeTiled = PFN_cuTensorMapEncodeTiled_v12000;
 EncodeTiled get_encoder() {
   static EncodeTiled fn = nullptr;
@@ -1374,6 +1393,16 @@ int oz_launch_recombine(const OzTile* tiles, int ntiles, int tile_rows, int tile
     default: return fail(A4G_ERR_ARG, "recombine: slices must be 1..7");
   }
   A4G_CUDA(cudaGetLastError());
+  return A4G_OK;
+}
+
+int oz_wait_timeout_selftest(int limit_ms, int* waited_ms, cudaStream_t s) {
+  int* d_ms = nullptr;
+  A4G_CUDA(cudaMallocAsync(reinterpret_cast<void**>(&d_ms), sizeof(int), s));
+  wait_timeout_selftest_kernel<<<1, 32, 0, s>>>((unsigned long long)limit_ms * 1000000ull, ctx()->d_error_flag, d_ms);
+  A4G_CUDA(cudaGetLastError());
+  A4G_CUDA(cudaMemcpyAsync(waited_ms, d_ms, sizeof(int), cudaMemcpyDeviceToHost, s));
+  A4G_CUDA(cudaFreeAsync(d_ms, s));
   return A4G_OK;
 }
 

@@ -190,6 +190,14 @@ int a4g_insert(int rank, double* tens, const int* tens_ext, const double* slice,
 int a4g_energy_denominator(int rank0, const int* index_values0, const int* ext0, double* data0,
                            int rank1, const int* ext1, const double* e_or_fock, int nsegs,
                            const int* seg_sizes, void* stream);
+/* Self-test of the device-side bounded waits (no reference counterpart):
+ * one thread waits on an mbarrier that nothing arrives at, gives up after
+ * limit_ms (1..5000), records the device error flag the pipelines use and
+ * returns.  Expected result: A4G_ERR_TIMEOUT, *waited_ms >= limit_ms, and the
+ * CUDA context still usable.  Every pipeline wait (TMA stages, MMA
+ * accumulators, bulk copies) takes the same path with a 20 s limit. */
+int a4g_selftest_wait_timeout(int limit_ms, int* waited_ms, void* stream);
+
 /* Amplitude update of one block (a,i,b,j): procedure updatet2 of
  * src/sialx/qm/cc/rlccd_rhf.sialx:557-600, both of its pardo passes fused
  * into one read of the inputs:
