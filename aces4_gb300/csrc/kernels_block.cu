@@ -147,78 +147,137 @@ void make_perm(int rank, const int* ext, const int* o2n, PermParams* p) {
     }
 }
 
-// Input dim 0 is also output dim 0: copy runs of dim 0, offsets per run.
-__global__ void __launch_bounds__(kThreads) permute_direct_kernel(PermParams p,
-                                                                  const double* __restrict__ in,
-                                                                  double* __restrict__ out,
-                                                                  int64_t total) {
-  const int64_t stride = int64_t(gridDim.x) * blockDim.x;
-  for (int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < total; i += stride) {
-    int64_t rem = i, o = 0;
-    for (int q = 0; q < p.rank; ++q) {
+// Element op of the permute family: OP 0 out = r (permute), 1 out = l + r,
+// 2 out = l - r (block add/subtract with a permuted right operand).
+template <int OP>
+__device__ __forceinline__ double perm_op(const double* l, int64_t o, double rv) {
+  if constexpr (OP == 0) return rv;
+  else if constexpr (OP == 1) return __dadd_rn(l[o], rv);
+  else return __dsub_rn(l[o], rv);
+}
+
+// Input dim 0 is also output dim 0: runs of dim 0 are contiguous on both
+// sides; a block takes several runs and decodes each run's output offset once.
+template <int OP>
+__global__ void __launch_bounds__(kThreads) perm_direct_kernel(PermParams p, const double* __restrict__ in,
+                                                               double* out, const double* l, int64_t nruns,
+                                                               int runs_per_block) {
+  const int E0 = p.ext[0];
+  const int64_t r0 = int64_t(blockIdx.x) * runs_per_block;
+  const int64_t r1 = r0 + runs_per_block < nruns ? r0 + runs_per_block : nruns;
+  for (int64_t run = r0; run < r1; ++run) {
+    int64_t rem = run, base_out = 0;
+    for (int q = 1; q < p.rank; ++q) {
       const int64_t x = rem % p.ext[q];
       rem /= p.ext[q];
-      o += x * p.sout[q];
+      base_out += x * p.sout[q];
     }
-    out[o] = __ldg(&in[i]);
+    const int64_t base_in = run * E0;
+    for (int e = threadIdx.x; e < E0; e += blockDim.x)
+      out[base_out + e] = perm_op<OP>(l, base_out + e, __ldg(&in[base_in + e]));
   }
 }
 
 // Shared-memory tiled transpose between input dim a (contiguous reads) and
-// input dim b (contiguous writes); the remaining dims index the grid.
+// input dim b (contiguous writes); the remaining dims index the grid, several
+// of them per block (a block moves 16 KB per slice, so one slice per block
+// would be bound by block scheduling, not by HBM).
 constexpr int kTile = 32;
-__global__ void __launch_bounds__(kTile * 8) permute_tiled_kernel(PermParams p,
-                                                                  const double* __restrict__ in,
-                                                                  double* __restrict__ out) {
-  __shared__ double tile[kTile][kTile + 1];
+template <int OP>
+__global__ void __launch_bounds__(kTile * 8) perm_tiled_kernel(PermParams p, const double* __restrict__ in,
+                                                               double* out, const double* l,
+                                                               int rest_per_block) {
+  __shared__ double tile[2][kTile][kTile + 1];
   const int Ea = p.ext[p.a_dim], Eb = p.ext[p.b_dim];
   const int ta = (Ea + kTile - 1) / kTile, tb = (Eb + kTile - 1) / kTile;
-  int64_t bid = blockIdx.x;
-  const int ia = int(bid % ta);
-  bid /= ta;
-  const int ib = int(bid % tb);
-  int64_t rest = bid / tb;
-  int64_t base_in = 0, base_out = 0;
-  for (int q = 0; q < p.n_rest; ++q) {
-    const int d = p.rest_dims[q];
-    const int64_t x = rest % p.ext[d];
-    rest /= p.ext[d];
-    base_in += x * p.sin[d];
-    base_out += x * p.sout[d];
-  }
+  const int64_t tiles = int64_t(ta) * tb;
+  const int64_t t = blockIdx.x % tiles;
+  const int ia = int(t % ta), ib = int(t / ta);
+  const int64_t rest0 = (blockIdx.x / tiles) * rest_per_block;
+  const int64_t rest1 = rest0 + rest_per_block < p.n_rest_total ? rest0 + rest_per_block : p.n_rest_total;
   const int tx = threadIdx.x, ty = threadIdx.y;
   const int a0 = ia * kTile, b0 = ib * kTile;
-  for (int r = ty; r < kTile; r += 8) {
-    const int a = a0 + tx, b = b0 + r;
-    if (a < Ea && b < Eb) tile[r][tx] = __ldg(&in[base_in + a + int64_t(b) * p.sin[p.b_dim]]);
-  }
-  __syncthreads();
-  for (int r = ty; r < kTile; r += 8) {
-    const int b = b0 + tx, a = a0 + r;
-    if (a < Ea && b < Eb) out[base_out + b + int64_t(a) * p.sout[p.a_dim]] = tile[tx][r];
+  const int64_t sb_in = p.sin[p.b_dim], sa_out = p.sout[p.a_dim];
+  // two slices per iteration: eight loads in flight per thread before the
+  // first shared-memory write
+  for (int64_t rest = rest0; rest < rest1; rest += 2) {
+    int64_t bin[2], bout[2];
+    bool have[2];
+#pragma unroll
+    for (int u = 0; u < 2; ++u) {
+      have[u] = rest + u < rest1;
+      int64_t rem = rest + u, bi = 0, bo = 0;
+      for (int q = 0; q < p.n_rest; ++q) {
+        const int d = p.rest_dims[q];
+        const int64_t x = rem % p.ext[d];
+        rem /= p.ext[d];
+        bi += x * p.sin[d];
+        bo += x * p.sout[d];
+      }
+      bin[u] = bi;
+      bout[u] = bo;
+    }
+    double v[2][kTile / 8];
+    double lv[2][kTile / 8];  // add/subtract: the left operand at this thread's store positions
+#pragma unroll
+    for (int u = 0; u < 2; ++u)
+#pragma unroll
+      for (int k = 0; k < kTile / 8; ++k) {
+        const int a = a0 + tx, b = b0 + ty + 8 * k;
+        v[u][k] = (have[u] && a < Ea && b < Eb) ? __ldg(&in[bin[u] + a + int64_t(b) * sb_in]) : 0.0;
+        if constexpr (OP != 0) {
+          const int bs = b0 + tx, as = a0 + ty + 8 * k;
+          lv[u][k] = (have[u] && as < Ea && bs < Eb) ? l[bout[u] + bs + int64_t(as) * sa_out] : 0.0;
+        }
+      }
+    __syncthreads();  // the previous iteration's stores have read the tiles
+#pragma unroll
+    for (int u = 0; u < 2; ++u)
+#pragma unroll
+      for (int k = 0; k < kTile / 8; ++k) tile[u][ty + 8 * k][tx] = v[u][k];
+    __syncthreads();
+#pragma unroll
+    for (int u = 0; u < 2; ++u) {
+      if (!have[u]) continue;
+#pragma unroll
+      for (int k = 0; k < kTile / 8; ++k) {
+        const int b = b0 + tx, a = a0 + ty + 8 * k;
+        if (a < Ea && b < Eb) {
+          const int64_t o = bout[u] + b + int64_t(a) * sa_out;
+          const double rv = tile[u][tx][ty + 8 * k];
+          if constexpr (OP == 0) out[o] = rv;
+          else out[o] = OP == 1 ? __dadd_rn(lv[u][k], rv) : __dsub_rn(lv[u][k], rv);
+        }
+      }
+    }
   }
 }
 
-// d = l +/- permute(r) with r's dims mapped by o2n; one pass, no temp block.
-__global__ void __launch_bounds__(kThreads) add_sub_perm_kernel(PermParams p, int subtract,
-                                                                double* d, const double* l,
-                                                                const double* __restrict__ r,
-                                                                int64_t total) {
-  // iterate in d order (output order) so d and l are streamed contiguously
-  const int64_t stride = int64_t(gridDim.x) * blockDim.x;
-  for (int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < total; i += stride) {
-    // decode i in output order: output dims sorted by sout
-    int64_t rem = i, src = 0;
-    // p.rest_dims holds the input dims sorted by output position (prepared on host)
-    for (int q = 0; q < p.rank; ++q) {
-      const int dim = p.rest_dims[q];
-      const int64_t x = rem % p.ext[dim];
-      rem /= p.ext[dim];
-      src += x * p.sin[dim];
-    }
-    const double rv = __ldg(&r[src]);
-    d[i] = subtract ? __dsub_rn(l[i], rv) : __dadd_rn(l[i], rv);
+// Launches the permute family for a described permute (make_perm) of
+// `total` elements: OP 0 permute in -> out; 1 / 2: out = l +/- permute(in).
+template <int OP>
+int launch_perm_op(const PermParams& p, const double* in, double* out, const double* l, int64_t total,
+                   cudaStream_t s) {
+  const int sms = ctx()->num_sms > 0 ? ctx()->num_sms : 152;
+  const int64_t want = int64_t(sms) * 16;  // blocks to aim for
+  if (p.rank <= 1 || p.b_dim == p.a_dim) {
+    const int E0 = p.rank >= 1 ? p.ext[0] : 1;
+    const int64_t nruns = total / E0;
+    const int threads = E0 >= kThreads ? kThreads : (E0 + 31) / 32 * 32;
+    const int rpb = int(std::max<int64_t>(1, std::min<int64_t>(64, nruns / want)));
+    const int64_t blocks = (nruns + rpb - 1) / rpb;
+    if (blocks > 0x7fffffffLL) return fail(A4G_ERR_RANGE, "permute grid too large");
+    if (blocks > 0) perm_direct_kernel<OP><<<unsigned(blocks), threads, 0, s>>>(p, in, out, l, nruns, rpb);
+  } else {
+    const int Ea = p.ext[p.a_dim], Eb = p.ext[p.b_dim];
+    const int64_t tiles = int64_t((Ea + kTile - 1) / kTile) * ((Eb + kTile - 1) / kTile);
+    const int rpb = 2 * int(std::max<int64_t>(1, std::min<int64_t>(8, p.n_rest_total * tiles / (2 * want))));
+    const int64_t blocks = tiles * ((p.n_rest_total + rpb - 1) / rpb);
+    if (blocks > 0x7fffffffLL) return fail(A4G_ERR_RANGE, "permute grid too large");
+    perm_tiled_kernel<OP><<<unsigned(blocks), dim3(kTile, 8), 0, s>>>(p, in, out, l, rpb);
   }
+  A4G_CUDA(cudaGetLastError());
+  return A4G_OK;
 }
 
 // ---------------------------------------------------------------- dot / norm
@@ -668,42 +727,38 @@ int launch_permute(int rank, const int* ext, const int* o2n_1based, const double
   }
   PermParams p;
   make_perm(rank, ext, o2n, &p);
-  if (p.rank <= 1 || p.b_dim == p.a_dim) {
-    if (p.rank <= 1) {
-      A4G_CUDA(cudaMemcpyAsync(out, in, total * sizeof(double), cudaMemcpyDeviceToDevice, s));
-      return A4G_OK;
-    }
-    permute_direct_kernel<<<grid_for(total), kThreads, 0, s>>>(p, in, out, total);
-  } else {
-    const int Ea = p.ext[p.a_dim], Eb = p.ext[p.b_dim];
-    const int64_t blocks = int64_t((Ea + kTile - 1) / kTile) * ((Eb + kTile - 1) / kTile) * p.n_rest_total;
-    if (blocks > 0x7fffffffLL) return fail(A4G_ERR_RANGE, "permute grid too large");
-    permute_tiled_kernel<<<unsigned(blocks), dim3(kTile, 8), 0, s>>>(p, in, out);
+  if (p.rank <= 1) {
+    A4G_CUDA(cudaMemcpyAsync(out, in, total * sizeof(double), cudaMemcpyDeviceToDevice, s));
+    return A4G_OK;
   }
-  A4G_CUDA(cudaGetLastError());
-  return A4G_OK;
+  return launch_perm_op<0>(p, in, out, nullptr, total, s);
 }
 
 int launch_add_sub_permuted(int subtract, int rank, const int* r_ext, const int* o2n_1based,
                             double* d, const double* l, const double* r, cudaStream_t s) {
   if (rank < 0 || rank > kMaxRank) return fail(A4G_ERR_ARG, "rank out of range");
   if (!d || !l || !r) return fail(A4G_ERR_ARG, "null block pointer");
-  PermParams p{};
-  p.rank = rank;
   int64_t total = 1;
-  int n2o[kPermMax];
+  int o2n[kPermMax];
   for (int i = 0; i < rank; ++i) {
-    p.ext[i] = r_ext[i];
-    p.sin[i] = total;
     total *= r_ext[i];
-    n2o[o2n_1based[i] - 1] = i;
+    o2n[i] = o2n_1based[i] - 1;
   }
-  for (int q = 0; q < rank; ++q) p.rest_dims[q] = n2o[q];  // input dims in output order
   if (total == 0) return A4G_OK;
-  if (rank == 0) total = 1;
-  add_sub_perm_kernel<<<grid_for(total), kThreads, 0, s>>>(p, subtract, d, l, r, total);
-  A4G_CUDA(cudaGetLastError());
-  return A4G_OK;
+  PermParams p{};
+  if (rank == 0) {
+    p.rank = 1;
+    p.ext[0] = 1;
+    p.sin[0] = p.sout[0] = 1;
+  } else {
+    make_perm(rank, r_ext, o2n, &p);
+  }
+  if (p.rank == 0) {  // every extent is 1
+    p.rank = 1;
+    p.ext[0] = 1;
+    p.sin[0] = p.sout[0] = 1;
+  }
+  return subtract ? launch_perm_op<2>(p, r, d, l, total, s) : launch_perm_op<1>(p, r, d, l, total, s);
 }
 
 int dot_scratch_len() { return kDotBlocks; }

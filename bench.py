@@ -473,6 +473,86 @@ def run_config(args, world, rank, local):
         }), flush=True)
 
 
+BLOCKOPS_METRIC = "achieved HBM GB/s of the block kernels (algorithmic bytes / CUDA-event time)"
+
+
+def run_blockops(args, world, rank, local):
+    """The HBM-bound block kernels on one 96^4 block (85 M doubles, 679 MB,
+    above L2): permute, permuted add, scale, fill, scaled add, squared norm,
+    orbital-energy denominator, fused amplitude update; GB/s from algorithmic
+    bytes per element against the measured copy bandwidth."""
+    import numpy as np
+    import torch
+
+    import aces4_gb300 as a4
+
+    torch.cuda.set_device(local)
+    a4.device.init(local)
+    st = torch.cuda.current_stream()
+    peaks, peak_kind = _peaks()
+    hbm = peaks.get("hbm_gbs", 6800.0)
+    e = 96
+    ext = [e] * 4
+    n = e ** 4
+    g = torch.Generator(device="cuda")
+    g.manual_seed(5)
+    x = torch.randn(n, dtype=torch.float64, device="cuda", generator=g)
+    y = torch.randn(n, dtype=torch.float64, device="cuda", generator=g)
+    z = torch.empty_like(x)
+    w = torch.empty_like(x)
+    w2, w3 = torch.empty_like(x), torch.empty_like(x)
+    segs = [96, 96, 96]  # one occupied segment of 96, two virtual segments of 96
+    orb = np.concatenate([np.linspace(-2.0, -0.5, 96), np.linspace(0.2, 5.0, 192)])
+    fock = torch.tensor(np.diag(orb).ravel(order="F"), device="cuda")
+    nrm = torch.zeros(1, dtype=torch.float64, device="cuda")
+    iv = [2, 1, 3, 1]  # (a, i, b, j): virtual, occupied, virtual, occupied
+    ops = [
+        ("permute (dims 3,2,1,4)", 16, lambda: a4.device.permute(ext, [3, 2, 1, 4], x, z, stream=st)),
+        ("add_sub d = l + r(permuted)", 24, lambda: a4.device.add_sub(False, [1, 2, 3, 4], [3, 2, 1, 4], ext, z, x, y,
+                                                                     stream=st)),
+        ("scale d *= f", 16, lambda: a4.device.scale(z, 1.0000001, stream=st)),
+        ("fill", 8, lambda: a4.device.fill(z, 0.5, stream=st)),
+        ("add_scaled t0 += s t1", 24, lambda: a4.device.add_scaled(z, x, 0.25, stream=st)),
+        ("energy_denominator (rank 4, in place)", 16,
+         lambda: a4.device.energy_denominator(iv, ext, z, [288, 288], fock, segs, stream=st)),
+        ("update_t2 (4 reads, 2 writes)", 48,
+         lambda: a4.device.update_t2(iv, ext, x, y, z, w, w2, w3, [288, 288], fock, segs, nrm, stream=st)),
+    ]
+    res = {}
+    for name, bpe, fn in ops:
+        for _ in range(args.warmup):
+            fn()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(st)
+        for _ in range(args.steps):
+            fn()
+        e1.record(st)
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / args.steps
+        gbs = n * bpe / (ms * 1e-3) / 1e9
+        res[name] = {"ms": ms, "bytes_per_elem": bpe, "gbs": gbs, "frac": gbs / hbm}
+    # norm2 returns to the host (a sync per call): timed on the host clock
+    for _ in range(args.warmup):
+        a4.device.norm2(x, stream=st)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        a4.device.norm2(x, stream=st)
+    ms = (time.perf_counter() - t0) / args.steps * 1e3
+    res["norm2 (to host)"] = {"ms": ms, "bytes_per_elem": 8, "gbs": n * 8 / (ms * 1e-3) / 1e9,
+                              "frac": n * 8 / (ms * 1e-3) / 1e9 / hbm}
+    if rank == 0:
+        permute = res["permute (dims 3,2,1,4)"]
+        print(json.dumps({
+            "metric": BLOCKOPS_METRIC, "value": permute["gbs"], "unit": "GB/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": permute["ms"], "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": f"one block of 96^4 doubles ({n * 8 / 1e9:.2f} GB), value = the permute's GB/s"},
+            "hbm_peak_gbs": hbm, "peak_kind": f"hbm_gbs of {peak_kind}", "kernels": res,
+        }), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -491,10 +571,11 @@ def main():
     ap.add_argument("--noseg", type=int, default=4, help="occupied segments of 16 (4: o=64)")
     ap.add_argument("--tseg", type=int, default=24, help="triples: segment size (occupied: one segment)")
     ap.add_argument("--tnv", type=int, default=10, help="triples: virtual segments")
-    ap.add_argument("--workload", default="ladder", choices=["ladder", "triples", "ladder-small", "ring", "sparse"],
+    ap.add_argument("--workload", default="ladder",
+                    choices=["ladder", "triples", "ladder-small", "ring", "sparse", "blockops"],
                     help="ladder: the o=64/v=512 ladder slab (the headline metric); triples: one triples energy "
                          "step; ladder-small / ring / sparse: one pardo step of the o=10/v=48 ladder, the "
-                         "o=40/v=300 ring, the o=48/v=400 sparse ladder")
+                         "o=40/v=300 ring, the o=48/v=400 sparse ladder; blockops: the HBM-bound block kernels")
     args = ap.parse_args()
 
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -508,6 +589,9 @@ def main():
         return
     if args.workload in ("ladder-small", "ring", "sparse"):
         run_config(args, world, rank, local)
+        return
+    if args.workload == "blockops":
+        run_blockops(args, world, rank, local)
         return
 
     import numpy as np
