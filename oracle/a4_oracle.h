@@ -4,8 +4,8 @@
  * TEST INFRASTRUCTURE ONLY.  This is a plain-C restatement of the reference
  * algorithms (tensor_dil_omp.F90, block.cpp, interpreter.cpp handlers,
  * energy_denominator_rhf.F).  Only tests/, __graft_entry__.smoke() and the
- * CPU-baseline leg of bench.py may load it, and only as the checker or as the
- * timed CPU baseline.  The product library never links or calls it.
+ * CPU-baseline leg of bench.py may load it, and only to check results against
+ * or as the timed CPU baseline.  The product library never links or calls it.
  *
  * Conventions follow the reference exactly: blocks are column-major (first
  * index fastest), extents are 32-bit ints, permutations are 1-based O2N

@@ -2,8 +2,8 @@
 
 The oracle restates the reference ACES4 block kernels in plain C
 (``oracle/a4_oracle.c``).  Tests, ``__graft_entry__.smoke()`` and the CPU
-baseline leg of ``bench.py`` load it as the checker; the product library never
-does.  Arrays are numpy float64 in column-major (Fortran) element order, passed
+baseline leg of ``bench.py`` load it to check results against (and to time the
+CPU baseline); the product library never does.  Arrays are numpy float64 in column-major (Fortran) element order, passed
 as flat buffers exactly like the reference's ``double*`` blocks.
 """
 from __future__ import annotations

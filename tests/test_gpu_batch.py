@@ -309,3 +309,47 @@ def test_batch_matrix_and_outer_product_patterns(a4, precision):
         a4.device.sync()
         want = sum(oracle.contract_blas(p, Ls[q], le, Rs[q], re, de) for q in range(pairs))
         np.testing.assert_array_equal(D.cpu().numpy(), want)
+
+
+def test_batch_edge_cases(a4):
+    """An empty step; rank-6 operands (four contracted indices); triples that
+    disagree on a destination block's extents and a rank-0 destination are
+    rejected with a status, not a fault."""
+    import torch
+
+    # empty step: creation and runs are no-ops
+    p = _ptrn(([1, 2], [1, 3], [3, 2]))
+    for prec in (0, 1):
+        b = a4.device.Batch(p, 2, 2, 2, [], precision=prec)
+        b.run()
+        b.run_graph()
+        a4.device.sync()
+        assert b.info()["pairs"] == 0
+    # rank-6 operands: D(a,b,c,d) = L(a,b,e,f,g,h) R(e,f,g,h,c,d)
+    rng = np.random.default_rng(17)
+    dl, ll, rl = [1, 2, 3, 4], [1, 2, 5, 6, 7, 8], [5, 6, 7, 8, 3, 4]
+    de, le, re = [5, 4, 3, 6], [5, 4, 3, 2, 4, 3], [3, 2, 4, 3, 3, 6]
+    ierr, p6 = oracle.get_contraction_ptrn(4, 6, 6, dl + ll + rl)
+    assert ierr == 0
+    Ls = [rng.integers(-50, 51, int(np.prod(le))).astype(np.float64) for _ in range(2)]
+    Rs = [rng.integers(-50, 51, int(np.prod(re))).astype(np.float64) for _ in range(2)]
+    want = sum(oracle.contract_blas(p6, Ls[q], le, Rs[q], re, de) for q in range(2))
+    for prec, slices in ((0, 5), (1, 2)):
+        D = torch.full((int(np.prod(de)),), float("nan"), dtype=torch.float64, device="cuda")
+        trip = [(D, torch.tensor(Ls[q], device="cuda"), torch.tensor(Rs[q], device="cuda"), de, le, re)
+                for q in range(2)]
+        b = a4.device.Batch(p6, 4, 6, 6, trip, precision=prec, slices=slices)
+        b.run()
+        a4.device.sync()
+        np.testing.assert_array_equal(D.cpu().numpy(), want)
+    # two triples on one destination with different extents
+    D = torch.zeros(64, dtype=torch.float64, device="cuda")
+    x = torch.zeros(256, dtype=torch.float64, device="cuda")
+    bad = [(D, x, x, [8, 8], [8, 8], [8, 8]), (D, x, x, [4, 16], [4, 8], [8, 16])]
+    with pytest.raises(a4.device.A4GError):
+        a4.device.Batch(p, 2, 2, 2, bad, precision=1)
+    # a scalar destination is not a batched contraction
+    ierr, p0 = oracle.get_contraction_ptrn(0, 2, 2, [1, 2, 1, 2])
+    assert ierr == 0
+    with pytest.raises(a4.device.A4GError):
+        a4.device.Batch(p0, 0, 2, 2, [(D, x, x, [], [8, 8], [8, 8])], precision=1)
