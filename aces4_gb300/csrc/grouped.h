@@ -66,7 +66,7 @@ struct OzSplitJob {
 // tables).
 enum OzLayout { kOzGeneric = 0, kOzRowsMajor = 1, kOzKMajor = 2 };
 
-// One 128x128 output tile of one destination block.
+// One output tile (the GEMM form's tile_rows x tile_cols) of one destination block.
 struct OzTile {
   int dblock;
   int m0, n0;
