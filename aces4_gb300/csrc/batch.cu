@@ -40,6 +40,9 @@ struct a4g_batch {
   GroupedF64Tile* d_f64_tiles = nullptr;
   GroupedPair* d_f64_pairs = nullptr;
   int n_f64_tiles = 0;
+  double* d_f64_ws = nullptr;           // partial tiles when tiles are spread
+  GroupedF64Reduce* d_f64_reds = nullptr;
+  int n_f64_reds = 0;
   // split precision
   OzPanel* d_pa = nullptr;
   OzPanel* d_pb = nullptr;
@@ -239,7 +242,36 @@ int build_f64(a4g_batch* b, const std::vector<DGroup>& groups, const std::vector
     const GemmPlan& h = plans[g.plan]->host;
     for (int64_t n0 = 0; n0 < h.N; n0 += TN)
       for (int64_t m0 = 0; m0 < h.M; m0 += TM)
-        tiles.push_back({g.d, int(m0), int(n0), begin, end, g.plan, 0});
+        tiles.push_back({g.d, int(m0), int(n0), begin, end, g.plan, -1});
+  }
+  // Few tiles with many pairs each (small blocks, long sums): spread each
+  // tile's pairs over G CTAs writing partial tiles, summed in order after.
+  const int sms = ctx()->num_sms > 0 ? ctx()->num_sms : 152;
+  const int64_t want = 4LL * sms;
+  int min_pairs = 1 << 30;
+  for (const auto& t : tiles) min_pairs = std::min(min_pairs, t.pair_end - t.pair_begin);
+  const int G = tiles.empty() ? 1
+                              : int(std::max<int64_t>(1, std::min<int64_t>({16, int64_t(min_pairs),
+                                                                            (want + int64_t(tiles.size()) - 1) /
+                                                                                int64_t(tiles.size())})));
+  if (G > 1) {
+    std::vector<GroupedF64Tile> spread;
+    std::vector<GroupedF64Reduce> reds;
+    int slot = 0;
+    for (const auto& t : tiles) {
+      const int np = t.pair_end - t.pair_begin;
+      reds.push_back({t.d, t.m0, t.n0, t.dplan, slot, G, 0});
+      for (int q = 0; q < G; ++q)
+        spread.push_back({t.d, t.m0, t.n0, t.pair_begin + np * q / G, t.pair_begin + np * (q + 1) / G, t.dplan,
+                          slot++});
+    }
+    void* ws = nullptr;
+    int rc = device_alloc(b, size_t(slot) * TM * TN * sizeof(double), &ws, false);
+    if (rc) return rc;
+    b->d_f64_ws = static_cast<double*>(ws);
+    if ((rc = upload(b, reds, &b->d_f64_reds))) return rc;
+    b->n_f64_reds = int(reds.size());
+    tiles.swap(spread);
   }
   if (tiles.size() > 0x7fffffffu) return fail(A4G_ERR_RANGE, "too many tiles");
   b->n_f64_tiles = int(tiles.size());
@@ -613,7 +645,8 @@ int run(a4g_batch* b, cudaStream_t s, const cudaEvent_t* ev = nullptr) {
   if ((rc = mark(1))) return rc;
   if (b->precision == A4G_PREC_FP64) {
     if ((rc = mark(2)) || (rc = mark(3))) return rc;
-    rc = launch_grouped_f64(b->d_f64_tiles, b->n_f64_tiles, b->d_f64_pairs, b->d_plans, b->store_mode(), s);
+    rc = launch_grouped_f64(b->d_f64_tiles, b->n_f64_tiles, b->d_f64_pairs, b->d_plans, b->store_mode(),
+                            b->d_f64_ws, b->d_f64_reds, b->n_f64_reds, s);
     if (rc) return rc;
     if ((rc = mark(4)) || (rc = mark(5))) return rc;
     return A4G_OK;
@@ -814,6 +847,7 @@ int a4g_batch_launches(const a4g_batch* b, int* kernels_per_run, int* gemm_parts
   int parts = 1;
   if (b->precision == A4G_PREC_FP64) {
     k += b->n_f64_tiles > 0 ? 1 : 0;
+    k += b->n_f64_reds > 0 ? 1 : 0;
   } else if (b->forms[b->form].n_tiles > 0) {
     parts = b->parts;
     k += 2 * int(b->jobsets.size()) + parts + 1;  // exponents + splits, GEMM parts, recombine

@@ -26,10 +26,20 @@ struct GroupedF64Tile {
   int m0, n0;
   int pair_begin, pair_end;  // pairs summed into this tile
   int dplan;                 // plan giving D's tables and M, N
+  int slot;                  // -1: store into D; else the partial-tile slot in the workspace
+};
+// Destination tiles whose pairs were spread over several CTAs: the partial
+// tiles in slots [slot0, slot0 + nparts) are summed in order and stored.
+struct GroupedF64Reduce {
+  double* d;
+  int m0, n0;
+  int dplan;
+  int slot0, nparts;
   int pad;
 };
 int launch_grouped_f64(const GroupedF64Tile* tiles, int ntiles, const GroupedPair* pairs,
-                       const PlanRef* plans, int mode, cudaStream_t s);  // mode: bit 0 accumulate, bit 1 negate
+                       const PlanRef* plans, int mode, double* ws, const GroupedF64Reduce* reds, int nreds,
+                       cudaStream_t s);  // mode: bit 0 accumulate, bit 1 negate
 int grouped_f64_tile_m();
 int grouped_f64_tile_n();
 

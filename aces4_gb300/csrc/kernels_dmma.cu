@@ -153,11 +153,13 @@ __global__ void __launch_bounds__(kThreadsF64) contract_f64_kernel(
   write_tile(acc, D, offDm, offDn, M, N, m0, n0, mode);
 }
 
-// One CTA per (destination block, 64x64 tile); the block's pairs are summed.
+// One CTA per (destination block, 64x64 tile, share of its pairs); the pairs
+// are summed and the tile stored into D, or into a workspace slot when the
+// tile's pairs are spread over several CTAs (few tiles, many pairs).
 __global__ void __launch_bounds__(kThreadsF64) grouped_f64_kernel(const GroupedF64Tile* __restrict__ tiles,
                                                                   const GroupedPair* __restrict__ pairs,
                                                                   const PlanRef* __restrict__ plans,
-                                                                  int mode) {
+                                                                  int mode, double* __restrict__ ws) {
   __shared__ __align__(16) Smem sm;
   const GroupedF64Tile tl = tiles[blockIdx.x];
   double acc[4][4][2];
@@ -171,8 +173,39 @@ __global__ void __launch_bounds__(kThreadsF64) grouped_f64_kernel(const GroupedF
     accumulate_pair(sm, acc, pr.l, pr.r, pl.offLm, pl.offLk, pl.offRk, pl.offRn, pl.M, pl.N, pl.K,
                     tl.m0, tl.n0, pl.a_kfast, pl.b_kfast);
   }
+  if (tl.slot >= 0) {  // partial tile, column-major 64x64 in its slot
+    double* w = ws + size_t(tl.slot) * BM * BN;
+    const int t = threadIdx.x, warp = t >> 5, lane = t & 31;
+    const int g = lane >> 2, tig = lane & 3;
+    const int wm = (warp & 1) * 32, wn = (warp >> 1) * 32;
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+#pragma unroll
+      for (int j = 0; j < 4; ++j)
+#pragma unroll
+        for (int h = 0; h < 2; ++h) w[(wn + j * 8 + 2 * tig + h) * BM + wm + i * 8 + g] = acc[i][j][h];
+    return;
+  }
   const PlanRef dp = plans[tl.dplan];
   write_tile(acc, tl.d, dp.offDm, dp.offDn, dp.M, dp.N, tl.m0, tl.n0, mode);
+}
+
+// Sums a spread tile's partials in slot order (deterministic) and stores it.
+__global__ void __launch_bounds__(256) grouped_f64_reduce_kernel(const GroupedF64Reduce* __restrict__ reds,
+                                                                 const PlanRef* __restrict__ plans,
+                                                                 const double* __restrict__ ws, int mode) {
+  const GroupedF64Reduce rd = reds[blockIdx.x];
+  const PlanRef dp = plans[rd.dplan];
+  for (int e = threadIdx.x; e < BM * BN; e += blockDim.x) {
+    const int ml = e % BM, nl = e / BM;
+    const int m = rd.m0 + ml, n = rd.n0 + nl;
+    if (m >= dp.M || n >= dp.N) continue;
+    double v = 0.0;
+    for (int q = 0; q < rd.nparts; ++q) v += ws[size_t(rd.slot0 + q) * BM * BN + e];
+    if (mode & 2) v = -v;
+    double* p = rd.d + dp.offDm[m] + dp.offDn[n];
+    *p = (mode & 1) ? *p + v : v;
+  }
 }
 
 }  // namespace
@@ -194,9 +227,11 @@ int launch_contract_f64(const DevPlan* p, const double* L, const double* R, doub
 }
 
 int launch_grouped_f64(const GroupedF64Tile* tiles, int ntiles, const GroupedPair* pairs,
-                       const PlanRef* plans, int mode, cudaStream_t s) {
+                       const PlanRef* plans, int mode, double* ws, const GroupedF64Reduce* reds, int nreds,
+                       cudaStream_t s) {
   if (ntiles <= 0) return A4G_OK;
-  grouped_f64_kernel<<<ntiles, kThreadsF64, 0, s>>>(tiles, pairs, plans, mode);
+  grouped_f64_kernel<<<ntiles, kThreadsF64, 0, s>>>(tiles, pairs, plans, mode, ws);
+  if (nreds > 0) grouped_f64_reduce_kernel<<<nreds, 256, 0, s>>>(reds, plans, ws, mode);
   A4G_CUDA(cudaGetLastError());
   return A4G_OK;
 }
