@@ -69,6 +69,7 @@ SIGNATURES = {
     "a4g_insert": (ctypes.c_int, None),
     "a4g_energy_denominator": (ctypes.c_int, None),
     "a4g_energy_contract": (ctypes.c_int, None),
+    "a4g_batch_splits": (ctypes.c_int, None),
     "a4g_selftest_wait_timeout": (ctypes.c_int, None),
     "a4g_clear_error": (None, []),
     "a4g_update_t2": (ctypes.c_int, None),

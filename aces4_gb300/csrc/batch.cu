@@ -79,6 +79,9 @@ struct a4g_batch {
   };
   GemmForm forms[kForms];
   int form = 0;  // the form run() uses (chosen by the autotuner or the caller)
+  // split-count tuning of the chosen form: candidates and their scores (ms)
+  int split_candidates[2] = {0, 0};
+  float split_cost_ms[2] = {-1.f, -1.f};
   // Split/GEMM pipeline of the chosen form: the GEMM runs as `parts` launches
   // over consecutive split-K ranges; the right-operand split jobs that only
   // later parts read run on `side` while earlier parts multiply.
@@ -129,6 +132,16 @@ int device_alloc(a4g_batch* b, size_t bytes, void** out, bool zero) {
   if (zero) A4G_CUDA(cudaMemset(p, 0, bytes));
   *out = p;
   return A4G_OK;
+}
+
+// Frees one allocation made by upload/device_alloc before the batch ends.
+void release(a4g_batch* b, void* p, size_t bytes) {
+  if (!p) return;
+  auto it = std::find(b->allocs.begin(), b->allocs.end(), p);
+  if (it == b->allocs.end()) return;
+  b->allocs.erase(it);
+  b->device_bytes -= int64_t(bytes);
+  cudaFree(p);
 }
 
 PlanRef ref_of(const DevPlan* p) {
@@ -447,6 +460,26 @@ int build_ozaki(a4g_batch* b, const std::vector<DGroup>& groups, const std::vect
   int pairs = 0;
   if ((rc = oz_max_pairs(&pairs))) return rc;
   size_t ws_elems = 0;
+  // Work units of one form: (level, split, tile), level-major, each split a
+  // 1/nsplit share of the tile's concatenated k blocks.
+  auto make_units = [&](const std::vector<OzTile>& tiles, int nsplit) {
+    std::vector<OzUnit> units;
+    for (int lv = 0; lv < S; ++lv)
+      for (int sp = 0; sp < nsplit; ++sp)
+        for (int ti = 0; ti < int(tiles.size()); ++ti) {
+          const OzTile& t = tiles[ti];
+          OzUnit u{};
+          u.tile = ti, u.level = lv, u.split = sp;
+          u.kb_begin = int(int64_t(t.kb_total) * sp / nsplit);
+          u.kb_end = int(int64_t(t.kb_total) * (sp + 1) / nsplit);
+          int acc = 0, q = t.trip_begin;
+          while (q < t.trip_end && acc + trips[q].nkb <= u.kb_begin) acc += trips[q].nkb, ++q;
+          u.trip_first = q;
+          u.kb_in_trip = u.kb_begin - acc;
+          units.push_back(u);
+        }
+    return units;
+  };
   std::vector<std::vector<OzTile>> form_tiles(a4g_batch::kForms);
   std::vector<std::vector<OzUnit>> form_units(a4g_batch::kForms);
   for (int f = 0; f < a4g_batch::kForms; ++f) {
@@ -485,20 +518,7 @@ int build_ozaki(a4g_batch* b, const std::vector<DGroup>& groups, const std::vect
     }
     gf.nsplit = nsplit;
     std::vector<OzUnit>& units = form_units[f];
-    for (int lv = 0; lv < S; ++lv)
-      for (int sp = 0; sp < nsplit; ++sp)
-        for (int ti = 0; ti < gf.n_tiles; ++ti) {
-          const OzTile& t = tiles[ti];
-          OzUnit u{};
-          u.tile = ti, u.level = lv, u.split = sp;
-          u.kb_begin = int(int64_t(t.kb_total) * sp / nsplit);
-          u.kb_end = int(int64_t(t.kb_total) * (sp + 1) / nsplit);
-          int acc = 0, q = t.trip_begin;
-          while (q < t.trip_end && acc + trips[q].nkb <= u.kb_begin) acc += trips[q].nkb, ++q;
-          u.trip_first = q;
-          u.kb_in_trip = u.kb_begin - acc;
-          units.push_back(u);
-        }
+    units = make_units(tiles, nsplit);
     ws_elems = std::max(ws_elems, size_t(gf.n_tiles) * S * nsplit * gf.tile_rows * gf.tile_cols);
     OzUnit* d_units = nullptr;
     if ((rc = upload(b, tiles, &gf.d_tiles)) || (rc = upload(b, units, &d_units))) return rc;
@@ -548,6 +568,69 @@ int build_ozaki(a4g_batch* b, const std::vector<DGroup>& groups, const std::vect
     cudaEventDestroy(e1);
     if (rc) return rc;
     if ((rc = check_device_flag(s))) return rc;
+  }
+  if (!b->variant) {
+    // split-count tuning of the chosen form: the balance-driven count against
+    // its double (shorter k windows per level), scored as the GEMM's measured
+    // time plus the recombine's reading of the int32 workspace at the copy
+    // rate (the recombine writes the caller's blocks, so it is not run here)
+    a4g_batch::GemmForm& gf = b->forms[b->form];
+    const std::vector<OzTile>& tiles = form_tiles[b->form];
+    int min_kb = 1 << 30;
+    for (const OzTile& t : tiles) min_kb = std::min(min_kb, t.kb_total);
+    const int ns1 = gf.nsplit, ns2 = 2 * ns1;
+    const double tile_bytes = double(gf.tile_rows) * gf.tile_cols * sizeof(int);
+    const double ws1 = double(gf.n_tiles) * S * ns1 * tile_bytes, ws2 = 2.0 * ws1;
+    const double read_ms_per_byte = 1.0 / 6.5e9;  // ~ the measured copy rate, bytes per ms
+    b->split_candidates[0] = ns1;
+    b->split_cost_ms[0] = gf.tuned_ms + float(ws1 * read_ms_per_byte);
+    if (gf.n_tiles > 0 && ns2 <= 64 && min_kb / ns2 >= 16 && ws2 <= 6.0 * (1u << 30)) {
+      std::vector<OzUnit> units2 = make_units(tiles, ns2);
+      OzUnit* d_units2 = nullptr;
+      void* ws2p = nullptr;
+      if ((rc = upload(b, units2, &d_units2)) || (rc = device_alloc(b, size_t(ws2), &ws2p, false))) return rc;
+      OzGemmArgs a2 = gf.args;
+      a2.units = d_units2;
+      a2.n_units = int(units2.size());
+      a2.nsplit = ns2;
+      a2.ws = static_cast<int*>(ws2p);
+      const int grid2 = gf.pair ? 2 * std::min(a2.n_units, pairs) : std::min(a2.n_units, ctx()->num_sms);
+      cudaStream_t s = ctx()->stream;
+      cudaEvent_t e0, e1;
+      A4G_CUDA(cudaEventCreate(&e0));
+      A4G_CUDA(cudaEventCreate(&e1));
+      float ms2 = 0.f;
+      rc = oz_launch_gemm(a2, grid2, gf.pair, gf.tile_cols, s);
+      if (!rc) A4G_CUDA(cudaEventRecord(e0, s));
+      if (!rc) rc = oz_launch_gemm(a2, grid2, gf.pair, gf.tile_cols, s);
+      if (!rc) {
+        A4G_CUDA(cudaEventRecord(e1, s));
+        A4G_CUDA(cudaEventSynchronize(e1));
+        A4G_CUDA(cudaEventElapsedTime(&ms2, e0, e1));
+      }
+      cudaEventDestroy(e0);
+      cudaEventDestroy(e1);
+      if (rc) return rc;
+      if ((rc = check_device_flag(s))) return rc;
+      b->split_candidates[1] = ns2;
+      b->split_cost_ms[1] = ms2 + float(ws2 * read_ms_per_byte);
+      if (b->split_cost_ms[1] < b->split_cost_ms[0]) {
+        // the other forms are not run any more: their units and the shared
+        // workspace go
+        for (int f = 0; f < a4g_batch::kForms; ++f)
+          if (b->forms[f].built)
+            release(b, const_cast<OzUnit*>(b->forms[f].args.units), form_units[f].size() * sizeof(OzUnit)), b->forms[f].args.units = nullptr;
+        release(b, b->d_ws, ws_elems * sizeof(int));
+        gf.args = a2;
+        gf.nsplit = ns2;
+        gf.grid = grid2;
+        b->d_ws = a2.ws;
+        form_units[b->form].swap(units2);
+      } else {
+        release(b, d_units2, units2.size() * sizeof(OzUnit));
+        release(b, ws2p, size_t(ws2));
+      }
+    }
   }
   // Pipeline of the chosen form (when the caller asks for one): GEMM parts
   // over consecutive split-K ranges; each k-major right-operand split job
@@ -854,6 +937,16 @@ int a4g_batch_launches(const a4g_batch* b, int* kernels_per_run, int* gemm_parts
   }
   if (kernels_per_run) *kernels_per_run = k;
   if (gemm_parts) *gemm_parts = parts;
+  return A4G_OK;
+}
+
+int a4g_batch_splits(const a4g_batch* b, int* nsplit, int* candidates, float* cost_ms, int n) {
+  if (!b) return fail(A4G_ERR_ARG, "null batch");
+  if (nsplit) *nsplit = b->precision == A4G_PREC_FP64 ? 0 : b->forms[b->form].nsplit;
+  for (int i = 0; i < n; ++i) {
+    if (candidates) candidates[i] = i < 2 ? b->split_candidates[i] : 0;
+    if (cost_ms) cost_ms[i] = i < 2 ? b->split_cost_ms[i] : -1.f;
+  }
   return A4G_OK;
 }
 

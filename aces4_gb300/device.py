@@ -242,6 +242,14 @@ class Batch:
                "a4g_batch_info")
         return {"pairs": pairs.value, "flops": flops.value, "device_bytes": ws.value}
 
+    def splits(self):
+        """Split-K count in use and the autotuner's {count: score ms}."""
+        ns = ctypes.c_int(0)
+        cand = (ctypes.c_int * 2)()
+        cost = (ctypes.c_float * 2)()
+        _check(lib().a4g_batch_splits(self._h, ctypes.byref(ns), cand, cost, 2), "a4g_batch_splits")
+        return {"nsplit": ns.value, "tuned_ms": {int(cand[i]): float(cost[i]) for i in range(2) if cand[i] > 0}}
+
     def launches(self):
         """Library kernels per run and the GEMM launches among them."""
         k, p = ctypes.c_int(0), ctypes.c_int(0)

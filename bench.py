@@ -790,7 +790,8 @@ def main():
             "rel_err_max_block_vs_fp64_gpu": max(blk_err) if blk_err else None,
             "rel_err_block_vs_cpu_oracle": err_oracle,
             "phases_ms_per_step": {k: phases[k] / runs for k in ("exponents", "split", "gemm", "recombine")},
-            "gemm_form": {"chosen": form["name"], "autotune_ms": form["tuned_ms"]},
+            "gemm_form": {"chosen": form["name"], "autotune_ms": form["tuned_ms"],
+                          "split_k": split.splits()},
             "hbm_phases": {
                 "exponents_gbs": exp_bytes / (phases["exponents"] / runs * 1e-3) / 1e9,
                 # with GEMM parts, "split" is only the exposed share (the rest runs beside the GEMM)

@@ -292,6 +292,11 @@ int a4g_batch_run_timed(a4g_batch* b, void* stream);
 int a4g_batch_timings(a4g_batch* b, float* phase_ms, int nphase, int* runs);
 /* Number of block pairs executed (zero blocks skipped) and FP64 flops. */
 int a4g_batch_info(const a4g_batch* b, int64_t* pairs, double* flops, int64_t* workspace_bytes);
+/* Split-K count of the tensor-core GEMM in use (0 for FP64 batches) and the
+ * autotuner's candidates with their scores in ms (GEMM time measured at
+ * creation + the recombine's workspace read at the copy rate; 0 / -1 when a
+ * candidate was not tried). */
+int a4g_batch_splits(const a4g_batch* b, int* nsplit, int* candidates, float* cost_ms, int n);
 /* Library kernels one run launches, and the number of tensor-core GEMM
  * launches among them (more than one when the right operand's split runs
  * beside the GEMM on a second stream). */

@@ -162,6 +162,21 @@ def test_split_long_k_integer_exact(a4, variant):
         np.testing.assert_array_equal(R.block(k).cpu().numpy(), want)
 
 
+def test_split_count_autotune_keeps_results_exact(a4):
+    # the autotuner scores the balance-driven split-K count against its
+    # double; whichever it keeps, integer data must come back exact
+    R, V, T, trip, labels = _make(a4, "ladder", [48] * 4, [8], 0.0, 4, integer=True)
+    b = _run(a4, R, trip, labels, a4.device.PREC_OZAKI_BF16, slices=2)
+    sp = b.splits()
+    assert sp["nsplit"] in sp["tuned_ms"], sp
+    assert all(v > 0 for v in sp["tuned_ms"].values()), sp
+    ref = _reference(R, trip, labels)
+    for k, want in ref.items():
+        np.testing.assert_array_equal(R.block(k).cpu().numpy(), want)
+    f64 = _run(a4, R, trip, labels, a4.device.PREC_FP64)
+    assert f64.splits()["nsplit"] == 0
+
+
 @pytest.mark.parametrize("slices,tol", [(3, 1e-5), (4, 1e-7), (5, TOL_SPLIT), (6, 1e-12), (7, 1e-13)])
 def test_split_ladder_outliers(a4, slices, tol):
     # config-4 distributions (V ~ U[-1,1]/v, T ~ N(0,1e-2) with 1% x1e3) on a
