@@ -9,7 +9,9 @@
 // is one call: pairs that feed the same destination block are summed in the
 // kernel, zero blocks (NULL operand) are never touched.
 #include <algorithm>
+#include <cmath>
 #include <cstring>
+#include <deque>
 #include <map>
 #include <set>
 #include <memory>
@@ -63,10 +65,13 @@ struct a4g_batch {
   std::vector<JobSet> jobsets;
   OzDBlock* d_dblocks = nullptr;
   // Tensor-core GEMM forms: [0] 1-SM 128x128 tiles, [1] CTA-pair 256x128,
-  // [2] 1-SM 128x256, [3] CTA-pair 256x256.
-  static constexpr int kForms = 4;
+  // [2] 1-SM 128x256, [3] CTA-pair 256x256 (level sums to the workspace, then
+  // the recombine kernel); [4] 1-SM 128x128 and [5] CTA-pair 256x128 direct
+  // (levels folded in TMEM, FP64 stored by the GEMM's epilogue).
+  static constexpr int kForms = 6;
   struct GemmForm {
     bool pair = false;
+    bool direct = false;
     bool built = false;
     int tile_rows = 128;
     int tile_cols = 128;
@@ -75,12 +80,17 @@ struct a4g_batch {
     int nsplit = 1;
     int grid = 0;
     OzGemmArgs args{};
-    float tuned_ms = -1.f;
+    float tuned_ms = -1.f;  // GEMM time measured at creation (direct: without its D stores)
+    float score_ms = -1.f;  // tuned_ms + modelled workspace read and D traffic
   };
   GemmForm forms[kForms];
   int form = 0;  // the form run() uses (chosen by the autotuner or the caller)
   // split-count tuning of the chosen form: candidates and their scores (ms)
   int split_candidates[2] = {0, 0};
+  // D = L R computed as D = R L with the operands' roles exchanged (so that
+  // D's unit-stride index runs along the tile rows)
+  bool swapped = false;
+  std::deque<DevPlan> own_plans;
   float split_cost_ms[2] = {-1.f, -1.f};
   // Split/GEMM pipeline of the chosen form: the GEMM runs as `parts` launches
   // over consecutive split-K ranges; the right-operand split jobs that only
@@ -461,12 +471,14 @@ int build_ozaki(a4g_batch* b, const std::vector<DGroup>& groups, const std::vect
   if ((rc = oz_max_pairs(&pairs))) return rc;
   size_t ws_elems = 0;
   // Work units of one form: (level, split, tile), level-major, each split a
-  // 1/nsplit share of the tile's concatenated k blocks.
-  auto make_units = [&](const std::vector<OzTile>& tiles, int nsplit) {
+  // 1/nsplit share of the tile's concatenated k blocks; direct forms: (tile,
+  // level), tile-major, one split.
+  auto make_units = [&](const std::vector<OzTile>& tiles, int nsplit, bool tile_major = false) {
     std::vector<OzUnit> units;
+    const int nt = int(tiles.size());
     for (int lv = 0; lv < S; ++lv)
       for (int sp = 0; sp < nsplit; ++sp)
-        for (int ti = 0; ti < int(tiles.size()); ++ti) {
+        for (int ti = 0; ti < nt; ++ti) {
           const OzTile& t = tiles[ti];
           OzUnit u{};
           u.tile = ti, u.level = lv, u.split = sp;
@@ -478,17 +490,37 @@ int build_ozaki(a4g_batch* b, const std::vector<DGroup>& groups, const std::vect
           u.kb_in_trip = u.kb_begin - acc;
           units.push_back(u);
         }
+    if (tile_major) {
+      std::vector<OzUnit> tm(units.size());
+      for (int lv = 0; lv < S; ++lv)
+        for (int ti = 0; ti < nt; ++ti) tm[size_t(ti) * S + lv] = units[size_t(lv) * nt + ti];
+      units.swap(tm);
+    }
     return units;
   };
+  // Direct forms fold the levels of a whole tile into one 64-bit integer,
+  //   sum_t S_t 256^(S-1-t),  |S_t| <= (t+1) * K * 2^14  (digits |d| <= 128),
+  // so they need |sum| < 2^63 for the longest k range (kept below 2^62 here),
+  // and at least one k block per tile.
+  bool direct_ok = S <= 6;
+  {
+    long double weight = 0.0L;
+    for (int t = 0; t < S; ++t) weight += (long double)(t + 1) * std::pow(2.0L, 8 * (S - 1 - t));
+    for (const OzTile& di : dinfo)
+      direct_ok = direct_ok && di.kb_total >= 1 &&
+                  (long double)di.kb_total * kOzBK * 16384.0L * weight < std::pow(2.0L, 62);
+  }
   std::vector<std::vector<OzTile>> form_tiles(a4g_batch::kForms);
   std::vector<std::vector<OzUnit>> form_units(a4g_batch::kForms);
   for (int f = 0; f < a4g_batch::kForms; ++f) {
     a4g_batch::GemmForm& gf = b->forms[f];
     gf.pair = f & 1;
+    gf.direct = f >= 4;
     gf.tile_rows = gf.pair ? 2 * kOzBM : kOzBM;
-    gf.tile_cols = f >= 2 ? 2 * kOzBN : kOzBN;
+    gf.tile_cols = (f == 2 || f == 3) ? 2 * kOzBN : kOzBN;
     const int P = gf.pair ? pairs : ctx()->num_sms;  // concurrent workers (CTAs or CTA pairs)
     if (P < 1 || (b->variant && b->variant != f + 1)) continue;
+    if (gf.direct && !direct_ok) continue;
     std::vector<OzTile>& tiles = form_tiles[f];
     for (const OzTile& di : dinfo)
       for (int64_t n0 = 0; n0 < di.n0; n0 += gf.tile_cols)
@@ -508,7 +540,7 @@ int build_ozaki(a4g_batch* b, const std::vector<DGroup>& groups, const std::vect
     const double tile_bytes = double(gf.tile_rows) * gf.tile_cols * sizeof(int);
     int nsplit = ns_min;
     double best = -1.0;
-    for (int ns = ns_min; ns <= std::max(64, ns_min); ++ns) {
+    for (int ns = ns_min; !gf.direct && ns <= std::max(64, ns_min); ++ns) {
       if (ns > ns_min && min_kb / ns < 16) break;
       if (ns > ns_min && double(gf.n_tiles) * S * ns * tile_bytes > 6.0 * (1u << 30)) break;
       const int64_t units = int64_t(gf.n_tiles) * ns;
@@ -516,10 +548,11 @@ int build_ozaki(a4g_batch* b, const std::vector<DGroup>& groups, const std::vect
       if (eff > best + 1e-9) best = eff, nsplit = ns;
       if (eff >= 0.999) break;
     }
+    if (gf.direct) nsplit = 1;
     gf.nsplit = nsplit;
     std::vector<OzUnit>& units = form_units[f];
-    units = make_units(tiles, nsplit);
-    ws_elems = std::max(ws_elems, size_t(gf.n_tiles) * S * nsplit * gf.tile_rows * gf.tile_cols);
+    units = make_units(tiles, nsplit, gf.direct);
+    if (!gf.direct) ws_elems = std::max(ws_elems, size_t(gf.n_tiles) * S * nsplit * gf.tile_rows * gf.tile_cols);
     OzUnit* d_units = nullptr;
     if ((rc = upload(b, tiles, &gf.d_tiles)) || (rc = upload(b, units, &d_units))) return rc;
     OzGemmArgs& ga = gf.args;
@@ -534,7 +567,13 @@ int build_ozaki(a4g_batch* b, const std::vector<DGroup>& groups, const std::vect
     ga.nsplit = nsplit;
     for (int t = 0; t < kOzMaxSlices; ++t) ga.chunk_kb[t] = t < S ? oz_chunk_kb(t) : 1;
     ga.err_flag = ctx()->d_error_flag;
-    gf.grid = gf.pair ? 2 * std::min(ga.n_units, pairs) : std::min(ga.n_units, ctx()->num_sms);
+    ga.direct = gf.direct ? 1 : 0;
+    ga.mode = b->store_mode();
+    ga.dry = 0;
+    ga.dblocks = b->d_dblocks;
+    ga.plans = b->d_plans;
+    const int workers = gf.direct ? gf.n_tiles : ga.n_units;
+    gf.grid = gf.pair ? 2 * std::min(workers, pairs) : std::min(workers, ctx()->num_sms);
     gf.built = true;
   }
   void* ws = nullptr;
@@ -546,91 +585,123 @@ int build_ozaki(a4g_batch* b, const std::vector<DGroup>& groups, const std::vect
     if (b->forms[f].built && (b->form < 0 || b->variant == f + 1)) b->form = f;
   if (b->form < 0) return fail(A4G_ERR_UNSUPPORTED, "no tensor-core GEMM form fits this GPU");
   if (!b->variant) {
-    // autotune: time each form's GEMM once (after one untimed run) on this
-    // batch's panels and keep the fastest
+    // Autotune on this batch's own panels: each form's GEMM and, for the
+    // workspace forms, the recombine after it, timed once after one untimed
+    // run, storing into a scratch destination (every destination block's
+    // tables pointed at one buffer of the largest block's size) so that the
+    // caller's blocks stay untouched; the lowest time wins.  Then the chosen
+    // workspace form's split-K count is timed against its double.  If the
+    // scratch cannot be had, direct forms run without their stores and the
+    // traffic left out is added at the copy rate.
+    size_t d_max = 0;
+    double d_bytes = 0.0;
+    for (const OzTile& di : dinfo) {
+      d_max = std::max(d_max, size_t(di.m0) * size_t(di.n0));
+      d_bytes += double(di.m0) * di.n0 * sizeof(double) * (b->beta ? 2 : 1);
+    }
+    const double ms_per_byte = 1.0 / 6.5e9;  // ~ the measured copy rate, bytes per ms
+    double* scratch = nullptr;
+    OzDBlock* sdb = nullptr;
+    if (cudaMalloc(&scratch, std::max<size_t>(d_max, 1) * sizeof(double)) == cudaSuccess) {
+      std::vector<OzDBlock> hs = dblocks;
+      for (OzDBlock& x : hs) x.d = scratch;
+      if (cudaMalloc(&sdb, hs.size() * sizeof(OzDBlock)) != cudaSuccess ||
+          cudaMemcpy(sdb, hs.data(), hs.size() * sizeof(OzDBlock), cudaMemcpyHostToDevice) != cudaSuccess) {
+        cudaFree(sdb);
+        cudaFree(scratch);
+        sdb = nullptr, scratch = nullptr;
+      }
+    }
+    cudaGetLastError();  // a failed scratch allocation is not an error of the batch
     cudaStream_t s = ctx()->stream;
     cudaEvent_t e0, e1;
     A4G_CUDA(cudaEventCreate(&e0));
     A4G_CUDA(cudaEventCreate(&e1));
-    float best_ms = 0.f;
+    // time one form (GEMM args ga, its tile list) in ms, modelled traffic included
+    auto time_form = [&](const a4g_batch::GemmForm& gf, const OzGemmArgs& ga, int grid, float* ms) -> int {
+      OzGemmArgs ta = ga;
+      if (sdb) ta.dblocks = sdb;
+      else ta.dry = 1;
+      int r = A4G_OK;
+      for (int rep = 0; rep < 2 && !r; ++rep) {
+        if (rep == 1 && cudaEventRecord(e0, s) != cudaSuccess) return cuda_fail(cudaGetLastError(), "event");
+        r = oz_launch_gemm(ta, grid, gf.pair, gf.tile_cols, s);
+        if (!r && !gf.direct && sdb)
+          r = oz_launch_recombine(gf.d_tiles, gf.n_tiles, gf.tile_rows, gf.tile_cols, sdb, b->d_plans, b->d_pa,
+                                  b->d_pb, ta.ws, S, ta.nsplit, b->store_mode(), s);
+      }
+      if (r) return r;
+      A4G_CUDA(cudaEventRecord(e1, s));
+      A4G_CUDA(cudaEventSynchronize(e1));
+      A4G_CUDA(cudaEventElapsedTime(ms, e0, e1));
+      if (!sdb) {
+        const double ws_bytes = gf.direct ? 0.0 : double(gf.n_tiles) * S * ta.nsplit * gf.tile_rows *
+                                                      gf.tile_cols * sizeof(int);
+        *ms += float((ws_bytes + d_bytes) * ms_per_byte);
+      }
+      return check_device_flag(s);
+    };
+    float best = 0.f;
     for (int f = 0; f < a4g_batch::kForms && !rc; ++f) {
       a4g_batch::GemmForm& gf = b->forms[f];
       if (!gf.built) continue;
-      if ((rc = oz_launch_gemm(gf.args, gf.grid, gf.pair, gf.tile_cols, s))) break;
-      A4G_CUDA(cudaEventRecord(e0, s));
-      if ((rc = oz_launch_gemm(gf.args, gf.grid, gf.pair, gf.tile_cols, s))) break;
-      A4G_CUDA(cudaEventRecord(e1, s));
-      A4G_CUDA(cudaEventSynchronize(e1));
-      A4G_CUDA(cudaEventElapsedTime(&gf.tuned_ms, e0, e1));
-      if (best_ms == 0.f || gf.tuned_ms < best_ms) best_ms = gf.tuned_ms, b->form = f;
+      if ((rc = time_form(gf, gf.args, gf.grid, &gf.score_ms))) break;
+      gf.tuned_ms = gf.score_ms;
+      if (best == 0.f || gf.score_ms < best) best = gf.score_ms, b->form = f;
     }
-    cudaEventDestroy(e0);
-    cudaEventDestroy(e1);
-    if (rc) return rc;
-    if ((rc = check_device_flag(s))) return rc;
-  }
-  if (!b->variant) {
-    // split-count tuning of the chosen form: the balance-driven count against
-    // its double (shorter k windows per level), scored as the GEMM's measured
-    // time plus the recombine's reading of the int32 workspace at the copy
-    // rate (the recombine writes the caller's blocks, so it is not run here)
+    // split-count tuning of the chosen workspace form: the balance-driven
+    // count against its double (shorter k windows per unit, twice the
+    // workspace for the recombine to read)
     a4g_batch::GemmForm& gf = b->forms[b->form];
     const std::vector<OzTile>& tiles = form_tiles[b->form];
     int min_kb = 1 << 30;
     for (const OzTile& t : tiles) min_kb = std::min(min_kb, t.kb_total);
     const int ns1 = gf.nsplit, ns2 = 2 * ns1;
-    const double tile_bytes = double(gf.tile_rows) * gf.tile_cols * sizeof(int);
-    const double ws1 = double(gf.n_tiles) * S * ns1 * tile_bytes, ws2 = 2.0 * ws1;
-    const double read_ms_per_byte = 1.0 / 6.5e9;  // ~ the measured copy rate, bytes per ms
-    b->split_candidates[0] = ns1;
-    b->split_cost_ms[0] = gf.tuned_ms + float(ws1 * read_ms_per_byte);
-    if (gf.n_tiles > 0 && ns2 <= 64 && min_kb / ns2 >= 16 && ws2 <= 6.0 * (1u << 30)) {
+    const double ws2 = 2.0 * double(gf.n_tiles) * S * ns1 * gf.tile_rows * gf.tile_cols * sizeof(int);
+    if (!rc && !gf.direct) {
+      b->split_candidates[0] = ns1;
+      b->split_cost_ms[0] = gf.score_ms;
+    }
+    if (!rc && !gf.direct && gf.n_tiles > 0 && ns2 <= 64 && min_kb / ns2 >= 16 && ws2 <= 6.0 * (1u << 30)) {
       std::vector<OzUnit> units2 = make_units(tiles, ns2);
       OzUnit* d_units2 = nullptr;
       void* ws2p = nullptr;
-      if ((rc = upload(b, units2, &d_units2)) || (rc = device_alloc(b, size_t(ws2), &ws2p, false))) return rc;
-      OzGemmArgs a2 = gf.args;
-      a2.units = d_units2;
-      a2.n_units = int(units2.size());
-      a2.nsplit = ns2;
-      a2.ws = static_cast<int*>(ws2p);
-      const int grid2 = gf.pair ? 2 * std::min(a2.n_units, pairs) : std::min(a2.n_units, ctx()->num_sms);
-      cudaStream_t s = ctx()->stream;
-      cudaEvent_t e0, e1;
-      A4G_CUDA(cudaEventCreate(&e0));
-      A4G_CUDA(cudaEventCreate(&e1));
-      float ms2 = 0.f;
-      rc = oz_launch_gemm(a2, grid2, gf.pair, gf.tile_cols, s);
-      if (!rc) A4G_CUDA(cudaEventRecord(e0, s));
-      if (!rc) rc = oz_launch_gemm(a2, grid2, gf.pair, gf.tile_cols, s);
-      if (!rc) {
-        A4G_CUDA(cudaEventRecord(e1, s));
-        A4G_CUDA(cudaEventSynchronize(e1));
-        A4G_CUDA(cudaEventElapsedTime(&ms2, e0, e1));
-      }
-      cudaEventDestroy(e0);
-      cudaEventDestroy(e1);
-      if (rc) return rc;
-      if ((rc = check_device_flag(s))) return rc;
-      b->split_candidates[1] = ns2;
-      b->split_cost_ms[1] = ms2 + float(ws2 * read_ms_per_byte);
-      if (b->split_cost_ms[1] < b->split_cost_ms[0]) {
-        // the other forms are not run any more: their units and the shared
-        // workspace go
-        for (int f = 0; f < a4g_batch::kForms; ++f)
-          if (b->forms[f].built)
-            release(b, const_cast<OzUnit*>(b->forms[f].args.units), form_units[f].size() * sizeof(OzUnit)), b->forms[f].args.units = nullptr;
-        release(b, b->d_ws, ws_elems * sizeof(int));
-        gf.args = a2;
-        gf.nsplit = ns2;
-        gf.grid = grid2;
-        b->d_ws = a2.ws;
-        form_units[b->form].swap(units2);
-      } else {
-        release(b, d_units2, units2.size() * sizeof(OzUnit));
-        release(b, ws2p, size_t(ws2));
+      if (!(rc = upload(b, units2, &d_units2)) && !(rc = device_alloc(b, size_t(ws2), &ws2p, false))) {
+        OzGemmArgs a2 = gf.args;
+        a2.units = d_units2;
+        a2.n_units = int(units2.size());
+        a2.nsplit = ns2;
+        a2.ws = static_cast<int*>(ws2p);
+        const int grid2 = gf.pair ? 2 * std::min(a2.n_units, pairs) : std::min(a2.n_units, ctx()->num_sms);
+        float ms2 = 0.f;
+        if (!(rc = time_form(gf, a2, grid2, &ms2))) {
+          b->split_candidates[1] = ns2;
+          b->split_cost_ms[1] = ms2;
+          if (ms2 < b->split_cost_ms[0]) {
+            // the other forms are not run any more: their units and the
+            // shared workspace go
+            for (int f = 0; f < a4g_batch::kForms; ++f)
+              if (b->forms[f].built)
+                release(b, const_cast<OzUnit*>(b->forms[f].args.units), form_units[f].size() * sizeof(OzUnit)),
+                    b->forms[f].args.units = nullptr;
+            release(b, b->d_ws, ws_elems * sizeof(int));
+            gf.args = a2;
+            gf.nsplit = ns2;
+            gf.grid = grid2;
+            b->d_ws = a2.ws;
+            form_units[b->form].swap(units2);
+          } else {
+            release(b, d_units2, units2.size() * sizeof(OzUnit));
+            release(b, ws2p, size_t(ws2));
+          }
+        }
       }
     }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (sdb) cudaFree(sdb);
+    if (scratch) cudaFree(scratch);
+    if (rc) return rc;
   }
   // Pipeline of the chosen form (when the caller asks for one): GEMM parts
   // over consecutive split-K ranges; each k-major right-operand split job
@@ -774,7 +845,7 @@ int run(a4g_batch* b, cudaStream_t s, const cudaEvent_t* ev = nullptr) {
     }
   }
   if ((rc = mark(4))) return rc;
-  if (gf.n_tiles > 0 &&
+  if (gf.n_tiles > 0 && !gf.direct &&
       (rc = oz_launch_recombine(gf.d_tiles, gf.n_tiles, gf.tile_rows, gf.tile_cols, b->d_dblocks, b->d_plans,
                                 b->d_pa, b->d_pb, b->d_ws, b->slices, gf.nsplit, b->store_mode(), s)))
     return rc;
@@ -851,6 +922,33 @@ int a4g_batch_create(a4g_batch** out, const int* ptrn, int drank, int lrank, int
   }
   for (auto& kv : all_d)
     if (!gindex.count(kv.first)) b->zero_blocks.push_back({kv.first, kv.second});
+  if (b->precision == A4G_PREC_OZAKI_BF16 && !groups.empty()) {
+    // The split form's epilogues walk a tile by rows (one TMEM lane per row),
+    // so D's unit-stride index belongs along the rows.  When the pattern puts
+    // it on the right operand's side, multiply with the roles exchanged: the
+    // level sums are exact integer sums over the same digit products, so the
+    // result is identical.
+    const GemmPlan& h = plans[groups[0].plan]->host;
+    if (h.N > 1 && h.offDn[1] - h.offDn[0] == 1 && !(h.M > 1 && h.offDm[1] - h.offDm[0] == 1)) {
+      b->swapped = true;
+      for (const DevPlan*& p : plans) {
+        b->own_plans.emplace_back();
+        DevPlan& q = b->own_plans.back();
+        q.host = p->host;
+        std::swap(q.host.M, q.host.N);
+        std::swap(q.host.offLm, q.host.offRn);
+        std::swap(q.host.offLk, q.host.offRk);
+        std::swap(q.host.offDm, q.host.offDn);
+        std::swap(q.host.a_kfast, q.host.b_kfast);
+        q.d_tables = nullptr;  // the tables stay owned by the plan cache
+        q.offLm = p->offRn, q.offLk = p->offRk, q.offRk = p->offLk, q.offRn = p->offLm;
+        q.offDm = p->offDn, q.offDn = p->offDm;
+        p = &q;
+      }
+      for (DGroup& g : groups)
+        for (Pair& pr : g.pairs) std::swap(pr.l, pr.r);
+    }
+  }
   std::vector<PlanRef> refs;
   for (const DevPlan* p : plans) refs.push_back(ref_of(p));
   if ((rc = upload(b.get(), refs, &b->d_plans))) return rc;
@@ -933,7 +1031,8 @@ int a4g_batch_launches(const a4g_batch* b, int* kernels_per_run, int* gemm_parts
     k += b->n_f64_reds > 0 ? 1 : 0;
   } else if (b->forms[b->form].n_tiles > 0) {
     parts = b->parts;
-    k += 2 * int(b->jobsets.size()) + parts + 1;  // exponents + splits, GEMM parts, recombine
+    // exponents + splits, GEMM parts, recombine (folded into the GEMM by direct forms)
+    k += 2 * int(b->jobsets.size()) + parts + (b->forms[b->form].direct ? 0 : 1);
   }
   if (kernels_per_run) *kernels_per_run = k;
   if (gemm_parts) *gemm_parts = parts;
@@ -942,7 +1041,7 @@ int a4g_batch_launches(const a4g_batch* b, int* kernels_per_run, int* gemm_parts
 
 int a4g_batch_splits(const a4g_batch* b, int* nsplit, int* candidates, float* cost_ms, int n) {
   if (!b) return fail(A4G_ERR_ARG, "null batch");
-  if (nsplit) *nsplit = b->precision == A4G_PREC_FP64 ? 0 : b->forms[b->form].nsplit;
+  if (nsplit) *nsplit = b->precision == A4G_PREC_FP64 ? 0 : b->forms[b->form].nsplit;  // direct forms: 1
   for (int i = 0; i < n; ++i) {
     if (candidates) candidates[i] = i < 2 ? b->split_candidates[i] : 0;
     if (cost_ms) cost_ms[i] = i < 2 ? b->split_cost_ms[i] : -1.f;
@@ -953,7 +1052,7 @@ int a4g_batch_splits(const a4g_batch* b, int* nsplit, int* candidates, float* co
 int a4g_batch_form(const a4g_batch* b, int* form, float* tuned_ms, int n) {
   if (!b) return fail(A4G_ERR_ARG, "null batch");
   if (form) *form = b->precision == A4G_PREC_FP64 ? 0 : b->form + 1;
-  for (int f = 0; f < n && tuned_ms; ++f) tuned_ms[f] = f < a4g_batch::kForms ? b->forms[f].tuned_ms : -1.f;
+  for (int f = 0; f < n && tuned_ms; ++f) tuned_ms[f] = f < a4g_batch::kForms ? b->forms[f].score_ms : -1.f;
   return A4G_OK;
 }
 

@@ -103,7 +103,9 @@ constexpr int kOzMaxPipelineParts = 8;  // GEMM launches per pardo step when the
 
 // Work unit of the tensor-core kernel: one level of one tile over a range of
 // its k blocks (split-K).  Units are ordered (level, split, tile) so that the
-// CTAs running at the same time stream the same k window of the panels.
+// CTAs running at the same time stream the same k window of the panels; in
+// the direct form (no split-K) they are ordered (tile, level) and one CTA (or
+// CTA pair) runs all levels of a tile in a row.
 struct OzUnit {
   int tile, level, split;
   int kb_begin, kb_end;  // range in the tile's concatenated k-block list
@@ -127,6 +129,14 @@ struct OzGemmArgs {
   int chunk_kb[kOzMaxSlices];  // k blocks per exact flush at each level
   int* ws;                     // [tile][level][split][col 128][row 128] exact integer level sums
   int* err_flag;
+  // Direct form (128-column tiles, one split): the levels of a tile are folded
+  // exactly in TMEM (64-bit Horner sum over levels) and the epilogue rounds
+  // once and stores D; no workspace, no recombine kernel.
+  int direct;
+  int mode;  // direct: bit 0 accumulate into D, bit 1 negate
+  int dry;   // direct: compute everything but store nothing (timing)
+  const OzDBlock* dblocks;
+  const PlanRef* plans;
 };
 
 }  // namespace a4g

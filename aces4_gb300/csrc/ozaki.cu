@@ -26,7 +26,7 @@
 //   oz_exp_*_kernel     max exponent per panel row          (HBM: 8 B/elem read)
 //   oz_split_*_kernel   FP64 -> BF16 digit slices, K-major   (HBM: 8 B read + 2*slices B write)
 //                       with the block's index permute folded into the gather
-//   oz_gemm_kernel<PAIR, BN>
+//   oz_gemm_kernel<PAIR, BN, DIRECT>
 //                       persistent warp-specialised tcgen05 GEMM: TMA (SW128)
 //                       -> smem ring -> tcgen05.mma into TMEM (2 accumulators)
 //                       -> epilogue warps fold each exact chunk into the level
@@ -52,6 +52,9 @@ namespace {
 
 constexpr int kDigitBits = 8;
 constexpr int kThreadsOz = 320;  // warp 0 TMA, warp 1 MMA, warps 2..9 epilogue
+// Direct forms: warps 2..17 epilogue (four per TMEM lane quadrant, 32 columns
+// each): their epilogue also rounds and stores every result.
+constexpr int kThreadsOzDirect = 576;
 constexpr uint32_t kTileBytes = kOzBM * kOzBK * 2;  // 16 KB per operand tile
 // TMEM columns, 128-column forms: [0,128) and [128,256) are the two FP32 MMA
 // accumulators; [256,384) and [384,512) hold the running exact (hi, lo) sums of
@@ -59,6 +62,9 @@ constexpr uint32_t kTileBytes = kOzBM * kOzBK * 2;  // 16 KB per operand tile
 // accumulators; the level sums live in the epilogue threads' registers.
 constexpr uint32_t kTmemCols = 512;
 constexpr uint32_t kTmemHi = 256, kTmemLo = 384;
+// Direct form: the same two regions hold the low and high 32-bit words of the
+// exact 64-bit running sum over levels.
+constexpr uint32_t kTmemW0 = 256, kTmemW1 = 384;
 constexpr unsigned long long kWaitLimitNs = 20ull * 1000 * 1000 * 1000;  // 20 s
 
 // tcgen05 instruction descriptor, kind::f16: D F32 (bits 4-5 = 1), A BF16
@@ -259,6 +265,34 @@ __device__ __forceinline__ void two_sum_acc(float& hi, float& lo, float x) {
   lo = __fadd_rn(lo, e);
 }
 
+// The double nearest (ties to even) to u * 2^e2 with sign `neg`, u an
+// unsigned 64-bit magnitude, built with integer operations only (FP64
+// arithmetic is scarce on this GPU).  Results outside the normal range take
+// an FP64 path.
+__device__ __forceinline__ double u64_scaled_to_double(unsigned long long u, bool neg, int e2) {
+  if (u == 0) return 0.0;
+  const int nbits = 64 - __clzll((long long)u);
+  unsigned long long mant;
+  int e = e2;
+  if (nbits <= 53) {
+    mant = u << (53 - nbits);
+    e -= 53 - nbits;
+  } else {
+    const int sh = nbits - 53;
+    mant = u >> sh;
+    const unsigned long long rem = u & ((1ull << sh) - 1), half = 1ull << (sh - 1);
+    if (rem > half || (rem == half && (mant & 1ull))) ++mant;
+    e += sh;
+    if (mant == (1ull << 53)) mant >>= 1, ++e;
+  }
+  const int field = e + 52 + 1023;  // value = mant * 2^e, mant in [2^52, 2^53)
+  if (field >= 1 && field <= 2046)
+    return __longlong_as_double((long long)((neg ? (1ull << 63) : 0ull) | ((unsigned long long)field << 52) |
+                                            (mant & ((1ull << 52) - 1))));
+  const double v = ldexp(double(mant), e);
+  return neg ? -v : v;
+}
+
 // ------------------------------------------------------------------ roles
 // Walks the k blocks of one unit: calls f(koff_a, koff_b, kb) per 64-wide
 // block (the panels are zero beyond the end of every stretch of pairs up to
@@ -284,12 +318,27 @@ __device__ __forceinline__ int unit_first() { return PAIR ? int(blockIdx.x >> 1)
 template <bool PAIR>
 __device__ __forceinline__ int unit_stride() { return PAIR ? int(gridDim.x >> 1) : int(gridDim.x); }
 
+// This CTA's (pair's) units in run order; f(u) returns false to stop.  The
+// direct form hands out whole tiles: units (tile, 0..slices-1) in a row.
+template <bool PAIR, class F>
+__device__ __forceinline__ void for_units(const OzGemmArgs& a, F&& f) {
+  if (a.direct) {
+    const int groups = a.n_units / a.slices;
+    for (int g = unit_first<PAIR>(); g < groups; g += unit_stride<PAIR>())
+      for (int lv = 0; lv < a.slices; ++lv)
+        if (!f(g * a.slices + lv)) return;
+  } else {
+    for (int u = unit_first<PAIR>(); u < a.n_units; u += unit_stride<PAIR>())
+      if (!f(u)) return;
+  }
+}
+
 template <bool PAIR, int BN>
 __device__ void producer(const OzGemmArgs& a, OzSmemT<PAIR, BN>& sm, uint32_t rank) {
   using SM = OzSmemT<PAIR, BN>;
   constexpr uint32_t kBytes = kTileBytes + SM::kBBytes;
   uint32_t it = 0;
-  for (int u = unit_first<PAIR>(); u < a.n_units; u += unit_stride<PAIR>()) {
+  for_units<PAIR>(a, [&](int u) {
     const OzUnit un = a.units[u];
     const OzTile tl = a.tiles[un.tile];
     const int level = un.level;
@@ -318,8 +367,8 @@ __device__ void producer(const OzGemmArgs& a, OzSmemT<PAIR, BN>& sm, uint32_t ra
       }
       return true;
     });
-    if (!ok) return;
-  }
+    return ok;
+  });
 }
 
 // One thread issues every MMA (the leader CTA's in the pair form).
@@ -327,7 +376,7 @@ template <bool PAIR, int BN>
 __device__ void mma_issuer(const OzGemmArgs& a, OzSmemT<PAIR, BN>& sm, uint32_t tmem) {
   using SM = OzSmemT<PAIR, BN>;
   uint32_t it = 0, chunk = 0;
-  for (int u = unit_first<PAIR>(); u < a.n_units; u += unit_stride<PAIR>()) {
+  for_units<PAIR>(a, [&](int u) {
     const OzUnit un = a.units[u];
     const OzTile tl = a.tiles[un.tile];
     const int level = un.level;
@@ -367,8 +416,8 @@ __device__ void mma_issuer(const OzGemmArgs& a, OzSmemT<PAIR, BN>& sm, uint32_t 
       }
       return true;
     });
-    if (!ok) return;
-  }
+    return ok;
+  });
 }
 
 __device__ __forceinline__ void tc_st32(uint32_t taddr, const uint32_t (&r)[32]) {
@@ -384,34 +433,228 @@ __device__ __forceinline__ void tc_st32(uint32_t taddr, const uint32_t (&r)[32])
       : "memory");
 }
 
+__device__ __forceinline__ void tc_st16(uint32_t taddr, const uint32_t (&r)[16]) {
+  asm volatile(
+      "tcgen05.st.sync.aligned.32x32b.x16.b32 [%0], "
+      "{%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16};" ::"r"(taddr),
+      "r"(r[0]), "r"(r[1]), "r"(r[2]), "r"(r[3]), "r"(r[4]), "r"(r[5]), "r"(r[6]), "r"(r[7]),
+      "r"(r[8]), "r"(r[9]), "r"(r[10]), "r"(r[11]), "r"(r[12]), "r"(r[13]), "r"(r[14]), "r"(r[15])
+      : "memory");
+}
+
+__device__ __forceinline__ void tc_st8(uint32_t taddr, const uint32_t (&r)[8]) {
+  asm volatile("tcgen05.st.sync.aligned.32x32b.x8.b32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8};" ::"r"(taddr),
+      "r"(r[0]), "r"(r[1]), "r"(r[2]), "r"(r[3]), "r"(r[4]), "r"(r[5]), "r"(r[6]), "r"(r[7]) : "memory");
+}
+__device__ __forceinline__ void tc_ld8_nowait(uint32_t taddr, uint32_t (&r)[8]) {
+  asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+               : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7])
+               : "r"(taddr));
+}
+
+// v * 2^e2 rounded once to the nearest double (ties to even), v a signed
+// 64-bit integer: normalise, keep 53 bits, round on the 11 below, and build
+// the bits by one addition (a mantissa that rounds up to 2^53 carries into
+// the exponent field).  Branch-free for results in the normal range; the
+// rest takes u64_scaled_to_double.  Same result as u64_scaled_to_double.
+__device__ __forceinline__ double i64_scaled_to_double(long long v, int e2) {
+  if (v == 0) return 0.0;
+  const unsigned long long u = v < 0 ? (unsigned long long)(-v) : (unsigned long long)v;
+  const int n = __clzll((long long)u);
+  const unsigned long long norm = u << n;  // leading one at bit 63
+  unsigned long long mant = norm >> 11;    // 53 bits, leading one at bit 52
+  const unsigned long long rem = norm & 0x7FFull;
+  mant += (rem > 0x400ull || (rem == 0x400ull && (mant & 1ull))) ? 1ull : 0ull;
+  const int field = e2 + 63 - n + 1023;  // biased exponent of the leading one
+  if (field < 1 || field > 2045) return u64_scaled_to_double(u, v < 0, e2);
+  return __longlong_as_double(
+      (long long)(((unsigned long long)v & (1ull << 63)) | ((((unsigned long long)(field - 1)) << 52) + mant)));
+}
+
+// Direct form: what a thread needs to store its part of a tile (its row,
+// columns col0..col0+31), gathered once when the tile starts (while the
+// tensor cores work on the tile's first level): the row's D address and
+// scale; the 32 columns' D offsets and scales go to the warp's table in
+// shared memory (read back as broadcasts).
+struct DirectCol {
+  long long off;  // -1: column outside D
+  int F;          // biased column exponent (at least 1)
+  int pad;
+};
+struct DirectTile {
+  double* drow;
+  DirectCol* cols;  // this warp's 32 entries
+  int ebase;        // row scale and constant part of the result's exponent
+  bool mlive;
+};
+
+__device__ __forceinline__ void direct_tile(DirectTile& t, const OzGemmArgs& a, const OzTile& tl, int row,
+                                            int col0, int lane) {
+  const OzDBlock db = a.dblocks[tl.dblock];
+  const PlanRef pl = a.plans[db.plan];
+  const int m = tl.m0 + row, n = tl.n0 + col0 + lane;
+  t.mlive = m < pl.M;
+  int Em = 1;
+  t.drow = db.d;
+  if (t.mlive) {
+    const int e = a.panels_a[tl.panel_a].exps[m];
+    Em = e ? e : 1;
+    t.drow += pl.offDm[m];
+  }
+  t.ebase = Em - 1022 - 1022 + 2 - kDigitBits * (a.slices + 1);
+  DirectCol c{-1, 1, 0};
+  if (n < pl.N) {
+    const int f = a.panels_b[tl.panel_b].exps[n];
+    c.F = f ? f : 1;
+    c.off = pl.offDn[n];
+  }
+  __syncwarp();  // the previous tile's entries are read
+  t.cols[lane] = c;
+  __syncwarp();
+}
+
+// Accumulate mode: asks L2 for the thread's 32 D elements when the tile
+// starts, so that the loads after its last chunk find them there.
+__device__ __forceinline__ void prefetch_direct(const DirectTile& t) {
+  if (!t.mlive) return;
+#pragma unroll 8
+  for (int j = 0; j < 32; ++j) {
+    const long long off = t.cols[j].off;
+    if (off >= 0) asm volatile("prefetch.global.L2 [%0];" ::"l"(t.drow + off));
+  }
+}
+
+__device__ __forceinline__ void load_d8(const DirectTile& t, int c0, bool acc, double (&d)[8]) {
+#pragma unroll
+  for (int j = 0; j < 8; ++j) {
+    const long long off = t.cols[c0 + j].off;
+    d[j] = 0.0;
+    if (acc && t.mlive && off >= 0) d[j] = t.drow[off];
+  }
+}
+
+// Direct form, after the last chunk of a tile's last level: rounds the 32
+// exact 64-bit sums of this thread's row held in TMEM (low words at w0addr,
+// high words kTmemW1 - kTmemW0 columns further) to FP64 with the row and
+// column scales and stores (or adds) them into D, 8 columns at a time; in the
+// accumulate mode the next 8 D loads are in flight while 8 are added.
+__device__ __forceinline__ void store_direct(const OzGemmArgs& a, const DirectTile& t, uint32_t w0addr) {
+  if (a.dry) return;
+  const bool acc = a.mode & 1;
+  double dn[8];
+  load_d8(t, 0, acc, dn);
+#pragma unroll 1
+  for (int p = 0; p < 4; ++p) {
+    double dc[8];
+#pragma unroll
+    for (int j = 0; j < 8; ++j) dc[j] = dn[j];
+    if (p < 3) load_d8(t, 8 * (p + 1), acc, dn);
+    uint32_t w0[8], w1[8];
+    tc_ld8_nowait(w0addr + 8 * p, w0);
+    tc_ld8_nowait(w0addr + (kTmemW1 - kTmemW0) + 8 * p, w1);
+    tc_wait_ld();
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+      const DirectCol c = t.cols[8 * p + j];
+      const long long v = (long long)(((unsigned long long)w1[j] << 32) | w0[j]);
+      double x = i64_scaled_to_double(v, t.ebase + c.F);
+      if (a.mode & 2) x = -x;
+      if (t.mlive && c.off >= 0) t.drow[c.off] = acc ? dc[j] + x : x;
+    }
+  }
+}
+
 // Eight warps, two per TMEM lane quadrant (warp % 4); each thread owns one
 // accumulator row and 64 of its 128 columns, in two groups of 32.  The three
 // TMEM loads of a group (chunk, hi, lo) are issued before one wait.  In the
 // pair form each CTA drains its own 128 rows and signals the leader.
-template <bool PAIR>
+//
+// Direct form: the running sum of a tile is the exact integer
+//     sum_t S_t * 256^(slices-1-t)
+// (Horner over the levels t, which arrive in order), kept as two 32-bit
+// TMEM words per element; the host admits a batch to this form only when the
+// sum stays below 2^63.  The last chunk of the last level is rounded once and
+// stored into D.
+template <bool PAIR, bool DIRECT>
 __device__ void epilogue(const OzGemmArgs& a, OzSmemT<PAIR, 128>& sm, uint32_t tmem, int warp, int lane,
                          uint32_t rank) {
   constexpr int kRows = PAIR ? 2 * kOzBM : kOzBM;  // rows of a tile
+  constexpr int kCols = DIRECT ? 32 : 64;          // columns of a thread
   const int q = warp & 3, h = (warp - 2) >> 2;
   const int row = int(rank) * kOzBM + 32 * q + lane;
-  const uint32_t lane_addr = tmem + (uint32_t(32 * q) << 16) + uint32_t(64 * h);
+  const uint32_t lane_addr = tmem + (uint32_t(32 * q) << 16) + uint32_t(kCols * h);
   uint32_t empty_bar[2];
   for (int b = 0; b < 2; ++b) empty_bar[b] = PAIR ? mapa_shared(&sm.acc_empty[b], 0) : smem_u32(&sm.acc_empty[b]);
   uint32_t chunk = 0;
-  for (int u = unit_first<PAIR>(); u < a.n_units; u += unit_stride<PAIR>()) {
+  [[maybe_unused]] DirectTile dt{};
+  if constexpr (DIRECT) {
+    __shared__ DirectCol direct_cols[kThreadsOzDirect / 32 - 2][32];  // one table per epilogue warp
+    dt.cols = direct_cols[warp - 2];
+  }
+  auto release = [&](uint32_t buf) {
+    tc_fence_before();
+    __syncwarp();
+    if (lane == 0) {
+      if constexpr (PAIR) mbar_arrive_cluster(empty_bar[buf]);
+      else mbar_arrive(&sm.acc_empty[buf]);
+    }
+  };
+  for_units<PAIR>(a, [&](int u) {
     const OzUnit un = a.units[u];
     const int ckb = a.chunk_kb[un.level];
     const int nchunks = (un.kb_end - un.kb_begin + ckb - 1) / ckb;
+    if constexpr (DIRECT) {
+      const bool last_level = un.level == a.slices - 1;
+      if (un.level == 0) {
+        direct_tile(dt, a, a.tiles[un.tile], row, kCols * h, lane);
+        if ((a.mode & 1) && !a.dry) prefetch_direct(dt);
+      }
+      for (int c = 0; c < nchunks; ++c) {
+        const uint32_t buf = chunk & 1;
+        if (!mbar_wait(&sm.acc_full[buf], (chunk >> 1) & 1, sm, a.err_flag, 4)) return false;
+        tc_fence_after();
+        const bool fresh = c == 0 && un.level == 0;  // no running sum yet
+        const uint32_t sh = c == 0 ? 8u : 0u;        // a new level: running sum * 256
+        const bool final = last_level && c == nchunks - 1;
+#pragma unroll 1
+        for (int g = 0; g < 4; ++g) {
+          uint32_t x[8], w0[8], w1[8];
+          tc_ld8_nowait(lane_addr + buf * kOzBN + 8 * g, x);
+          if (!fresh) {
+            tc_ld8_nowait(lane_addr + kTmemW0 + 8 * g, w0);
+            tc_ld8_nowait(lane_addr + kTmemW1 + 8 * g, w1);
+          } else {
+#pragma unroll
+            for (int j = 0; j < 8; ++j) w0[j] = w1[j] = 0u;
+          }
+          tc_wait_ld();
+#pragma unroll
+          for (int j = 0; j < 8; ++j) {
+            unsigned long long v = ((unsigned long long)w1[j] << 32) | w0[j];
+            v = (v << sh) + (unsigned long long)(long long)__float2int_rz(__uint_as_float(x[j]));  // exact
+            w0[j] = uint32_t(v);
+            w1[j] = uint32_t(v >> 32);
+          }
+          tc_st8(lane_addr + kTmemW0 + 8 * g, w0);
+          tc_st8(lane_addr + kTmemW1 + 8 * g, w1);
+        }
+        tc_wait_st();
+        release(buf);  // the next MMAs may start while this thread stores D
+        ++chunk;
+        if (final) store_direct(a, dt, lane_addr + kTmemW0);
+      }
+      return true;
+    } else {
     int* w = a.ws + ((size_t(un.tile) * a.slices + un.level) * a.nsplit + un.split) * kOzBN * kRows +
              size_t(64 * h) * kRows + row;
     if (nchunks == 0) {  // empty k range: its partial sum is zero
 #pragma unroll 8
       for (int j = 0; j < 64; ++j) w[size_t(j) * kRows] = 0;
-      continue;
+      return true;
     }
     for (int c = 0; c < nchunks; ++c) {
       const uint32_t buf = chunk & 1;
-      if (!mbar_wait(&sm.acc_full[buf], (chunk >> 1) & 1, sm, a.err_flag, 4)) return;
+      if (!mbar_wait(&sm.acc_full[buf], (chunk >> 1) & 1, sm, a.err_flag, 4)) return false;
       tc_fence_after();
       const bool first = c == 0, last = c == nchunks - 1;
 #pragma unroll 1
@@ -447,15 +690,12 @@ __device__ void epilogue(const OzGemmArgs& a, OzSmemT<PAIR, 128>& sm, uint32_t t
         }
       }
       if (!last) tc_wait_st();
-      tc_fence_before();
-      __syncwarp();
-      if (lane == 0) {
-        if constexpr (PAIR) mbar_arrive_cluster(empty_bar[buf]);
-        else mbar_arrive(&sm.acc_empty[buf]);
-      }
+      release(buf);
       ++chunk;
     }
-  }
+    return true;
+    }
+  });
 }
 
 // 256-column tiles: the two FP32 accumulators use all 512 TMEM columns, so the
@@ -474,7 +714,7 @@ __device__ void epilogue_int(const OzGemmArgs& a, OzSmemT<PAIR, 256>& sm, uint32
   uint32_t empty_bar[2];
   for (int b = 0; b < 2; ++b) empty_bar[b] = PAIR ? mapa_shared(&sm.acc_empty[b], 0) : smem_u32(&sm.acc_empty[b]);
   uint32_t chunk = 0;
-  for (int u = unit_first<PAIR>(); u < a.n_units; u += unit_stride<PAIR>()) {
+  for_units<PAIR>(a, [&](int u) {
     const OzUnit un = a.units[u];
     const int ckb = a.chunk_kb[un.level];
     const int nchunks = (un.kb_end - un.kb_begin + ckb - 1) / ckb;
@@ -485,7 +725,7 @@ __device__ void epilogue_int(const OzGemmArgs& a, OzSmemT<PAIR, 256>& sm, uint32
     for (int j = 0; j < 128; ++j) sum[j] = 0;
     for (int c = 0; c < nchunks; ++c) {
       const uint32_t buf = chunk & 1;
-      if (!mbar_wait(&sm.acc_full[buf], (chunk >> 1) & 1, sm, a.err_flag, 4)) return;
+      if (!mbar_wait(&sm.acc_full[buf], (chunk >> 1) & 1, sm, a.err_flag, 4)) return false;
       tc_fence_after();
 #pragma unroll
       for (int g = 0; g < 8; ++g) {
@@ -505,11 +745,13 @@ __device__ void epilogue_int(const OzGemmArgs& a, OzSmemT<PAIR, 256>& sm, uint32
     }
 #pragma unroll
     for (int j = 0; j < 128; ++j) w[size_t(j) * kRows] = sum[j];
-  }
+    return true;
+  });
 }
 
-template <bool PAIR, int BN>
-__global__ void __launch_bounds__(kThreadsOz, 1) oz_gemm_kernel(const __grid_constant__ OzGemmArgs a) {
+template <bool PAIR, int BN, bool DIRECT = false>
+__global__ void __launch_bounds__(DIRECT ? kThreadsOzDirect : kThreadsOz, 1)
+    oz_gemm_kernel(const __grid_constant__ OzGemmArgs a) {
   using SM = OzSmemT<PAIR, BN>;
   extern __shared__ uint8_t smem_raw[];
   SM& sm = *reinterpret_cast<SM*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
@@ -522,7 +764,8 @@ __global__ void __launch_bounds__(kThreadsOz, 1) oz_gemm_kernel(const __grid_con
     }
     for (int b = 0; b < 2; ++b) {
       mbar_init(&sm.acc_full[b], 1);
-      mbar_init(&sm.acc_empty[b], PAIR ? 16 : 8);  // one arrive per epilogue warp (of both CTAs)
+      // one arrive per epilogue warp (of both CTAs)
+      mbar_init(&sm.acc_empty[b], (DIRECT ? 16 : 8) * (PAIR ? 2 : 1));
     }
     mbar_init(&sm.drain, 1);
     sm.abort = 0;
@@ -559,7 +802,7 @@ __global__ void __launch_bounds__(kThreadsOz, 1) oz_gemm_kernel(const __grid_con
     }
   } else {
     if constexpr (BN == 256) epilogue_int<PAIR>(a, sm, tmem, warp, lane, rank);
-    else epilogue<PAIR>(a, sm, tmem, warp, lane, rank);
+    else epilogue<PAIR, DIRECT>(a, sm, tmem, warp, lane, rank);
   }
   tc_fence_before();
   __syncthreads();
@@ -895,34 +1138,6 @@ __global__ void __launch_bounds__(256) oz_split_rows_kernel(const OzSplitJob* __
 }
 
 // ------------------------------------------------------------------ recombine
-// The double nearest (ties to even) to u * 2^e2 with sign `neg`, u an
-// unsigned 64-bit magnitude, built with integer operations only (FP64
-// arithmetic is scarce on this GPU).  Results outside the normal range take
-// an FP64 path.
-__device__ __forceinline__ double u64_scaled_to_double(unsigned long long u, bool neg, int e2) {
-  if (u == 0) return 0.0;
-  const int nbits = 64 - __clzll((long long)u);
-  unsigned long long mant;
-  int e = e2;
-  if (nbits <= 53) {
-    mant = u << (53 - nbits);
-    e -= 53 - nbits;
-  } else {
-    const int sh = nbits - 53;
-    mant = u >> sh;
-    const unsigned long long rem = u & ((1ull << sh) - 1), half = 1ull << (sh - 1);
-    if (rem > half || (rem == half && (mant & 1ull))) ++mant;
-    e += sh;
-    if (mant == (1ull << 53)) mant >>= 1, ++e;
-  }
-  const int field = e + 52 + 1023;  // value = mant * 2^e, mant in [2^52, 2^53)
-  if (field >= 1 && field <= 2046)
-    return __longlong_as_double((long long)((neg ? (1ull << 63) : 0ull) | ((unsigned long long)field << 52) |
-                                            (mant & ((1ull << 52) - 1))));
-  const double v = ldexp(double(mant), e);
-  return neg ? -v : v;
-}
-
 // The same for a two's-complement 128-bit integer N.
 __device__ __forceinline__ double i128_scaled_to_double(__int128 N, int e2) {
   const bool neg = N < 0;
@@ -1271,9 +1486,9 @@ int oz_launch_split(int layout, const OzSplitJob* jobs, const int64_t* prefix, i
   return A4G_OK;
 }
 
-template <bool PAIR, int BN>
+template <bool PAIR, int BN, bool DIRECT = false>
 int set_smem_attr() {
-  A4G_CUDA(cudaFuncSetAttribute(oz_gemm_kernel<PAIR, BN>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+  A4G_CUDA(cudaFuncSetAttribute(oz_gemm_kernel<PAIR, BN, DIRECT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                 int(sizeof(OzSmemT<PAIR, BN>)) + 1024));
   return A4G_OK;
 }
@@ -1292,7 +1507,8 @@ int oz_prepare() {
   if (first_on_device(done)) {
     int rc;
     if ((rc = set_smem_attr<false, 128>()) || (rc = set_smem_attr<true, 128>()) ||
-        (rc = set_smem_attr<false, 256>()) || (rc = set_smem_attr<true, 256>())) {
+        (rc = set_smem_attr<false, 256>()) || (rc = set_smem_attr<true, 256>()) ||
+        (rc = set_smem_attr<false, 128, true>()) || (rc = set_smem_attr<true, 128, true>())) {
       done.store(0);
       return rc;
     }
@@ -1320,16 +1536,16 @@ int oz_max_pairs(int* pairs) {
   return A4G_OK;
 }
 
-template <bool PAIR, int BN>
+template <bool PAIR, int BN, bool DIRECT = false>
 int launch_form(const OzGemmArgs& args, int grid, cudaStream_t s) {
   const size_t smem = sizeof(OzSmemT<PAIR, BN>) + 1024;
   if constexpr (!PAIR) {
-    oz_gemm_kernel<false, BN><<<grid, kThreadsOz, smem, s>>>(args);
+    oz_gemm_kernel<false, BN, DIRECT><<<grid, DIRECT ? kThreadsOzDirect : kThreadsOz, smem, s>>>(args);
   } else {
     if (grid % 2) return fail(A4G_ERR_ARG, "CTA-pair grid must be even");
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3(grid, 1, 1);
-    cfg.blockDim = dim3(kThreadsOz, 1, 1);
+    cfg.blockDim = dim3(DIRECT ? kThreadsOzDirect : kThreadsOz, 1, 1);
     cfg.dynamicSmemBytes = smem;
     cfg.stream = s;
     cudaLaunchAttribute attr[1];
@@ -1337,7 +1553,7 @@ int launch_form(const OzGemmArgs& args, int grid, cudaStream_t s) {
     attr[0].val.clusterDim.x = 2, attr[0].val.clusterDim.y = 1, attr[0].val.clusterDim.z = 1;
     cfg.attrs = attr;
     cfg.numAttrs = 1;
-    A4G_CUDA(cudaLaunchKernelEx(&cfg, oz_gemm_kernel<true, BN>, args));
+    A4G_CUDA(cudaLaunchKernelEx(&cfg, oz_gemm_kernel<true, BN, DIRECT>, args));
   }
   A4G_CUDA(cudaGetLastError());
   return A4G_OK;
@@ -1348,6 +1564,11 @@ int oz_launch_gemm(const OzGemmArgs& args, int grid, bool pair, int tile_cols, c
   int rc = oz_prepare();
   if (rc) return rc;
   if (args.n_units <= 0) return A4G_OK;
+  if (args.direct) {
+    if (tile_cols != 128 || args.nsplit != 1 || args.n_units % args.slices)
+      return fail(A4G_ERR_ARG, "direct form: 128-column tiles, one split, whole tiles");
+    return pair ? launch_form<true, 128, true>(args, grid, s) : launch_form<false, 128, true>(args, grid, s);
+  }
   if (tile_cols == 256) return pair ? launch_form<true, 256>(args, grid, s) : launch_form<false, 256>(args, grid, s);
   return pair ? launch_form<true, 128>(args, grid, s) : launch_form<false, 128>(args, grid, s);
 }

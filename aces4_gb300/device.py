@@ -257,15 +257,17 @@ class Batch:
         return {"kernels_per_run": k.value, "gemm_parts": p.value}
 
     FORMS = {1: "one SM per 128x128 tile", 2: "CTA pair per 256x128 tile", 3: "one SM per 128x256 tile",
-             4: "CTA pair per 256x256 tile"}
+             4: "CTA pair per 256x256 tile", 5: "one SM per 128x128 tile, direct FP64 store",
+             6: "CTA pair per 256x128 tile, direct FP64 store"}
 
     def form(self):
-        """The tensor-core GEMM form in use and the autotuner's ms per form."""
+        """The tensor-core GEMM form in use and the autotuner's score (ms) per form."""
         f = ctypes.c_int(0)
-        ms = (ctypes.c_float * 4)()
-        _check(lib().a4g_batch_form(self._h, ctypes.byref(f), ms, 4), "a4g_batch_form")
+        n = len(self.FORMS)
+        ms = (ctypes.c_float * n)()
+        _check(lib().a4g_batch_form(self._h, ctypes.byref(f), ms, n), "a4g_batch_form")
         return {"form": f.value, "name": self.FORMS.get(f.value),
-                "tuned_ms": {self.FORMS[i + 1]: float(ms[i]) for i in range(4) if ms[i] >= 0}}
+                "tuned_ms": {self.FORMS[i + 1]: float(ms[i]) for i in range(n) if ms[i] >= 0}}
 
     def close(self):
         if getattr(self, "_h", None) and self._h.value:

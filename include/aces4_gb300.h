@@ -260,10 +260,16 @@ typedef struct a4g_batch_opts {
                       the relative error near 1e-11, 6 near 1e-13.          */
   int beta;        /* 0: D = sum of products (overwrite); 1: D += sum        */
   int variant;     /* split precision, tensor-core GEMM form: 0 autotuned at
-                      creation (each form timed once, the fastest kept),
-                      1: one SM per 128x128 tile, 2: a CTA pair per 256x128
-                      tile (cta_group::2), 3: one SM per 128x256 tile,
-                      4: a CTA pair per 256x256 tile                          */
+                      creation (each form timed once and scored with the
+                      HBM traffic it leaves to the rest of the step, the
+                      lowest score kept), 1: one SM per 128x128 tile, 2: a
+                      CTA pair per 256x128 tile (cta_group::2), 3: one SM per
+                      128x256 tile, 4: a CTA pair per 256x256 tile (1-4 write
+                      integer level sums, a second kernel combines them),
+                      5 / 6: forms 1 / 2 storing FP64 directly (the levels of
+                      a tile folded exactly in TMEM; available when no split-K
+                      is needed and the 64-bit sum cannot overflow, i.e. up
+                      to 5 slices for k ranges below ~100000)               */
   int negate;      /* 1: subtract the products: D = -sum (beta 0) or
                       D -= sum (beta 1), e.g. the second term of
                       W = A*B - C*E run as a second batch on the same D      */
@@ -302,7 +308,8 @@ int a4g_batch_splits(const a4g_batch* b, int* nsplit, int* candidates, float* co
  * beside the GEMM on a second stream). */
 int a4g_batch_launches(const a4g_batch* b, int* kernels_per_run, int* gemm_parts);
 /* The tensor-core GEMM form in use (the `variant` numbering; 0 for FP64
- * batches) and the autotuner's timing of each form in ms (-1: not run). */
+ * batches) and the autotuner's score of each form in ms (-1: not run): the
+ * GEMM's measured time + the workspace read and D traffic at the copy rate. */
 int a4g_batch_form(const a4g_batch* b, int* form, float* tuned_ms, int n);
 void a4g_batch_destroy(a4g_batch* b);
 

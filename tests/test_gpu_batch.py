@@ -138,7 +138,7 @@ def test_fp64_uneven_sparse_ring(a4):
     assert errs.max() <= TOL_FP64
 
 
-@pytest.mark.parametrize("variant", [1, 2, 3, 4])
+@pytest.mark.parametrize("variant", [1, 2, 3, 4, 5, 6])
 def test_split_one_slice_integer_exact(a4, variant):
     # integers in [-127, 127] are exact single 8-bit digits: the tensor-core
     # products and the chunked FP32 accumulation must reproduce FP64 exactly,
@@ -151,7 +151,7 @@ def test_split_one_slice_integer_exact(a4, variant):
         np.testing.assert_array_equal(R.block(k).cpu().numpy(), want)
 
 
-@pytest.mark.parametrize("variant", [1, 2, 3, 4])
+@pytest.mark.parametrize("variant", [1, 2, 3, 4, 5, 6])
 def test_split_long_k_integer_exact(a4, variant):
     # K per destination row = 16 * 48^2 = 36864 (several exact flush chunks,
     # several levels' chunk sizes) with 2 slices on integer data
@@ -168,8 +168,11 @@ def test_split_count_autotune_keeps_results_exact(a4):
     R, V, T, trip, labels = _make(a4, "ladder", [48] * 4, [8], 0.0, 4, integer=True)
     b = _run(a4, R, trip, labels, a4.device.PREC_OZAKI_BF16, slices=2)
     sp = b.splits()
-    assert sp["nsplit"] in sp["tuned_ms"], sp
-    assert all(v > 0 for v in sp["tuned_ms"].values()), sp
+    if b.form()["form"] <= 4:
+        assert sp["nsplit"] in sp["tuned_ms"], sp
+        assert all(v > 0 for v in sp["tuned_ms"].values()), sp
+    else:  # a direct form won: one split, nothing to tune
+        assert sp == {"nsplit": 1, "tuned_ms": {}}, sp
     ref = _reference(R, trip, labels)
     for k, want in ref.items():
         np.testing.assert_array_equal(R.block(k).cpu().numpy(), want)
@@ -185,6 +188,79 @@ def test_split_ladder_outliers(a4, slices, tol):
     _run(a4, R, trip, labels, a4.device.PREC_OZAKI_BF16, slices=slices, variant=1 + slices % 4)
     errs = _errors(R, _reference(R, trip, labels))
     assert errs.max() <= tol, (slices, errs.max())
+
+
+def _bits(t):
+    import torch
+
+    return t.clone().view(torch.int64)
+
+
+@pytest.mark.parametrize("variant", [5, 6])
+def test_direct_forms_bit_identical_to_workspace_forms(a4, variant):
+    """The direct forms fold a tile's levels exactly in TMEM and store FP64
+    from the GEMM's epilogue; they must give the bits of the workspace +
+    recombine form with the same tile shape: the ladder with outliers at 5
+    slices, then the accumulate and negate modes on an uneven sparse ring."""
+    import torch
+
+    R, V, T, trip, labels = _make(a4, "ladder", [32, 32], [16, 16], 0.0, 5, outliers=True)
+    ws_form = _run(a4, R, trip, labels, a4.device.PREC_OZAKI_BF16, slices=5, variant=variant - 4)
+    want = _bits(R.buf)
+    R.buf.fill_(float("nan"))
+    direct = _run(a4, R, trip, labels, a4.device.PREC_OZAKI_BF16, slices=5, variant=variant)
+    assert direct.form()["form"] == variant
+    assert direct.launches()["kernels_per_run"] == ws_form.launches()["kernels_per_run"] - 1
+    assert direct.splits()["nsplit"] == 1
+    assert torch.equal(_bits(R.buf), want)
+    assert _errors(R, _reference(R, trip, labels)).max() <= TOL_SPLIT
+
+    R, V, T, trip, labels = _make(a4, "ring", [12, 16, 24, 32], [5, 8], 0.3, 6)
+    base = torch.randn(R.buf.numel(), dtype=torch.float64, device=R.buf.device)
+    outs = []
+    for v in (variant - 4, variant):
+        R.buf.copy_(base)
+        b = a4.device.Batch(_ptrn(labels), 4, 4, 4, trip, precision=a4.device.PREC_OZAKI_BF16, slices=5,
+                            beta=1, negate=True, variant=v)
+        b.run_graph()
+        a4.device.sync()
+        torch.cuda.synchronize()
+        outs.append(_bits(R.buf))
+    assert torch.equal(outs[0], outs[1])
+    ref = _reference(R, trip, labels)
+    for k, w in ref.items():
+        got = R.block(k).cpu().numpy()
+        want2 = base[R.offsets[k]:R.offsets[k] + w.size].cpu().numpy() - w
+        assert np.linalg.norm(got - want2) <= TOL_SPLIT * np.linalg.norm(want2)
+
+
+@pytest.mark.parametrize("variant", [0, 1, 4, 5, 6])
+def test_destination_unit_stride_on_the_right_operand(a4, variant):
+    """D(a,b) = sum_k L(b,k) R(k,a): D's unit-stride index comes from the
+    right operand, so the split form multiplies with the operands' roles
+    exchanged.  Integer data with 2 slices is exact; several tiles, ragged
+    edges, three pairs per destination block."""
+    import torch
+
+    rng = np.random.default_rng(77)
+    dl, ll, rl = [1, 2], [2, 3], [3, 1]
+    de, le, re = [300, 261], [261, 45], [45, 300]
+    ierr, p = oracle.get_contraction_ptrn(2, 2, 2, dl + ll + rl)
+    assert ierr == 0
+    Ls = [rng.integers(-127, 128, int(np.prod(le))).astype(np.float64) for _ in range(3)]
+    Rs = [rng.integers(-127, 128, int(np.prod(re))).astype(np.float64) for _ in range(3)]
+    D = torch.full((int(np.prod(de)),), float("nan"), dtype=torch.float64, device="cuda")
+    tl = [torch.tensor(x, device="cuda") for x in Ls]
+    tr = [torch.tensor(x, device="cuda") for x in Rs]
+    trip = [(D, tl[q], tr[q], de, le, re) for q in range(3)]
+    b = a4.device.Batch(p, 2, 2, 2, trip, precision=a4.device.PREC_OZAKI_BF16, slices=2, variant=variant)
+    b.run()
+    a4.device.sync()
+    torch.cuda.synchronize()
+    if variant:
+        assert b.form()["form"] == variant
+    want = sum(oracle.contract_blas(p, Ls[q], le, Rs[q], re, de) for q in range(3))
+    np.testing.assert_array_equal(D.cpu().numpy(), want)
 
 
 def test_split_uneven_sparse_ring_graph_and_beta(a4):
