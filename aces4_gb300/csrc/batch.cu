@@ -677,7 +677,7 @@ int build_ozaki(a4g_batch* b, const std::vector<DGroup>& groups, const std::vect
         if (!(rc = time_form(gf, a2, grid2, &ms2))) {
           b->split_candidates[1] = ns2;
           b->split_cost_ms[1] = ms2;
-          if (ms2 < b->split_cost_ms[0]) {
+          if (ms2 < 0.97f * b->split_cost_ms[0]) {  // a clear win only: one timed run each is noisy
             // the other forms are not run any more: their units and the
             // shared workspace go
             for (int f = 0; f < a4g_batch::kForms; ++f)

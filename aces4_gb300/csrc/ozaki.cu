@@ -452,13 +452,16 @@ __device__ __forceinline__ void tc_ld8_nowait(uint32_t taddr, uint32_t (&r)[8]) 
                : "r"(taddr));
 }
 
-// v * 2^e2 rounded once to the nearest double (ties to even), v a signed
-// 64-bit integer: normalise, keep 53 bits, round on the 11 below, and build
-// the bits by one addition (a mantissa that rounds up to 2^53 carries into
-// the exponent field).  Branch-free for results in the normal range; the
-// rest takes u64_scaled_to_double.  Same result as u64_scaled_to_double.
-__device__ __forceinline__ double i64_scaled_to_double(long long v, int e2) {
-  if (v == 0) return 0.0;
+// (neg ? -1 : 1) * v * 2^e2 rounded once to the nearest double (ties to
+// even), v a signed 64-bit integer: normalise, keep 53 bits, round on the 11
+// below, and build the bits by one addition (a mantissa that rounds up to
+// 2^53 carries into the exponent field).  Integer operations only (the FP64
+// pipe is scarce), branch-free for results in the normal range; the rest
+// takes u64_scaled_to_double.  Same bits as negating the result of
+// u64_scaled_to_double (a zero keeps the sign the negation gives it).
+__device__ __forceinline__ double i64_scaled_to_double(long long v, int e2, bool neg) {
+  const unsigned long long sign = (v < 0) != neg ? (1ull << 63) : 0ull;
+  if (v == 0) return __longlong_as_double((long long)(neg ? (1ull << 63) : 0ull));
   const unsigned long long u = v < 0 ? (unsigned long long)(-v) : (unsigned long long)v;
   const int n = __clzll((long long)u);
   const unsigned long long norm = u << n;  // leading one at bit 63
@@ -466,9 +469,8 @@ __device__ __forceinline__ double i64_scaled_to_double(long long v, int e2) {
   const unsigned long long rem = norm & 0x7FFull;
   mant += (rem > 0x400ull || (rem == 0x400ull && (mant & 1ull))) ? 1ull : 0ull;
   const int field = e2 + 63 - n + 1023;  // biased exponent of the leading one
-  if (field < 1 || field > 2045) return u64_scaled_to_double(u, v < 0, e2);
-  return __longlong_as_double(
-      (long long)(((unsigned long long)v & (1ull << 63)) | ((((unsigned long long)(field - 1)) << 52) + mant)));
+  if (field < 1 || field > 2045) return u64_scaled_to_double(u, sign != 0, e2);
+  return __longlong_as_double((long long)(sign | ((((unsigned long long)(field - 1)) << 52) + mant)));
 }
 
 // Direct form: what a thread needs to store its part of a tile (its row,
@@ -557,8 +559,7 @@ __device__ __forceinline__ void store_direct(const OzGemmArgs& a, const DirectTi
     for (int j = 0; j < 8; ++j) {
       const DirectCol c = t.cols[8 * p + j];
       const long long v = (long long)(((unsigned long long)w1[j] << 32) | w0[j]);
-      double x = i64_scaled_to_double(v, t.ebase + c.F);
-      if (a.mode & 2) x = -x;
+      const double x = i64_scaled_to_double(v, t.ebase + c.F, a.mode & 2);
       if (t.mlive && c.off >= 0) t.drow[c.off] = acc ? dc[j] + x : x;
     }
   }
