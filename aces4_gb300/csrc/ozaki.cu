@@ -461,16 +461,17 @@ __device__ __forceinline__ void tc_ld8_nowait(uint32_t taddr, uint32_t (&r)[8]) 
 // u64_scaled_to_double (a zero keeps the sign the negation gives it).
 __device__ __forceinline__ double i64_scaled_to_double(long long v, int e2, bool neg) {
   const unsigned long long sign = (v < 0) != neg ? (1ull << 63) : 0ull;
-  if (v == 0) return __longlong_as_double((long long)(neg ? (1ull << 63) : 0ull));
   const unsigned long long u = v < 0 ? (unsigned long long)(-v) : (unsigned long long)v;
-  const int n = __clzll((long long)u);
+  const int n = __clzll((long long)(u | 1ull));  // u = 0 is mapped to a signed zero at the end
   const unsigned long long norm = u << n;  // leading one at bit 63
   unsigned long long mant = norm >> 11;    // 53 bits, leading one at bit 52
   const unsigned long long rem = norm & 0x7FFull;
   mant += (rem > 0x400ull || (rem == 0x400ull && (mant & 1ull))) ? 1ull : 0ull;
   const int field = e2 + 63 - n + 1023;  // biased exponent of the leading one
-  if (field < 1 || field > 2045) return u64_scaled_to_double(u, sign != 0, e2);
-  return __longlong_as_double((long long)(sign | ((((unsigned long long)(field - 1)) << 52) + mant)));
+  if (u != 0 && (field < 1 || field > 2045)) return u64_scaled_to_double(u, sign != 0, e2);
+  const unsigned long long bits = u ? sign | ((((unsigned long long)(field - 1)) << 52) + mant)
+                                    : (neg ? (1ull << 63) : 0ull);
+  return __longlong_as_double((long long)bits);
 }
 
 // Direct form: what a thread needs to store its part of a tile (its row,
@@ -615,7 +616,7 @@ __device__ void epilogue(const OzGemmArgs& a, OzSmemT<PAIR, 128>& sm, uint32_t t
         if (!mbar_wait(&sm.acc_full[buf], (chunk >> 1) & 1, sm, a.err_flag, 4)) return false;
         tc_fence_after();
         const bool fresh = c == 0 && un.level == 0;  // no running sum yet
-        const uint32_t sh = c == 0 ? 8u : 0u;        // a new level: running sum * 256
+        const uint32_t mul = c == 0 ? 256u : 1u;     // a new level: running sum * 256
         const bool final = last_level && c == nchunks - 1;
 #pragma unroll 1
         for (int g = 0; g < 4; ++g) {
@@ -631,10 +632,13 @@ __device__ void epilogue(const OzGemmArgs& a, OzSmemT<PAIR, 128>& sm, uint32_t t
           tc_wait_ld();
 #pragma unroll
           for (int j = 0; j < 8; ++j) {
-            unsigned long long v = ((unsigned long long)w1[j] << 32) | w0[j];
-            v = (v << sh) + (unsigned long long)(long long)__float2int_rz(__uint_as_float(x[j]));  // exact
-            w0[j] = uint32_t(v);
-            w1[j] = uint32_t(v >> 32);
+            // (w1:w0) * mul + x modulo 2^64 in 32-bit multiply-adds (x is an
+            // integer below 2^24, exact in FP32): low word with its carry, then
+            // the high word
+            const unsigned long long lo =
+                (unsigned long long)w0[j] * mul + (unsigned long long)(long long)__float2int_rz(__uint_as_float(x[j]));
+            w0[j] = uint32_t(lo);
+            w1[j] = w1[j] * mul + uint32_t(lo >> 32);
           }
           tc_st8(lane_addr + kTmemW0 + 8 * g, w0);
           tc_st8(lane_addr + kTmemW1 + 8 * g, w1);
