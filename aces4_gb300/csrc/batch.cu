@@ -587,24 +587,34 @@ int build_ozaki(a4g_batch* b, const std::vector<DGroup>& groups, const std::vect
   if (!b->variant) {
     // Autotune on this batch's own panels: each form's GEMM and, for the
     // workspace forms, the recombine after it, timed once after one untimed
-    // run, storing into a scratch destination (every destination block's
-    // tables pointed at one buffer of the largest block's size) so that the
-    // caller's blocks stay untouched; the lowest time wins.  Then the chosen
+    // run, storing into scratch destination blocks so that the caller's
+    // blocks stay untouched; the lowest time wins.  Then the chosen
     // workspace form's split-K count is timed against its double.  If the
     // scratch cannot be had, direct forms run without their stores and the
     // traffic left out is added at the copy rate.
-    size_t d_max = 0;
+    size_t d_max = 0, d_total = 0;
     double d_bytes = 0.0;
     for (const OzTile& di : dinfo) {
       d_max = std::max(d_max, size_t(di.m0) * size_t(di.n0));
+      d_total += size_t(di.m0) * size_t(di.n0);
       d_bytes += double(di.m0) * di.n0 * sizeof(double) * (b->beta ? 2 : 1);
     }
     const double ms_per_byte = 1.0 / 6.5e9;  // ~ the measured copy rate, bytes per ms
+    // One scratch block per destination block (the real store pattern and
+    // footprint) when a quarter of the free memory holds them, else one
+    // shared block of the largest size.
+    size_t free_b = 0, total_b = 0;
+    const bool spread = cudaMemGetInfo(&free_b, &total_b) == cudaSuccess && d_total * sizeof(double) <= free_b / 4;
+    cudaGetLastError();
     double* scratch = nullptr;
     OzDBlock* sdb = nullptr;
-    if (cudaMalloc(&scratch, std::max<size_t>(d_max, 1) * sizeof(double)) == cudaSuccess) {
+    if (cudaMalloc(&scratch, std::max<size_t>(spread ? d_total : d_max, 1) * sizeof(double)) == cudaSuccess) {
       std::vector<OzDBlock> hs = dblocks;
-      for (OzDBlock& x : hs) x.d = scratch;
+      size_t off = 0;
+      for (size_t i = 0; i < hs.size(); ++i) {
+        hs[i].d = scratch + (spread ? off : 0);
+        off += size_t(dinfo[i].m0) * size_t(dinfo[i].n0);
+      }
       if (cudaMalloc(&sdb, hs.size() * sizeof(OzDBlock)) != cudaSuccess ||
           cudaMemcpy(sdb, hs.data(), hs.size() * sizeof(OzDBlock), cudaMemcpyHostToDevice) != cudaSuccess) {
         cudaFree(sdb);

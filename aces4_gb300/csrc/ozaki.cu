@@ -1223,7 +1223,7 @@ __global__ void __launch_bounds__(256) oz_recombine_kernel(const OzTile* __restr
           long long acc = 0;
 #pragma unroll
           for (int lv = 0; lv < S; ++lv) acc += lev[p][lv] * (1ll << (kDigitBits * (S - 1 - lv)));
-          v = u64_scaled_to_double(acc < 0 ? (unsigned long long)(-acc) : (unsigned long long)acc, acc < 0, e2);
+          v = i64_scaled_to_double(acc, e2, false);
         } else {
           unsigned __int128 acc = 0;  // two's complement, wrapping (exact: |sum| < 2^101)
 #pragma unroll
@@ -1338,8 +1338,11 @@ __global__ void __launch_bounds__(1024, 1) oz_recombine_bulk_kernel(const OzTile
     const int* ea = pa[tl.panel_a].exps;
     const int* eb = pb[tl.panel_b].exps;
     const int sc = pc * cols_pp;
+    constexpr int kPerT = kRecPiece / 1024;
+    double vals[kPerT];
+    double* dsts[kPerT];
 #pragma unroll
-    for (int p = 0; p < kRecPiece / 1024; ++p) {
+    for (int p = 0; p < kPerT; ++p) {
       const int e = p * 1024 + threadIdx.x;
       const int row = e & (rows - 1), cl = e >> log_rows;
       const int m = tl.m0 + row, n = tl.n0 + sc + cl;
@@ -1351,15 +1354,20 @@ __global__ void __launch_bounds__(1024, 1) oz_recombine_bulk_kernel(const OzTile
         long long acc = 0;  // a unit's level-t sum is below (t+1) 2^31 / S: the 64-bit sum is exact
 #pragma unroll
         for (int lv = 0; lv < S; ++lv) acc += (long long)sm.lev[st][lv][e] * (1ll << (kDigitBits * (S - 1 - lv)));
-        v = u64_scaled_to_double(acc < 0 ? (unsigned long long)(-acc) : (unsigned long long)acc, acc < 0, e2);
-        if (mode & 2) v = -v;
+        v = i64_scaled_to_double(acc, e2, mode & 2);  // negated term: the sign folded into the rounding
       }
-      if (db.col_fast) {
-        sm.val[cl * (rows + 1) + row] = v;
-      } else if (live) {
-        double* dst = db.d + pl.offDm[m] + pl.offDn[n];
-        *dst = (mode & 1) ? *dst + v : v;
-      }
+      vals[p] = v;
+      dsts[p] = nullptr;
+      if (db.col_fast) sm.val[cl * (rows + 1) + row] = v;
+      else if (live) dsts[p] = db.d + pl.offDm[m] + pl.offDn[n];
+    }
+    if (!db.col_fast) {
+      double old[kPerT];  // accumulate mode: the old values' loads in flight together
+#pragma unroll
+      for (int p = 0; p < kPerT; ++p) old[p] = (dsts[p] && (mode & 1)) ? *dsts[p] : 0.0;
+#pragma unroll
+      for (int p = 0; p < kPerT; ++p)
+        if (dsts[p]) *dsts[p] = (mode & 1) ? old[p] + vals[p] : vals[p];
     }
     if (db.col_fast) {
       __syncthreads();

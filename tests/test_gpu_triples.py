@@ -89,7 +89,7 @@ def _triples_problem(o_segs, v_segs, seed):
     return V1, V2, T, e, fock
 
 
-def _run_step(a4, V1, V2, T, o_segs, v_segs, a, b, precision, fock_t):
+def _run_step(a4, V1, V2, T, o_segs, v_segs, a, b, precision, fock_t, variant=0):
     import torch
 
     from aces4_gb300.blocks import (TRIPLES_TERM1_LABELS, TRIPLES_TERM2_LABELS, BlockArray,
@@ -100,7 +100,7 @@ def _run_step(a4, V1, V2, T, o_segs, v_segs, a, b, precision, fock_t):
     t1, t2 = triples_step(W, V1, V2, T, a, b)
     p1 = oracle.get_contraction_ptrn(6, 4, 4, sum(TRIPLES_TERM1_LABELS, []))[1]
     p2 = oracle.get_contraction_ptrn(6, 4, 4, sum(TRIPLES_TERM2_LABELS, []))[1]
-    kw = dict(precision=precision, slices=5)
+    kw = dict(precision=precision, slices=5, variant=variant)
     b1 = a4.device.Batch(p1, 6, 4, 4, t1, **kw)
     b2 = a4.device.Batch(p2, 6, 4, 4, t2, beta=1, negate=True, **kw)
     b1.run()
@@ -154,6 +154,26 @@ def test_triples_step_small_vs_oracle(a4):
     assert abs(E64 - E_ref) <= 1e-12 * abs(E_ref)
     assert abs(Esp - E_ref) <= 1e-10 * abs(E_ref)
     assert abs(flops - 2 * 24 * 12 * 12 * 6 ** 3 * (24 + 6)) < 1  # 2 v_a v_b v o^3 (v + o) for this step
+
+
+def test_triples_step_every_form_gives_the_same_bits(a4):
+    """o=8, v=48 (3 x 16): the two terms through each tensor-core form (the
+    workspace forms and the direct ones, W unit-stride on the right operand so
+    both batches run with the operands' roles exchanged) give identical W."""
+    import torch
+
+    o_segs, v_segs = [8], [16, 16, 16]
+    V1, V2, T, e, fock = _triples_problem(o_segs, v_segs, 13)
+    ft = torch.tensor(fock, device="cuda")
+    ref = None
+    for variant in range(1, 7):
+        W, E, _, _ = _run_step(a4, V1, V2, T, o_segs, v_segs, 1, 2, a4.device.PREC_OZAKI_BF16, ft, variant)
+        bits = W.buf.clone().view(torch.int64)
+        if ref is None:
+            ref, E_ref = bits, E
+        else:
+            assert torch.equal(bits, ref), variant
+            assert E == E_ref, variant
 
 
 def test_triples_full_size_step(a4):
