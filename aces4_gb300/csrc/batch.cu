@@ -585,6 +585,30 @@ int build_ozaki(a4g_batch* b, const std::vector<DGroup>& groups, const std::vect
     if (b->forms[f].built && (b->form < 0 || b->variant == f + 1)) b->form = f;
   if (b->form < 0) return fail(A4G_ERR_UNSUPPORTED, "no tensor-core GEMM form fits this GPU");
   if (!b->variant) {
+    // The panels hold the operands' digits during the autotune: the tensor
+    // cores draw far less power on zero panels and would run at clocks the
+    // real step does not get.  So the exponent and split passes run once here
+    // (on the blocks' contents at creation; every run repeats them).
+    for (int side = 0; side < 2 && !rc; ++side)
+      for (int lay = 0; lay < 3 && !rc; ++lay) rc = add_jobset(side == 0, lay, 0, host_jobs[side][lay]);
+    if (!rc) {
+      cudaStream_t s = ctx()->stream;
+      A4G_CUDA(cudaMemsetAsync(b->d_exps, 0, b->exps_bytes, s));
+      for (const auto& js : b->jobsets)
+        if (!rc) rc = oz_launch_exp(js.layout, js.d_jobs, js.d_prefix_exp, js.njobs, js.tiles_exp,
+                                    js.left ? b->d_pa : b->d_pb, s);
+      for (const auto& js : b->jobsets)
+        if (!rc) rc = oz_launch_split(js.layout, js.d_jobs, js.d_prefix_split, js.njobs, js.tiles_split,
+                                      js.left ? b->d_pa : b->d_pb, S, s);
+      if (!rc) rc = check_device_flag(s);
+    }
+    for (const auto& js : b->jobsets) {
+      release(b, js.d_jobs, size_t(js.njobs) * sizeof(OzSplitJob));
+      release(b, js.d_prefix_exp, size_t(js.njobs + 1) * sizeof(int64_t));
+      release(b, js.d_prefix_split, size_t(js.njobs + 1) * sizeof(int64_t));
+    }
+    b->jobsets.clear();
+    if (rc) return rc;
     // Autotune on this batch's own panels: each form's GEMM and, for the
     // workspace forms, the recombine after it, timed once after one untimed
     // run, storing into scratch destination blocks so that the caller's

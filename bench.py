@@ -449,8 +449,16 @@ def run_config(args, world, rank, local):
             b.run_graph(stream)
         e1.record(stream)
         torch.cuda.synchronize()
+        phases = None
+        if prec:  # per-phase CUDA-event times of a few eager runs (after the graph timing)
+            b.timings()
+            for _ in range(3):
+                b.run_timed(stream)
+            t = b.timings()
+            phases = {k: t[k] / max(1, t["runs"]) for k in b.PHASES}
         res[prec] = {"ms": e0.elapsed_time(e1) / steps, "out": R.buf.clone(), "info": b.info(),
-                     "form": b.form() if prec else None, "launches": b.launches()}
+                     "form": b.form() if prec else None, "launches": b.launches(), "phases": phases,
+                     "splits": b.splits() if prec else None}
         b.close()
     sp, fp = res[a4.device.PREC_OZAKI_BF16], res[a4.device.PREC_FP64]
     errs = []
@@ -468,7 +476,9 @@ def run_config(args, world, rank, local):
                        "graph": True},
             "fp64_plain": {"value": flops / (fp["ms"] * 1e-3) / 1e12, "unit": "TFLOP/s", "ms_per_step": fp["ms"]},
             "split_over_fp64": fp["ms"] / sp["ms"], "rel_err_max_block_vs_fp64_gpu": max(errs),
-            "gemm_form": {"chosen": sp["form"]["name"], "autotune_ms": sp["form"]["tuned_ms"]},
+            "gemm_form": {"chosen": sp["form"]["name"], "autotune_ms": sp["form"]["tuned_ms"],
+                          "split_k": sp["splits"]},
+            "phases_ms_per_step": sp["phases"],
             "gpu_launches": sp["launches"]["kernels_per_run"] * args.steps,
         }), flush=True)
 
