@@ -48,6 +48,7 @@ struct a4g_batch {
   // split precision
   OzPanel* d_pa = nullptr;
   OzPanel* d_pb = nullptr;
+  OzPanel* d_pb_view = nullptr;  // the split kernels' views of the B panels (stacked panels: one per member)
   int* d_exps = nullptr;
   size_t exps_bytes = 0;
   // split jobs grouped by operand side (A: left blocks, B: right blocks) and
@@ -195,6 +196,10 @@ struct PanelBuild {
   std::set<const double*> pad_before, pad_after;  // stretch starts / ends (A panels)
   int rows = 0;
   int64_t kpad = 0;
+  // A stacked B panel: the rows of other panels (first row, panel index) one
+  // after another, each with its own blocks at its own k offsets.
+  std::vector<std::pair<int, int>> members;
+  bool used = true;  // some tile reads it (stacked member panels are not read themselves)
 };
 
 // (Re)assign the k offsets of a panel's blocks in panel order.
@@ -333,22 +338,97 @@ int build_ozaki(a4g_batch* b, const std::vector<DGroup>& groups, const std::vect
     if (changed)
       for (auto& p : pa) layout_panel(p, plans);
   }
+  // Stacks: destination blocks whose pairs multiply the same left blocks at
+  // the same k positions of one A panel, whose B panels lay their pairs out
+  // alike, and whose rows are addressed alike (equal offDm) are laid side by
+  // side along n: one tile grid over all their columns, so that only the
+  // stack's last tile column is ragged instead of every block's (the ring's
+  // 480..800-column blocks left ~30 % of the 256-column tiles empty).
+  std::map<std::vector<int64_t>, int> offdm_ids;
+  std::map<std::vector<int64_t>, int> stack_index;
+  std::vector<std::vector<int>> stacks;
   for (size_t gi = 0; gi < groups.size(); ++gi) {
     const DGroup& g = groups[gi];
     const GemmPlan& h = plans[g.plan]->host;
-    const int a = ga[gi], c = gb[gi];
+    const int od = offdm_ids.emplace(h.offDm, int(offdm_ids.size())).first->second;
+    std::vector<int64_t> sig = {ga[gi], h.M, od, pb[gb[gi]].kpad};
+    for (const Pair& p : g.pairs) {
+      sig.push_back(int64_t(reinterpret_cast<uintptr_t>(p.l)));
+      sig.push_back(plans[p.plan]->host.K);
+      sig.push_back(pa[ga[gi]].koff.at(p.l));
+      sig.push_back(pb[gb[gi]].koff.at(p.r));
+    }
+    auto it = stack_index.find(sig);
+    if (it == stack_index.end()) {
+      stack_index.emplace(sig, int(stacks.size()));
+      stacks.push_back({int(gi)});
+    } else {
+      stacks[it->second].push_back(int(gi));
+    }
+  }
+  for (auto& p : pb) p.used = false;
+  std::map<std::vector<int>, int> stacked_index;  // member panels -> stacked panel
+  std::vector<double*> colptr_host;  // every destination's column bases, concatenated
+  std::vector<size_t> colptr_at;
+  for (const std::vector<int>& st : stacks) {
+    const int g0 = st[0];
+    const DGroup& g = groups[g0];
+    const GemmPlan& h = plans[g.plan]->host;
+    const int a = ga[g0];
+    int c = gb[g0];
+    int64_t ncols = 0;
+    colptr_at.push_back(colptr_host.size());
+    for (int gm : st) {
+      const GemmPlan& hm = plans[groups[gm].plan]->host;
+      for (int64_t n = 0; n < hm.N; ++n) colptr_host.push_back(groups[gm].d + hm.offDn[n]);
+      ncols += hm.N;
+    }
+    if (ncols > 0x7fffffffLL) return fail(A4G_ERR_RANGE, "stacked destination too wide");
+    if (st.size() > 1) {
+      // stacks over the same member panels (the ring: every (a,i) row block
+      // over all (b,j) columns) share one stacked panel, split once
+      std::vector<int> key;
+      for (int gm : st) key.push_back(gb[gm]);
+      auto it = stacked_index.find(key);
+      if (it != stacked_index.end()) {
+        c = it->second;
+      } else {
+        PanelBuild sp;
+        sp.rows = int(ncols);
+        sp.kpad = pb[c].kpad;
+        int row0 = 0;
+        for (int gm : st) {
+          sp.members.push_back({row0, gb[gm]});
+          row0 += pb[gb[gm]].rows;
+        }
+        pb.push_back(sp);
+        c = int(pb.size()) - 1;
+        stacked_index.emplace(key, c);
+      }
+    }
+    pb[c].used = true;
     const int db = int(dblocks.size());
     const bool col_fast = h.N > 1 && h.offDn[1] - h.offDn[0] == 1 && !(h.M > 1 && h.offDm[1] - h.offDm[0] == 1);
-    dblocks.push_back({g.d, g.plan, a, c, col_fast ? 1 : 0});
+    OzDBlock od{};
+    od.d = g.d, od.plan = g.plan, od.panel_a = a, od.panel_b = c, od.col_fast = col_fast ? 1 : 0;
+    od.M = int(h.M), od.N = int(ncols);
+    od.rowoff = plans[g.plan]->offDm;
+    dblocks.push_back(od);
     const int tb = int(trips.size());
     int kb_total = 0;
-    for_stretches(g, pa[a], pb[c], plans, [&](int, int, int64_t ka, int64_t kbo, int64_t kk) {
+    for_stretches(g, pa[a], pb[gb[g0]], plans, [&](int, int, int64_t ka, int64_t kbo, int64_t kk) {
       const int nkb = int(ceil_to(kk, kOzBK) / kOzBK);
       trips.push_back({ka, kbo, nkb, 0});
       kb_total += nkb;
     });
     const int te = int(trips.size());
-    dinfo.push_back({db, int(h.M), int(h.N), a, c, tb, te, kb_total});
+    dinfo.push_back({db, int(h.M), int(ncols), a, c, tb, te, kb_total});
+  }
+  {
+    double** d_colptr = nullptr;
+    int r = upload(b, colptr_host, &d_colptr);
+    if (r) return r;
+    for (size_t i = 0; i < dblocks.size(); ++i) dblocks[i].colptr = d_colptr + colptr_at[i];
   }
   const int S = b->slices;
   int rc0 = oz_prepare();
@@ -360,7 +440,8 @@ int build_ozaki(a4g_batch* b, const std::vector<DGroup>& groups, const std::vect
   std::vector<MapBytes> maps_a(pa.size()), maps_b64(pb.size()), maps_b128(pb.size()), maps_b256(pb.size());
   size_t exps_total = 0;
   for (auto& p : pa) exps_total += ceil_to(p.rows, 2 * kOzBM);
-  for (auto& p : pb) exps_total += ceil_to(p.rows, 2 * kOzBN);
+  for (auto& p : pb)
+    if (p.used) exps_total += ceil_to(p.rows, 2 * kOzBN);
   void* exps = nullptr;
   int rc = device_alloc(b, exps_total * sizeof(int), &exps, true);
   if (rc) return rc;
@@ -372,6 +453,10 @@ int build_ozaki(a4g_batch* b, const std::vector<DGroup>& groups, const std::vect
                          std::vector<MapBytes>* maps2, std::vector<MapBytes>* maps3, int rows_tile) -> int {
     for (size_t i = 0; i < src.size(); ++i) {
       OzPanel p{};
+      if (!src[i].used) {  // read by no tile: no memory, no tensor map
+        dst.push_back(p);
+        continue;
+      }
       p.rows = src[i].rows;
       p.rows_pad = int(ceil_to(src[i].rows, rows_tile));
       p.kpad = src[i].kpad;
@@ -410,12 +495,17 @@ int build_ozaki(a4g_batch* b, const std::vector<DGroup>& groups, const std::vect
     return rm ? int(kOzRowsMajor) : km ? int(kOzKMajor) : int(kOzGeneric);
   };
   std::vector<OzSplitJob> host_jobs[2][3];  // [side][layout]
+  // The split kernels see B panels through views: a plain panel as it is, a
+  // stacked one as one view per member (base and exponents moved down to the
+  // member's first row; the slice stride stays the stacked panel's).
+  std::vector<OzPanel> hpb_view;
+  std::vector<int> view_full;
   for (int side = 0; side < 2; ++side) {
     const bool left = side == 0;
     std::vector<PanelBuild>& src = left ? pa : pb;
-    for (size_t pi = 0; pi < src.size(); ++pi)
-      for (auto& kv : src[pi].koff) {
-        const DevPlan* dp = plans[src[pi].plan.at(kv.first)];
+    auto add_jobs = [&](const PanelBuild& blocks, int panel_index) {
+      for (auto& kv : blocks.koff) {
+        const DevPlan* dp = plans[blocks.plan.at(kv.first)];
         OzSplitJob j{};
         j.src = kv.first;
         j.offRow = left ? dp->offLm : dp->offRn;
@@ -423,12 +513,33 @@ int build_ozaki(a4g_batch* b, const std::vector<DGroup>& groups, const std::vect
         j.rows = int(left ? dp->host.M : dp->host.N);
         j.K = int(dp->host.K);
         j.kfast = left ? dp->host.a_kfast : dp->host.b_kfast;
-        j.panel = int(pi);
+        j.panel = panel_index;
         j.koff = kv.second;
         int lay = layout_of(dp, left);
         if ((reinterpret_cast<uintptr_t>(kv.first) & 15) != 0) lay = kOzGeneric;  // vector loads need 16 B
         host_jobs[side][lay].push_back(j);
       }
+    };
+    for (size_t pi = 0; pi < src.size(); ++pi) {
+      if (!src[pi].used) continue;
+      if (left) {
+        add_jobs(src[pi], int(pi));
+      } else if (src[pi].members.empty()) {
+        hpb_view.push_back(hpb[pi]);
+        view_full.push_back(int(pi));
+        add_jobs(src[pi], int(hpb_view.size()) - 1);
+      } else {
+        for (const auto& mem : src[pi].members) {
+          OzPanel v = hpb[pi];
+          v.base += size_t(mem.first) * size_t(v.kpad);
+          v.exps += mem.first;
+          v.rows = pb[mem.second].rows;
+          hpb_view.push_back(v);
+          view_full.push_back(int(pi));
+          add_jobs(pb[mem.second], int(hpb_view.size()) - 1);
+        }
+      }
+    }
   }
   auto add_jobset = [&](bool left, int lay, int group, const std::vector<OzSplitJob>& jobs) -> int {
     if (jobs.empty()) return A4G_OK;
@@ -463,7 +574,7 @@ int build_ozaki(a4g_batch* b, const std::vector<DGroup>& groups, const std::vect
   A4G_CUDA(cudaMemcpy(dmaps_b256, maps_b256.data(), mbytes_b, cudaMemcpyHostToDevice));
   OzTrip* d_trips = nullptr;
   if ((rc = upload(b, hpa, &b->d_pa)) || (rc = upload(b, hpb, &b->d_pb)) || (rc = upload(b, trips, &d_trips)) ||
-      (rc = upload(b, dblocks, &b->d_dblocks)))
+      (rc = upload(b, dblocks, &b->d_dblocks)) || (rc = upload(b, hpb_view, &b->d_pb_view)))
     return rc;
   for (int t = 0; t < S; ++t)
     if (oz_chunk_kb(t) < 1) return fail(A4G_ERR_ARG, "slice count too large for exact accumulation");
@@ -596,10 +707,10 @@ int build_ozaki(a4g_batch* b, const std::vector<DGroup>& groups, const std::vect
       A4G_CUDA(cudaMemsetAsync(b->d_exps, 0, b->exps_bytes, s));
       for (const auto& js : b->jobsets)
         if (!rc) rc = oz_launch_exp(js.layout, js.d_jobs, js.d_prefix_exp, js.njobs, js.tiles_exp,
-                                    js.left ? b->d_pa : b->d_pb, s);
+                                    js.left ? b->d_pa : b->d_pb_view, s);
       for (const auto& js : b->jobsets)
         if (!rc) rc = oz_launch_split(js.layout, js.d_jobs, js.d_prefix_split, js.njobs, js.tiles_split,
-                                      js.left ? b->d_pa : b->d_pb, S, s);
+                                      js.left ? b->d_pa : b->d_pb_view, S, s);
       if (!rc) rc = check_device_flag(s);
     }
     for (const auto& js : b->jobsets) {
@@ -618,32 +729,44 @@ int build_ozaki(a4g_batch* b, const std::vector<DGroup>& groups, const std::vect
     // traffic left out is added at the copy rate.
     size_t d_max = 0, d_total = 0;
     double d_bytes = 0.0;
-    for (const OzTile& di : dinfo) {
-      d_max = std::max(d_max, size_t(di.m0) * size_t(di.n0));
-      d_total += size_t(di.m0) * size_t(di.n0);
-      d_bytes += double(di.m0) * di.n0 * sizeof(double) * (b->beta ? 2 : 1);
+    for (const DGroup& g : groups) {
+      const GemmPlan& h = plans[g.plan]->host;
+      d_max = std::max(d_max, size_t(h.M) * size_t(h.N));
+      d_total += size_t(h.M) * size_t(h.N);
+      d_bytes += double(h.M) * double(h.N) * sizeof(double) * (b->beta ? 2 : 1);
     }
     const double ms_per_byte = 1.0 / 6.5e9;  // ~ the measured copy rate, bytes per ms
     // One scratch block per destination block (the real store pattern and
     // footprint) when a quarter of the free memory holds them, else one
-    // shared block of the largest size.
+    // shared block of the largest size; the column bases point into them.
     size_t free_b = 0, total_b = 0;
     const bool spread = cudaMemGetInfo(&free_b, &total_b) == cudaSuccess && d_total * sizeof(double) <= free_b / 4;
     cudaGetLastError();
     double* scratch = nullptr;
     OzDBlock* sdb = nullptr;
+    double** scols = nullptr;
     if (cudaMalloc(&scratch, std::max<size_t>(spread ? d_total : d_max, 1) * sizeof(double)) == cudaSuccess) {
-      std::vector<OzDBlock> hs = dblocks;
+      std::vector<double*> cps;
+      cps.reserve(colptr_host.size());
       size_t off = 0;
-      for (size_t i = 0; i < hs.size(); ++i) {
-        hs[i].d = scratch + (spread ? off : 0);
-        off += size_t(dinfo[i].m0) * size_t(dinfo[i].n0);
-      }
-      if (cudaMalloc(&sdb, hs.size() * sizeof(OzDBlock)) != cudaSuccess ||
-          cudaMemcpy(sdb, hs.data(), hs.size() * sizeof(OzDBlock), cudaMemcpyHostToDevice) != cudaSuccess) {
+      for (const std::vector<int>& st : stacks)
+        for (int gm : st) {
+          const GemmPlan& hm = plans[groups[gm].plan]->host;
+          double* base = scratch + (spread ? off : 0);
+          for (int64_t n = 0; n < hm.N; ++n) cps.push_back(base + hm.offDn[n]);
+          off += size_t(hm.M) * size_t(hm.N);
+        }
+      std::vector<OzDBlock> hs = dblocks;
+      bool ok = cudaMalloc(&scols, std::max<size_t>(cps.size(), 1) * sizeof(double*)) == cudaSuccess &&
+                cudaMemcpy(scols, cps.data(), cps.size() * sizeof(double*), cudaMemcpyHostToDevice) == cudaSuccess;
+      for (size_t i = 0; i < hs.size(); ++i) hs[i].d = scratch, hs[i].colptr = scols + colptr_at[i];
+      ok = ok && cudaMalloc(&sdb, hs.size() * sizeof(OzDBlock)) == cudaSuccess &&
+           cudaMemcpy(sdb, hs.data(), hs.size() * sizeof(OzDBlock), cudaMemcpyHostToDevice) == cudaSuccess;
+      if (!ok) {
         cudaFree(sdb);
+        cudaFree(scols);
         cudaFree(scratch);
-        sdb = nullptr, scratch = nullptr;
+        sdb = nullptr, scols = nullptr, scratch = nullptr;
       }
     }
     cudaGetLastError();  // a failed scratch allocation is not an error of the batch
@@ -734,6 +857,7 @@ int build_ozaki(a4g_batch* b, const std::vector<DGroup>& groups, const std::vect
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     if (sdb) cudaFree(sdb);
+    if (scols) cudaFree(scols);
     if (scratch) cudaFree(scratch);
     if (rc) return rc;
   }
@@ -768,7 +892,7 @@ int build_ozaki(a4g_batch* b, const std::vector<DGroup>& groups, const std::vect
     }
     bool any_late = false;
     for (size_t i = 0; i < kmaj.size(); ++i) {
-      const std::vector<int>& nd = need[kmaj[i].panel];
+      const std::vector<int>& nd = need[view_full[kmaj[i].panel]];
       int g = P;
       for (int64_t c = kmaj[i].koff / kOzK16; c <= (kmaj[i].koff + kmaj[i].K - 1) / kOzK16; ++c) g = std::min(g, nd[c]);
       job_group[i] = g >= P ? 0 : g;
@@ -844,7 +968,7 @@ int run(a4g_batch* b, cudaStream_t s, const cudaEvent_t* ev = nullptr) {
     A4G_CUDA(cudaMemsetAsync(b->d_exps, 0, b->exps_bytes, s));
     for (const auto& js : b->jobsets)
       if ((rc = oz_launch_exp(js.layout, js.d_jobs, js.d_prefix_exp, js.njobs, js.tiles_exp,
-                              js.left ? b->d_pa : b->d_pb, s)))
+                              js.left ? b->d_pa : b->d_pb_view, s)))
         return rc;
   }
   if ((rc = mark(2))) return rc;
@@ -852,7 +976,7 @@ int run(a4g_batch* b, cudaStream_t s, const cudaEvent_t* ev = nullptr) {
     for (const auto& js : b->jobsets)
       if (js.group == g) {
         const int r = oz_launch_split(js.layout, js.d_jobs, js.d_prefix_split, js.njobs, js.tiles_split,
-                                      js.left ? b->d_pa : b->d_pb, b->slices, st);
+                                      js.left ? b->d_pa : b->d_pb_view, b->slices, st);
         if (r) return r;
       }
     return A4G_OK;

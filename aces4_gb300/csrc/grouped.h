@@ -91,11 +91,17 @@ struct OzTrip {
   int nkb;
   int pad;
 };
+// Destination of a tile grid: one destination block, or a stack of blocks
+// that share the rows (the same left blocks, the same row addressing) laid
+// side by side along n.  Element (m, n) lives at colptr[n] + rowoff[m].
 struct OzDBlock {
   double* d;
-  int plan;  // PlanRef index for offDm/offDn and M, N
+  int plan;  // PlanRef index of the (first) block
   int panel_a, panel_b;
   int col_fast;  // D is unit-stride along n, not along m: store by columns
+  int M, N;      // rows; columns of all stacked blocks
+  const int64_t* rowoff;  // [M] row offsets (the blocks' common offDm)
+  double* const* colptr;  // [N] column bases (block + offDn of its column)
 };
 
 constexpr int kOzBM = 128, kOzBN = 128, kOzBK = 64, kOzK16 = 16, kOzMaxSlices = 8;

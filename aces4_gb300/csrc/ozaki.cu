@@ -476,16 +476,16 @@ __device__ __forceinline__ double i64_scaled_to_double(long long v, int e2, bool
 
 // Direct form: what a thread needs to store its part of a tile (its row,
 // columns col0..col0+31), gathered once when the tile starts (while the
-// tensor cores work on the tile's first level): the row's D address and
-// scale; the 32 columns' D offsets and scales go to the warp's table in
-// shared memory (read back as broadcasts).
+// tensor cores work on the tile's first level): the row's D offset and
+// scale; the 32 columns' D bases and scales go to the warp's table in shared
+// memory (read back as broadcasts).
 struct DirectCol {
-  long long off;  // -1: column outside D
-  int F;          // biased column exponent (at least 1)
+  double* colp;  // column base in D; null: column outside D
+  int F;         // biased column exponent (at least 1)
   int pad;
 };
 struct DirectTile {
-  double* drow;
+  long long roff;   // the row's offset from a column base
   DirectCol* cols;  // this warp's 32 entries
   int ebase;        // row scale and constant part of the result's exponent
   bool mlive;
@@ -494,22 +494,21 @@ struct DirectTile {
 __device__ __forceinline__ void direct_tile(DirectTile& t, const OzGemmArgs& a, const OzTile& tl, int row,
                                             int col0, int lane) {
   const OzDBlock db = a.dblocks[tl.dblock];
-  const PlanRef pl = a.plans[db.plan];
   const int m = tl.m0 + row, n = tl.n0 + col0 + lane;
-  t.mlive = m < pl.M;
+  t.mlive = m < db.M;
   int Em = 1;
-  t.drow = db.d;
+  t.roff = 0;
   if (t.mlive) {
     const int e = a.panels_a[tl.panel_a].exps[m];
     Em = e ? e : 1;
-    t.drow += pl.offDm[m];
+    t.roff = db.rowoff[m];
   }
   t.ebase = Em - 1022 - 1022 + 2 - kDigitBits * (a.slices + 1);
-  DirectCol c{-1, 1, 0};
-  if (n < pl.N) {
+  DirectCol c{nullptr, 1, 0};
+  if (n < db.N) {
     const int f = a.panels_b[tl.panel_b].exps[n];
     c.F = f ? f : 1;
-    c.off = pl.offDn[n];
+    c.colp = db.colptr[n];
   }
   __syncwarp();  // the previous tile's entries are read
   t.cols[lane] = c;
@@ -522,17 +521,17 @@ __device__ __forceinline__ void prefetch_direct(const DirectTile& t) {
   if (!t.mlive) return;
 #pragma unroll 8
   for (int j = 0; j < 32; ++j) {
-    const long long off = t.cols[j].off;
-    if (off >= 0) asm volatile("prefetch.global.L2 [%0];" ::"l"(t.drow + off));
+    double* cp = t.cols[j].colp;
+    if (cp) asm volatile("prefetch.global.L2 [%0];" ::"l"(cp + t.roff));
   }
 }
 
 __device__ __forceinline__ void load_d8(const DirectTile& t, int c0, bool acc, double (&d)[8]) {
 #pragma unroll
   for (int j = 0; j < 8; ++j) {
-    const long long off = t.cols[c0 + j].off;
+    double* cp = t.cols[c0 + j].colp;
     d[j] = 0.0;
-    if (acc && t.mlive && off >= 0) d[j] = t.drow[off];
+    if (acc && t.mlive && cp) d[j] = cp[t.roff];
   }
 }
 
@@ -561,7 +560,7 @@ __device__ __forceinline__ void store_direct(const OzGemmArgs& a, const DirectTi
       const DirectCol c = t.cols[8 * p + j];
       const long long v = (long long)(((unsigned long long)w1[j] << 32) | w0[j]);
       const double x = i64_scaled_to_double(v, t.ebase + c.F, a.mode & 2);
-      if (t.mlive && c.off >= 0) t.drow[c.off] = acc ? dc[j] + x : x;
+      if (t.mlive && c.colp) c.colp[t.roff] = acc ? dc[j] + x : x;
     }
   }
 }
@@ -1180,12 +1179,11 @@ __global__ void __launch_bounds__(256) oz_recombine_kernel(const OzTile* __restr
   const int sc = (blockIdx.x & ((1 << strips_log) - 1)) * kSub;
   const OzTile tl = tiles[tile];
   const OzDBlock db = dblocks[tl.dblock];
-  const PlanRef pl = plans[db.plan];
   const int* ea = pa[tl.panel_a].exps;
   const int* eb = pb[tl.panel_b].exps;
   const size_t plane = size_t(1) << (log_rows + log_cols);     // one split's [cols][rows]
   const int* wtile = ws + size_t(tile) * S * nsplit * plane;
-  const int rows_here = min(1 << log_rows, pl.M - tl.m0);
+  const int rows_here = min(1 << log_rows, db.M - tl.m0);
   for (int sr = 0; sr < rows_here; sr += kSub) {
     long long lev[kPer][S];
 #pragma unroll
@@ -1213,7 +1211,7 @@ __global__ void __launch_bounds__(256) oz_recombine_kernel(const OzTile* __restr
       const int row = sr + (e & (kSub - 1)), col = sc + (e >> 5);
       const int m = tl.m0 + row, n = tl.n0 + col;
       double v = 0.0;
-      const bool live = m < pl.M && n < pl.N;
+      const bool live = m < db.M && n < db.N;
       if (live) {
         // value = sum_t lev[t] 2^(8(S-1-t)) * 2^(E + F + 2 - 8(S+1))
         const int E = (ea[m] ? ea[m] : 1) - 1022, F = (eb[n] ? eb[n] : 1) - 1022;
@@ -1236,7 +1234,7 @@ __global__ void __launch_bounds__(256) oz_recombine_kernel(const OzTile* __restr
       if (db.col_fast) {
         sm[e & (kSub - 1)][e >> 5] = v;
       } else if (live) {
-        double* dst = db.d + pl.offDm[m] + pl.offDn[n];
+        double* dst = db.colptr[n] + db.rowoff[m];
         *dst = (mode & 1) ? *dst + v : v;
       }
     }
@@ -1247,9 +1245,9 @@ __global__ void __launch_bounds__(256) oz_recombine_kernel(const OzTile* __restr
       const int e = p * 256 + threadIdx.x;
       const int col = sc + (e & (kSub - 1)), row = sr + (e >> 5);
       const int m = tl.m0 + row, n = tl.n0 + col;
-      if (m < pl.M && n < pl.N) {
+      if (m < db.M && n < db.N) {
         const double v = sm[e >> 5][e & (kSub - 1)];
-        double* dst = db.d + pl.offDm[m] + pl.offDn[n];
+        double* dst = db.colptr[n] + db.rowoff[m];
         *dst = (mode & 1) ? *dst + v : v;
       }
     }
@@ -1334,7 +1332,6 @@ __global__ void __launch_bounds__(1024, 1) oz_recombine_bulk_kernel(const OzTile
     const int tile = q / pieces_per_tile, pc = q % pieces_per_tile;
     const OzTile tl = tiles[tile];
     const OzDBlock db = dblocks[tl.dblock];
-    const PlanRef pl = plans[db.plan];
     const int* ea = pa[tl.panel_a].exps;
     const int* eb = pb[tl.panel_b].exps;
     const int sc = pc * cols_pp;
@@ -1347,7 +1344,7 @@ __global__ void __launch_bounds__(1024, 1) oz_recombine_bulk_kernel(const OzTile
       const int row = e & (rows - 1), cl = e >> log_rows;
       const int m = tl.m0 + row, n = tl.n0 + sc + cl;
       double v = 0.0;
-      const bool live = m < pl.M && n < pl.N;
+      const bool live = m < db.M && n < db.N;
       if (live) {
         const int E = (ea[m] ? ea[m] : 1) - 1022, F = (eb[n] ? eb[n] : 1) - 1022;
         const int e2 = E + F + 2 - kDigitBits * (S + 1);
@@ -1359,7 +1356,7 @@ __global__ void __launch_bounds__(1024, 1) oz_recombine_bulk_kernel(const OzTile
       vals[p] = v;
       dsts[p] = nullptr;
       if (db.col_fast) sm.val[cl * (rows + 1) + row] = v;
-      else if (live) dsts[p] = db.d + pl.offDm[m] + pl.offDn[n];
+      else if (live) dsts[p] = db.colptr[n] + db.rowoff[m];
     }
     if (!db.col_fast) {
       double old[kPerT];  // accumulate mode: the old values' loads in flight together
@@ -1379,7 +1376,7 @@ __global__ void __launch_bounds__(1024, 1) oz_recombine_bulk_kernel(const OzTile
         const int e = p * 1024 + threadIdx.x;
         const int cl = e % cols_pp, row = e / cols_pp;
         const int m = tl.m0 + row, n = tl.n0 + sc + cl;
-        dst[p] = (m < pl.M && n < pl.N) ? db.d + pl.offDm[m] + pl.offDn[n] : nullptr;
+        dst[p] = (m < db.M && n < db.N) ? db.colptr[n] + db.rowoff[m] : nullptr;
         old[p] = (dst[p] && (mode & 1)) ? *dst[p] : 0.0;
       }
 #pragma unroll
