@@ -682,7 +682,6 @@ int build_ozaki(a4g_batch* b, const std::vector<DGroup>& groups, const std::vect
     ga.mode = b->store_mode();
     ga.dry = 0;
     ga.dblocks = b->d_dblocks;
-    ga.plans = b->d_plans;
     const int workers = gf.direct ? gf.n_tiles : ga.n_units;
     gf.grid = gf.pair ? 2 * std::min(workers, pairs) : std::min(workers, ctx()->num_sms);
     gf.built = true;
@@ -784,7 +783,7 @@ int build_ozaki(a4g_batch* b, const std::vector<DGroup>& groups, const std::vect
         if (rep == 1 && cudaEventRecord(e0, s) != cudaSuccess) return cuda_fail(cudaGetLastError(), "event");
         r = oz_launch_gemm(ta, grid, gf.pair, gf.tile_cols, s);
         if (!r && !gf.direct && sdb)
-          r = oz_launch_recombine(gf.d_tiles, gf.n_tiles, gf.tile_rows, gf.tile_cols, sdb, b->d_plans, b->d_pa,
+          r = oz_launch_recombine(gf.d_tiles, gf.n_tiles, gf.tile_rows, gf.tile_cols, sdb, b->d_pa,
                                   b->d_pb, ta.ws, S, ta.nsplit, b->store_mode(), s);
       }
       if (r) return r;
@@ -1004,7 +1003,7 @@ int run(a4g_batch* b, cudaStream_t s, const cudaEvent_t* ev = nullptr) {
   }
   if ((rc = mark(4))) return rc;
   if (gf.n_tiles > 0 && !gf.direct &&
-      (rc = oz_launch_recombine(gf.d_tiles, gf.n_tiles, gf.tile_rows, gf.tile_cols, b->d_dblocks, b->d_plans,
+      (rc = oz_launch_recombine(gf.d_tiles, gf.n_tiles, gf.tile_rows, gf.tile_cols, b->d_dblocks,
                                 b->d_pa, b->d_pb, b->d_ws, b->slices, gf.nsplit, b->store_mode(), s)))
     return rc;
   return mark(5);

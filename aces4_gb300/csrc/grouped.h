@@ -142,7 +142,6 @@ struct OzGemmArgs {
   int mode;  // direct: bit 0 accumulate into D, bit 1 negate
   int dry;   // direct: compute everything but store nothing (timing)
   const OzDBlock* dblocks;
-  const PlanRef* plans;
 };
 
 }  // namespace a4g

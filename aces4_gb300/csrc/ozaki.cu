@@ -1167,7 +1167,6 @@ __device__ __forceinline__ double i128_scaled_to_double(__int128 N, int e2) {
 template <int S>
 __global__ void __launch_bounds__(256) oz_recombine_kernel(const OzTile* __restrict__ tiles,
                                                            const OzDBlock* __restrict__ dblocks,
-                                                           const PlanRef* __restrict__ plans,
                                                            const OzPanel* __restrict__ pa,
                                                            const OzPanel* __restrict__ pb,
                                                            const int* __restrict__ ws, int log_rows, int log_cols,
@@ -1292,8 +1291,7 @@ __device__ __forceinline__ bool wait_bounded(uint64_t* bar, uint32_t parity) {
 template <int S>
 __global__ void __launch_bounds__(1024, 1) oz_recombine_bulk_kernel(const OzTile* __restrict__ tiles,
                                                                   const OzDBlock* __restrict__ dblocks,
-                                                                  const PlanRef* __restrict__ plans,
-                                                                  const OzPanel* __restrict__ pa,
+                                                                         const OzPanel* __restrict__ pa,
                                                                   const OzPanel* __restrict__ pb,
                                                                   const int* __restrict__ ws, int log_rows,
                                                                   int log_cols, int n_tiles, int mode, int* err) {
@@ -1584,7 +1582,7 @@ int oz_launch_gemm(const OzGemmArgs& args, int grid, bool pair, int tile_cols, c
 }
 
 int oz_launch_recombine(const OzTile* tiles, int ntiles, int tile_rows, int tile_cols, const OzDBlock* dblocks,
-                        const PlanRef* plans, const OzPanel* pa, const OzPanel* pb, const int* ws, int slices,
+                        const OzPanel* pa, const OzPanel* pb, const int* ws, int slices,
                         int nsplit, int mode, cudaStream_t s) {
   if (ntiles <= 0) return A4G_OK;
   if ((tile_rows != 128 && tile_rows != 256) || (tile_cols != 128 && tile_cols != 256))
@@ -1602,7 +1600,7 @@ int oz_launch_recombine(const OzTile* tiles, int ntiles, int tile_rows, int tile
     if (first_on_device(attr))                                                                                   \
       A4G_CUDA(cudaFuncSetAttribute(oz_recombine_bulk_kernel<SL>, cudaFuncAttributeMaxDynamicSharedMemorySize,  \
                                     int(sizeof(RecSmem<SL>))));                                                 \
-    oz_recombine_bulk_kernel<SL><<<grid, 1024, sizeof(RecSmem<SL>), s>>>(tiles, dblocks, plans, pa, pb, ws, lr, lc, \
+    oz_recombine_bulk_kernel<SL><<<grid, 1024, sizeof(RecSmem<SL>), s>>>(tiles, dblocks, pa, pb, ws, lr, lc, \
                                                                        ntiles, mode, err);                       \
     break;                                                                                                       \
   }
@@ -1617,7 +1615,7 @@ int oz_launch_recombine(const OzTile* tiles, int ntiles, int tile_rows, int tile
   const unsigned g = unsigned(ntiles * per);
   switch (slices) {
 #define A4G_RECOMBINE(SL) \
-  case SL: oz_recombine_kernel<SL><<<g, 256, 0, s>>>(tiles, dblocks, plans, pa, pb, ws, lr, lc, nsplit, mode); break;
+  case SL: oz_recombine_kernel<SL><<<g, 256, 0, s>>>(tiles, dblocks, pa, pb, ws, lr, lc, nsplit, mode); break;
     A4G_RECOMBINE(1) A4G_RECOMBINE(2) A4G_RECOMBINE(3) A4G_RECOMBINE(4) A4G_RECOMBINE(5) A4G_RECOMBINE(6)
     A4G_RECOMBINE(7)
 #undef A4G_RECOMBINE

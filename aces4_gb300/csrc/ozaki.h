@@ -24,7 +24,7 @@ int oz_launch_split(int layout, const OzSplitJob* jobs, const int64_t* prefix, i
 int oz_launch_gemm(const OzGemmArgs& args, int grid, bool pair, int tile_cols, cudaStream_t s);
 int oz_wait_timeout_selftest(int limit_ms, int* waited_ms, cudaStream_t s);
 int oz_launch_recombine(const OzTile* tiles, int ntiles, int tile_rows, int tile_cols, const OzDBlock* dblocks,
-                        const PlanRef* plans, const OzPanel* pa, const OzPanel* pb, const int* ws, int slices,
+                        const OzPanel* pa, const OzPanel* pb, const int* ws, int slices,
                         int nsplit, int mode, cudaStream_t s);  // mode: bit 0 accumulate, bit 1 negate
 
 }  // namespace a4g
