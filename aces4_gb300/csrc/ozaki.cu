@@ -1263,12 +1263,16 @@ __global__ void __launch_bounds__(256) oz_recombine_kernel(const OzTile* __restr
 // while this one is combined and stored.  Waits are bounded (error flag, then
 // a bounded drain of the copy still in flight).
 constexpr int kRecPiece = 4096;  // int32 elements per level per piece (16 KB)
+// Pieces in flight: one ahead of the one being combined.  (Four stages of
+// 2048-element pieces were measured slower: 14 instead of 11 ms on the
+// triples' term 1, the per-piece overhead doubling.)
+constexpr int kRecStages = 2;
 
 template <int S>
 struct __align__(128) RecSmem {
-  int lev[2][S][kRecPiece];
+  int lev[kRecStages][S][kRecPiece];
   double val[kRecPiece + 64];  // [col][rows + 1] transpose buffer
-  uint64_t full[2];
+  uint64_t full[kRecStages];
 };
 
 __device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
@@ -1303,8 +1307,7 @@ __global__ void __launch_bounds__(1024, 1) oz_recombine_bulk_kernel(const OzTile
   const int npieces = n_tiles * pieces_per_tile;
   const size_t plane = size_t(1) << (log_rows + log_cols);
   if (threadIdx.x == 0) {
-    mbar_init(&sm.full[0], 1);
-    mbar_init(&sm.full[1], 1);
+    for (int st = 0; st < kRecStages; ++st) mbar_init(&sm.full[st], 1);
     fence_mbar_init();
   }
   __syncthreads();
@@ -1317,14 +1320,22 @@ __global__ void __launch_bounds__(1024, 1) oz_recombine_bulk_kernel(const OzTile
                &sm.full[st]);
   };
   int q = blockIdx.x;
-  if (threadIdx.x == 0 && q < npieces) issue(q, 0);
-  for (int it = 0; q < npieces; q += gridDim.x, ++it) {
-    const int st = it & 1;
-    if (threadIdx.x == 0 && q + int(gridDim.x) < npieces) issue(q + gridDim.x, st ^ 1);
-    if (!wait_bounded(&sm.full[st], uint32_t(it >> 1) & 1u)) {
+  const int G = gridDim.x;
+  if (threadIdx.x == 0)
+    for (int i = 0; i < kRecStages - 1; ++i)
+      if (q + i * G < npieces) issue(q + i * G, i);
+  for (int it = 0; q < npieces; q += G, ++it) {
+    const int st = it % kRecStages;
+    // the stage of piece it + kRecStages - 1 was combined in iteration it - 1
+    // (the barrier at the end of that iteration freed it)
+    const int ahead = q + (kRecStages - 1) * G;
+    if (threadIdx.x == 0 && ahead < npieces) issue(ahead, (it + kRecStages - 1) % kRecStages);
+    if (!wait_bounded(&sm.full[st], uint32_t(it / kRecStages) & 1u)) {
       atomicExch(err, 5);
-      // drain the next piece's copies (if issued) before this CTA's memory is released
-      if (threadIdx.x == 0 && q + int(gridDim.x) < npieces) wait_bounded(&sm.full[st ^ 1], uint32_t((it + 1) >> 1) & 1u);
+      // drain the later pieces' copies (those issued) before this CTA's memory is released
+      if (threadIdx.x == 0)
+        for (int i = 1; i < kRecStages && q + i * G < npieces; ++i)
+          wait_bounded(&sm.full[(it + i) % kRecStages], uint32_t((it + i) / kRecStages) & 1u);
       return;
     }
     const int tile = q / pieces_per_tile, pc = q % pieces_per_tile;
