@@ -293,6 +293,12 @@ __device__ __forceinline__ double u64_scaled_to_double(unsigned long long u, boo
   return neg ? -v : v;
 }
 
+// A row or column exponent of 2047 (the field of Inf and NaN) marks a panel
+// row that holds a non-finite value: digits cannot carry it, so every result
+// that row or column feeds is stored as NaN (in FP64 a NaN or an infinity in
+// an operand makes the whole row or column of the product NaN or infinite).
+constexpr int kNonFiniteExp = 2047;
+
 // ------------------------------------------------------------------ roles
 // Walks the k blocks of one unit: calls f(koff_a, koff_b, kb) per 64-wide
 // block (the panels are zero beyond the end of every stretch of pairs up to
@@ -489,6 +495,7 @@ struct DirectTile {
   DirectCol* cols;  // this warp's 32 entries
   int ebase;        // row scale and constant part of the result's exponent
   bool mlive;
+  bool nonfinite;   // the row holds a non-finite operand value
 };
 
 __device__ __forceinline__ void direct_tile(DirectTile& t, const OzGemmArgs& a, const OzTile& tl, int row,
@@ -498,9 +505,11 @@ __device__ __forceinline__ void direct_tile(DirectTile& t, const OzGemmArgs& a, 
   t.mlive = m < db.M;
   int Em = 1;
   t.roff = 0;
+  t.nonfinite = false;
   if (t.mlive) {
     const int e = a.panels_a[tl.panel_a].exps[m];
     Em = e ? e : 1;
+    t.nonfinite = e == kNonFiniteExp;
     t.roff = db.rowoff[m];
   }
   t.ebase = Em - 1022 - 1022 + 2 - kDigitBits * (a.slices + 1);
@@ -559,7 +568,8 @@ __device__ __forceinline__ void store_direct(const OzGemmArgs& a, const DirectTi
     for (int j = 0; j < 8; ++j) {
       const DirectCol c = t.cols[8 * p + j];
       const long long v = (long long)(((unsigned long long)w1[j] << 32) | w0[j]);
-      const double x = i64_scaled_to_double(v, t.ebase + c.F, a.mode & 2);
+      double x = i64_scaled_to_double(v, t.ebase + c.F, a.mode & 2);
+      if (t.nonfinite || c.F == kNonFiniteExp) x = __longlong_as_double(0x7FF8000000000000ll);
       if (t.mlive && c.colp) c.colp[t.roff] = acc ? dc[j] + x : x;
     }
   }
@@ -1229,6 +1239,7 @@ __global__ void __launch_bounds__(256) oz_recombine_kernel(const OzTile* __restr
           v = i128_scaled_to_double((__int128)acc, e2);
         }
         if (mode & 2) v = -v;  // negated term
+        if (ea[m] == kNonFiniteExp || eb[n] == kNonFiniteExp) v = __longlong_as_double(0x7FF8000000000000ll);
       }
       if (db.col_fast) {
         sm[e & (kSub - 1)][e >> 5] = v;
@@ -1361,6 +1372,7 @@ __global__ void __launch_bounds__(1024, 1) oz_recombine_bulk_kernel(const OzTile
 #pragma unroll
         for (int lv = 0; lv < S; ++lv) acc += (long long)sm.lev[st][lv][e] * (1ll << (kDigitBits * (S - 1 - lv)));
         v = i64_scaled_to_double(acc, e2, mode & 2);  // negated term: the sign folded into the rounding
+        if (ea[m] == kNonFiniteExp || eb[n] == kNonFiniteExp) v = __longlong_as_double(0x7FF8000000000000ll);
       }
       vals[p] = v;
       dsts[p] = nullptr;

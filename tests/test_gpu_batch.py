@@ -263,6 +263,28 @@ def test_destination_unit_stride_on_the_right_operand(a4, variant):
     np.testing.assert_array_equal(D.cpu().numpy(), want)
 
 
+@pytest.mark.parametrize("variant", [1, 4, 5])
+def test_non_finite_operands_poison_their_rows_and_columns(a4, variant):
+    """A NaN in a left block and an infinity in a right block: digits cannot
+    carry them, so the split form stores NaN wherever FP64 gives a non-finite
+    result (the whole row / column they feed) and the FP64 values elsewhere."""
+    import torch
+
+    R, V, T, trip, labels = _make(a4, "ladder", [32, 32], [16, 16], 0.0, 31)
+    V.buf[V.offsets[(0, 1, 1, 0)] + 5] = float("nan")
+    T.buf[T.offsets[(1, 1, 0, 1)] + 77] = float("inf")
+    _run(a4, R, trip, labels, a4.device.PREC_FP64)
+    want = R.buf.clone()
+    R.buf.fill_(0.0)
+    _run(a4, R, trip, labels, a4.device.PREC_OZAKI_BF16, variant=variant)
+    got = R.buf.clone()
+    bad = ~torch.isfinite(want)
+    assert int(bad.sum()) > 0
+    assert torch.equal(torch.isnan(got), bad)
+    ok = ~bad
+    assert float((got[ok] - want[ok]).abs().max()) <= TOL_SPLIT * float(want[ok].abs().max())
+
+
 def test_split_uneven_sparse_ring_graph_and_beta(a4):
     import torch
 
