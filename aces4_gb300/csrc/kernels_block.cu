@@ -349,7 +349,14 @@ struct DenParams {
   int ext[6];  // extents in storage order
   int off[6];  // first orbital of each storage dimension's segment
   int pos[6];  // storage dimension holding denominator position q
+  int poff[6];  // off[pos[q]]: first orbital of the segment at position q
 };
+
+// x[k] for a run-time k without indexing a register array (which would put
+// it in local memory)
+__device__ __forceinline__ int pick6(const int (&x)[6], int k) {
+  return k == 0 ? x[0] : k == 1 ? x[1] : k == 2 ? x[2] : k == 3 ? x[3] : k == 4 ? x[4] : x[5];
+}
 
 __device__ __forceinline__ double eps_at(const DenParams& p, const double* e, int orb) {
   return p.rank1 == 2 ? e[int64_t(orb) + int64_t(orb) * p.ld1] : e[orb];
@@ -358,15 +365,69 @@ __device__ __forceinline__ double eps_at(const DenParams& p, const double* e, in
 // Denominator of the element with storage coordinates x, in the reference's
 // order of additions (energy_denominator_rhf.F do_rhf_den2/4/6): positions
 // 0, 2, 4 are virtual (subtracted), 1, 3, 5 occupied (added).
+// a / b rounded to the nearest double (ties to even; a quotient of two
+// doubles is never exactly halfway) in integer arithmetic, for normal a, b
+// and a normal result; false otherwise (the caller divides in FP64).  The FP64
+// pipe of this GPU retires ~2 operations per clock per SM, a division takes
+// several, and the denominator and amplitude-update passes would be bound by
+// it; integer multiplies run far wider.  Method: a reciprocal R ~ 2^116/mb of
+// the divisor's 53-bit significand by Newton-Raphson (seed: the FP32
+// reciprocal of its top 24 bits; two steps R += R(2^116 - mb R)/2^116 in
+// 64-bit fixed point), the 55-bit quotient estimate Q = ma 2^s R / 2^116, and
+// the exact remainder ma 2^s - Q mb, which corrects Q to floor(ma 2^s / mb)
+// (Knuth, TAOCP vol. 2, 4.3.1: estimate a quotient digit, then fix it from
+// the remainder) and gives the sticky bit for the rounding.
+__device__ __forceinline__ bool div_rn_int(double a, double b, double* q) {
+  const uint64_t ua = uint64_t(__double_as_longlong(a)), ub = uint64_t(__double_as_longlong(b));
+  const int ea = int((ua >> 52) & 0x7FF), eb = int((ub >> 52) & 0x7FF);
+  if (ea == 0 || ea == 2047 || eb == 0 || eb == 2047) return false;
+  const uint64_t ma = (ua & ((1ull << 52) - 1)) | (1ull << 52);
+  const uint64_t mb = (ub & ((1ull << 52) - 1)) | (1ull << 52);
+  const uint32_t rb = uint32_t(__float_as_uint(__frcp_rn(float(uint32_t(mb >> 29)))));  // mb's top 24 bits: exact
+  const int er = int((rb >> 23) & 0xFF) - 127;  // the reciprocal lies in (2^-24, 2^-23]
+  const uint64_t rm = (rb & 0x7FFFFFu) | 0x800000u;
+  uint64_t R = er == -23 ? ~0ull : rm << (er + 64);  // 2^-23 exactly would be 2^64
+#pragma unroll
+  for (int it = 0; it < 2; ++it) {
+    const uint64_t plo = mb * R, phi = __umul64hi(mb, R);  // mb R (117 bits)
+    const uint64_t elo = 0ull - plo, ehi = (1ull << 52) - phi - (plo != 0 ? 1ull : 0ull);  // 2^116 - mb R
+    const int64_t e52 = int64_t((ehi << 12) | (elo >> 52));  // (2^116 - mb R) / 2^52, |.| < 2^43
+    const uint64_t d = __umul64hi(R, e52 < 0 ? uint64_t(-e52) : uint64_t(e52));
+    R = e52 < 0 ? R - d : R + d;
+  }
+  const int adj = ma < mb ? 1 : 0;
+  const int sh = 54 + adj;  // floor(ma 2^sh / mb) lies in [2^54, 2^55)
+  const int rs = 116 - sh;
+  uint64_t Q = (__umul64hi(ma, R) << (64 - rs)) | ((ma * R) >> rs);
+  int64_t rem = int64_t((ma << sh) - Q * mb);  // exact: |rem| < 2^63
+#pragma unroll
+  for (int it = 0; it < 3; ++it)
+    if (rem < 0) --Q, rem += int64_t(mb);
+#pragma unroll
+  for (int it = 0; it < 3; ++it)
+    if (rem >= int64_t(mb)) ++Q, rem -= int64_t(mb);
+  uint64_t mant = Q >> 2;
+  const uint64_t guard = (Q >> 1) & 1ull, sticky = (Q & 1ull) | (rem != 0 ? 1ull : 0ull);
+  mant += (guard && (sticky || (mant & 1ull))) ? 1ull : 0ull;
+  const int field = ea - eb + 1023 - adj;  // biased exponent of the quotient's leading bit
+  if (field < 1 || field > 2045) return false;
+  *q = __longlong_as_double(int64_t(((ua ^ ub) & (1ull << 63)) | ((uint64_t(field - 1) << 52) + mant)));
+  return true;
+}
+__device__ __forceinline__ double div_rn(double a, double b) {
+  double q;
+  return div_rn_int(a, b, &q) ? q : __ddiv_rn(a, b);
+}
+
 __device__ __forceinline__ double den_eps(const DenParams& p, const double* e, const int (&x)[6]) {
-  const double ea = eps_at(p, e, x[p.pos[0]] + p.off[p.pos[0]]);
-  const double eb = eps_at(p, e, x[p.pos[1]] + p.off[p.pos[1]]);
+  const double ea = eps_at(p, e, pick6(x, p.pos[0]) + p.poff[0]);
+  const double eb = eps_at(p, e, pick6(x, p.pos[1]) + p.poff[1]);
   if (p.rank0 == 2) return __dsub_rn(eb, ea);  // epsb - epsa
-  const double ec = eps_at(p, e, x[p.pos[2]] + p.off[p.pos[2]]);
-  const double ed = eps_at(p, e, x[p.pos[3]] + p.off[p.pos[3]]);
+  const double ec = eps_at(p, e, pick6(x, p.pos[2]) + p.poff[2]);
+  const double ed = eps_at(p, e, pick6(x, p.pos[3]) + p.poff[3]);
   if (p.rank0 == 4) return __dsub_rn(__dsub_rn(__dadd_rn(eb, ed), ea), ec);  // epsb + epsd - epsa - epsc
-  const double e5 = eps_at(p, e, x[p.pos[4]] + p.off[p.pos[4]]);
-  const double e6 = eps_at(p, e, x[p.pos[5]] + p.off[p.pos[5]]);
+  const double e5 = eps_at(p, e, pick6(x, p.pos[4]) + p.poff[4]);
+  const double e6 = eps_at(p, e, pick6(x, p.pos[5]) + p.poff[5]);
   return __dsub_rn(__dsub_rn(__dsub_rn(__dadd_rn(__dadd_rn(eb, ed), e6), ea), ec), e5);
 }
 
@@ -382,14 +443,31 @@ __device__ __forceinline__ void den_coords(const DenParams& p, int64_t i, int (&
   }
 }
 
+// Four consecutive elements per thread: the coordinates are decoded once
+// (64-bit divisions are dear) and stepped along dimension 0 with carries.
+constexpr int kDenRun = 4;
+
 __global__ void __launch_bounds__(kThreads) denominator_kernel(DenParams p, double* data,
                                                                const double* __restrict__ e,
                                                                int64_t n) {
-  const int64_t stride = int64_t(gridDim.x) * blockDim.x;
-  for (int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n; i += stride) {
+  const int64_t stride = int64_t(gridDim.x) * blockDim.x * kDenRun;
+  for (int64_t i0 = (int64_t(blockIdx.x) * blockDim.x + threadIdx.x) * kDenRun; i0 < n; i0 += stride) {
     int x[6];
-    den_coords(p, i, x);
-    data[i] = __ddiv_rn(data[i], den_eps(p, e, x));
+    den_coords(p, i0, x);
+    double v[kDenRun];
+#pragma unroll
+    for (int u = 0; u < kDenRun; ++u) v[u] = i0 + u < n ? data[i0 + u] : 0.0;
+#pragma unroll
+    for (int u = 0; u < kDenRun; ++u) {
+      if (i0 + u >= n) break;
+      data[i0 + u] = div_rn(v[u], den_eps(p, e, x));
+#pragma unroll
+      for (int q = 0; q < 6; ++q) {  // next element: x[0] + 1 with carries
+        if (q >= p.rank0) break;
+        if (++x[q] < p.ext[q]) break;
+        x[q] = 0;
+      }
+    }
   }
 }
 
@@ -612,7 +690,7 @@ __global__ void __launch_bounds__(256) update_t2_kernel(UpdParams p, const doubl
     const double t = __dadd_rn(pn[tx][k], __ldg(xn + q));
     const double t1 = __dadd_rn(po[tx][k], __ldg(xo + q));
     const double eps = __dsub_rn(__dsub_rn(eij, eps_at_upd(p, e, p.oa + a)), eps_at_upd(p, e, p.ob + b));
-    const double td = __ddiv_rn(t, eps);
+    const double td = div_rn(t, eps);
     const double ev = __dmul_rn(__dsub_rn(t1, td), -0.5);
     if (err) err[q] = ev;
     next[q] = fabs(td) >= 0x1p-1021 ? __dmul_rn(td, 0.5) : __ddiv_rn(__dmul_rn(t, 0.5), eps);
@@ -814,6 +892,7 @@ static DenParams den_params(int rank0, const int* off, const int* ext0, const in
     p.pos[q] = pos ? pos[q] : q;
     *n *= ext0[q];
   }
+  for (int q = 0; q < rank0; ++q) p.poff[q] = p.off[p.pos[q]];
   return p;
 }
 
@@ -821,7 +900,7 @@ int launch_denominator(int rank0, const int* off, const int* ext0, double* data,
                        int ld1, const double* e_or_fock, cudaStream_t s) {
   int64_t n = 0;
   const DenParams p = den_params(rank0, off, ext0, nullptr, rank1, ld1, &n);
-  denominator_kernel<<<grid_for(n), kThreads, 0, s>>>(p, data, e_or_fock, n);
+  denominator_kernel<<<grid_for((n + kDenRun - 1) / kDenRun), kThreads, 0, s>>>(p, data, e_or_fock, n);
   A4G_CUDA(cudaGetLastError());
   return A4G_OK;
 }
