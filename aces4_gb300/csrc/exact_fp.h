@@ -1,0 +1,169 @@
+// Exactly rounded FP64 results built with integer arithmetic (the FP64 pipe of
+// this GPU retires ~2 operations per clock per SM; integer multiplies and
+// shifts run far wider).  Host and device share these definitions, so the
+// CPU tests check the very code the kernels run against IEEE arithmetic.
+#pragma once
+
+#include <stdint.h>
+#include <string.h>
+
+#include <cmath>
+
+#if defined(__CUDACC__)
+#define A4G_HD __host__ __device__ __forceinline__
+#else
+#define A4G_HD inline
+#endif
+
+namespace a4g {
+
+A4G_HD int clz64(unsigned long long x) {
+#if defined(__CUDA_ARCH__)
+  return __clzll((long long)x);
+#else
+  return x ? __builtin_clzll(x) : 64;
+#endif
+}
+A4G_HD unsigned long long mulhi64(unsigned long long a, unsigned long long b) {
+#if defined(__CUDA_ARCH__)
+  return __umul64hi(a, b);
+#else
+  return (unsigned long long)(((unsigned __int128)a * b) >> 64);
+#endif
+}
+A4G_HD unsigned long long bits_of(double x) {
+#if defined(__CUDA_ARCH__)
+  return (unsigned long long)__double_as_longlong(x);
+#else
+  unsigned long long u;
+  memcpy(&u, &x, 8);
+  return u;
+#endif
+}
+A4G_HD double double_of(unsigned long long u) {
+#if defined(__CUDA_ARCH__)
+  return __longlong_as_double((long long)u);
+#else
+  double x;
+  memcpy(&x, &u, 8);
+  return x;
+#endif
+}
+// 1/x rounded to the nearest float
+A4G_HD float frcp_rn(float x) {
+#if defined(__CUDA_ARCH__)
+  return __frcp_rn(x);
+#else
+  return 1.0f / x;
+#endif
+}
+
+// The double nearest (ties to even) to u * 2^e2 with sign `neg`, u an
+// unsigned 64-bit magnitude.  Results outside the normal range take an FP64
+// path (ldexp).
+A4G_HD double u64_scaled_to_double(unsigned long long u, bool neg, int e2) {
+  if (u == 0) return 0.0;
+  const int nbits = 64 - clz64(u);
+  unsigned long long mant;
+  int e = e2;
+  if (nbits <= 53) {
+    mant = u << (53 - nbits);
+    e -= 53 - nbits;
+  } else {
+    const int sh = nbits - 53;
+    mant = u >> sh;
+    const unsigned long long rem = u & ((1ull << sh) - 1), half = 1ull << (sh - 1);
+    if (rem > half || (rem == half && (mant & 1ull))) ++mant;
+    e += sh;
+    if (mant == (1ull << 53)) mant >>= 1, ++e;
+  }
+  const int field = e + 52 + 1023;  // value = mant * 2^e, mant in [2^52, 2^53)
+  if (field >= 1 && field <= 2046)
+    return double_of((neg ? (1ull << 63) : 0ull) | ((unsigned long long)field << 52) | (mant & ((1ull << 52) - 1)));
+  const double v = ldexp(double(mant), e);
+  return neg ? -v : v;
+}
+
+// (neg ? -1 : 1) * v * 2^e2 rounded once to the nearest double (ties to
+// even), v a signed 64-bit integer: normalise, keep 53 bits, round on the 11
+// below, and build the bits by one addition (a mantissa that rounds up to
+// 2^53 carries into the exponent field).  Branch-free for results in the
+// normal range; the rest takes u64_scaled_to_double.  Same bits as negating
+// the result of u64_scaled_to_double (a zero keeps the sign the negation
+// gives it).
+A4G_HD double i64_scaled_to_double(long long v, int e2, bool neg) {
+  const unsigned long long sign = (v < 0) != neg ? (1ull << 63) : 0ull;
+  const unsigned long long u = v < 0 ? (unsigned long long)(-v) : (unsigned long long)v;
+  const int n = clz64(u | 1ull);  // u = 0 is mapped to a signed zero at the end
+  const unsigned long long norm = u << n;  // leading one at bit 63
+  unsigned long long mant = norm >> 11;    // 53 bits, leading one at bit 52
+  const unsigned long long rem = norm & 0x7FFull;
+  mant += (rem > 0x400ull || (rem == 0x400ull && (mant & 1ull))) ? 1ull : 0ull;
+  const int field = e2 + 63 - n + 1023;  // biased exponent of the leading one
+  if (u != 0 && (field < 1 || field > 2045)) return u64_scaled_to_double(u, sign != 0, e2);
+  const unsigned long long bits =
+      u ? sign | ((((unsigned long long)(field - 1)) << 52) + mant) : (neg ? (1ull << 63) : 0ull);
+  return double_of(bits);
+}
+
+// The same for a two's-complement 128-bit integer N.
+A4G_HD double i128_scaled_to_double(__int128 N, int e2) {
+  const bool neg = N < 0;
+  const unsigned __int128 u = neg ? (unsigned __int128)(-N) : (unsigned __int128)N;
+  const unsigned long long hi = (unsigned long long)(u >> 64);
+  if (hi == 0) return u64_scaled_to_double((unsigned long long)u, neg, e2);
+  // keep the top 63 bits and fold the rest into a sticky bit below them (the
+  // rounding position lies above it, so the rounding is exact)
+  const int sh = 65 - clz64(hi);  // u >> sh has 63 bits
+  const unsigned long long top = (unsigned long long)(u >> sh);
+  const bool sticky = (u & ((((unsigned __int128)1) << sh) - 1)) != 0;
+  return u64_scaled_to_double((top << 1) | (sticky ? 1ull : 0ull), neg, e2 + sh - 1);
+}
+
+// a / b rounded to the nearest double (ties to even; a quotient of two
+// doubles is never exactly halfway) for normal a, b and a normal result;
+// false otherwise (the caller divides in FP64).  Method: a reciprocal
+// R ~ 2^116/mb of the divisor's 53-bit significand by Newton-Raphson (seed:
+// the FP32 reciprocal of its top 24 bits; two steps R += R(2^116 - mb R)/2^116
+// in 64-bit fixed point), the 55-bit quotient estimate Q = ma 2^s R / 2^116,
+// and the exact remainder ma 2^s - Q mb, which corrects Q to
+// floor(ma 2^s / mb) (Knuth, TAOCP vol. 2, 4.3.1: estimate a quotient digit,
+// then fix it from the remainder) and gives the sticky bit for the rounding.
+A4G_HD bool div_rn_int(double a, double b, double* q) {
+  const unsigned long long ua = bits_of(a), ub = bits_of(b);
+  const int ea = int((ua >> 52) & 0x7FF), eb = int((ub >> 52) & 0x7FF);
+  if (ea == 0 || ea == 2047 || eb == 0 || eb == 2047) return false;
+  const unsigned long long ma = (ua & ((1ull << 52) - 1)) | (1ull << 52);
+  const unsigned long long mb = (ub & ((1ull << 52) - 1)) | (1ull << 52);
+  const float rf = frcp_rn(float(uint32_t(mb >> 29)));  // mb's top 24 bits: exact in FP32
+  uint32_t rb;
+  memcpy(&rb, &rf, 4);
+  const int er = int((rb >> 23) & 0xFF) - 127;  // the reciprocal lies in (2^-24, 2^-23]
+  const unsigned long long rm = (rb & 0x7FFFFFu) | 0x800000u;
+  unsigned long long R = er == -23 ? ~0ull : rm << (er + 64);  // 2^-23 exactly would be 2^64
+  for (int it = 0; it < 2; ++it) {
+    const unsigned long long plo = mb * R, phi = mulhi64(mb, R);  // mb R (117 bits)
+    const unsigned long long elo = 0ull - plo, ehi = (1ull << 52) - phi - (plo != 0 ? 1ull : 0ull);  // 2^116 - mb R
+    const long long e52 = (long long)((ehi << 12) | (elo >> 52));  // (2^116 - mb R) / 2^52, |.| < 2^43
+    const unsigned long long d = mulhi64(R, e52 < 0 ? (unsigned long long)(-e52) : (unsigned long long)e52);
+    R = e52 < 0 ? R - d : R + d;
+  }
+  const int adj = ma < mb ? 1 : 0;
+  const int sh = 54 + adj;  // floor(ma 2^sh / mb) lies in [2^54, 2^55)
+  const int rs = 116 - sh;
+  unsigned long long Q = (mulhi64(ma, R) << (64 - rs)) | ((ma * R) >> rs);
+  long long rem = (long long)((ma << sh) - Q * mb);  // exact: |rem| < 2^63
+  for (int it = 0; it < 3; ++it)
+    if (rem < 0) --Q, rem += (long long)mb;
+  for (int it = 0; it < 3; ++it)
+    if (rem >= (long long)mb) ++Q, rem -= (long long)mb;
+  unsigned long long mant = Q >> 2;
+  const unsigned long long guard = (Q >> 1) & 1ull, sticky = (Q & 1ull) | (rem != 0 ? 1ull : 0ull);
+  mant += (guard && (sticky || (mant & 1ull))) ? 1ull : 0ull;
+  const int field = ea - eb + 1023 - adj;  // biased exponent of the quotient's leading bit
+  if (field < 1 || field > 2045) return false;
+  *q = double_of(((ua ^ ub) & (1ull << 63)) | ((((unsigned long long)(field - 1)) << 52) + mant));
+  return true;
+}
+
+}  // namespace a4g

@@ -9,6 +9,7 @@
 #include <cstring>
 
 #include "a4g_internal.h"
+#include "exact_fp.h"
 
 namespace a4g {
 
@@ -365,55 +366,8 @@ __device__ __forceinline__ double eps_at(const DenParams& p, const double* e, in
 // Denominator of the element with storage coordinates x, in the reference's
 // order of additions (energy_denominator_rhf.F do_rhf_den2/4/6): positions
 // 0, 2, 4 are virtual (subtracted), 1, 3, 5 occupied (added).
-// a / b rounded to the nearest double (ties to even; a quotient of two
-// doubles is never exactly halfway) in integer arithmetic, for normal a, b
-// and a normal result; false otherwise (the caller divides in FP64).  The FP64
-// pipe of this GPU retires ~2 operations per clock per SM, a division takes
-// several, and the denominator and amplitude-update passes would be bound by
-// it; integer multiplies run far wider.  Method: a reciprocal R ~ 2^116/mb of
-// the divisor's 53-bit significand by Newton-Raphson (seed: the FP32
-// reciprocal of its top 24 bits; two steps R += R(2^116 - mb R)/2^116 in
-// 64-bit fixed point), the 55-bit quotient estimate Q = ma 2^s R / 2^116, and
-// the exact remainder ma 2^s - Q mb, which corrects Q to floor(ma 2^s / mb)
-// (Knuth, TAOCP vol. 2, 4.3.1: estimate a quotient digit, then fix it from
-// the remainder) and gives the sticky bit for the rounding.
-__device__ __forceinline__ bool div_rn_int(double a, double b, double* q) {
-  const uint64_t ua = uint64_t(__double_as_longlong(a)), ub = uint64_t(__double_as_longlong(b));
-  const int ea = int((ua >> 52) & 0x7FF), eb = int((ub >> 52) & 0x7FF);
-  if (ea == 0 || ea == 2047 || eb == 0 || eb == 2047) return false;
-  const uint64_t ma = (ua & ((1ull << 52) - 1)) | (1ull << 52);
-  const uint64_t mb = (ub & ((1ull << 52) - 1)) | (1ull << 52);
-  const uint32_t rb = uint32_t(__float_as_uint(__frcp_rn(float(uint32_t(mb >> 29)))));  // mb's top 24 bits: exact
-  const int er = int((rb >> 23) & 0xFF) - 127;  // the reciprocal lies in (2^-24, 2^-23]
-  const uint64_t rm = (rb & 0x7FFFFFu) | 0x800000u;
-  uint64_t R = er == -23 ? ~0ull : rm << (er + 64);  // 2^-23 exactly would be 2^64
-#pragma unroll
-  for (int it = 0; it < 2; ++it) {
-    const uint64_t plo = mb * R, phi = __umul64hi(mb, R);  // mb R (117 bits)
-    const uint64_t elo = 0ull - plo, ehi = (1ull << 52) - phi - (plo != 0 ? 1ull : 0ull);  // 2^116 - mb R
-    const int64_t e52 = int64_t((ehi << 12) | (elo >> 52));  // (2^116 - mb R) / 2^52, |.| < 2^43
-    const uint64_t d = __umul64hi(R, e52 < 0 ? uint64_t(-e52) : uint64_t(e52));
-    R = e52 < 0 ? R - d : R + d;
-  }
-  const int adj = ma < mb ? 1 : 0;
-  const int sh = 54 + adj;  // floor(ma 2^sh / mb) lies in [2^54, 2^55)
-  const int rs = 116 - sh;
-  uint64_t Q = (__umul64hi(ma, R) << (64 - rs)) | ((ma * R) >> rs);
-  int64_t rem = int64_t((ma << sh) - Q * mb);  // exact: |rem| < 2^63
-#pragma unroll
-  for (int it = 0; it < 3; ++it)
-    if (rem < 0) --Q, rem += int64_t(mb);
-#pragma unroll
-  for (int it = 0; it < 3; ++it)
-    if (rem >= int64_t(mb)) ++Q, rem -= int64_t(mb);
-  uint64_t mant = Q >> 2;
-  const uint64_t guard = (Q >> 1) & 1ull, sticky = (Q & 1ull) | (rem != 0 ? 1ull : 0ull);
-  mant += (guard && (sticky || (mant & 1ull))) ? 1ull : 0ull;
-  const int field = ea - eb + 1023 - adj;  // biased exponent of the quotient's leading bit
-  if (field < 1 || field > 2045) return false;
-  *q = __longlong_as_double(int64_t(((ua ^ ub) & (1ull << 63)) | ((uint64_t(field - 1) << 52) + mant)));
-  return true;
-}
+// a / b rounded to the nearest double: integer arithmetic (exact_fp.h) for
+// normal operands and results, the FP64 divide otherwise.
 __device__ __forceinline__ double div_rn(double a, double b) {
   double q;
   return div_rn_int(a, b, &q) ? q : __ddiv_rn(a, b);

@@ -44,6 +44,7 @@
 #include <type_traits>
 
 #include "a4g_internal.h"
+#include "exact_fp.h"
 #include "grouped.h"
 #include "ozaki.h"
 
@@ -265,34 +266,6 @@ __device__ __forceinline__ void two_sum_acc(float& hi, float& lo, float x) {
   lo = __fadd_rn(lo, e);
 }
 
-// The double nearest (ties to even) to u * 2^e2 with sign `neg`, u an
-// unsigned 64-bit magnitude, built with integer operations only (FP64
-// arithmetic is scarce on this GPU).  Results outside the normal range take
-// an FP64 path.
-__device__ __forceinline__ double u64_scaled_to_double(unsigned long long u, bool neg, int e2) {
-  if (u == 0) return 0.0;
-  const int nbits = 64 - __clzll((long long)u);
-  unsigned long long mant;
-  int e = e2;
-  if (nbits <= 53) {
-    mant = u << (53 - nbits);
-    e -= 53 - nbits;
-  } else {
-    const int sh = nbits - 53;
-    mant = u >> sh;
-    const unsigned long long rem = u & ((1ull << sh) - 1), half = 1ull << (sh - 1);
-    if (rem > half || (rem == half && (mant & 1ull))) ++mant;
-    e += sh;
-    if (mant == (1ull << 53)) mant >>= 1, ++e;
-  }
-  const int field = e + 52 + 1023;  // value = mant * 2^e, mant in [2^52, 2^53)
-  if (field >= 1 && field <= 2046)
-    return __longlong_as_double((long long)((neg ? (1ull << 63) : 0ull) | ((unsigned long long)field << 52) |
-                                            (mant & ((1ull << 52) - 1))));
-  const double v = ldexp(double(mant), e);
-  return neg ? -v : v;
-}
-
 // A row or column exponent of 2047 (the field of Inf and NaN) marks a panel
 // row that holds a non-finite value: digits cannot carry it, so every result
 // that row or column feeds is stored as NaN (in FP64 a NaN or an infinity in
@@ -456,28 +429,6 @@ __device__ __forceinline__ void tc_ld8_nowait(uint32_t taddr, uint32_t (&r)[8]) 
   asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
                : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7])
                : "r"(taddr));
-}
-
-// (neg ? -1 : 1) * v * 2^e2 rounded once to the nearest double (ties to
-// even), v a signed 64-bit integer: normalise, keep 53 bits, round on the 11
-// below, and build the bits by one addition (a mantissa that rounds up to
-// 2^53 carries into the exponent field).  Integer operations only (the FP64
-// pipe is scarce), branch-free for results in the normal range; the rest
-// takes u64_scaled_to_double.  Same bits as negating the result of
-// u64_scaled_to_double (a zero keeps the sign the negation gives it).
-__device__ __forceinline__ double i64_scaled_to_double(long long v, int e2, bool neg) {
-  const unsigned long long sign = (v < 0) != neg ? (1ull << 63) : 0ull;
-  const unsigned long long u = v < 0 ? (unsigned long long)(-v) : (unsigned long long)v;
-  const int n = __clzll((long long)(u | 1ull));  // u = 0 is mapped to a signed zero at the end
-  const unsigned long long norm = u << n;  // leading one at bit 63
-  unsigned long long mant = norm >> 11;    // 53 bits, leading one at bit 52
-  const unsigned long long rem = norm & 0x7FFull;
-  mant += (rem > 0x400ull || (rem == 0x400ull && (mant & 1ull))) ? 1ull : 0ull;
-  const int field = e2 + 63 - n + 1023;  // biased exponent of the leading one
-  if (u != 0 && (field < 1 || field > 2045)) return u64_scaled_to_double(u, sign != 0, e2);
-  const unsigned long long bits = u ? sign | ((((unsigned long long)(field - 1)) << 52) + mant)
-                                    : (neg ? (1ull << 63) : 0ull);
-  return __longlong_as_double((long long)bits);
 }
 
 // Direct form: what a thread needs to store its part of a tile (its row,
@@ -1152,20 +1103,6 @@ __global__ void __launch_bounds__(256) oz_split_rows_kernel(const OzSplitJob* __
 }
 
 // ------------------------------------------------------------------ recombine
-// The same for a two's-complement 128-bit integer N.
-__device__ __forceinline__ double i128_scaled_to_double(__int128 N, int e2) {
-  const bool neg = N < 0;
-  const unsigned __int128 u = neg ? (unsigned __int128)(-N) : (unsigned __int128)N;
-  const unsigned long long hi = (unsigned long long)(u >> 64);
-  if (hi == 0) return u64_scaled_to_double((unsigned long long)u, neg, e2);
-  // keep the top 63 bits and fold the rest into a sticky bit below them (the
-  // rounding position lies above it, so the rounding is exact)
-  const int sh = 65 - __clzll((long long)hi);  // u >> sh has 63 bits
-  const unsigned long long top = (unsigned long long)(u >> sh);
-  const bool sticky = (u & ((((unsigned __int128)1) << sh) - 1)) != 0;
-  return u64_scaled_to_double((top << 1) | (sticky ? 1ull : 0ull), neg, e2 + sh - 1);
-}
-
 // One block of 256 threads per 32-column strip of a tile, walked as 32x32
 // pieces (four elements per thread): every level's split partials of a piece
 // are loaded before any is used (20 loads in flight per thread at 5 slices),
