@@ -240,6 +240,11 @@ int a4g_energy_contract(int rank0, const int* index_values0, const int* ext0, co
  * extents may differ per triple (uneven segments).  Triples that share the
  * same D pointer are summed into that block.  A triple whose L or R pointer
  * is NULL is a zero block and is skipped (the `where`-clause skip).
+ * Split precision: a4g_batch_create reads the L and R blocks once (the
+ * autotuner times the GEMM forms on their digits; their values need not be
+ * final) and writes no D block.  A NaN or an infinity in an operand block
+ * makes every result of the row or column it feeds NaN (FP64 gives NaN or
+ * +-infinity there); other results keep the split form's accuracy.
  * ------------------------------------------------------------------------- */
 typedef struct a4g_triple {
   double* d;
