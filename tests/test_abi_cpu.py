@@ -69,3 +69,17 @@ def test_interpreter_style_caller_compiles_and_links(tmp_path):
     assert os.path.exists(exe)
     c_abi_helper.write_cases(str(tmp_path / "cases.txt"))
     assert (tmp_path / "cases.txt").stat().st_size > 0
+
+
+def test_header_compiles_as_c_and_cpp():
+    """The ABI header is plain C (a Fortran bind(c) or C host can include it)
+    and also compiles as C++."""
+    import shutil
+    import subprocess
+
+    for comp, lang, std in (("gcc", "c", "-std=c99"), ("g++", "c++", "-std=c++11")):
+        if not shutil.which(comp):
+            pytest.skip(f"no {comp}")
+        r = subprocess.run([comp, "-fsyntax-only", "-Wall", "-Werror", "-x", lang, std, HEADER],
+                           capture_output=True, text=True)
+        assert r.returncode == 0, r.stderr
