@@ -155,3 +155,39 @@ def triples_index_values(key, n_occ_segs: int):
     first, then virtual, as moa_seg_ranges lists them)."""
     a, i, b, j, c, k = key
     return [n_occ_segs + a + 1, i + 1, n_occ_segs + b + 1, j + 1, n_occ_segs + c + 1, k + 1]
+
+
+def ladder_slab_triples(R: BlockArray, V: BlockArray, T: BlockArray, a: int, b: int, v_slab: bool = False):
+    """Triples of one (a,b) slab of the ladder: R(a,b,i,j) += V(a,b,c,d)
+    T(c,d,i,j) for every (i,j) and (c,d).  v_slab: V holds only this slab's
+    blocks, keyed (0,0,c,d) (a buffer reused slab after slab)."""
+    nc, nd = len(V.segs[2]), len(V.segs[3])
+    ni, nj = len(T.segs[2]), len(T.segs[3])
+    out = []
+    for i, j in itertools.product(range(ni), range(nj)):
+        for c, d in itertools.product(range(nc), range(nd)):
+            rk, vk, tk = (a, b, i, j), ((0, 0, c, d) if v_slab else (a, b, c, d)), (c, d, i, j)
+            out.append((R.block(rk), V.block(vk), T.block(tk), R.ext(rk), V.ext(vk), T.ext(tk)))
+    return out
+
+
+def ladder_slab_array(R: BlockArray, V: BlockArray, T: BlockArray, a: int, b: int, v_slab: bool = True):
+    """The triples of ladder_slab_triples as a numpy a4g_triple array (block
+    addresses and extents), which the batch calls take without building a
+    Python tuple per triple."""
+    from .device import TRIPLE_DTYPE
+
+    nc, nd = len(V.segs[2]), len(V.segs[3])
+    ni, nj = len(T.segs[2]), len(T.segs[3])
+    ij = list(itertools.product(range(ni), range(nj)))
+    cd = list(itertools.product(range(nc), range(nd)))
+    rks = [(a, b) + x for x in ij for _ in cd]
+    vks = [((0, 0) if v_slab else (a, b)) + y for _ in ij for y in cd]
+    tks = [y + x for x in ij for y in cd]
+    out = np.zeros(len(rks), TRIPLE_DTYPE)
+    for col, arr, ks in (("d", R, rks), ("l", V, vks), ("r", T, tks)):
+        out[col] = np.uint64(arr.buf.data_ptr()) + np.uint64(8) * np.array([arr.offsets[k] for k in ks], np.uint64)
+        ext = out[col + "ext"]
+        ext[:, :4] = np.array([arr.ext(k) for k in ks], np.int32)
+        ext[:, 4:] = 1
+    return out

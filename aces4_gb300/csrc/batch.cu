@@ -9,12 +9,17 @@
 // is one call: pairs that feed the same destination block are summed in the
 // kernel, zero blocks (NULL operand) are never touched.
 #include <algorithm>
+#include <chrono>
 #include <cmath>
+#include <cstdio>
 #include <cstring>
 #include <deque>
 #include <map>
-#include <set>
 #include <memory>
+#include <mutex>
+#include <set>
+#include <unordered_map>
+#include <unordered_set>
 #include <vector>
 
 #include "a4g_internal.h"
@@ -38,6 +43,11 @@ struct a4g_batch {
   std::vector<void*> allocs;
   std::vector<std::pair<double*, int64_t>> zero_blocks;  // D blocks with no live pair (beta = 0)
   PlanRef* d_plans = nullptr;
+  // The triples as given at creation (or at the last rebind): a rebind maps
+  // their block pointers to the new ones and rewrites every device table that
+  // holds a block pointer from its host copy below.
+  int drank = 0, lrank = 0, rrank = 0;
+  std::vector<a4g_triple> bound;
   // FP64 grouped
   GroupedF64Tile* d_f64_tiles = nullptr;
   GroupedPair* d_f64_pairs = nullptr;
@@ -45,12 +55,28 @@ struct a4g_batch {
   double* d_f64_ws = nullptr;           // partial tiles when tiles are spread
   GroupedF64Reduce* d_f64_reds = nullptr;
   int n_f64_reds = 0;
+  std::vector<GroupedF64Tile> h_f64_tiles;
+  std::vector<GroupedPair> h_f64_pairs;
+  std::vector<GroupedF64Reduce> h_f64_reds;
   // split precision
   OzPanel* d_pa = nullptr;
   OzPanel* d_pb = nullptr;
   OzPanel* d_pb_view = nullptr;  // the split kernels' views of the B panels (stacked panels: one per member)
   int* d_exps = nullptr;
   size_t exps_bytes = 0;
+  size_t exps_a_bytes = 0;  // the A panels' exponents come first in d_exps, then the B panels'
+  // Held operand sides (0: A panels, 1: B panels, after any role exchange):
+  // their digits were sliced by a4g_batch_hold and runs do not slice them again.
+  bool held[2] = {false, false};
+  std::vector<OzDBlock> h_dblocks;
+  double** d_colptr = nullptr;
+  std::vector<double*> h_colptr;        // column bases: block + offDn of the column
+  std::vector<double*> h_colptr_block;  // the block each column base lies in
+  // Autotuning: taken from the process's tuning cache (keyed by the batch's
+  // structure), and the host time the autotuner spent at creation.
+  uint64_t signature = 0;
+  bool tuned_from_cache = false;
+  float autotune_ms = 0.f;
   // split jobs grouped by operand side (A: left blocks, B: right blocks) and
   // source layout; each set has its own CTA prefix sums for both passes
   struct JobSet {
@@ -62,6 +88,7 @@ struct a4g_batch {
     int64_t* d_prefix_split = nullptr;
     int njobs = 0;
     int64_t tiles_exp = 0, tiles_split = 0;
+    std::vector<OzSplitJob> h_jobs;  // host copy (a rebind rewrites the source pointers)
   };
   std::vector<JobSet> jobsets;
   OzDBlock* d_dblocks = nullptr;
@@ -120,6 +147,78 @@ struct a4g_batch {
 };
 
 namespace {
+
+// ------------------------------------------------------------ tuning cache
+// The autotuner's choice (GEMM form and split-K count) for one batch
+// structure, kept for the life of the process (and optionally saved to and
+// loaded from a file), so that a batch built again for the same structure (the
+// next iteration of the same contraction, a batch rebuilt per step) skips the
+// timing runs.
+struct TuneRecord {
+  int form = -1;
+  int nsplit = 0;
+  float score_ms[a4g_batch::kForms];
+  int split_candidates[2] = {0, 0};
+  float split_cost_ms[2] = {-1.f, -1.f};
+};
+std::mutex g_tune_mu;
+std::unordered_map<uint64_t, TuneRecord> g_tune;
+
+bool tune_get(uint64_t key, TuneRecord* out) {
+  std::lock_guard<std::mutex> lock(g_tune_mu);
+  auto it = g_tune.find(key);
+  if (it == g_tune.end()) return false;
+  *out = it->second;
+  return true;
+}
+
+void tune_put(uint64_t key, const TuneRecord& r) {
+  std::lock_guard<std::mutex> lock(g_tune_mu);
+  g_tune[key] = r;
+}
+
+// 64-bit FNV-1a over the bytes that decide the tuning.
+struct Fnv {
+  uint64_t h = 1469598103934665603ull;
+  void add(const void* p, size_t n) {
+    const unsigned char* c = static_cast<const unsigned char*>(p);
+    for (size_t i = 0; i < n; ++i) h = (h ^ c[i]) * 1099511628211ull;
+  }
+  template <class T>
+  void put(const T& v) {
+    add(&v, sizeof(v));
+  }
+};
+
+// Structure of a batch as the autotuner sees it: the options, the pattern,
+// every triple's extents, which triples share a block (blocks numbered in
+// order of first appearance, NULL as -1), the 16-byte alignment of each
+// operand block (it selects the split kernels' vector loads) and the GPU.
+uint64_t batch_signature(const a4g_batch* b, const int* ptrn, const a4g_triple* t, int64_t n) {
+  Fnv f;
+  f.put(uint32_t(0x41344731));  // format tag
+  f.put(ctx()->num_sms);
+  f.put(b->precision), f.put(b->slices), f.put(b->beta), f.put(b->negate), f.put(b->pipeline);
+  f.put(b->drank), f.put(b->lrank), f.put(b->rrank);
+  f.add(ptrn, sizeof(int) * size_t(b->lrank + b->rrank));
+  f.put(n);
+  std::unordered_map<const void*, int> id;
+  auto ident = [&](const void* p) -> int {
+    if (!p) return -1;
+    return id.emplace(p, int(id.size())).first->second;
+  };
+  for (int64_t i = 0; i < n; ++i) {
+    const a4g_triple& x = t[i];
+    f.add(x.dext, sizeof(int) * size_t(b->drank));
+    f.add(x.lext, sizeof(int) * size_t(b->lrank));
+    f.add(x.rext, sizeof(int) * size_t(b->rrank));
+    const int ids[3] = {ident(x.d), ident(x.l), ident(x.r)};
+    f.put(ids);
+    const int al = ((reinterpret_cast<uintptr_t>(x.l) & 15) == 0) | (((reinterpret_cast<uintptr_t>(x.r) & 15) == 0) << 1);
+    f.put(al);
+  }
+  return f.h;
+}
 
 template <class T>
 int upload(a4g_batch* b, const std::vector<T>& v, T** out) {
@@ -299,12 +398,15 @@ int build_f64(a4g_batch* b, const std::vector<DGroup>& groups, const std::vector
     b->d_f64_ws = static_cast<double*>(ws);
     if ((rc = upload(b, reds, &b->d_f64_reds))) return rc;
     b->n_f64_reds = int(reds.size());
+    b->h_f64_reds = reds;
     tiles.swap(spread);
   }
   if (tiles.size() > 0x7fffffffu) return fail(A4G_ERR_RANGE, "too many tiles");
   b->n_f64_tiles = int(tiles.size());
   int rc = upload(b, tiles, &b->d_f64_tiles);
   if (!rc) rc = upload(b, pairs, &b->d_f64_pairs);
+  b->h_f64_tiles = tiles;
+  b->h_f64_pairs = pairs;
   return rc;
 }
 
@@ -380,7 +482,10 @@ int build_ozaki(a4g_batch* b, const std::vector<DGroup>& groups, const std::vect
     colptr_at.push_back(colptr_host.size());
     for (int gm : st) {
       const GemmPlan& hm = plans[groups[gm].plan]->host;
-      for (int64_t n = 0; n < hm.N; ++n) colptr_host.push_back(groups[gm].d + hm.offDn[n]);
+      for (int64_t n = 0; n < hm.N; ++n) {
+        colptr_host.push_back(groups[gm].d + hm.offDn[n]);
+        b->h_colptr_block.push_back(groups[gm].d);
+      }
       ncols += hm.N;
     }
     if (ncols > 0x7fffffffLL) return fail(A4G_ERR_RANGE, "stacked destination too wide");
@@ -429,6 +534,9 @@ int build_ozaki(a4g_batch* b, const std::vector<DGroup>& groups, const std::vect
     int r = upload(b, colptr_host, &d_colptr);
     if (r) return r;
     for (size_t i = 0; i < dblocks.size(); ++i) dblocks[i].colptr = d_colptr + colptr_at[i];
+    b->d_colptr = d_colptr;
+    b->h_colptr = colptr_host;
+    b->h_dblocks = dblocks;
   }
   const int S = b->slices;
   int rc0 = oz_prepare();
@@ -440,6 +548,7 @@ int build_ozaki(a4g_batch* b, const std::vector<DGroup>& groups, const std::vect
   std::vector<MapBytes> maps_a(pa.size()), maps_b64(pb.size()), maps_b128(pb.size()), maps_b256(pb.size());
   size_t exps_total = 0;
   for (auto& p : pa) exps_total += ceil_to(p.rows, 2 * kOzBM);
+  b->exps_a_bytes = exps_total * sizeof(int);
   for (auto& p : pb)
     if (p.used) exps_total += ceil_to(p.rows, 2 * kOzBN);
   void* exps = nullptr;
@@ -555,6 +664,7 @@ int build_ozaki(a4g_batch* b, const std::vector<DGroup>& groups, const std::vect
     js.njobs = int(jobs.size());
     js.tiles_exp = pe.back();
     js.tiles_split = ps.back();
+    js.h_jobs = jobs;
     int r;
     if ((r = upload(b, jobs, &js.d_jobs)) || (r = upload(b, pe, &js.d_prefix_exp)) ||
         (r = upload(b, ps, &js.d_prefix_split)))
@@ -621,6 +731,11 @@ int build_ozaki(a4g_batch* b, const std::vector<DGroup>& groups, const std::vect
       direct_ok = direct_ok && di.kb_total >= 1 &&
                   (long double)di.kb_total * kOzBK * 16384.0L * weight < std::pow(2.0L, 62);
   }
+  // A batch of the same structure tuned before in this process: build only
+  // the form it chose, with the split-K count it chose.
+  TuneRecord cached;
+  const bool have_cached = !b->variant && tune_get(b->signature, &cached) && cached.form >= 0 &&
+                           cached.form < a4g_batch::kForms && (cached.form < 4 || direct_ok);
   std::vector<std::vector<OzTile>> form_tiles(a4g_batch::kForms);
   std::vector<std::vector<OzUnit>> form_units(a4g_batch::kForms);
   for (int f = 0; f < a4g_batch::kForms; ++f) {
@@ -631,6 +746,7 @@ int build_ozaki(a4g_batch* b, const std::vector<DGroup>& groups, const std::vect
     gf.tile_cols = (f == 2 || f == 3) ? 2 * kOzBN : kOzBN;
     const int P = gf.pair ? pairs : ctx()->num_sms;  // concurrent workers (CTAs or CTA pairs)
     if (P < 1 || (b->variant && b->variant != f + 1)) continue;
+    if (have_cached && f != cached.form) continue;
     if (gf.direct && !direct_ok) continue;
     std::vector<OzTile>& tiles = form_tiles[f];
     for (const OzTile& di : dinfo)
@@ -660,6 +776,7 @@ int build_ozaki(a4g_batch* b, const std::vector<DGroup>& groups, const std::vect
       if (eff >= 0.999) break;
     }
     if (gf.direct) nsplit = 1;
+    if (have_cached && !gf.direct && cached.nsplit > 0) nsplit = std::max(cached.nsplit, ns_min);
     gf.nsplit = nsplit;
     std::vector<OzUnit>& units = form_units[f];
     units = make_units(tiles, nsplit, gf.direct);
@@ -694,7 +811,14 @@ int build_ozaki(a4g_batch* b, const std::vector<DGroup>& groups, const std::vect
   for (int f = 0; f < a4g_batch::kForms; ++f)
     if (b->forms[f].built && (b->form < 0 || b->variant == f + 1)) b->form = f;
   if (b->form < 0) return fail(A4G_ERR_UNSUPPORTED, "no tensor-core GEMM form fits this GPU");
-  if (!b->variant) {
+  if (have_cached) {
+    for (int f = 0; f < a4g_batch::kForms; ++f) b->forms[f].score_ms = b->forms[f].tuned_ms = cached.score_ms[f];
+    for (int i = 0; i < 2; ++i)
+      b->split_candidates[i] = cached.split_candidates[i], b->split_cost_ms[i] = cached.split_cost_ms[i];
+    b->tuned_from_cache = true;
+  }
+  const auto tune_t0 = std::chrono::steady_clock::now();
+  if (!b->variant && !have_cached) {
     // The panels hold the operands' digits during the autotune: the tensor
     // cores draw far less power on zero panels and would run at clocks the
     // real step does not get.  So the exponent and split passes run once here
@@ -859,6 +983,15 @@ int build_ozaki(a4g_batch* b, const std::vector<DGroup>& groups, const std::vect
     if (scols) cudaFree(scols);
     if (scratch) cudaFree(scratch);
     if (rc) return rc;
+    TuneRecord rec;
+    rec.form = b->form;
+    rec.nsplit = b->forms[b->form].nsplit;
+    for (int f = 0; f < a4g_batch::kForms; ++f) rec.score_ms[f] = b->forms[f].score_ms;
+    for (int i = 0; i < 2; ++i)
+      rec.split_candidates[i] = b->split_candidates[i], rec.split_cost_ms[i] = b->split_cost_ms[i];
+    tune_put(b->signature, rec);
+    b->autotune_ms =
+        std::chrono::duration<float, std::milli>(std::chrono::steady_clock::now() - tune_t0).count();
   }
   // Pipeline of the chosen form (when the caller asks for one): GEMM parts
   // over consecutive split-K ranges; each k-major right-operand split job
@@ -942,6 +1075,44 @@ int build_ozaki(a4g_batch* b, const std::vector<DGroup>& groups, const std::vect
   return A4G_OK;
 }
 
+// Zeroes the exponents of the A panels (side 0) and/or the B panels (side 1).
+int clear_exps(a4g_batch* b, bool side_a, bool side_b, cudaStream_t s) {
+  const size_t a = b->exps_a_bytes, all = b->exps_bytes;
+  if (side_a && side_b) {
+    A4G_CUDA(cudaMemsetAsync(b->d_exps, 0, all, s));
+  } else if (side_a && a > 0) {
+    A4G_CUDA(cudaMemsetAsync(b->d_exps, 0, a, s));
+  } else if (side_b && all > a) {
+    A4G_CUDA(cudaMemsetAsync(reinterpret_cast<char*>(b->d_exps) + a, 0, all - a, s));
+  }
+  return A4G_OK;
+}
+
+// Exponent and split passes of the split jobs of one side (0: A, 1: B) or of
+// both (side < 0), split pipeline groups included.
+int slice_side(a4g_batch* b, int side, cudaStream_t s) {
+  int rc = clear_exps(b, side != 1, side != 0, s);
+  for (const auto& js : b->jobsets)
+    if (!rc && (side < 0 || side == (js.left ? 0 : 1)))
+      rc = oz_launch_exp(js.layout, js.d_jobs, js.d_prefix_exp, js.njobs, js.tiles_exp,
+                         js.left ? b->d_pa : b->d_pb_view, s);
+  for (const auto& js : b->jobsets)
+    if (!rc && (side < 0 || side == (js.left ? 0 : 1)))
+      rc = oz_launch_split(js.layout, js.d_jobs, js.d_prefix_split, js.njobs, js.tiles_split,
+                           js.left ? b->d_pa : b->d_pb_view, b->slices, s);
+  return rc;
+}
+
+// Drops the captured graph (its recorded launches no longer match the
+// batch), after the work queued on the device has finished with it.
+int drop_graph(a4g_batch* b) {
+  if (!b->graph) return A4G_OK;
+  A4G_CUDA(cudaDeviceSynchronize());
+  A4G_CUDA(cudaGraphExecDestroy(b->graph));
+  b->graph = nullptr;
+  return A4G_OK;
+}
+
 // ev (optional) receives 6 events: before phase 0 and after each of phases 0..4.
 int run(a4g_batch* b, cudaStream_t s, const cudaEvent_t* ev = nullptr) {
   int rc = A4G_OK;
@@ -963,17 +1134,19 @@ int run(a4g_batch* b, cudaStream_t s, const cudaEvent_t* ev = nullptr) {
     return A4G_OK;
   }
   const a4g_batch::GemmForm& gf = b->forms[b->form];
+  // a held side keeps the digits a4g_batch_hold sliced: no passes over it
+  auto sliced = [&](const a4g_batch::JobSet& js) { return !b->held[js.left ? 0 : 1]; };
   if (gf.n_tiles > 0) {
-    A4G_CUDA(cudaMemsetAsync(b->d_exps, 0, b->exps_bytes, s));
+    if ((rc = clear_exps(b, !b->held[0], !b->held[1], s))) return rc;
     for (const auto& js : b->jobsets)
-      if ((rc = oz_launch_exp(js.layout, js.d_jobs, js.d_prefix_exp, js.njobs, js.tiles_exp,
-                              js.left ? b->d_pa : b->d_pb_view, s)))
+      if (sliced(js) && (rc = oz_launch_exp(js.layout, js.d_jobs, js.d_prefix_exp, js.njobs, js.tiles_exp,
+                                            js.left ? b->d_pa : b->d_pb_view, s)))
         return rc;
   }
   if ((rc = mark(2))) return rc;
   auto split_group = [&](int g, cudaStream_t st) -> int {
     for (const auto& js : b->jobsets)
-      if (js.group == g) {
+      if (js.group == g && sliced(js)) {
         const int r = oz_launch_split(js.layout, js.d_jobs, js.d_prefix_split, js.njobs, js.tiles_split,
                                       js.left ? b->d_pa : b->d_pb_view, b->slices, st);
         if (r) return r;
@@ -1035,6 +1208,9 @@ int a4g_batch_create(a4g_batch** out, const int* ptrn, int drank, int lrank, int
   if (b->precision != A4G_PREC_FP64 && b->precision != A4G_PREC_OZAKI_BF16)
     return fail(A4G_ERR_ARG, "unknown precision mode");
   if (b->slices < 1 || b->slices > kOzMaxUsableSlices) return fail(A4G_ERR_ARG, "slices must be 1..7");
+  b->drank = drank, b->lrank = lrank, b->rrank = rrank;
+  if (n > 0) b->bound.assign(trip, trip + n);
+  if (b->precision == A4G_PREC_OZAKI_BF16) b->signature = batch_signature(b.get(), ptrn, trip, n);
 
   std::vector<const DevPlan*> plans;
   std::map<const DevPlan*, int> plan_index;
@@ -1188,8 +1364,10 @@ int a4g_batch_launches(const a4g_batch* b, int* kernels_per_run, int* gemm_parts
     k += b->n_f64_reds > 0 ? 1 : 0;
   } else if (b->forms[b->form].n_tiles > 0) {
     parts = b->parts;
+    int sliced = 0;  // job sets of a held side are not run
+    for (const auto& js : b->jobsets) sliced += b->held[js.left ? 0 : 1] ? 0 : 1;
     // exponents + splits, GEMM parts, recombine (folded into the GEMM by direct forms)
-    k += 2 * int(b->jobsets.size()) + parts + (b->forms[b->form].direct ? 0 : 1);
+    k += 2 * sliced + parts + (b->forms[b->form].direct ? 0 : 1);
   }
   if (kernels_per_run) *kernels_per_run = k;
   if (gemm_parts) *gemm_parts = parts;
@@ -1210,6 +1388,178 @@ int a4g_batch_form(const a4g_batch* b, int* form, float* tuned_ms, int n) {
   if (!b) return fail(A4G_ERR_ARG, "null batch");
   if (form) *form = b->precision == A4G_PREC_FP64 ? 0 : b->form + 1;
   for (int f = 0; f < n && tuned_ms; ++f) tuned_ms[f] = f < a4g_batch::kForms ? b->forms[f].score_ms : -1.f;
+  return A4G_OK;
+}
+
+int a4g_batch_rebind(a4g_batch* b, const a4g_triple* trip, int64_t n, void* stream) {
+  if (!b) return fail(A4G_ERR_ARG, "null batch");
+  if (n != int64_t(b->bound.size())) return fail(A4G_ERR_ARG, "rebind: the triple count differs from the batch's");
+  if (n > 0 && !trip) return fail(A4G_ERR_ARG, "null argument");
+  // old block -> new block, one entry per distinct block whatever its role
+  std::unordered_map<const void*, const void*> to;
+  auto map_one = [&](const void* o, const void* nw) { return to.emplace(o, nw).first->second == nw; };
+  bool moved = false, moved_l = false, moved_r = false;
+  for (int64_t i = 0; i < n; ++i) {
+    const a4g_triple &o = b->bound[size_t(i)], &t = trip[i];
+    if (!t.d) return fail(A4G_ERR_ARG, "rebind: triple with NULL destination");
+    if ((o.l == nullptr) != (t.l == nullptr) || (o.r == nullptr) != (t.r == nullptr))
+      return fail(A4G_ERR_ARG, "rebind: a zero block (NULL operand) must stay zero and a live block live (triple " +
+                                   std::to_string(i) + ")");
+    if (std::memcmp(o.dext, t.dext, sizeof(int) * size_t(b->drank)) ||
+        std::memcmp(o.lext, t.lext, sizeof(int) * size_t(b->lrank)) ||
+        std::memcmp(o.rext, t.rext, sizeof(int) * size_t(b->rrank)))
+      return fail(A4G_ERR_ARG, "rebind: block extents differ from the batch's (triple " + std::to_string(i) + ")");
+    if (!map_one(o.d, t.d) || (o.l && !map_one(o.l, t.l)) || (o.r && !map_one(o.r, t.r)))
+      return fail(A4G_ERR_ARG, "rebind: a block the batch's triples share maps to different new blocks (triple " +
+                                   std::to_string(i) + ")");
+    moved_l |= o.l != t.l;
+    moved_r |= o.r != t.r;
+    moved |= o.d != t.d || o.l != t.l || o.r != t.r;
+  }
+  {  // distinct destination blocks stay distinct (their sums would merge)
+    std::unordered_set<const void*> old_d, new_d;
+    for (const a4g_triple& o : b->bound)
+      if (old_d.insert(o.d).second && !new_d.insert(to[o.d]).second)
+        return fail(A4G_ERR_ARG, "rebind: two destination blocks map to one block");
+  }
+  if (!moved) return A4G_OK;
+  if ((b->held[b->swapped ? 1 : 0] && moved_l) || (b->held[b->swapped ? 0 : 1] && moved_r))
+    return fail(A4G_ERR_ARG, "rebind: the blocks of a held operand cannot move (release the hold first)");
+  auto mp = [&](const void* p) -> const void* {
+    if (!p) return p;
+    auto it = to.find(p);
+    return it == to.end() ? p : it->second;
+  };
+  cudaStream_t s = pick(stream);
+  // every table is rebuilt on the host, checked, then copied in stream order
+  // (runs queued before on `stream` still read the old tables)
+  auto put = [&](void* dev, const void* host, size_t bytes) -> int {
+    if (bytes) A4G_CUDA(cudaMemcpyAsync(dev, host, bytes, cudaMemcpyHostToDevice, s));
+    return A4G_OK;
+  };
+  int rc = A4G_OK;
+  if (b->precision == A4G_PREC_FP64) {
+    std::vector<GroupedPair> pairs = b->h_f64_pairs;
+    std::vector<GroupedF64Tile> tiles = b->h_f64_tiles;
+    std::vector<GroupedF64Reduce> reds = b->h_f64_reds;
+    for (auto& p : pairs)
+      p.l = static_cast<const double*>(mp(p.l)), p.r = static_cast<const double*>(mp(p.r));
+    for (auto& t : tiles) t.d = const_cast<double*>(static_cast<const double*>(mp(t.d)));
+    for (auto& r : reds) r.d = const_cast<double*>(static_cast<const double*>(mp(r.d)));
+    if ((rc = put(b->d_f64_pairs, pairs.data(), pairs.size() * sizeof(GroupedPair))) ||
+        (rc = put(b->d_f64_tiles, tiles.data(), tiles.size() * sizeof(GroupedF64Tile))) ||
+        (rc = put(b->d_f64_reds, reds.data(), reds.size() * sizeof(GroupedF64Reduce))))
+      return rc;
+    b->h_f64_pairs.swap(pairs);
+    b->h_f64_tiles.swap(tiles);
+    b->h_f64_reds.swap(reds);
+  } else {
+    std::vector<std::vector<OzSplitJob>> jobs(b->jobsets.size());
+    for (size_t i = 0; i < b->jobsets.size(); ++i) {
+      jobs[i] = b->jobsets[i].h_jobs;
+      for (OzSplitJob& j : jobs[i]) {
+        j.src = static_cast<const double*>(mp(j.src));
+        if (b->jobsets[i].layout != kOzGeneric && (reinterpret_cast<uintptr_t>(j.src) & 15) != 0)
+          return fail(A4G_ERR_ARG, "rebind: an operand block the batch reads with 16-byte loads is not 16-byte aligned");
+      }
+    }
+    std::vector<OzDBlock> dbl = b->h_dblocks;
+    for (OzDBlock& d : dbl) d.d = const_cast<double*>(static_cast<const double*>(mp(d.d)));
+    std::vector<double*> cols(b->h_colptr.size()), colblk(b->h_colptr.size());
+    for (size_t i = 0; i < cols.size(); ++i) {
+      double* blk = b->h_colptr_block[i];
+      colblk[i] = const_cast<double*>(static_cast<const double*>(mp(blk)));
+      cols[i] = colblk[i] + (b->h_colptr[i] - blk);
+    }
+    for (size_t i = 0; i < b->jobsets.size() && !rc; ++i)
+      rc = put(b->jobsets[i].d_jobs, jobs[i].data(), jobs[i].size() * sizeof(OzSplitJob));
+    if (rc || (rc = put(b->d_dblocks, dbl.data(), dbl.size() * sizeof(OzDBlock))) ||
+        (rc = put(b->d_colptr, cols.data(), cols.size() * sizeof(double*))))
+      return rc;
+    for (size_t i = 0; i < b->jobsets.size(); ++i) b->jobsets[i].h_jobs.swap(jobs[i]);
+    b->h_dblocks.swap(dbl);
+    b->h_colptr.swap(cols);
+    b->h_colptr_block.swap(colblk);
+  }
+  // zero-filled destination blocks are kernel arguments of a captured graph
+  bool zero_moved = false;
+  for (auto& z : b->zero_blocks) {
+    double* nz = const_cast<double*>(static_cast<const double*>(mp(z.first)));
+    zero_moved |= nz != z.first;
+    z.first = nz;
+  }
+  if (zero_moved && b->beta == 0 && (rc = drop_graph(b))) return rc;
+  b->bound.assign(trip, trip + n);
+  return A4G_OK;
+}
+
+int a4g_batch_hold(a4g_batch* b, int operand, int hold, void* stream) {
+  if (!b) return fail(A4G_ERR_ARG, "null batch");
+  if (operand != 0 && operand != 1) return fail(A4G_ERR_ARG, "operand must be 0 (left blocks) or 1 (right blocks)");
+  if (b->precision == A4G_PREC_FP64) return A4G_OK;  // nothing is sliced
+  const int side = b->swapped ? 1 - operand : operand;
+  const bool on = hold != 0;
+  int rc = A4G_OK;
+  if (on && b->forms[b->form].n_tiles > 0 && (rc = slice_side(b, side, pick(stream)))) return rc;
+  if (b->held[side] != on && (rc = drop_graph(b))) return rc;
+  b->held[side] = on;
+  return A4G_OK;
+}
+
+int a4g_batch_tuning(const a4g_batch* b, int* from_cache, float* autotune_ms) {
+  if (!b) return fail(A4G_ERR_ARG, "null batch");
+  if (from_cache) *from_cache = b->tuned_from_cache ? 1 : 0;
+  if (autotune_ms) *autotune_ms = b->autotune_ms;
+  return A4G_OK;
+}
+
+void a4g_tune_cache_clear(void) {
+  std::lock_guard<std::mutex> lock(g_tune_mu);
+  g_tune.clear();
+}
+
+int a4g_tune_cache_save(const char* path) {
+  if (!path) return fail(A4G_ERR_ARG, "null path");
+  std::FILE* f = std::fopen(path, "w");
+  if (!f) return fail(A4G_ERR_ARG, std::string("cannot write ") + path);
+  std::lock_guard<std::mutex> lock(g_tune_mu);
+  std::fprintf(f, "a4g-tune 1\n");
+  for (const auto& kv : g_tune) {
+    const TuneRecord& r = kv.second;
+    std::fprintf(f, "%016llx %d %d %d %d %.6g %.6g", static_cast<unsigned long long>(kv.first), r.form, r.nsplit,
+                 r.split_candidates[0], r.split_candidates[1], r.split_cost_ms[0], r.split_cost_ms[1]);
+    for (int i = 0; i < a4g_batch::kForms; ++i) std::fprintf(f, " %.6g", r.score_ms[i]);
+    std::fprintf(f, "\n");
+  }
+  const bool ok = std::fclose(f) == 0;
+  return ok ? A4G_OK : fail(A4G_ERR_ARG, std::string("cannot write ") + path);
+}
+
+int a4g_tune_cache_load(const char* path) {
+  if (!path) return fail(A4G_ERR_ARG, "null path");
+  std::FILE* f = std::fopen(path, "r");
+  if (!f) return fail(A4G_ERR_ARG, std::string("cannot read ") + path);
+  int version = 0;
+  if (std::fscanf(f, "a4g-tune %d", &version) != 1 || version != 1) {
+    std::fclose(f);
+    return fail(A4G_ERR_ARG, std::string(path) + " is not a tuning cache of this library");
+  }
+  std::vector<std::pair<uint64_t, TuneRecord>> recs;
+  for (;;) {
+    unsigned long long key = 0;
+    TuneRecord r;
+    if (std::fscanf(f, "%llx %d %d %d %d %g %g", &key, &r.form, &r.nsplit, &r.split_candidates[0],
+                    &r.split_candidates[1], &r.split_cost_ms[0], &r.split_cost_ms[1]) != 7)
+      break;
+    bool ok = true;
+    for (int i = 0; i < a4g_batch::kForms && ok; ++i) ok = std::fscanf(f, "%g", &r.score_ms[i]) == 1;
+    if (!ok || r.form < 0 || r.form >= a4g_batch::kForms || r.nsplit < 1) break;
+    recs.push_back({uint64_t(key), r});
+  }
+  const bool eof = std::feof(f) != 0;
+  std::fclose(f);
+  if (!eof) return fail(A4G_ERR_ARG, std::string("malformed record in ") + path);
+  for (const auto& kv : recs) tune_put(kv.first, kv.second);
   return A4G_OK;
 }
 

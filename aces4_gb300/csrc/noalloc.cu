@@ -69,7 +69,16 @@ extern "C" int a4g_add_sub_noalloc(int subtract, int rank, const int* d_labels, 
   }
   bool trivial = true;
   for (int i = 0; i < rank; ++i) trivial &= o2n[i] == i + 1;
-  cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);  // NULL: the legacy default stream
+  // NULL stream: the library's own stream when the library context already
+  // exists on this device (so the call stays ordered with the other a4g_*
+  // calls given NULL, which run there), else the CUDA legacy default stream.
+  // Neither choice allocates: the context is never created here.
+  cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+  if (!s) {
+    int dev = -1;
+    A4G_CUDA(cudaGetDevice(&dev));
+    if (ctx()->device >= 0 && ctx()->device == dev) s = ctx()->stream;
+  }
   const char *rb = reinterpret_cast<const char*>(r), *db = reinterpret_cast<const char*>(d);
   const bool overlap = rb < db + n * sizeof(double) && db < rb + n * sizeof(double);
   if (!trivial && overlap) {

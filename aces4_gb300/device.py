@@ -9,6 +9,8 @@ from __future__ import annotations
 
 import ctypes
 
+import numpy as np
+
 from ._lib import lib, last_error
 
 _i = ctypes.c_int
@@ -194,6 +196,43 @@ def _ext6(e):
     return (ctypes.c_int * 6)(*e)
 
 
+# numpy image of a4g_triple (96 bytes): block addresses and extents
+TRIPLE_DTYPE = np.dtype([("d", "<u8"), ("l", "<u8"), ("r", "<u8"), ("dext", "<i4", (6,)),
+                         ("lext", "<i4", (6,)), ("rext", "<i4", (6,))])
+
+
+def _triple_array(tl):
+    arr = (_Triple * max(1, len(tl)))()
+    for i, (d, l, r, de, le, re) in enumerate(tl):
+        arr[i].d, arr[i].l, arr[i].r = _ptr(d), _ptr(l), _ptr(r)
+        arr[i].dext, arr[i].lext, arr[i].rext = _ext6(de), _ext6(le), _ext6(re)
+    return arr
+
+
+def _triples_arg(triples):
+    """(pointer to an a4g_triple array, count, object keeping it alive) from
+    a list of (d, l, r, dext, lext, rext) or a TRIPLE_DTYPE numpy array."""
+    if isinstance(triples, np.ndarray):
+        if triples.dtype != TRIPLE_DTYPE or not triples.flags.c_contiguous:
+            raise TypeError("triple arrays must be contiguous numpy arrays of TRIPLE_DTYPE")
+        return ctypes.c_void_p(triples.ctypes.data), len(triples), triples
+    tl = list(triples)
+    return ctypes.cast(_triple_array(tl), ctypes.c_void_p), len(tl), tl
+
+
+def tune_cache_clear():
+    """Forget every autotuned choice of this process (a4g_tune_cache_clear)."""
+    lib().a4g_tune_cache_clear()
+
+
+def tune_cache_save(path: str):
+    _check(lib().a4g_tune_cache_save(str(path).encode()), "a4g_tune_cache_save")
+
+
+def tune_cache_load(path: str):
+    _check(lib().a4g_tune_cache_load(str(path).encode()), "a4g_tune_cache_load")
+
+
 class Batch:
     """One pardo step: every (D, L, R) block triple of one SIAL contraction
     statement, executed by one call.  Triples with the same D are summed into
@@ -205,21 +244,35 @@ class Batch:
 
     def __init__(self, ptrn, drank, lrank, rrank, triples, precision=PREC_FP64, slices=5, beta=0, variant=0,
                  negate=False, pipeline=0):
-        tl = list(triples)
-        arr = (_Triple * max(1, len(tl)))()
-        for i, (d, l, r, de, le, re) in enumerate(tl):
-            arr[i].d, arr[i].l, arr[i].r = _ptr(d), _ptr(l), _ptr(r)
-            arr[i].dext, arr[i].lext, arr[i].rext = _ext6(de), _ext6(le), _ext6(re)
+        arr, n, keep = _triples_arg(triples)
         opts = _Opts(precision, slices, beta, variant, int(bool(negate)), int(pipeline))
         h = ctypes.c_void_p(0)
         rc = lib().a4g_batch_create(ctypes.byref(h), _iarr(ptrn), _i(drank), _i(lrank), _i(rrank), arr,
-                                    ctypes.c_int64(len(tl)), ctypes.byref(opts))
+                                    ctypes.c_int64(n), ctypes.byref(opts))
         _check(rc, "a4g_batch_create")
         self._h = h
-        self._keep = tl  # the caller's buffers must outlive the batch
+        self._keep = keep  # the caller's buffers must outlive the batch
 
     def run(self, stream=None):
         _check(lib().a4g_batch_run(self._h, _stream(stream)), "a4g_batch_run")
+
+    def rebind(self, triples, stream=None):
+        """Point the batch at other blocks of the same shapes and sharing
+        (a4g_batch_rebind): triple i replaces triple i of the creation."""
+        arr, n, keep = _triples_arg(triples)
+        _check(lib().a4g_batch_rebind(self._h, arr, ctypes.c_int64(n), _stream(stream)), "a4g_batch_rebind")
+        self._keep = keep
+
+    def hold(self, operand: int, on: bool = True, stream=None):
+        """Slice operand 0 (L blocks) or 1 (R blocks) now and reuse its digits
+        in later runs (on=True), or release it (a4g_batch_hold)."""
+        _check(lib().a4g_batch_hold(self._h, _i(operand), _i(int(bool(on))), _stream(stream)), "a4g_batch_hold")
+
+    def tuning(self):
+        """{"from_cache": bool, "autotune_ms": host ms spent autotuning at creation}."""
+        c, ms = ctypes.c_int(0), ctypes.c_float(0)
+        _check(lib().a4g_batch_tuning(self._h, ctypes.byref(c), ctypes.byref(ms)), "a4g_batch_tuning")
+        return {"from_cache": bool(c.value), "autotune_ms": float(ms.value)}
 
     def run_graph(self, stream=None):
         _check(lib().a4g_batch_run_graph(self._h, _stream(stream)), "a4g_batch_run_graph")

@@ -192,18 +192,51 @@ def time_cpu_reference(pairs, ptrn, min_seconds: float = 0.0):
     return flops / dt / 1e12, n, dt, acc
 
 
+def reference_pairs(n_pairs: int):
+    """Host copies of the first n_pairs (V, T) block pairs of R(0,0,0,0) of
+    the bench's own data (the same generators and seed as the GPU arm: V slab
+    0 and the first chunk of T, generated on the device and copied out); on a
+    machine without a GPU, numpy data of the same distributions."""
+    import numpy as np
+
+    try:
+        import torch
+
+        gpu = torch.cuda.is_available()
+    except Exception:
+        gpu = False
+    nv = 16
+    vblk, tblk = 32 ** 4, 32 * 32 * 16 * 16
+    if gpu:
+        from aces4_gb300.blocks import BlockArray
+
+        vb = BlockArray([[V_SEG], [V_SEG], [V_SEG] * nv, [V_SEG] * nv])
+        gen_V_slab(torch, vb, 1234, 0)
+        t0 = torch.empty(1 << 27, dtype=torch.float64, device="cuda")
+        gen_T(torch, t0, 1234, limit=1 << 27)
+        torch.cuda.synchronize()
+        out = []
+        for q in range(n_pairs):  # pairs (c=0, d) of R(0,0,0,0): V(0,0,0,d), T(0,d,0,0)
+            d = q % nv
+            v = vb.block((0, 0, 0, d)).cpu().numpy().copy()
+            o = d * 16 * tblk  # T block (0,d,0,0) in (c,d,i,j) key order
+            out.append((v, t0[o:o + tblk].cpu().numpy().copy()))
+        del vb, t0
+        return out, True
+    rng = np.random.default_rng(11)
+    return [(rng.uniform(-1, 1, vblk) / 512.0, rng.normal(0, 0.1, tblk)) for _ in range(n_pairs)], False
+
+
 def run_reference_arm(args, rank: int):
     """--impl reference: CPU arm, rank 0 only."""
     if rank != 0:
         return
-    import numpy as np
     from oracle import oracle
 
     oracle.build()
     _, ptrn = oracle.get_contraction_ptrn(4, 4, 4, [1, 2, 3, 4, 1, 2, 5, 6, 5, 6, 3, 4])
-    rng = np.random.default_rng(11)
     n_pairs = args.cpu_pairs
-    pairs = [(rng.uniform(-1, 1, 32 ** 4) / 512.0, rng.normal(0, 0.1, 32 * 32 * 16 * 16)) for _ in range(n_pairs)]
+    pairs, same = reference_pairs(n_pairs)
     for _ in range(args.warmup):
         time_cpu_reference(pairs[:1], ptrn)
     vals = []
@@ -219,11 +252,15 @@ def run_reference_arm(args, rank: int):
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": "TFLOP/s", "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": step_s * 1e3, "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": WORKLOAD, "sample": f"{n_pairs} block pairs per step"},
+        "scaling": "strong" if args.workload == "ladder-full" else "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic",
+        "config": {"workload": full_workload_name(16, 4, 256) if args.workload == "ladder-full" else WORKLOAD,
+                   "sample": f"{n_pairs} block pairs per step", "same_data_as_gpu_arm": same},
         "cpu_baseline": {"value": value, "unit": "TFLOP/s", "cores": cores, "kind": "port",
-                         "sample": f"{n_pairs} of the 4096 block pairs (1024x256x1024) per step; oracle permute "
-                                   f"(OpenMP) + numpy OpenBLAS dgemm, all {cores} host threads"},
+                         "sample": f"{n_pairs} of the 4096 block pairs (1024x256x1024) of slab (0,0) per step "
+                                   + ("(the GPU arm's V slab 0 and T, same generators and seed)" if same else
+                                      "(numpy data of the same distributions: no GPU to generate the arm's own)")
+                                   + f"; oracle permute (OpenMP) + numpy OpenBLAS dgemm, all {cores} host threads"},
         "e2e": {"value": value, "unit": "TFLOP/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -367,6 +404,353 @@ def run_triples(args, world, rank, local):
             "clocks": clk.summary(),
         }
         print(json.dumps(line), flush=True)
+    if world > 1:
+        dist.destroy_process_group()
+
+
+def gen_T(torch, buf, seed: int, limit: int = 0):
+    """T(c,d,i,j) ~ N(0, 1e-2) with 1 % of its entries scaled by 1e3, on the
+    device from one seeded generator, in 2^27-element chunks of the flat
+    buffer (limit > 0: only the chunks below it, with the same values)."""
+    g = torch.Generator(device="cuda")
+    g.manual_seed(seed)
+    step = 1 << 27
+    for s in range(0, limit or buf.numel(), step):
+        t = buf[s:s + step]
+        t.normal_(0.0, 0.1, generator=g)
+        m = torch.rand(t.shape, device="cuda", generator=g) < 0.01
+        t[m] *= 1e3
+        del m
+
+
+def gen_V_slab(torch, buf, seed: int, slab: int, gen=None):
+    """V(a,b,c,d) of one (a,b) slab ~ U[-1,1]/512 (one kernel, seeded per slab)."""
+    g = gen if gen is not None else torch.Generator(device="cuda")
+    g.manual_seed(seed + 1 + slab)
+    buf.buf.uniform_(-1.0 / 512.0, 1.0 / 512.0, generator=g)
+
+
+FULL_FLOP_NOTE = "2*32^2*64^2*512^2 per slab"
+
+
+def full_workload_name(nv: int, no: int, nslabs: int) -> str:
+    v, o = V_SEG * nv, O_SEG * no
+    flop = 2.0 * V_SEG ** 2 * (O_SEG * no) ** 2 * v * v * nslabs
+    return (f"ladder R(a,b,i,j)+=V(a,b,c,d)T(c,d,i,j), o={o} ({no}x{O_SEG}), v={v} ({nv}x{V_SEG}), whole "
+            f"contraction: {nslabs} (a,b) slabs x {nv * nv * no * no} block pairs of "
+            f"{V_SEG * V_SEG}x{O_SEG * O_SEG}x{V_SEG * V_SEG} ({flop:.3g} flop)")
+
+
+def run_ladder_full(args, world, rank, local):
+    """The whole ladder contraction (the metric's definition): every (a,b) slab
+    of R(a,b,i,j) += V(a,b,c,d) T(c,d,i,j) at o=64, v=512.  One step = one
+    contraction: the batch is created (its tuning taken from the library's
+    tuning cache after the first, cold creation, which is timed apart), the T
+    blocks are sliced once (a4g_batch_hold), then for every slab its V blocks
+    are produced on the device into one of two slab buffers (the stand-in for
+    the integral or served-array source of V; full V is 550 GB), the batch is
+    rebound to that buffer and to the slab's R blocks, and run.  R (8.6 GB)
+    stays resident.  e2e: the same through the public API with T copied from
+    pinned host memory once per step, every slab's V streamed from a pinned
+    host pool and every slab's R blocks copied back, the copies on two copy
+    streams overlapping the compute."""
+    import numpy as np
+    import torch
+    import torch.distributed as dist
+
+    import aces4_gb300 as a4
+    from aces4_gb300.blocks import BlockArray, ladder_slab_array
+    from oracle import oracle
+
+    torch.cuda.set_device(local)
+    if world > 1:
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    a4.device.init(local)
+    stream = torch.cuda.Stream()
+    peaks, peak_kind = _peaks()
+    nv, no = args.nvseg, args.noseg
+    vs, os_ = [V_SEG] * nv, [O_SEG] * no
+    all_slabs = [(a, b) for a in range(nv) for b in range(nv)]
+    if args.slabs:
+        all_slabs = all_slabs[:args.slabs]
+    slabs = all_slabs[rank::world]  # pardo iterations are independent: ranks take disjoint slabs
+    S = args.slices
+    seed = 1234
+    T = BlockArray([vs, vs, os_, os_])
+    R = BlockArray([vs, vs, os_, os_])
+    Vb = [BlockArray([[V_SEG], [V_SEG], vs, vs]) for _ in range(2)]
+    gen_T(torch, T.buf, seed)
+    gvs = torch.Generator(device="cuda")
+    ierr, ptrn = a4.ref.get_contraction_ptrn(4, 4, 4, [1, 2, 3, 4, 1, 2, 5, 6, 5, 6, 3, 4])
+    assert ierr == 0
+    # the triple arrays of every slab (block addresses), built before timing
+    arrs = [ladder_slab_array(R, Vb[q % 2], T, a, b) for q, (a, b) in enumerate(slabs)]
+    slab_flop = 2.0 * V_SEG ** 2 * (O_SEG * no) ** 2 * (V_SEG * nv) ** 2
+    flops_total = slab_flop * len(all_slabs)
+    torch.cuda.synchronize()
+
+    def create():
+        return a4.device.Batch(ptrn, 4, 4, 4, arrs[0], precision=a4.device.PREC_OZAKI_BF16, slices=S,
+                               variant=args.variant)
+
+    # cold creation: the autotuner times the GEMM forms on slab 0's digits
+    gen_V_slab(torch, Vb[0], seed, 0, gvs)
+    torch.cuda.synchronize()
+    a4.device.tune_cache_clear()
+    t0 = time.perf_counter()
+    b = create()
+    cold_ms = (time.perf_counter() - t0) * 1e3
+    cold = {"create_ms": cold_ms, **b.tuning(), "form": b.form(), "split_k": b.splits(), "info": b.info()}
+    launches_full = b.launches()["kernels_per_run"]
+    b.close()
+
+    ev_hold = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+
+    def contraction(stats=None, check_last=False):
+        """One whole contraction on `stream`; stats (dict) collects per-phase sums."""
+        t_c = time.perf_counter()
+        bt = create()
+        create_ms = (time.perf_counter() - t_c) * 1e3
+        with torch.cuda.stream(stream):
+            ev_hold[0].record(stream)
+            bt.hold(1, True, stream=stream)
+            ev_hold[1].record(stream)
+            for q, (a, bb) in enumerate(slabs):
+                gen_V_slab(torch, Vb[q % 2], seed, a * nv + bb, gvs)
+                if q:
+                    bt.rebind(arrs[q], stream=stream)
+                bt.run_timed(stream)
+        ph = bt.timings()  # synchronises
+        if stats is not None:
+            stats["create_ms"] += create_ms
+            stats["hold_ms"] += ev_hold[0].elapsed_time(ev_hold[1])
+            stats["runs"] += ph["runs"]
+            for k in a4.device.Batch.PHASES:
+                stats[k] += ph[k]
+            stats["launches_held"] = bt.launches()["kernels_per_run"]
+        bt.close()
+
+    for _ in range(args.warmup):
+        contraction()
+    torch.cuda.synchronize()
+    stats = {"create_ms": 0.0, "hold_ms": 0.0, "runs": 0, **{k: 0.0 for k in a4.device.Batch.PHASES}}
+    if world > 1:
+        dist.barrier()
+    torch.cuda.synchronize()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    props = torch.cuda.get_device_properties(local)
+    gpu_id = f"GPU-{props.uuid}" if getattr(props, "uuid", None) else str(local)
+    with ClockSampler(gpu_id) as clk:
+        ev0.record(stream)
+        w0 = time.perf_counter()
+        for _ in range(args.steps):
+            contraction(stats)
+        ev1.record(stream)
+        torch.cuda.synchronize()
+        wall_ms = (time.perf_counter() - w0) * 1e3 / args.steps
+    if world > 1:
+        dist.barrier()
+    ms = max_over_ranks(ev0.elapsed_time(ev1) / args.steps)
+    value = flops_total / (ms * 1e-3) / 1e12
+    runs = max(1, stats["runs"])
+    phases = {k: stats[k] / runs for k in a4.device.Batch.PHASES if k != "zero_fill"}
+    per_step = {"create_ms": stats["create_ms"] / args.steps, "hold_T_ms": stats["hold_ms"] / args.steps,
+                "wall_ms": wall_ms}
+    # V generation alone (the slab source inside each step), 8 slabs
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with torch.cuda.stream(stream):
+        e0.record(stream)
+        for q in range(8):
+            gen_V_slab(torch, Vb[0], seed, q, gvs)
+        e1.record(stream)
+    torch.cuda.synchronize()
+    vgen_ms = e0.elapsed_time(e1) / 8
+
+    # checks: the last slab of the final step (its V is still in its buffer)
+    # and slab 0 (regenerated), each against the plain FP64 form on the GPU;
+    # one R block of slab 0 against the CPU oracle's BLAS path
+    fp64_ms = fp64_value = dgemm_tflops = None
+    blk_err = []
+    last_q = len(slabs) - 1
+    check = [(last_q, slabs[last_q], Vb[last_q % 2])]
+    if last_q != 0:
+        check.append((0, slabs[0], Vb[0]))
+    Rchk = BlockArray([[V_SEG], [V_SEG], os_, os_])
+    for q, (a, bb), buf in check:
+        if q == 0 and last_q != 0:
+            gen_V_slab(torch, buf, seed, a * nv + bb, gvs)
+            torch.cuda.synchronize()
+        arr = ladder_slab_array(Rchk, buf, T, 0, 0)
+        f = a4.device.Batch(ptrn, 4, 4, 4, arr, precision=a4.device.PREC_FP64)
+        f.run(stream)
+        torch.cuda.synchronize()
+        if fp64_ms is None and args.fp64_steps > 0:
+            e0.record(stream)
+            for _ in range(args.fp64_steps):
+                f.run(stream)
+            e1.record(stream)
+            torch.cuda.synchronize()
+            fp64_ms = e0.elapsed_time(e1) / args.fp64_steps
+            fp64_value = slab_flop / (fp64_ms * 1e-3) / 1e12
+        f.close()
+        for i in range(no):
+            for j in range(no):
+                o, n = R.offsets[(a, bb, i, j)], R.size((a, bb, i, j))
+                oc = Rchk.offsets[(0, 0, i, j)]
+                ref = Rchk.buf[oc:oc + n]
+                blk_err.append(float(torch.linalg.norm(R.buf[o:o + n] - ref) / torch.linalg.norm(ref)))
+    if fp64_ms is not None:
+        ga = torch.randn(4096, 4096, dtype=torch.float64, device="cuda")
+        gb = torch.randn(4096, 4096, dtype=torch.float64, device="cuda")
+        for _ in range(2):
+            torch.matmul(ga, gb)
+        torch.cuda.synchronize()
+        e0.record()
+        for _ in range(3):
+            torch.matmul(ga, gb)
+        e1.record()
+        torch.cuda.synchronize()
+        dgemm_tflops = 3 * 2 * 4096 ** 3 / (e0.elapsed_time(e1) * 1e-3) / 1e12
+        del ga, gb
+    err_oracle = cpu = None
+    if rank == 0 and not args.no_cpu and (nv, no) == (16, 4):
+        oracle.build()
+        a, bb = slabs[0]
+        pairs = [(Vb[0].block((0, 0, c, d)).cpu().numpy().copy(), T.block((c, d, 0, 0)).cpu().numpy().copy())
+                 for c in range(nv) for d in range(nv)]
+        _, _, _, acc = time_cpu_reference(pairs, ptrn)
+        o, n = R.offsets[(a, bb, 0, 0)], R.size((a, bb, 0, 0))
+        got = R.buf[o:o + n].cpu().numpy()
+        err_oracle = float(np.linalg.norm(got - acc) / np.linalg.norm(acc))
+        v_cpu, n_s, dt_s, _ = time_cpu_reference(pairs[: args.cpu_pairs], ptrn, min_seconds=args.cpu_seconds)
+        cores = os.cpu_count()
+        cpu = {"value": v_cpu, "unit": "TFLOP/s", "cores": cores, "kind": "port",
+               "sample": f"{n_s} block pairs (1024x256x1024) of slab (0,0) in {dt_s:.1f} s; oracle permute "
+                         f"(OpenMP) + numpy OpenBLAS dgemm, all {cores} host threads"}
+
+    # e2e through the public API from pinned host memory
+    e2e = None
+    if args.e2e_steps > 0:
+        P = max(1, min(args.e2e_pool, len(slabs)))
+        Th = torch.empty_like(T.buf, device="cpu").pin_memory()
+        Th.copy_(T.buf)
+        Rh = torch.empty_like(R.buf, device="cpu").pin_memory()
+        Vh = []
+        for q in range(P):
+            gen_V_slab(torch, Vb[0], seed, q, gvs)
+            h = torch.empty_like(Vb[0].buf, device="cpu").pin_memory()
+            h.copy_(Vb[0].buf)
+            Vh.append(h)
+        torch.cuda.synchronize()
+        h2d, d2h = torch.cuda.Stream(), torch.cuda.Stream()
+        # the host link alone: 4 V slabs host -> device on the copy stream
+        h0, h1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        with torch.cuda.stream(h2d):
+            h0.record(h2d)
+            for q in range(4):
+                Vb[q % 2].buf.copy_(Vh[q % P], non_blocking=True)
+            h1.record(h2d)
+        torch.cuda.synchronize()
+        h2d_gbs = 4 * Vh[0].numel() * 8 / (h0.elapsed_time(h1) * 1e-3) / 1e9
+        loaded = [torch.cuda.Event(), torch.cuda.Event()]
+        done = [torch.cuda.Event(), torch.cuda.Event()]
+        t_loaded = torch.cuda.Event()
+        slab_rng = []
+        for (a, bb) in slabs:
+            o0 = R.offsets[(a, bb, 0, 0)]
+            o1 = R.offsets[(a, bb, no - 1, no - 1)] + R.size((a, bb, no - 1, no - 1))
+            slab_rng.append((o0, o1))
+
+        def e2e_contraction():
+            with torch.cuda.stream(h2d):
+                T.buf.copy_(Th, non_blocking=True)
+                t_loaded.record(h2d)
+                Vb[0].buf.copy_(Vh[0], non_blocking=True)
+                loaded[0].record(h2d)
+            bt = create()
+            stream.wait_event(t_loaded)
+            bt.hold(1, True, stream=stream)
+            for q in range(len(slabs)):
+                k = q % 2
+                if q + 1 < len(slabs):  # the next slab's V, once slab q-1 is done with its buffer
+                    with torch.cuda.stream(h2d):
+                        if q >= 1:
+                            h2d.wait_event(done[(q + 1) % 2])
+                        Vb[(q + 1) % 2].buf.copy_(Vh[(q + 1) % P], non_blocking=True)
+                        loaded[(q + 1) % 2].record(h2d)
+                stream.wait_event(loaded[k])
+                if q:
+                    bt.rebind(arrs[q], stream=stream)
+                bt.run(stream)
+                done[k].record(stream)
+                with torch.cuda.stream(d2h):
+                    d2h.wait_event(done[k])
+                    o0, o1 = slab_rng[q]
+                    Rh[o0:o1].copy_(R.buf[o0:o1], non_blocking=True)
+            torch.cuda.synchronize()
+            bt.close()
+
+        e2e_contraction()  # warm-up (pinned pages touched, tuning cached)
+        torch.cuda.synchronize()
+        w0 = time.perf_counter()
+        for _ in range(args.e2e_steps):
+            e2e_contraction()
+        e2e_ms = max_over_ranks((time.perf_counter() - w0) * 1e3 / args.e2e_steps, device="cuda")
+        v_bytes = Vh[0].numel() * 8
+        e2e = {"value": flops_total / (e2e_ms * 1e-3) / 1e12, "unit": "TFLOP/s",
+               "h2d_bytes_per_step": T.buf.numel() * 8 + v_bytes * len(slabs),
+               "d2h_bytes_per_step": sum(o1 - o0 for o0, o1 in slab_rng) * 8, "ms_per_step": e2e_ms,
+               "steps": args.e2e_steps, "timer": "host wall clock around whole contractions (synchronised)",
+               "h2d_gbs_alone": h2d_gbs,
+               "v_source": f"each slab's V copied from a pool of {P} pinned host slabs (slab q reads pool[q % {P}])",
+               "pipelining": "slab q+1's V upload and slab q's R download overlap slab q's compute"}
+        del Th, Rh, Vh
+
+    if rank == 0:
+        gemm_ms = phases["gemm"]
+        bf16_flops = S * (S + 1) / 2 * slab_flop
+        achieved = bf16_flops / (gemm_ms * 1e-3) / 1e12
+        long_run = ms * args.steps >= 2000.0
+        peak_key = "bf16_tflops_sustained" if long_run else "bf16_tflops"
+        peak = peaks.get(peak_key, 1743.3 if long_run else 1933.6)
+        n_v = Vb[0].buf.numel()
+        launches = stats.get("launches_held", 0) * len(slabs) + (launches_full - stats.get("launches_held", 0))
+        out = {
+            "metric": METRIC, "value": value, "unit": "TFLOP/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "strong",
+            "vs_baseline": None, "dtype": f"f64 (Ozaki, {S} BF16 slices)", "data": "synthetic",
+            "config": {"workload": full_workload_name(nv, no, len(all_slabs)), "slices": S,
+                       "digits": "balanced base-256 (8-bit)", "slabs": len(all_slabs), "slabs_this_rank": len(slabs),
+                       "block_pairs_per_slab": cold["info"]["pairs"],
+                       "l2": f"per slab V {n_v * 8 / 1e9:.2f} GB + T {T.buf.numel() * 8 / 1e9:.2f} GB > 126 MB L2 "
+                             "(no flush needed)",
+                       "v_source": "each slab's V generated on the device inside the step (seeded per slab)",
+                       "parallelism": f"slabs split over {world} rank(s), no collective"},
+            "e2e": e2e,
+            "roofline": {"kernel": "oz_gemm_kernel (tcgen05 BF16 slice products)", "bound": "tensor",
+                         "achieved": achieved, "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak,
+                         "peak_kind": f"{peak_key} of {peak_kind} (timed region {ms * args.steps / 1e3:.1f} s)",
+                         "algorithmic_per_launch": f"{S * (S + 1) // 2} slice-pair GEMMs x {slab_flop:.3e} flop",
+                         "traffic": _traffic("oz_gemm_kernel")},
+            "fp64_plain": ({"value": fp64_value, "unit": "TFLOP/s", "ms_per_slab": fp64_ms,
+                            "kernel": "grouped DMMA (mma.sync f64), one slab",
+                            "roofline": {"bound": "fp64 pipe", "peak": dgemm_tflops,
+                                         "peak_kind": "cuBLAS DGEMM 4096^3 measured in this run",
+                                         "frac": fp64_value / dgemm_tflops}} if fp64_value else None),
+            "split_over_fp64": (value / world / fp64_value) if fp64_value else None,
+            "rel_err_max_block_vs_fp64_gpu": max(blk_err) if blk_err else None,
+            "rel_err_checked_slabs": [list(c[1]) for c in check],
+            "rel_err_block_vs_cpu_oracle": err_oracle,
+            "phases_ms_per_slab": phases,
+            "per_step": {**per_step, "v_generate_ms_per_slab": vgen_ms},
+            "create_cold": {"create_ms": cold["create_ms"], "autotune_ms": cold["autotune_ms"],
+                            "chosen": cold["form"]["name"], "autotune_scores_ms": cold["form"]["tuned_ms"],
+                            "split_k": cold["split_k"]},
+            "gpu_launches": launches * args.steps,
+            "cpu_baseline": cpu,
+            "clocks": clk.summary(),
+        }
+        print(json.dumps(out), flush=True)
     if world > 1:
         dist.destroy_process_group()
 
@@ -571,7 +955,8 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--slices", type=int, default=5)
     ap.add_argument("--fp64-steps", type=int, default=1)
-    ap.add_argument("--e2e-steps", type=int, default=10)
+    ap.add_argument("--e2e-steps", type=int, default=None,
+                    help="e2e steps (default: 2 whole contractions for ladder-full, 10 slab steps for ladder)")
     ap.add_argument("--cpu-pairs", type=int, default=16)
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--no-cpu", action="store_true")
@@ -581,13 +966,18 @@ def main():
     ap.add_argument("--noseg", type=int, default=4, help="occupied segments of 16 (4: o=64)")
     ap.add_argument("--tseg", type=int, default=24, help="triples: segment size (occupied: one segment)")
     ap.add_argument("--tnv", type=int, default=10, help="triples: virtual segments")
-    ap.add_argument("--workload", default="ladder",
-                    choices=["ladder", "triples", "ladder-small", "ring", "sparse", "blockops"],
-                    help="ladder: the o=64/v=512 ladder slab (the headline metric); triples: one triples energy "
-                         "step; ladder-small / ring / sparse: one pardo step of the o=10/v=48 ladder, the "
-                         "o=40/v=300 ring, the o=48/v=400 sparse ladder; blockops: the HBM-bound block kernels")
+    ap.add_argument("--e2e-pool", type=int, default=2, help="ladder-full e2e: distinct V slabs in pinned host memory")
+    ap.add_argument("--slabs", type=int, default=0, help="ladder-full: only the first N (a,b) slabs (0: all)")
+    ap.add_argument("--workload", default="ladder-full",
+                    choices=["ladder-full", "ladder", "triples", "ladder-small", "ring", "sparse", "blockops"],
+                    help="ladder-full: the whole o=64/v=512 ladder contraction, all (a,b) slabs (the headline "
+                         "metric); ladder: one slab of it; triples: one triples energy step; ladder-small / ring / "
+                         "sparse: one pardo step of the o=10/v=48 ladder, the o=40/v=300 ring, the o=48/v=400 "
+                         "sparse ladder; blockops: the HBM-bound block kernels")
     args = ap.parse_args()
 
+    if args.e2e_steps is None:
+        args.e2e_steps = 2 if args.workload == "ladder-full" else 10
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
@@ -602,6 +992,9 @@ def main():
         return
     if args.workload == "blockops":
         run_blockops(args, world, rank, local)
+        return
+    if args.workload == "ladder-full":
+        run_ladder_full(args, world, rank, local)
         return
 
     import numpy as np
@@ -620,7 +1013,8 @@ def main():
 
     V, T, R, trip = make_workload(torch, a4, slab=rank, seed=1234, nv=args.nvseg, no=args.noseg)
     workload = workload_name(args.nvseg, args.noseg)
-    _, ptrn = oracle.get_contraction_ptrn(4, 4, 4, [1, 2, 3, 4, 1, 2, 5, 6, 5, 6, 3, 4])
+    ierr, ptrn = a4.ref.get_contraction_ptrn(4, 4, 4, [1, 2, 3, 4, 1, 2, 5, 6, 5, 6, 3, 4])
+    assert ierr == 0
     split = a4.device.Batch(ptrn, 4, 4, 4, trip, precision=a4.device.PREC_OZAKI_BF16, slices=args.slices,
                             variant=args.variant)
     info = split.info()
@@ -781,7 +1175,7 @@ def main():
         out = {
             "metric": METRIC, "value": value, "unit": "TFLOP/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "bf16", "data": "synthetic",
+            "vs_baseline": None, "dtype": f"f64 (Ozaki, {S} BF16 slices)", "data": "synthetic",
             "config": {"workload": workload, "slices": S, "digits": "balanced base-256 (8-bit)", "block_pairs": info["pairs"],
                        "l2": f"inputs {n_elem * 8 / 1e9:.2f} GB > 126 MB L2 (no flush needed)",
                        "parallelism": f"replicas x{world}"},

@@ -174,8 +174,10 @@ int a4g_add_sub(int subtract, int rank, const int* d_labels, const int* r_labels
  * A4G_ERR_RANGE.  The array's device address is looked up on the first call
  * per device, so make that first call outside stream capture.  Calls share
  * the array: calls that overlap on the GPU race.  stream: the caller's
- * stream, NULL = the CUDA legacy default stream (this entry point never
- * creates the library's own stream). */
+ * stream; NULL = the library's own stream when the library is already
+ * initialised on the current device (the stream every other a4g_* call given
+ * NULL uses, so such calls stay ordered), else the CUDA legacy default stream
+ * (this entry point never creates the library's context or stream). */
 int a4g_add_sub_noalloc(int subtract, int rank, const int* d_labels, const int* r_labels,
                         const int* r_ext, double* d, const double* l, const double* r, void* stream);
 /* Sum of squares into *h_result (host), tensor_block_norm2_. Synchronous. */
@@ -317,6 +319,52 @@ int a4g_batch_launches(const a4g_batch* b, int* kernels_per_run, int* gemm_parts
  * GEMM's measured time + the workspace read and D traffic at the copy rate. */
 int a4g_batch_form(const a4g_batch* b, int* form, float* tuned_ms, int n);
 void a4g_batch_destroy(a4g_batch* b);
+
+/* ----------------------------------------------------------------------------
+ * One batch for a whole pardo loop.  A pardo loop runs the same statement over
+ * many segment tuples (src/sip/worker/loop_manager.cpp:289-314): every
+ * iteration has the same block shapes and differs only in which blocks it
+ * reads and writes (the ladder's 256 (a,b) slabs all read the same T blocks).
+ * These calls let one planned, autotuned batch serve every iteration.
+ * ------------------------------------------------------------------------- */
+
+/* Points the batch at other blocks of the same shapes.  Triple i replaces
+ * triple i of the creation (or of the previous rebind): the same count, the
+ * same extents, the same NULL (skipped) operands, and the same sharing —
+ * triples that named one block still name one block, distinct destination
+ * blocks stay distinct.  Operand blocks read with 16-byte loads must stay
+ * 16-byte aligned (blocks of a BlockArray-style allocation always are).  The
+ * batch's tables are rewritten by copies queued on `stream`, so runs queued
+ * earlier on that stream still use the old blocks and later runs the new
+ * ones: rebind on the stream the batch runs on.  A graph captured by
+ * a4g_batch_run_graph stays valid (it reads the tables), except that it is
+ * recaptured when a zero-filled destination block (beta 0, no live pair)
+ * moves.  Blocks of a held operand (a4g_batch_hold) cannot move. */
+int a4g_batch_rebind(a4g_batch* b, const a4g_triple* h_triples, int64_t n_triples, void* stream);
+
+/* Split precision: reuse an operand's BF16 digits across runs.  operand 0 =
+ * the triples' L blocks, 1 = their R blocks.  hold = 1 slices those blocks now
+ * (exponent and split passes queued on `stream`) and makes every later run
+ * skip both passes for them, so the caller promises not to change their
+ * values while held; hold = 1 again re-slices them (after the caller changed
+ * them).  hold = 0 releases: runs slice them again.  A captured graph is
+ * recaptured when the hold state changes.  FP64 batches accept and ignore it.
+ * The ladder's T blocks, identical for all 256 slabs, are sliced once per
+ * contraction this way. */
+int a4g_batch_hold(a4g_batch* b, int operand, int hold, void* stream);
+
+/* Whether the batch's GEMM form and split-K count came from the tuning cache
+ * (1) or from timing runs at creation (0), and the host milliseconds the
+ * autotuner spent at creation (0 from the cache or with a pinned variant). */
+int a4g_batch_tuning(const a4g_batch* b, int* from_cache, float* autotune_ms);
+/* The tuning cache: every autotuned split-precision batch records its choice
+ * under a key made from its structure (options, pattern, extents, block
+ * sharing, operand alignment, SM count); a batch created later with the same
+ * key takes the choice without timing.  The cache lives for the process;
+ * save/load keep it in a text file across processes. */
+void a4g_tune_cache_clear(void);
+int a4g_tune_cache_save(const char* path);
+int a4g_tune_cache_load(const char* path);
 
 #ifdef __cplusplus
 }

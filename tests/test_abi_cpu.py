@@ -83,3 +83,31 @@ def test_header_compiles_as_c_and_cpp():
         r = subprocess.run([comp, "-fsyntax-only", "-Wall", "-Werror", "-x", lang, std, HEADER],
                            capture_output=True, text=True)
         assert r.returncode == 0, r.stderr
+
+
+def test_tune_cache_file_round_trip(so, tmp_path):
+    """The tuning cache's text file loads and saves without a GPU; a file of
+    another format is rejected with A4G_ERR_ARG and leaves the cache as it was."""
+    so.a4g_tune_cache_save.argtypes = [ctypes.c_char_p]
+    so.a4g_tune_cache_load.argtypes = [ctypes.c_char_p]
+    so.a4g_tune_cache_clear()
+    src = tmp_path / "in.txt"
+    src.write_text("a4g-tune 1\n"
+                   "00000000deadbeef 3 19 19 38 16.9 17.2 39.3 39.9 19.8 16.9 -1 -1\n"
+                   "0123456789abcdef 4 1 0 0 -1 -1 53 54 29.4 24.4 25 25.3\n")
+    assert so.a4g_tune_cache_load(str(src).encode()) == 0
+    out = tmp_path / "out.txt"
+    assert so.a4g_tune_cache_save(str(out).encode()) == 0
+    lines = out.read_text().splitlines()
+    assert lines[0] == "a4g-tune 1"
+    recs = sorted(l.split()[:3] for l in lines[1:])
+    assert recs == [["00000000deadbeef", "3", "19"], ["0123456789abcdef", "4", "1"]]
+    bad = tmp_path / "bad.txt"
+    bad.write_text("something else\n")
+    assert so.a4g_tune_cache_load(str(bad).encode()) == 1
+    torn = tmp_path / "torn.txt"
+    torn.write_text("a4g-tune 1\n00000000deadbeef 3 nineteen\n")
+    assert so.a4g_tune_cache_load(str(torn).encode()) == 1
+    so.a4g_tune_cache_clear()
+    assert so.a4g_tune_cache_save(str(out).encode()) == 0
+    assert out.read_text().splitlines() == ["a4g-tune 1"]
