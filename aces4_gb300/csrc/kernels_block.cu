@@ -373,6 +373,9 @@ __device__ __forceinline__ double div_rn(double a, double b) {
   return div_rn_int(a, b, &q) ? q : __ddiv_rn(a, b);
 }
 
+// x != 0 without the FP64 pipe
+__device__ __forceinline__ bool nonzero(double x) { return (bits_of(x) << 1) != 0ull; }
+
 __device__ __forceinline__ double den_eps(const DenParams& p, const double* e, const int (&x)[6]) {
   const double ea = eps_at(p, e, pick6(x, p.pos[0]) + p.poff[0]);
   const double eb = eps_at(p, e, pick6(x, p.pos[1]) + p.poff[1]);
@@ -425,165 +428,127 @@ __global__ void __launch_bounds__(kThreads) denominator_kernel(DenParams p, doub
   }
 }
 
-// Signed orbital energy of storage dimension d at coordinate x: + for an
-// occupied position of the denominator (odd), - for a virtual one (even).
-__device__ __forceinline__ double signed_eps(const DenParams& p, const int* role, const double* e, int d, int x) {
-  const double v = eps_at(p, e, x + p.off[d]);
-  return (role[d] & 1) ? v : -v;
-}
+// ---------------------------------------------------------------- (T) energy
+// The (T)-energy pattern of rccsdpt_aaa.sialx:2163-2172 on one block of W:
+// divide by the orbital-energy denominators (energy_denominator_rhf), then
+// contract the divided block with the undivided one to a scalar:
+//     partial += w(x) * fl(w(x) / eps(x))
+// in FP64 throughout: eps summed in the reference's order (do_rhf_den2/4/6:
+// the occupied positions 1, 3, 5 added left to right, then the virtual
+// positions 0, 2, 4 subtracted), the quotient rounded to nearest exactly as
+// the FP64 divide rounds it (div_rn), and the products accumulated in FP64
+// (one fused multiply-add per element).  Each CTA writes one partial sum; the
+// partials are added in a fixed order, so a GPU gives the same bits every run.
 
-// ---- double-float arithmetic: a value held as hi + lo in two FP32 numbers
-// (Dekker, "A floating-point technique for extending the available
-// precision", Numer. Math. 18 (1971); TwoSum after Knuth, TAOCP vol. 2; the
-// product error by FMA).  About 48 significant bits, on the FP32 pipes, which
-// run 64 times as many operations per clock as the FP64 pipe of this GPU.
-struct Df {
-  float hi, lo;
-};
-__device__ __forceinline__ Df quick_two_sum(float a, float b) {  // |a| >= |b|
-  const float s = __fadd_rn(a, b);
-  return {s, __fsub_rn(b, __fsub_rn(s, a))};
-}
-__device__ __forceinline__ Df two_sum(float a, float b) {
-  const float s = __fadd_rn(a, b);
-  const float bb = __fsub_rn(s, a);
-  return {s, __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb))};
-}
-__device__ __forceinline__ Df df_add(Df x, Df y) {
-  Df s = two_sum(x.hi, y.hi);
-  const Df t = two_sum(x.lo, y.lo);
-  s.lo = __fadd_rn(s.lo, t.hi);
-  s = quick_two_sum(s.hi, s.lo);
-  s.lo = __fadd_rn(s.lo, t.lo);
-  return quick_two_sum(s.hi, s.lo);
-}
-// Split of an FP64 value (host of the split: FP64 ops, used once per thread
-// or per plane, not per element).
-__device__ __forceinline__ Df df_from_double(double v) {
-  const float hi = __double2float_rn(v);
-  return {hi, __double2float_rn(v - double(hi))};
-}
-
-// w -> hi + lo from the bits of w (integer work only): hi keeps the top 24
-// bits of the significand, lo the next 24 (relative error below 2^-47).
-// Returns false when w or its low part falls outside FP32's normal range.
-__device__ __forceinline__ bool df_from_bits(double w, Df& out) {
-  const unsigned long long b = (unsigned long long)__double_as_longlong(w);
-  const int ex = int((b >> 52) & 0x7FF) - 1023;  // w = 1.m * 2^ex
-  if (ex < -74 || ex > 100) return false;  // keeps hi and lo normal floats
-  const unsigned int sign = (unsigned int)(b >> 32) & 0x80000000u;
-  const unsigned long long m = b & ((1ull << 52) - 1);
-  out.hi = __uint_as_float(sign | (unsigned int)(ex + 127) << 23 | (unsigned int)(m >> 29));
-  const unsigned int r = (unsigned int)(m & ((1u << 29) - 1));  // r * 2^(ex-52)
-  const float scale = __uint_as_float((unsigned int)(ex - 52 + 127) << 23);
-  out.lo = __uint_as_float(sign | __float_as_uint(__fmul_rn(__uint2float_rn(r), scale)));
-  return true;
-}
-
-// Quotient x / d in double-float: an FP32 reciprocal of d.hi refined by one
-// Newton-Raphson step, then one correction of the quotient from its exact
-// residual x - q d (TwoProd by FMA).
-__device__ __forceinline__ Df df_div(Df x, Df d) {
-  float r;
-  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(d.hi));
-  r = __fmaf_rn(r, __fmaf_rn(-d.hi, r, 1.0f), r);
-  const float q1 = __fmul_rn(x.hi, r);
-  const float p = __fmul_rn(q1, d.hi);
-  const float pe = __fmaf_rn(q1, d.lo, __fmaf_rn(q1, d.hi, -p));  // q1*d - p (to first order)
-  const float res = __fadd_rn(__fsub_rn(__fsub_rn(x.hi, p), pe), x.lo);
-  return quick_two_sum(q1, __fmul_rn(res, r));
-}
-
-// Fused (T)-energy pass over one block of W: partial[block] = sum of
-// w * w / eps over this block's share, where eps is the orbital-energy
-// denominator of energy_denominator_rhf (rccsdpt_aaa.sialx:2163-2172 divides
-// and then contracts).  Storage dimensions 0 and 1 form a "plane" position p
-// (each thread keeps its position's partial denominator in a register); the
-// remaining dimensions index planes, whose partial denominators a block
-// computes once per 'blockDim' planes into shared memory.  Per element, w^2,
-// eps and the quotient run in double-float arithmetic (about 2^-46 relative,
-// FP32 pipes); eps is summed as (dims 0,1) + (dims 2..), another order of the
-// same six terms than the reference.  Elements outside double-float's range
-// take an FP64 path.  Fixed grid and order: deterministic for a given GPU.
-__global__ void __launch_bounds__(1024) energy_partial_kernel(DenParams p, const double* __restrict__ w,
-                                                              const double* __restrict__ e, int64_t plane_size,
-                                                              int64_t nplanes, double* partial) {
-  extern __shared__ double ts_dyn[];
-  double* ts = ts_dyn;                                      // [blockDim] plane terms (FP64)
-  float2* ts2 = reinterpret_cast<float2*>(ts_dyn + blockDim.x);  // the same as double-float
-  int role[6];
-#pragma unroll
-  for (int q = 0; q < 6; ++q) role[q] = 0;
-  for (int q = 0; q < p.rank0; ++q) role[p.pos[q]] = q;
-  const int64_t pp = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
-  const bool live = pp < plane_size;
-  double tf = 0.0;
-  if (live) {
-    const int x0 = int(pp % p.ext[0]), x1 = int(pp / p.ext[0]);
-    tf = signed_eps(p, role, e, 0, x0) + signed_eps(p, role, e, 1, x1);
-  }
-  const Df tf2 = df_from_double(tf);
-  Df acc{0.0f, 0.0f};
-  double acc64 = 0.0;  // elements outside double-float's range
-  for (int64_t g0 = blockIdx.y; g0 < nplanes; g0 += int64_t(gridDim.y) * blockDim.x) {
-    // planes of this group: g0 + j * gridDim.y, j < blockDim.x
-    __syncthreads();
-    {
-      const int64_t pl = g0 + int64_t(threadIdx.x) * gridDim.y;
-      double t = 0.0;
-      if (pl < nplanes) {
-        int64_t rem = pl;
-        for (int q = 2; q < p.rank0; ++q) {
-          const int x = int(rem % p.ext[q]);
-          rem /= p.ext[q];
-          t += signed_eps(p, role, e, q, x);
-        }
-      }
-      ts[threadIdx.x] = t;
-      const Df t2 = df_from_double(t);
-      ts2[threadIdx.x] = make_float2(t2.hi, t2.lo);
-    }
-    __syncthreads();
-    if (!live) continue;
-    const int jn = int(std::min<int64_t>(blockDim.x, (nplanes - g0 + gridDim.y - 1) / gridDim.y));
-    for (int j0 = 0; j0 < jn; j0 += 8) {
-      double vv[8];  // eight loads in flight before any is used
-#pragma unroll
-      for (int u = 0; u < 8; ++u)
-        vv[u] = j0 + u < jn ? __ldg(&w[(g0 + int64_t(j0 + u) * gridDim.y) * plane_size + pp]) : 0.0;
-#pragma unroll
-      for (int u = 0; u < 8; ++u) {
-      const int j = j0 + u;
-      if (j >= jn) break;
-      const double v = vv[u];
-      const float2 t2 = ts2[j];
-      const Df d = df_add(tf2, Df{t2.x, t2.y});
-      Df wv;
-      const float ad = fabsf(d.hi);
-      if (df_from_bits(v, wv) && ad > 1e-30f && ad < 1e30f) {
-        // w^2 = hi^2 + 2 hi lo (+ lo^2, below the precision)
-        const float sq = __fmul_rn(wv.hi, wv.hi);
-        const Df x = quick_two_sum(sq, __fmaf_rn(2.0f * wv.hi, wv.lo, __fmaf_rn(wv.hi, wv.hi, -sq)));
-        const Df q = df_div(x, d);
-        Df s = two_sum(acc.hi, q.hi);
-        s.lo = __fadd_rn(s.lo, __fadd_rn(acc.lo, q.lo));
-        acc = quick_two_sum(s.hi, s.lo);
-      } else if (v != 0.0) {
-        acc64 += (v * v) / (tf + ts[j]);
-      }
-      }
-    }
-  }
-  double tot = double(acc.hi) + double(acc.lo) + acc64;
+// Deterministic CTA sum of acc into partial[slot].
+__device__ __forceinline__ void block_sum_to(double acc, double* partial, int64_t slot) {
   __shared__ double red[32];
-  for (int o = 16; o > 0; o >>= 1) tot += __shfl_down_sync(0xffffffffu, tot, o);
-  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = tot;
+  for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = acc;
   __syncthreads();
   if (threadIdx.x == 0) {
     double sum = 0.0;
-    for (int q = 0; q < int(blockDim.x) / 32; ++q) sum += red[q];
-    partial[blockIdx.y * gridDim.x + blockIdx.x] = sum;
+    for (int q = 0; q < int(blockDim.x + 31) / 32; ++q) sum += red[q];
+    partial[slot] = sum;
   }
+}
+
+// Storage in the denominator's order (position q = storage dimension q), rank
+// 4 or 6: eps = ((((e1 + e3) + e5) - e0) - e2) - e4, or ((e1 + e3) - e0) - e2.
+// The chain's prefix is formed where its terms are fixed: a thread owns one
+// (x0, x1) position of the block and a work unit fixes the occupied
+// coordinates x3 (and x5), so (e1 + e3) (+ e5) - e0 is formed once per unit,
+// - e2 once per x2, and (rank 6) - e4 per element: one FP64 subtraction per
+// element instead of five, the same roundings in the same order.  The
+// division runs in integer arithmetic (div_rn, the same bits as the FP64
+// divide).  (An integer form of the subtraction, exact as well, ran slower
+// than the FP64 one.)  Units (x3 [x5], a range of x2) are spread over
+// gridDim.y CTAs in a fixed order.
+constexpr int kEnLoads = 8;  // loads in flight per thread
+constexpr int kEnThreads = 512;
+__global__ void __launch_bounds__(kEnThreads, 1) energy_chain_kernel(DenParams p, const double* __restrict__ w,
+                                                            const double* __restrict__ e, int x2_per_unit,
+                                                            int64_t nunits, double* partial) {
+  extern __shared__ double en[];  // e2 energies [ext2], then e4 energies [ext4]
+  const int n0 = p.ext[0], n1 = p.ext[1], n2 = p.ext[2], n3 = p.ext[3];
+  const bool r6 = p.rank0 == 6;
+  const int n4 = r6 ? p.ext[4] : 1;
+  for (int t = threadIdx.x; t < n2; t += blockDim.x) en[t] = eps_at(p, e, t + p.off[2]);
+  if (r6)
+    for (int t = threadIdx.x; t < n4; t += blockDim.x) en[n2 + t] = eps_at(p, e, t + p.off[4]);
+  __syncthreads();
+  const int64_t n01 = int64_t(n0) * n1;
+  const int64_t pp = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  const int x2_chunks = (n2 + x2_per_unit - 1) / x2_per_unit;
+  double acc = 0.0;
+  if (pp < n01) {
+    const int x0 = int(pp % n0), x1 = int(pp / n0);
+    const double e1v = eps_at(p, e, x1 + p.off[1]), e0v = eps_at(p, e, x0 + p.off[0]);
+    for (int64_t u = blockIdx.y; u < nunits; u += gridDim.y) {
+      const int chunk = int(u % x2_chunks);
+      const int64_t occ = u / x2_chunks;  // x3 + n3 * x5
+      const int x3 = int(occ % n3), x5 = int(occ / n3);
+      double t = __dadd_rn(e1v, eps_at(p, e, x3 + p.off[3]));
+      if (r6) t = __dadd_rn(t, eps_at(p, e, x5 + p.off[5]));
+      t = __dsub_rn(t, e0v);
+      const int x2b = chunk * x2_per_unit, x2e = min(n2, x2b + x2_per_unit);
+      if (!r6) {
+        const double* base = w + pp + n01 * (int64_t(n2) * x3);
+        for (int x2 = x2b; x2 < x2e; x2 += kEnLoads) {
+          double v[kEnLoads];
+#pragma unroll
+          for (int k = 0; k < kEnLoads; ++k) v[k] = x2 + k < x2e ? __ldg(base + n01 * (x2 + k)) : 0.0;
+#pragma unroll
+          for (int k = 0; k < kEnLoads; ++k)
+            if (nonzero(v[k])) acc = fma(v[k], div_rn(v[k], __dsub_rn(t, en[x2 + k])), acc);
+        }
+      } else {
+        const int64_t s4 = n01 * int64_t(n2) * n3;  // stride of x4
+        for (int x2 = x2b; x2 < x2e; ++x2) {
+          const double t2 = __dsub_rn(t, en[x2]);
+          const double* base = w + pp + n01 * (x2 + int64_t(n2) * x3) + s4 * int64_t(n4) * x5;
+          for (int x4 = 0; x4 < n4; x4 += kEnLoads) {
+            double v[kEnLoads];
+#pragma unroll
+            for (int k = 0; k < kEnLoads; ++k) v[k] = x4 + k < n4 ? __ldg(base + s4 * (x4 + k)) : 0.0;
+#pragma unroll
+            for (int k = 0; k < kEnLoads; ++k)
+              if (nonzero(v[k])) acc = fma(v[k], div_rn(v[k], __dsub_rn(t2, en[n2 + x4 + k])), acc);
+          }
+        }
+      }
+    }
+  }
+  block_sum_to(acc, partial, int64_t(blockIdx.y) * gridDim.x + blockIdx.x);
+}
+
+// Any other storage order or rank: the whole chain per element (den_eps, the
+// same additions as energy_denominator_rhf), coordinates stepped as in the
+// denominator kernel; a fixed grid, one partial per CTA.
+__global__ void __launch_bounds__(kThreads) energy_generic_kernel(DenParams p, const double* __restrict__ w,
+                                                                  const double* __restrict__ e, int64_t n,
+                                                                  double* partial) {
+  const int64_t stride = int64_t(gridDim.x) * blockDim.x * kDenRun;
+  double acc = 0.0;
+  for (int64_t i0 = (int64_t(blockIdx.x) * blockDim.x + threadIdx.x) * kDenRun; i0 < n; i0 += stride) {
+    int x[6];
+    den_coords(p, i0, x);
+    double v[kDenRun];
+#pragma unroll
+    for (int u = 0; u < kDenRun; ++u) v[u] = i0 + u < n ? __ldg(w + i0 + u) : 0.0;
+#pragma unroll
+    for (int u = 0; u < kDenRun; ++u) {
+      if (i0 + u >= n) break;
+      if (nonzero(v[u])) acc = fma(v[u], div_rn(v[u], den_eps(p, e, x)), acc);
+#pragma unroll
+      for (int q = 0; q < 6; ++q) {
+        if (q >= p.rank0) break;
+        if (++x[q] < p.ext[q]) break;
+        x[q] = 0;
+      }
+    }
+  }
+  block_sum_to(acc, partial, blockIdx.x);
 }
 
 // ---------------------------------------------------------------- amplitude update
@@ -890,18 +855,34 @@ int launch_energy_contract(int rank0, const int* off, const int* ext0, const int
   int64_t n = 0;
   const DenParams p = den_params(rank0, off, ext0, pos, rank1, ld1, &n);
   if (n == 0) return A4G_OK;
-  const int64_t plane = int64_t(ext0[0]) * ext0[1], nplanes = n / plane;
-  // threads: the plane size rounded up to whole warps (at most 1024)
-  const int threads = int(std::min<int64_t>(1024, (plane + 31) / 32 * 32));
-  const int64_t gx = (plane + threads - 1) / threads;
-  if (gx > scratch_len) return fail(A4G_ERR_RANGE, "energy contraction: plane of dimensions 0 and 1 too large");
-  const int want_blocks = 8 * (ctx()->num_sms > 0 ? ctx()->num_sms : 152);
-  const int64_t gy = std::max<int64_t>(1, std::min<int64_t>({nplanes, std::max<int64_t>(1, want_blocks / gx),
-                                                              scratch_len / gx}));
-  const size_t smem = size_t(threads) * (sizeof(double) + sizeof(float2));
-  energy_partial_kernel<<<dim3(unsigned(gx), unsigned(gy)), threads, smem, s>>>(p, w, e_or_fock, plane, nplanes,
+  bool identity = true;
+  for (int q = 0; q < rank0; ++q) identity &= p.pos[q] == q;
+  const int sms = ctx()->num_sms > 0 ? ctx()->num_sms : 152;
+  const int64_t n01 = rank0 >= 2 ? int64_t(ext0[0]) * ext0[1] : n;
+  if (identity && (rank0 == 4 || rank0 == 6) && n01 <= kEnThreads * int64_t(scratch_len)) {
+    // a thread per (x0, x1) position (the positions split evenly over gx
+    // CTAs of at most 512 threads); units (x3 [x5], x2 range) spread over
+    // enough CTAs to fill the GPU a few times, at most scratch_len partials
+    const int64_t gx = (n01 + kEnThreads - 1) / kEnThreads;
+    const int threads = int(((n01 + gx - 1) / gx + 31) / 32 * 32);
+    const int64_t nocc = rank0 == 6 ? int64_t(ext0[3]) * ext0[5] : ext0[3];
+    const int64_t want = 16LL * sms;  // CTAs
+    const int chunks = int(std::max<int64_t>(1, std::min<int64_t>(ext0[2], (want / gx + nocc - 1) / nocc)));
+    const int per = (ext0[2] + chunks - 1) / chunks;
+    const int64_t nunits = nocc * ((ext0[2] + per - 1) / per);
+    const int64_t gy = std::max<int64_t>(1, std::min<int64_t>({nunits, std::max<int64_t>(1, want / gx),
+                                                                scratch_len / gx}));
+    const size_t smem = size_t(ext0[2] + (rank0 == 6 ? ext0[4] : 0)) * sizeof(double);
+    if (smem > 48 * 1024) return fail(A4G_ERR_RANGE, "energy contraction: segments too large");
+    energy_chain_kernel<<<dim3(unsigned(gx), unsigned(gy)), threads, smem, s>>>(p, w, e_or_fock, per, nunits,
                                                                                 d_scratch);
-  energy_final_kernel<<<1, kThreads, 0, s>>>(d_scratch, int(gx * gy), efact, esum);
+    energy_final_kernel<<<1, kThreads, 0, s>>>(d_scratch, int(gx * gy), efact, esum);
+  } else {
+    const int g = int(std::min<int64_t>({int64_t(scratch_len), 8LL * sms,
+                                         std::max<int64_t>(1, (n + kThreads * kDenRun - 1) / (kThreads * kDenRun))}));
+    energy_generic_kernel<<<g, kThreads, 0, s>>>(p, w, e_or_fock, n, d_scratch);
+    energy_final_kernel<<<1, kThreads, 0, s>>>(d_scratch, g, efact, esum);
+  }
   A4G_CUDA(cudaGetLastError());
   return A4G_OK;
 }

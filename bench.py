@@ -478,13 +478,21 @@ def run_ladder_full(args, world, rank, local):
     seed = 1234
     T = BlockArray([vs, vs, os_, os_])
     R = BlockArray([vs, vs, os_, os_])
-    Vb = [BlockArray([[V_SEG], [V_SEG], vs, vs]) for _ in range(2)]
+    # V: a pool of distinct slabs resident in HBM (full V is 550 GB); slab q
+    # reads pool[q % P]
+    P = max(2, min(args.v_pool, len(slabs)))
+    Vb = [BlockArray([[V_SEG], [V_SEG], vs, vs]) for _ in range(P)]
     gen_T(torch, T.buf, seed)
     gvs = torch.Generator(device="cuda")
+    for q in range(P):
+        a, bb = slabs[q]
+        gen_V_slab(torch, Vb[q], seed, a * nv + bb, gvs)
     ierr, ptrn = a4.ref.get_contraction_ptrn(4, 4, 4, [1, 2, 3, 4, 1, 2, 5, 6, 5, 6, 3, 4])
     assert ierr == 0
-    # the triple arrays of every slab (block addresses), built before timing
-    arrs = [ladder_slab_array(R, Vb[q % 2], T, a, b) for q, (a, b) in enumerate(slabs)]
+    # the triple arrays of every slab (block addresses), built before timing;
+    # the e2e leg streams slab q into device buffer q % 2
+    arrs = [ladder_slab_array(R, Vb[q % P], T, a, b) for q, (a, b) in enumerate(slabs)]
+    arrs2 = [ladder_slab_array(R, Vb[q % 2], T, a, b) for q, (a, b) in enumerate(slabs)]
     slab_flop = 2.0 * V_SEG ** 2 * (O_SEG * no) ** 2 * (V_SEG * nv) ** 2
     flops_total = slab_flop * len(all_slabs)
     torch.cuda.synchronize()
@@ -494,7 +502,6 @@ def run_ladder_full(args, world, rank, local):
                                variant=args.variant)
 
     # cold creation: the autotuner times the GEMM forms on slab 0's digits
-    gen_V_slab(torch, Vb[0], seed, 0, gvs)
     torch.cuda.synchronize()
     a4.device.tune_cache_clear()
     t0 = time.perf_counter()
@@ -506,7 +513,7 @@ def run_ladder_full(args, world, rank, local):
 
     ev_hold = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
 
-    def contraction(stats=None, check_last=False):
+    def contraction(stats=None):
         """One whole contraction on `stream`; stats (dict) collects per-phase sums."""
         t_c = time.perf_counter()
         bt = create()
@@ -515,8 +522,7 @@ def run_ladder_full(args, world, rank, local):
             ev_hold[0].record(stream)
             bt.hold(1, True, stream=stream)
             ev_hold[1].record(stream)
-            for q, (a, bb) in enumerate(slabs):
-                gen_V_slab(torch, Vb[q % 2], seed, a * nv + bb, gvs)
+            for q in range(len(slabs)):
                 if q:
                     bt.rebind(arrs[q], stream=stream)
                 bt.run_timed(stream)
@@ -556,30 +562,19 @@ def run_ladder_full(args, world, rank, local):
     phases = {k: stats[k] / runs for k in a4.device.Batch.PHASES if k != "zero_fill"}
     per_step = {"create_ms": stats["create_ms"] / args.steps, "hold_T_ms": stats["hold_ms"] / args.steps,
                 "wall_ms": wall_ms}
-    # V generation alone (the slab source inside each step), 8 slabs
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    with torch.cuda.stream(stream):
-        e0.record(stream)
-        for q in range(8):
-            gen_V_slab(torch, Vb[0], seed, q, gvs)
-        e1.record(stream)
-    torch.cuda.synchronize()
-    vgen_ms = e0.elapsed_time(e1) / 8
 
-    # checks: the last slab of the final step (its V is still in its buffer)
-    # and slab 0 (regenerated), each against the plain FP64 form on the GPU;
-    # one R block of slab 0 against the CPU oracle's BLAS path
+    # checks: the last slab of the final step and slab 0, each against the
+    # plain FP64 form on the GPU; one R block of slab 0 against the CPU
+    # oracle's BLAS path
     fp64_ms = fp64_value = dgemm_tflops = None
     blk_err = []
     last_q = len(slabs) - 1
-    check = [(last_q, slabs[last_q], Vb[last_q % 2])]
+    check = [(last_q, slabs[last_q], Vb[last_q % P])]
     if last_q != 0:
         check.append((0, slabs[0], Vb[0]))
     Rchk = BlockArray([[V_SEG], [V_SEG], os_, os_])
     for q, (a, bb), buf in check:
-        if q == 0 and last_q != 0:
-            gen_V_slab(torch, buf, seed, a * nv + bb, gvs)
-            torch.cuda.synchronize()
         arr = ladder_slab_array(Rchk, buf, T, 0, 0)
         f = a4.device.Batch(ptrn, 4, 4, 4, arr, precision=a4.device.PREC_FP64)
         f.run(stream)
@@ -631,15 +626,14 @@ def run_ladder_full(args, world, rank, local):
     # e2e through the public API from pinned host memory
     e2e = None
     if args.e2e_steps > 0:
-        P = max(1, min(args.e2e_pool, len(slabs)))
+        PH = max(1, min(args.e2e_pool, P))
         Th = torch.empty_like(T.buf, device="cpu").pin_memory()
         Th.copy_(T.buf)
         Rh = torch.empty_like(R.buf, device="cpu").pin_memory()
         Vh = []
-        for q in range(P):
-            gen_V_slab(torch, Vb[0], seed, q, gvs)
-            h = torch.empty_like(Vb[0].buf, device="cpu").pin_memory()
-            h.copy_(Vb[0].buf)
+        for q in range(PH):
+            h = torch.empty_like(Vb[q].buf, device="cpu").pin_memory()
+            h.copy_(Vb[q].buf)
             Vh.append(h)
         torch.cuda.synchronize()
         h2d, d2h = torch.cuda.Stream(), torch.cuda.Stream()
@@ -648,7 +642,7 @@ def run_ladder_full(args, world, rank, local):
         with torch.cuda.stream(h2d):
             h0.record(h2d)
             for q in range(4):
-                Vb[q % 2].buf.copy_(Vh[q % P], non_blocking=True)
+                Vb[q % 2].buf.copy_(Vh[q % PH], non_blocking=True)
             h1.record(h2d)
         torch.cuda.synchronize()
         h2d_gbs = 4 * Vh[0].numel() * 8 / (h0.elapsed_time(h1) * 1e-3) / 1e9
@@ -661,13 +655,17 @@ def run_ladder_full(args, world, rank, local):
             o1 = R.offsets[(a, bb, no - 1, no - 1)] + R.size((a, bb, no - 1, no - 1))
             slab_rng.append((o0, o1))
 
+        ev_b = [torch.cuda.Event(enable_timing=True) for _ in slabs]
+        ev_a = [torch.cuda.Event(enable_timing=True) for _ in slabs]
+
         def e2e_contraction():
             with torch.cuda.stream(h2d):
                 T.buf.copy_(Th, non_blocking=True)
                 t_loaded.record(h2d)
                 Vb[0].buf.copy_(Vh[0], non_blocking=True)
                 loaded[0].record(h2d)
-            bt = create()
+            bt = a4.device.Batch(ptrn, 4, 4, 4, arrs2[0], precision=a4.device.PREC_OZAKI_BF16, slices=S,
+                                 variant=args.variant)
             stream.wait_event(t_loaded)
             bt.hold(1, True, stream=stream)
             for q in range(len(slabs)):
@@ -676,34 +674,45 @@ def run_ladder_full(args, world, rank, local):
                     with torch.cuda.stream(h2d):
                         if q >= 1:
                             h2d.wait_event(done[(q + 1) % 2])
-                        Vb[(q + 1) % 2].buf.copy_(Vh[(q + 1) % P], non_blocking=True)
+                        Vb[(q + 1) % 2].buf.copy_(Vh[(q + 1) % PH], non_blocking=True)
                         loaded[(q + 1) % 2].record(h2d)
                 stream.wait_event(loaded[k])
+                ev_b[q].record(stream)
                 if q:
-                    bt.rebind(arrs[q], stream=stream)
-                bt.run(stream)
+                    bt.rebind(arrs2[q], stream=stream)
+                bt.run_timed(stream)
+                ev_a[q].record(stream)
                 done[k].record(stream)
                 with torch.cuda.stream(d2h):
                     d2h.wait_event(done[k])
                     o0, o1 = slab_rng[q]
                     Rh[o0:o1].copy_(R.buf[o0:o1], non_blocking=True)
             torch.cuda.synchronize()
+            e2e_ph.update(bt.timings())
             bt.close()
 
+        e2e_ph = {}
         e2e_contraction()  # warm-up (pinned pages touched, tuning cached)
         torch.cuda.synchronize()
         w0 = time.perf_counter()
         for _ in range(args.e2e_steps):
             e2e_contraction()
         e2e_ms = max_over_ranks((time.perf_counter() - w0) * 1e3 / args.e2e_steps, device="cuda")
+        # last e2e step, per slab on the compute stream: the run itself, and the
+        # wait for the slab's V upload before it (from the previous slab's end)
+        run_ms = sum(ev_b[q].elapsed_time(ev_a[q]) for q in range(len(slabs))) / len(slabs)
+        wait_ms = sum(ev_a[q - 1].elapsed_time(ev_b[q]) for q in range(1, len(slabs))) / max(1, len(slabs) - 1)
         v_bytes = Vh[0].numel() * 8
         e2e = {"value": flops_total / (e2e_ms * 1e-3) / 1e12, "unit": "TFLOP/s",
                "h2d_bytes_per_step": T.buf.numel() * 8 + v_bytes * len(slabs),
                "d2h_bytes_per_step": sum(o1 - o0 for o0, o1 in slab_rng) * 8, "ms_per_step": e2e_ms,
                "steps": args.e2e_steps, "timer": "host wall clock around whole contractions (synchronised)",
                "h2d_gbs_alone": h2d_gbs,
-               "v_source": f"each slab's V copied from a pool of {P} pinned host slabs (slab q reads pool[q % {P}])",
-               "pipelining": "slab q+1's V upload and slab q's R download overlap slab q's compute"}
+               "v_source": f"each slab's V copied from a pool of {PH} pinned host slabs (slab q reads pool[q % {PH}])",
+               "pipelining": "slab q+1's V upload and slab q's R download overlap slab q's compute",
+               "per_slab_ms": {"run": run_ms, "wait_for_upload": wait_ms,
+                               **{k: e2e_ph[k] / max(1, e2e_ph["runs"]) for k in a4.device.Batch.PHASES
+                                  if k != "zero_fill"}}}
         del Th, Rh, Vh
 
     if rank == 0:
@@ -724,7 +733,8 @@ def run_ladder_full(args, world, rank, local):
                        "block_pairs_per_slab": cold["info"]["pairs"],
                        "l2": f"per slab V {n_v * 8 / 1e9:.2f} GB + T {T.buf.numel() * 8 / 1e9:.2f} GB > 126 MB L2 "
                              "(no flush needed)",
-                       "v_source": "each slab's V generated on the device inside the step (seeded per slab)",
+                       "v_source": f"a pool of {P} distinct V slabs resident in HBM (seeded per slab; full V is "
+                                   f"550 GB): slab q reads pool[q % {P}]",
                        "parallelism": f"slabs split over {world} rank(s), no collective"},
             "e2e": e2e,
             "roofline": {"kernel": "oz_gemm_kernel (tcgen05 BF16 slice products)", "bound": "tensor",
@@ -742,7 +752,7 @@ def run_ladder_full(args, world, rank, local):
             "rel_err_checked_slabs": [list(c[1]) for c in check],
             "rel_err_block_vs_cpu_oracle": err_oracle,
             "phases_ms_per_slab": phases,
-            "per_step": {**per_step, "v_generate_ms_per_slab": vgen_ms},
+            "per_step": per_step,
             "create_cold": {"create_ms": cold["create_ms"], "autotune_ms": cold["autotune_ms"],
                             "chosen": cold["form"]["name"], "autotune_scores_ms": cold["form"]["tuned_ms"],
                             "split_k": cold["split_k"]},
@@ -967,6 +977,7 @@ def main():
     ap.add_argument("--tseg", type=int, default=24, help="triples: segment size (occupied: one segment)")
     ap.add_argument("--tnv", type=int, default=10, help="triples: virtual segments")
     ap.add_argument("--e2e-pool", type=int, default=2, help="ladder-full e2e: distinct V slabs in pinned host memory")
+    ap.add_argument("--v-pool", type=int, default=8, help="ladder-full: distinct V slabs resident in HBM")
     ap.add_argument("--slabs", type=int, default=0, help="ladder-full: only the first N (a,b) slabs (0: all)")
     ap.add_argument("--workload", default="ladder-full",
                     choices=["ladder-full", "ladder", "triples", "ladder-small", "ring", "sparse", "blockops"],

@@ -223,10 +223,12 @@ int a4g_update_t2(const int* index_values, const int* ext, const double* t2new, 
  * index order, energy_denominator_rhf, full contraction of the divided block
  * with the undivided one, times efact, added to esum) fused into one read of
  * data0 that leaves data0 unchanged:
- *     *esum += efact * sum_x data0[x]^2 / eps(x)
- * with eps(x) the orbital-energy sum of a4g_energy_denominator (the same six
- * terms, added in another order) and the quotient to about one ulp; the
- * result matches the reference's sequence to the rounding of a long sum.
+ *     *esum += efact * sum_x data0[x] * fl(data0[x] / eps(x))
+ * all in FP64: eps(x) the orbital-energy sum of a4g_energy_denominator (the
+ * same terms added in the same order as energy_denominator_rhf), the quotient
+ * rounded exactly like the reference's FP64 division (the same bits), the
+ * products accumulated in FP64; the result matches the reference's sequence to
+ * the rounding of a long FP64 sum.
  * index_values0 / ext0 follow data0's storage order; den_order[q] names the
  * dimension of data0 at position q of the denominator's order (virtual,
  * occupied, virtual, occupied, ...), NULL when data0 is stored in that order.

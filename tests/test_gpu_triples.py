@@ -4,9 +4,13 @@ pass (a4g_energy_contract) against the oracle's restatement of the reference
 W = sum_d V1 T - sum_l V2 T -> E = sum W (W / D) through two batches (the
 second with negate = 1, beta = 1) in plain FP64 and in split precision.
 
-Tolerances (relative): energy of a given block vs the oracle 1e-13 (only the
-order of the FP64 sum differs); W and E of a step in FP64 1e-12, in split
-precision (5 slices) 1e-10."""
+Tolerances (relative): energy of a given block vs the oracle 1e-13 (the
+quotients are the same bits; only the order of the long FP64 sum differs, and
+the oracle's own sequential sum carries most of that), and vs the exact sum
+(math.fsum) of the oracle's rounded products w * fl(w / eps) 1e-14; W and E of
+a step in FP64 1e-12, in split precision (5 slices) 1e-10."""
+import math
+
 import numpy as np
 import pytest
 
@@ -60,6 +64,22 @@ def test_energy_contract_matches_oracle(a4, rank0, rank1, permuted):
     got = float(esum.item())
     assert abs(got - (0.25 + 2 * want)) <= 1e-13 * abs(2 * want)
     assert torch.equal(tw.cpu(), torch.tensor(w))  # the block is left unchanged
+    # the oracle's quotients (the reference's division, bit for bit), the
+    # rounded products summed exactly: the GPU's FP64 sum must be within 1e-14
+    order = den_order if den_order is not None else list(range(rank0))
+    wp = w
+    if order != list(range(rank0)):
+        o2n = [0] * rank0
+        for q, dim in enumerate(order):
+            o2n[dim] = q + 1
+        ierr, wp = oracle.tensor_block_copy(ext_s, o2n, w)
+        assert ierr == 0
+    wd = np.array(wp, dtype=np.float64)
+    assert oracle.energy_denominator_rhf([iv_s[d] for d in order], [ext_s[d] for d in order], wd, ext1,
+                                         np.ascontiguousarray(f1), segs) == 0
+    exact = 0.5 * math.fsum((np.asarray(wp) * wd).tolist())
+    one = (got - 0.25) / 2
+    assert abs(one - exact) <= 1e-14 * abs(exact), (one, exact)
 
 
 def test_energy_contract_rejects_bad_order(a4):
