@@ -77,6 +77,15 @@ struct a4g_batch {
   uint64_t signature = 0;
   bool tuned_from_cache = false;
   float autotune_ms = 0.f;
+  // A rebind's tables travel through a ring of pinned, mapped host slots and
+  // are put in place by a kernel (see copy_tables_kernel).
+  static constexpr int kStageRing = 4;
+  char* h_stage = nullptr;
+  char* d_stage = nullptr;  // the same memory as the device sees it
+  size_t stage_bytes = 0;
+  int stage_next = 0;
+  cudaEvent_t stage_ev[kStageRing] = {};
+  bool stage_busy[kStageRing] = {};
   // split jobs grouped by operand side (A: left blocks, B: right blocks) and
   // source layout; each set has its own CTA prefix sums for both passes
   struct JobSet {
@@ -136,6 +145,9 @@ struct a4g_batch {
   int timed_runs = 0;
 
   ~a4g_batch() {
+    for (int i = 0; i < kStageRing; ++i)
+      if (stage_ev[i]) cudaEventSynchronize(stage_ev[i]), cudaEventDestroy(stage_ev[i]);
+    if (h_stage) cudaFreeHost(h_stage);
     for (auto& ev : events)
       for (cudaEvent_t e : ev) cudaEventDestroy(e);
     for (cudaEvent_t e : part_ev) cudaEventDestroy(e);
@@ -1075,6 +1087,98 @@ int build_ozaki(a4g_batch* b, const std::vector<DGroup>& groups, const std::vect
   return A4G_OK;
 }
 
+// ------------------------------------------------------------ rebind tables
+// The tables a rebind rewrites are copied into place by this kernel, reading
+// a pinned, mapped host slot over the host link, on the caller's stream.  A
+// copy-engine transfer (cudaMemcpyAsync) would queue behind the caller's own
+// bulk host-to-device copies on the same engine — the next pardo iteration's
+// operands streaming in — and hold the stream for as long as they take.
+struct TableCopy {
+  const unsigned long long* src;
+  unsigned long long* dst;
+  int64_t words;  // 8-byte words
+};
+constexpr int kMaxTableCopies = 16;
+struct TableCopies {
+  TableCopy c[kMaxTableCopies];
+  int n;
+};
+
+__global__ void __launch_bounds__(256) copy_tables_kernel(TableCopies t) {
+  const int64_t stride = int64_t(gridDim.x) * blockDim.x;
+  for (int i = 0; i < t.n; ++i) {
+    const TableCopy c = t.c[i];
+    for (int64_t w = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; w < c.words; w += stride) c.dst[w] = c.src[w];
+  }
+}
+
+static_assert(sizeof(OzSplitJob) % 8 == 0 && sizeof(OzDBlock) % 8 == 0 && sizeof(GroupedPair) % 8 == 0 &&
+                  sizeof(GroupedF64Tile) % 8 == 0 && sizeof(GroupedF64Reduce) % 8 == 0,
+              "tables are copied in 8-byte words");
+
+// One rebind's worth of table copies staged in the next ring slot.
+struct Staging {
+  a4g_batch* b;
+  size_t used = 0;
+  int slot = 0;
+  std::vector<TableCopy> copies;
+  int add(void* dev, const void* host, size_t bytes) {
+    if (!bytes) return A4G_OK;
+    if (used + bytes > b->stage_bytes) return fail(A4G_ERR_RANGE, "rebind: staging slot overflow");
+    const size_t at = size_t(slot) * b->stage_bytes + used;
+    std::memcpy(b->h_stage + at, host, bytes);
+    copies.push_back({reinterpret_cast<const unsigned long long*>(b->d_stage + at),
+                      static_cast<unsigned long long*>(dev), int64_t(bytes / 8)});
+    used += bytes;
+    return A4G_OK;
+  }
+};
+
+// Takes the next ring slot (waiting for the copy that last read it), sized
+// for every table of the batch.
+int stage_begin(a4g_batch* b, size_t bytes, Staging* st) {
+  if (!b->h_stage || b->stage_bytes < bytes) {
+    for (int i = 0; i < a4g_batch::kStageRing; ++i)
+      if (b->stage_busy[i]) {
+        A4G_CUDA(cudaEventSynchronize(b->stage_ev[i]));
+        b->stage_busy[i] = false;
+      }
+    if (b->h_stage) cudaFreeHost(b->h_stage), b->h_stage = nullptr;
+    b->stage_bytes = std::max<size_t>(bytes, 8);
+    void* h = nullptr;
+    A4G_CUDA(cudaHostAlloc(&h, b->stage_bytes * a4g_batch::kStageRing, cudaHostAllocMapped));
+    b->h_stage = static_cast<char*>(h);
+    void* d = nullptr;
+    A4G_CUDA(cudaHostGetDevicePointer(&d, h, 0));
+    b->d_stage = static_cast<char*>(d);
+    for (int i = 0; i < a4g_batch::kStageRing; ++i)
+      if (!b->stage_ev[i]) A4G_CUDA(cudaEventCreateWithFlags(&b->stage_ev[i], cudaEventDisableTiming));
+  }
+  st->b = b;
+  st->slot = b->stage_next;
+  b->stage_next = (b->stage_next + 1) % a4g_batch::kStageRing;
+  if (b->stage_busy[st->slot]) A4G_CUDA(cudaEventSynchronize(b->stage_ev[st->slot]));
+  b->stage_busy[st->slot] = false;
+  return A4G_OK;
+}
+
+int stage_launch(Staging& st, cudaStream_t s) {
+  a4g_batch* b = st.b;
+  int64_t words = 0;
+  for (const TableCopy& c : st.copies) words = std::max(words, c.words);
+  const int grid = int(std::max<int64_t>(1, std::min<int64_t>(64, (words + 255) / 256)));
+  for (size_t i = 0; i < st.copies.size(); i += kMaxTableCopies) {
+    TableCopies t{};
+    t.n = int(std::min<size_t>(kMaxTableCopies, st.copies.size() - i));
+    for (int k = 0; k < t.n; ++k) t.c[k] = st.copies[i + size_t(k)];
+    copy_tables_kernel<<<grid, 256, 0, s>>>(t);
+    A4G_CUDA(cudaGetLastError());
+  }
+  A4G_CUDA(cudaEventRecord(b->stage_ev[st.slot], s));
+  b->stage_busy[st.slot] = true;
+  return A4G_OK;
+}
+
 // Zeroes the exponents of the A panels (side 0) and/or the B panels (side 1).
 int clear_exps(a4g_batch* b, bool side_a, bool side_b, cudaStream_t s) {
   const size_t a = b->exps_a_bytes, all = b->exps_bytes;
@@ -1433,11 +1537,18 @@ int a4g_batch_rebind(a4g_batch* b, const a4g_triple* trip, int64_t n, void* stre
   cudaStream_t s = pick(stream);
   // every table is rebuilt on the host, checked, then copied in stream order
   // (runs queued before on `stream` still read the old tables)
-  auto put = [&](void* dev, const void* host, size_t bytes) -> int {
-    if (bytes) A4G_CUDA(cudaMemcpyAsync(dev, host, bytes, cudaMemcpyHostToDevice, s));
-    return A4G_OK;
-  };
-  int rc = A4G_OK;
+  size_t total = 0;
+  if (b->precision == A4G_PREC_FP64) {
+    total = b->h_f64_pairs.size() * sizeof(GroupedPair) + b->h_f64_tiles.size() * sizeof(GroupedF64Tile) +
+            b->h_f64_reds.size() * sizeof(GroupedF64Reduce);
+  } else {
+    for (const auto& js : b->jobsets) total += js.h_jobs.size() * sizeof(OzSplitJob);
+    total += b->h_dblocks.size() * sizeof(OzDBlock) + b->h_colptr.size() * sizeof(double*);
+  }
+  Staging stg;
+  int rc = stage_begin(b, total, &stg);
+  if (rc) return rc;
+  auto put = [&](void* dev, const void* host, size_t bytes) { return stg.add(dev, host, bytes); };
   if (b->precision == A4G_PREC_FP64) {
     std::vector<GroupedPair> pairs = b->h_f64_pairs;
     std::vector<GroupedF64Tile> tiles = b->h_f64_tiles;
@@ -1448,7 +1559,8 @@ int a4g_batch_rebind(a4g_batch* b, const a4g_triple* trip, int64_t n, void* stre
     for (auto& r : reds) r.d = const_cast<double*>(static_cast<const double*>(mp(r.d)));
     if ((rc = put(b->d_f64_pairs, pairs.data(), pairs.size() * sizeof(GroupedPair))) ||
         (rc = put(b->d_f64_tiles, tiles.data(), tiles.size() * sizeof(GroupedF64Tile))) ||
-        (rc = put(b->d_f64_reds, reds.data(), reds.size() * sizeof(GroupedF64Reduce))))
+        (rc = put(b->d_f64_reds, reds.data(), reds.size() * sizeof(GroupedF64Reduce))) ||
+        (rc = stage_launch(stg, s)))
       return rc;
     b->h_f64_pairs.swap(pairs);
     b->h_f64_tiles.swap(tiles);
@@ -1474,7 +1586,7 @@ int a4g_batch_rebind(a4g_batch* b, const a4g_triple* trip, int64_t n, void* stre
     for (size_t i = 0; i < b->jobsets.size() && !rc; ++i)
       rc = put(b->jobsets[i].d_jobs, jobs[i].data(), jobs[i].size() * sizeof(OzSplitJob));
     if (rc || (rc = put(b->d_dblocks, dbl.data(), dbl.size() * sizeof(OzDBlock))) ||
-        (rc = put(b->d_colptr, cols.data(), cols.size() * sizeof(double*))))
+        (rc = put(b->d_colptr, cols.data(), cols.size() * sizeof(double*))) || (rc = stage_launch(stg, s)))
       return rc;
     for (size_t i = 0; i < b->jobsets.size(); ++i) b->jobsets[i].h_jobs.swap(jobs[i]);
     b->h_dblocks.swap(dbl);

@@ -659,13 +659,14 @@ def run_ladder_full(args, world, rank, local):
         ev_a = [torch.cuda.Event(enable_timing=True) for _ in slabs]
 
         def e2e_contraction():
+            # the batch first (its set-up copies would queue behind the uploads)
+            bt = a4.device.Batch(ptrn, 4, 4, 4, arrs2[0], precision=a4.device.PREC_OZAKI_BF16, slices=S,
+                                 variant=args.variant)
             with torch.cuda.stream(h2d):
                 T.buf.copy_(Th, non_blocking=True)
                 t_loaded.record(h2d)
                 Vb[0].buf.copy_(Vh[0], non_blocking=True)
                 loaded[0].record(h2d)
-            bt = a4.device.Batch(ptrn, 4, 4, 4, arrs2[0], precision=a4.device.PREC_OZAKI_BF16, slices=S,
-                                 variant=args.variant)
             stream.wait_event(t_loaded)
             bt.hold(1, True, stream=stream)
             for q in range(len(slabs)):
