@@ -85,6 +85,7 @@ SIGNATURES = {
     "a4g_batch_rebind": (ctypes.c_int, [c_void_p, c_void_p, ctypes.c_int64, c_void_p]),
     "a4g_batch_hold": (ctypes.c_int, [c_void_p, ctypes.c_int, ctypes.c_int, c_void_p]),
     "a4g_batch_tuning": (ctypes.c_int, None),
+    "a4g_batch_error_bound": (ctypes.c_int, [c_void_p, ctypes.c_double, c_double_p, c_void_p]),
     "a4g_tune_cache_clear": (None, []),
     "a4g_tune_cache_save": (ctypes.c_int, [ctypes.c_char_p]),
     "a4g_tune_cache_load": (ctypes.c_int, [ctypes.c_char_p]),

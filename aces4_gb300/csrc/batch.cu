@@ -14,6 +14,7 @@
 #include <cstdio>
 #include <cstring>
 #include <deque>
+#include <limits>
 #include <map>
 #include <memory>
 #include <mutex>
@@ -68,6 +69,17 @@ struct a4g_batch {
   // Held operand sides (0: A panels, 1: B panels, after any role exchange):
   // their digits were sliced by a4g_batch_hold and runs do not slice them again.
   bool held[2] = {false, false};
+  // Per destination block, what the certified error bound needs: the block,
+  // where its rows' and columns' exponents sit in d_exps, and the length of
+  // its k sum (the same for all of its elements).
+  struct ErrGroup {
+    double* d;
+    int64_t size;
+    int64_t rows, cols;
+    size_t exp_rows, exp_cols;  // element offsets into d_exps
+    double K;
+  };
+  std::vector<ErrGroup> err_groups;
   std::vector<OzDBlock> h_dblocks;
   double** d_colptr = nullptr;
   std::vector<double*> h_colptr;        // column bases: block + offDn of the column
@@ -481,6 +493,7 @@ int build_ozaki(a4g_batch* b, const std::vector<DGroup>& groups, const std::vect
     }
   }
   for (auto& p : pb) p.used = false;
+  std::vector<std::pair<int, int>> col_panel(groups.size());  // (B panel read, first row in it) per group
   std::map<std::vector<int>, int> stacked_index;  // member panels -> stacked panel
   std::vector<double*> colptr_host;  // every destination's column bases, concatenated
   std::vector<size_t> colptr_at;
@@ -524,6 +537,13 @@ int build_ozaki(a4g_batch* b, const std::vector<DGroup>& groups, const std::vect
       }
     }
     pb[c].used = true;
+    {
+      int row0 = 0;
+      for (int gm : st) {
+        col_panel[size_t(gm)] = {c, row0};
+        row0 += pb[gb[gm]].rows;
+      }
+    }
     const int db = int(dblocks.size());
     const bool col_fast = h.N > 1 && h.offDn[1] - h.offDn[0] == 1 && !(h.M > 1 && h.offDm[1] - h.offDm[0] == 1);
     OzDBlock od{};
@@ -598,6 +618,17 @@ int build_ozaki(a4g_batch* b, const std::vector<DGroup>& groups, const std::vect
   };
   if ((rc = make_panels(pa, hpa, maps_a, nullptr, nullptr, 2 * kOzBM))) return rc;
   if ((rc = make_panels(pb, hpb, maps_b128, &maps_b64, &maps_b256, 2 * kOzBN))) return rc;
+  for (size_t gi = 0; gi < groups.size(); ++gi) {
+    const DGroup& g = groups[gi];
+    const GemmPlan& h = plans[g.plan]->host;
+    a4g_batch::ErrGroup eg{};
+    eg.d = g.d;
+    eg.rows = h.M, eg.cols = h.N, eg.size = h.M * h.N;
+    eg.exp_rows = size_t(hpa[size_t(ga[gi])].exps - b->d_exps);
+    eg.exp_cols = size_t(hpb[size_t(col_panel[gi].first)].exps - b->d_exps) + size_t(col_panel[gi].second);
+    for (const Pair& p : g.pairs) eg.K += double(plans[p.plan]->host.K);
+    b->err_groups.push_back(eg);
+  }
   for (auto& p : hpa)
     if (p.kpad > 0x7fffffffLL || int64_t(S) * p.rows_pad > 0x7fffffffLL)
       return fail(A4G_ERR_RANGE, "panel exceeds TMA coordinate range");
@@ -1589,6 +1620,7 @@ int a4g_batch_rebind(a4g_batch* b, const a4g_triple* trip, int64_t n, void* stre
         (rc = put(b->d_colptr, cols.data(), cols.size() * sizeof(double*))) || (rc = stage_launch(stg, s)))
       return rc;
     for (size_t i = 0; i < b->jobsets.size(); ++i) b->jobsets[i].h_jobs.swap(jobs[i]);
+    for (auto& eg : b->err_groups) eg.d = const_cast<double*>(static_cast<const double*>(mp(eg.d)));
     b->h_dblocks.swap(dbl);
     b->h_colptr.swap(cols);
     b->h_colptr_block.swap(colblk);
@@ -1615,6 +1647,79 @@ int a4g_batch_hold(a4g_batch* b, int operand, int hold, void* stream) {
   if (on && b->forms[b->form].n_tiles > 0 && (rc = slice_side(b, side, pick(stream)))) return rc;
   if (b->held[side] != on && (rc = drop_graph(b))) return rc;
   b->held[side] = on;
+  return A4G_OK;
+}
+
+int a4g_batch_error_bound(a4g_batch* b, double target, double* h_bound, void* stream) {
+  if (!b || !h_bound) return fail(A4G_ERR_ARG, "null argument");
+  *h_bound = 0.0;
+  if (b->precision != A4G_PREC_OZAKI_BF16) return fail(A4G_ERR_UNSUPPORTED, "error bound: split-precision batches only");
+  if (b->beta) return fail(A4G_ERR_UNSUPPORTED, "error bound: the product alone is in D only with beta = 0");
+  cudaStream_t s = pick(stream);
+  const int S = b->slices;
+  // exponents of the last run, and the squared norm of every destination block
+  std::vector<int> ex(b->exps_bytes / sizeof(int));
+  const size_t ng = b->err_groups.size();
+  double* dev = nullptr;
+  const int64_t scratch = dot_scratch_len();
+  A4G_CUDA(cudaMallocAsync(reinterpret_cast<void**>(&dev), (ng + size_t(scratch)) * sizeof(double), s));
+  int rc = A4G_OK;
+  for (size_t i = 0; i < ng && !rc; ++i) {
+    const a4g_batch::ErrGroup& eg = b->err_groups[i];
+    rc = launch_dot(eg.d, eg.d, nullptr, nullptr, eg.size, dev + scratch + i, dev, scratch, s);
+  }
+  std::vector<double> nrm2(ng);
+  if (!rc && ng) {
+    A4G_CUDA(cudaMemcpyAsync(nrm2.data(), dev + scratch, ng * sizeof(double), cudaMemcpyDeviceToHost, s));
+  }
+  if (!rc) A4G_CUDA(cudaMemcpyAsync(ex.data(), b->d_exps, b->exps_bytes, cudaMemcpyDeviceToHost, s));
+  cudaFreeAsync(dev, s);
+  if (rc) return rc;
+  A4G_CUDA(cudaStreamSynchronize(s));
+  // |x| < 2^E for the stored biased exponent field f: E = f - 1022.  Per
+  // k, the digits carry each operand to within 2^(E - 8S) and the dropped
+  // levels t >= S add at most (S - 1) 2^(E + F - 8S) (1 + 2^-8 + ...), so
+  //   |D - LR|_mn <= c_S K 2^(E_m + F_n - 8S),  c_S = 1.004 (S - 1) + 2.001,
+  // and over a block ||D - LR||_F <= c_S K 2^-8S sqrt(sum_m 4^E_m sum_n 4^F_n)
+  // + 2^-53 ||D||_F (the final rounding); relative to ||LR||_F >= ||D||_F -
+  // that.  Sums in log2 to keep every exponent in range.
+  const double cS = 1.004 * (S - 1) + 2.001;
+  auto log2_sum4 = [&](size_t off, int64_t n, bool* nonfinite) {
+    int mx = 0;
+    for (int64_t i = 0; i < n; ++i) {
+      const int f = ex[off + size_t(i)];
+      if (f == 2047) *nonfinite = true;
+      mx = std::max(mx, f);
+    }
+    if (mx == 0) return -std::numeric_limits<double>::infinity();
+    double acc = 0.0;
+    for (int64_t i = 0; i < n; ++i) {
+      const int f = ex[off + size_t(i)];
+      if (f) acc += std::ldexp(1.0, 2 * (f - mx));
+    }
+    return 2.0 * (mx - 1022) + std::log2(acc);
+  };
+  double worst = 0.0;
+  for (size_t i = 0; i < ng; ++i) {
+    const a4g_batch::ErrGroup& eg = b->err_groups[i];
+    bool nonfinite = false;
+    const double lr = log2_sum4(eg.exp_rows, eg.rows, &nonfinite), lc = log2_sum4(eg.exp_cols, eg.cols, &nonfinite);
+    const double dn = std::sqrt(nrm2[i]);
+    double rel;
+    if (nonfinite || !std::isfinite(dn)) {
+      rel = std::numeric_limits<double>::infinity();
+    } else if (std::isinf(lr) || std::isinf(lc)) {
+      rel = 0.0;  // an all-zero operand side: the product is exactly zero
+    } else {
+      const double beta = std::exp2(std::log2(cS * eg.K) - 8.0 * S + 0.5 * (lr + lc)) + 0x1p-53 * dn;
+      rel = dn > beta ? beta / (dn - beta) : std::numeric_limits<double>::infinity();
+    }
+    worst = std::max(worst, rel);
+  }
+  *h_bound = worst;
+  if (target > 0.0 && !(worst <= target))
+    return fail(A4G_ERR_PRECISION, "certified relative error bound " + std::to_string(worst) + " exceeds the target " +
+                                       std::to_string(target) + " at " + std::to_string(S) + " slices");
   return A4G_OK;
 }
 

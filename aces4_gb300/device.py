@@ -268,6 +268,19 @@ class Batch:
         in later runs (on=True), or release it (a4g_batch_hold)."""
         _check(lib().a4g_batch_hold(self._h, _i(operand), _i(int(bool(on))), _stream(stream)), "a4g_batch_hold")
 
+    def error_bound(self, target: float = 0.0, stream=None):
+        """Certified relative Frobenius error bound of the last run, largest
+        over the destination blocks (a4g_batch_error_bound); raises
+        A4GError (status 8) when target > 0 and the bound exceeds it."""
+        out = ctypes.c_double(0.0)
+        rc = lib().a4g_batch_error_bound(self._h, ctypes.c_double(target), ctypes.byref(out), _stream(stream))
+        if rc == 8:
+            err = A4GError(rc, "a4g_batch_error_bound")
+            err.bound = out.value
+            raise err
+        _check(rc, "a4g_batch_error_bound")
+        return out.value
+
     def tuning(self):
         """{"from_cache": bool, "autotune_ms": host ms spent autotuning at creation}."""
         c, ms = ctypes.c_int(0), ctypes.c_float(0)

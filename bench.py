@@ -528,6 +528,7 @@ def run_ladder_full(args, world, rank, local):
                 bt.run_timed(stream)
         ph = bt.timings()  # synchronises
         if stats is not None:
+            stats["bound_last_slab"] = bt.error_bound(stream=stream)
             stats["create_ms"] += create_ms
             stats["hold_ms"] += ev_hold[0].elapsed_time(ev_hold[1])
             stats["runs"] += ph["runs"]
@@ -751,6 +752,7 @@ def run_ladder_full(args, world, rank, local):
             "split_over_fp64": (value / world / fp64_value) if fp64_value else None,
             "rel_err_max_block_vs_fp64_gpu": max(blk_err) if blk_err else None,
             "rel_err_checked_slabs": [list(c[1]) for c in check],
+            "certified_rel_err_bound_last_slab": stats.get("bound_last_slab"),
             "rel_err_block_vs_cpu_oracle": err_oracle,
             "phases_ms_per_slab": phases,
             "per_step": per_step,
@@ -1059,6 +1061,7 @@ def main():
     phases = split.timings()
     value = world * flops / (ms * 1e-3) / 1e12
     R_split = R.buf.clone()
+    bound = split.error_bound(stream=stream)
 
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     fp64_value = fp64_ms = dgemm_tflops = None
@@ -1205,6 +1208,7 @@ def main():
             "split_over_fp64": (value / world / fp64_value) if fp64_value else None,
             "rel_err_max_block_vs_fp64_gpu": max(blk_err) if blk_err else None,
             "rel_err_block_vs_cpu_oracle": err_oracle,
+            "certified_rel_err_bound": bound,
             "phases_ms_per_step": {k: phases[k] / runs for k in ("exponents", "split", "gemm", "recombine")},
             "gemm_form": {"chosen": form["name"], "autotune_ms": form["tuned_ms"],
                           "split_k": split.splits()},

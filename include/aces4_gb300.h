@@ -44,6 +44,7 @@ extern "C" {
 #define A4G_ERR_TIMEOUT 5    /* a device-side wait hit its iteration limit; kernel bailed out */
 #define A4G_ERR_UNSUPPORTED 6
 #define A4G_ERR_RANGE 7      /* size beyond a documented maximum                              */
+#define A4G_ERR_PRECISION 8  /* a certified error bound exceeds the requested target           */
 
 /* Text of the last error on the calling thread ("" when none). */
 const char* a4g_last_error(void);
@@ -354,6 +355,25 @@ int a4g_batch_rebind(a4g_batch* b, const a4g_triple* h_triples, int64_t n_triple
  * The ladder's T blocks, identical for all 256 slabs, are sliced once per
  * contraction this way. */
 int a4g_batch_hold(a4g_batch* b, int operand, int hold, void* stream);
+
+/* Certified accuracy of the last run of a split-precision batch (beta 0, so
+ * that D holds the product alone).  For every destination block it bounds
+ * the relative Frobenius error ||D - L*R||_F / ||L*R||_F for ANY data, from
+ * the run's own row and column exponents (E_m, F_n: |x| < 2^E over a row of
+ * the step) and the digit count S: per element and per k the digits carry each
+ * operand to within 2^(E - 8S) and the levels dropped by the triangular
+ * truncation add at most (S - 1) 2^(E + F - 8S) (1 + 2^-8 + ...), so
+ *   ||D - LR||_F <= c_S K 2^-8S sqrt(sum_m 4^E_m * sum_n 4^F_n) + 2^-53 ||D||_F
+ * with c_S = 1.004 (S - 1) + 2.001 and K the block's k length (the
+ * error-free-splitting bounds of Ozaki, Ogita, Oishi, Rump, Numer. Algorithms
+ * 59 (2012), for this digit layout), divided by ||LR||_F >= ||D||_F - bound.
+ * It is a worst case: every product's error is taken at its maximum with one
+ * sign, so on random data it lies orders of magnitude above the error
+ * measured against FP64.  *h_bound = the largest over the blocks (infinity
+ * for a block with a NaN or infinite operand).  Returns A4G_ERR_PRECISION when
+ * target > 0 and the bound exceeds it: more slices are needed to guarantee it.
+ * Synchronises `stream` (the stream of the run). */
+int a4g_batch_error_bound(a4g_batch* b, double target, double* h_bound, void* stream);
 
 /* Whether the batch's GEMM form and split-K count came from the tuning cache
  * (1) or from timing runs at creation (0), and the host milliseconds the
