@@ -48,36 +48,55 @@ static void stable_sort_by_key(int ni, const int* key, int* trn) {
   }
 }
 
-/* get_contraction_ptrn (tensor_dil_omp.F90:87-142).
+/* get_contraction_ptrn (tensor_dil_omp.F90:87-142), restated by counting
+ * labels instead of sorting them (the library's planner transliterates the
+ * reference's stable sort; this restatement takes another route to the same
+ * results, so each checks the other).
  * aces_ptrn = [d labels (drank), l labels (lrank), r labels (rrank)].
  * my_ptrn[0 .. lrank+rrank-1]: for an uncontracted operand index the 1-based
  * destination position; for a contracted one minus the 1-based position of
- * its partner in the other operand.  Returns ierr 1..6 as the reference. */
+ * its partner in the other operand.
+ * The reference sorts the positions by label (stably) and walks the sorted
+ * list in pairs: the first pair, in ascending label order, whose labels
+ * differ gives ierr 4, and a pair equal to the pair before it ierr 5.  In
+ * terms of counts: visiting the distinct labels in ascending order, the
+ * first label not used exactly twice decides: used once or three times,
+ * ierr 4 (its last use pairs with the next label); four or more times, ierr
+ * 5.  Then each label's two positions p < q (in index order) must be a
+ * destination position and an operand position (uncontracted), or a left
+ * and a right position (contracted); anything else is ierr 6. */
 int a4o_get_contraction_ptrn(int drank, int lrank, int rrank, const int* aces_ptrn, int* my_ptrn) {
   if (!(drank >= 0 && lrank >= 0 && rrank >= 0)) return 1;
   const int m = lrank + rrank, n = drank + m;
   if (n % 2 != 0) return 2;
   if (m <= 0) return drank > 0 ? 3 : 0;
-  int trn[3 * A4O_MAX_RANK + 2];
   if (n > 3 * A4O_MAX_RANK) return 1;
-  for (int i = 0; i < n; ++i) trn[i] = i + 1;
-  stable_sort_by_key(n, aces_ptrn, trn);
-  /* validity check, F90:108-116 (pairs (1,2),(3,4),... in 1-based terms) */
-  for (int i = 0; i + 1 < n; i += 2) {
-    if (aces_ptrn[trn[i] - 1] == aces_ptrn[trn[i + 1] - 1]) {
-      if (i > 0 && aces_ptrn[trn[i] - 1] == aces_ptrn[trn[i - 1] - 1]) return 5;
-    } else {
-      return 4;
-    }
+  /* the distinct labels in ascending order, each with its use count */
+  int below = 0, started = 0; /* every label <= below has been visited */
+  for (;;) {
+    int next = 0, found = 0;
+    for (int i = 0; i < n; ++i)
+      if ((!started || aces_ptrn[i] > below) && (!found || aces_ptrn[i] < next)) next = aces_ptrn[i], found = 1;
+    if (!found) break;
+    int count = 0;
+    for (int i = 0; i < n; ++i) count += aces_ptrn[i] == next;
+    if (count == 1 || count == 3) return 4;
+    if (count >= 4) return 5;
+    below = next, started = 1;
   }
-  /* pattern construction, F90:118-127 */
-  for (int i = 0; i + 1 < n; i += 2) {
-    const int j = trn[i], k = trn[i + 1];
-    if (j <= drank && k > drank) {
-      my_ptrn[k - drank - 1] = j;
-    } else if (j > drank && j <= drank + lrank && k > drank + lrank) {
-      my_ptrn[j - drank - 1] = -(k - (drank + lrank));
-      my_ptrn[k - drank - 1] = -(j - drank);
+  /* every label is used exactly twice: classify each pair of positions */
+  for (int p = 0; p < n; ++p) {
+    int q = -1;
+    for (int t = p + 1; t < n; ++t)
+      if (aces_ptrn[t] == aces_ptrn[p]) q = t;
+    if (q < 0) continue; /* p is the second use of its label */
+    const int p_in_d = p < drank, p_in_l = p >= drank && p < drank + lrank;
+    const int q_in_d = q < drank, q_in_r = q >= drank + lrank;
+    if (p_in_d && !q_in_d) {
+      my_ptrn[q - drank] = p + 1;
+    } else if (p_in_l && q_in_r) {
+      my_ptrn[p - drank] = -(q - drank - lrank + 1);
+      my_ptrn[q - drank] = -(p - drank + 1);
     } else {
       return 6;
     }

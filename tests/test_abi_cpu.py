@@ -111,3 +111,44 @@ def test_tune_cache_file_round_trip(so, tmp_path):
     so.a4g_tune_cache_clear()
     assert so.a4g_tune_cache_save(str(out).encode()) == 0
     assert out.read_text().splitlines() == ["a4g-tune 1"]
+
+
+def _lib_ptrn(so, dr, lr, rr, aces):
+    ierr = ctypes.c_int(-7)
+    out = (ctypes.c_int * max(1, lr + rr))()
+    arr = (ctypes.c_int * max(1, len(aces)))(*aces)
+    so.get_contraction_ptrn_(ctypes.byref(ctypes.c_int(dr)), ctypes.byref(ctypes.c_int(lr)),
+                             ctypes.byref(ctypes.c_int(rr)), arr, out, ctypes.byref(ierr))
+    return ierr.value, list(out)[: lr + rr]
+
+
+def test_pattern_golden_and_oracle_agree_with_library(so):
+    """The library's get_contraction_ptrn_ (a transliteration of the
+    reference's sort-based routine) against the fixtures and, on 20000 random
+    label lists of ranks 0..6, against the oracle's counting restatement."""
+    import random
+
+    from oracle import oracle
+    from tests import kat
+
+    for c in kat.cases():
+        if c["kind"] != "pattern" or min(c["drank"], c["lrank"], c["rrank"]) < 0:
+            continue
+        ierr, my = _lib_ptrn(so, c["drank"], c["lrank"], c["rrank"], c["aces"])
+        assert ierr == c["ierr"], c["name"]
+        if ierr == 0:
+            assert my == c["my_ptrn"], c["name"]
+    rng = random.Random(1142)
+    seen = set()
+    for _ in range(20000):
+        dr, lr, rr = rng.randint(0, 6), rng.randint(0, 6), rng.randint(0, 6)
+        if (dr + lr + rr) % 2 and rng.random() < 0.8:
+            rr = max(0, rr - 1) if rr else rr + 1
+        aces = [rng.randint(1, max(1, (dr + lr + rr) // 2 + rng.randint(0, 2))) for _ in range(dr + lr + rr)]
+        i1, m1 = _lib_ptrn(so, dr, lr, rr, aces)
+        i2, m2 = oracle.get_contraction_ptrn(dr, lr, rr, aces)
+        assert i1 == i2, (dr, lr, rr, aces, i1, i2)
+        if i1 == 0:
+            assert m1 == m2[: lr + rr], (dr, lr, rr, aces)
+        seen.add(i1)
+    assert seen >= {0, 2, 3, 4, 5, 6}

@@ -299,3 +299,64 @@ def test_legacy_gpu_api(lib):
     L._gpu_free(g)
     L._gpu_free(g2)
     assert ctypes.c_char_p(L.a4g_last_error()).value in (b"", None)
+
+
+# ---------------------------------------------------------------- restated reference routines on the GPU
+def _golden(kind):
+    return [c for c in kat.cases() if c["kind"] == kind]
+
+
+@pytest.mark.parametrize("c", _golden("denominator"), ids=lambda c: c["name"])
+def test_golden_denominator_gpu(lib, c):
+    """The fp2 drop-in and the device entry against the fixtures restated
+    from energy_denominator_rhf.F, bit for bit (rank 6 with 1-D energies:
+    left untouched, as the reference leaves it)."""
+    import torch
+
+    x = np.array(c["data"], dtype=np.float64)
+    e = np.array(c["e"], dtype=np.float64)
+    assert lib.ref.set_predefined_int_array("moa_seg_ranges", c["seg_sizes"]) == 0
+    assert lib.ref.energy_denominator_rhf(c["index_values"], c["ext"], x, c["ext1"], e) == 0
+    np.testing.assert_array_equal(x, np.array(c["expected"]))
+    if c["rank0"] == 6 and c["rank1"] != 2:
+        return  # the device entry rejects the combination the reference ignores
+    t = torch.tensor(c["data"], dtype=torch.float64, device="cuda")
+    lib.device.energy_denominator(c["index_values"], c["ext"], t, c["ext1"], torch.tensor(e, device="cuda"),
+                                  c["seg_sizes"])
+    np.testing.assert_array_equal(t.cpu().numpy(), np.array(c["expected"]))
+
+
+@pytest.mark.parametrize("c", _golden("update_t2"), ids=lambda c: c["name"])
+def test_golden_update_t2_gpu(lib, c):
+    import torch
+
+    d = lambda k: torch.tensor(c[k], dtype=torch.float64, device="cuda")
+    err, nxt = torch.empty_like(d("t2new")), torch.empty_like(d("t2new"))
+    nrm = torch.zeros(1, dtype=torch.float64, device="cuda")
+    lib.device.update_t2(c["index_values"], c["ext"], d("t2new"), d("t2new_pair"), d("t2old"), d("t2old_pair"),
+                         err, nxt, c["ext1"], d("fock"), c["seg_sizes"], nrm)
+    lib.device.sync()
+    np.testing.assert_array_equal(err.cpu().numpy(), np.array(c["expected_err"]))
+    np.testing.assert_array_equal(nxt.cpu().numpy(), np.array(c["expected_next"]))
+    assert abs(float(nrm.item()) - c["expected_norm2"]) <= 1e-14 * c["expected_norm2"]
+
+
+@pytest.mark.parametrize("c", _golden("energy"), ids=lambda c: c["name"])
+def test_golden_energy_gpu(lib, c):
+    import torch
+
+    esum = torch.zeros(1, dtype=torch.float64, device="cuda")
+    lib.device.energy_contract(c["index_values"], c["ext"], torch.tensor(c["w"], device="cuda"), c["ext1"],
+                               torch.tensor(c["fock"], device="cuda"), c["seg_sizes"], c["efact"], esum,
+                               den_order=c["den_order"])
+    lib.device.sync()
+    assert abs(float(esum.item()) - c["expected"]) <= 1e-14 * abs(c["expected"])
+
+
+@pytest.mark.parametrize("c", [c for c in _golden("pattern") if min(c["drank"], c["lrank"], c["rrank"]) >= 0],
+                         ids=lambda c: c["name"])
+def test_golden_pattern_dropin(lib, c):
+    ierr, my = lib.ref.get_contraction_ptrn(c["drank"], c["lrank"], c["rrank"], c["aces"])
+    assert ierr == c["ierr"]
+    if ierr == 0:
+        assert list(my)[: c["lrank"] + c["rrank"]] == c["my_ptrn"]

@@ -320,3 +320,48 @@ def test_update_t2_oracle_against_loops(diagonal):
     np.testing.assert_array_equal(err, er.ravel(order="F"))
     np.testing.assert_array_equal(nxt, nr.ravel(order="F"))
     assert abs(nrm - (er ** 2).sum()) <= 1e-13 * nrm
+
+
+# ---------------------------------------------------------------- restated reference routines
+def _golden(kind):
+    return [c for c in kat.cases() if c["kind"] == kind]
+
+
+@pytest.mark.parametrize("c", _golden("pattern"), ids=lambda c: c["name"])
+def test_golden_pattern(c):
+    """get_contraction_ptrn: the oracle's counting restatement against the
+    fixtures transliterated from tensor_dil_omp.F90:87-142 (ierr and pattern)."""
+    ierr, my = oracle.get_contraction_ptrn(c["drank"], c["lrank"], c["rrank"], c["aces"])
+    assert ierr == c["ierr"]
+    if ierr == 0:
+        assert my[: c["lrank"] + c["rrank"]] == c["my_ptrn"]
+
+
+@pytest.mark.parametrize("c", _golden("denominator"), ids=lambda c: c["name"])
+def test_golden_denominator(c):
+    """energy_denominator_rhf, bit for bit against the fixtures' loops."""
+    x = np.array(c["data"], dtype=np.float64)
+    assert oracle.energy_denominator_rhf(c["index_values"], c["ext"], x, c["ext1"], np.array(c["e"]),
+                                         c["seg_sizes"]) == 0
+    np.testing.assert_array_equal(x, np.array(c["expected"]))
+
+
+@pytest.mark.parametrize("c", _golden("update_t2"), ids=lambda c: c["name"])
+def test_golden_update_t2(c):
+    """updatet2's two passes: error block and next amplitudes bit for bit; the
+    squared norm (a long sum) to 1e-14 of the exact sum."""
+    a = lambda k: np.array(c[k], dtype=np.float64)
+    err, nxt, nrm = oracle.update_t2(c["index_values"], c["ext"], a("t2new"), a("t2new_pair"), a("t2old"),
+                                     a("t2old_pair"), c["ext1"], a("fock"), c["seg_sizes"])
+    np.testing.assert_array_equal(err, a("expected_err"))
+    np.testing.assert_array_equal(nxt, a("expected_next"))
+    assert abs(nrm - c["expected_norm2"]) <= 1e-14 * c["expected_norm2"]
+
+
+@pytest.mark.parametrize("c", _golden("energy"), ids=lambda c: c["name"])
+def test_golden_energy(c):
+    """The (T) energy pattern: the same quotients as the fixture, summed in
+    another order: 1e-14 of the fixture's exact sum."""
+    got = oracle.energy_contract(c["index_values"], c["ext"], np.array(c["w"]), c["ext1"], np.array(c["fock"]),
+                                 c["seg_sizes"], c["efact"], den_order=c["den_order"])
+    assert abs(got - c["expected"]) <= 1e-14 * abs(c["expected"])
