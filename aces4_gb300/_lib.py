@@ -87,6 +87,14 @@ SIGNATURES = {
     "a4g_batch_tuning": (ctypes.c_int, None),
     "a4g_batch_error_bound": (ctypes.c_int, [c_void_p, ctypes.c_double, c_double_p, c_void_p]),
     "a4g_tune_cache_clear": (None, []),
+    "a4g_blocks_create": (ctypes.c_int, [c_void_p, ctypes.c_size_t]),
+    "a4g_blocks_destroy": (None, [c_void_p]),
+    "a4g_blocks_on_device": (ctypes.c_int, [c_void_p, c_void_p, ctypes.c_int64, ctypes.c_int, c_void_p, c_void_p]),
+    "a4g_blocks_on_host": (ctypes.c_int, [c_void_p, c_void_p, ctypes.c_int, c_void_p]),
+    "a4g_blocks_flush": (ctypes.c_int, [c_void_p, c_void_p]),
+    "a4g_blocks_forget": (ctypes.c_int, [c_void_p, c_void_p]),
+    "a4g_blocks_stats": (ctypes.c_int, [c_void_p, c_void_p, c_void_p, c_void_p, c_void_p]),
+    "a4g_blocks_attach": (ctypes.c_int, [c_void_p]),
     "a4g_tune_cache_save": (ctypes.c_int, [ctypes.c_char_p]),
     "a4g_tune_cache_load": (ctypes.c_int, [ctypes.c_char_p]),
 }

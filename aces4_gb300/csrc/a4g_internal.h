@@ -43,6 +43,12 @@ cudaStream_t pick(void* stream);
 int arena_reserve(size_t bytes, void** out);  // arena is reused across calls
 int check_device_flag(cudaStream_t s);        // syncs s, reads and clears the flag
 
+// ---------------------------------------------------------------- block cache
+// The cache the drop-in entry points use (a4g_blocks_attach), or null; and
+// the lazy host -> device step of blocks.cpp (mode: A4G_BLOCK_*).
+a4g_blocks* attached_blocks();
+int blocks_on_device(a4g_blocks* c, double* h, int64_t n, int mode, double** d, cudaStream_t s);
+
 // ---------------------------------------------------------------- planner
 // Pattern handling restated from tensor_dil_omp.F90 (get_contraction_ptrn
 // :87-142, contr_ptrn_ok :861-896) plus the GEMM view used by the kernels.

@@ -67,6 +67,71 @@ int d2h(double* h, const double* d, int64_t n, cudaStream_t s) {
 
 std::mutex g_host_mu;  // host-buffer entries share one arena
 
+// Device views of one drop-in call's host blocks.  Detached (the default):
+// operands staged through the arena, results copied back before the call
+// returns, like the Fortran kernels.  With a block cache attached: the
+// cache's device copies (copied in only when missing or stale); results stay
+// there, newer than the host copy, until the host asks for them.  Operands
+// are declared before results, so a result that is also an operand (the same
+// host block) is seen: element-wise operations work on the shared device
+// copy, the others compute into a temporary that then replaces it.
+struct HostIO {
+  cudaStream_t s = nullptr;
+  a4g_blocks* cache = nullptr;
+  Staged st;
+  struct Copy {
+    double* dst;
+    const double* src;
+    int64_t n;
+    cudaMemcpyKind kind;
+  };
+  std::vector<Copy> after;  // results back to the host, or temporaries into device copies
+  std::vector<const double*> operands;
+
+  int begin(size_t arena_bytes) {
+    s = ctx()->stream;
+    cache = attached_blocks();
+    return stage(arena_bytes, &st);
+  }
+  int in(const double* h, int64_t n, double** d) {
+    operands.push_back(h);
+    if (cache) return blocks_on_device(cache, const_cast<double*>(h), n, A4G_BLOCK_READ, d, s);
+    *d = st.take(n);
+    return h2d(*d, h, n, s);
+  }
+  // reads: the operation reads the result block's old values;
+  // elementwise: it may run in place on an operand's device copy
+  int out(double* h, int64_t n, bool reads, bool elementwise, double** d) {
+    if (cache) {
+      double* dc = nullptr;
+      int rc = blocks_on_device(cache, h, n, reads ? A4G_BLOCK_UPDATE : A4G_BLOCK_OVERWRITE, &dc, s);
+      if (rc) return rc;
+      const bool aliased = std::find(operands.begin(), operands.end(), h) != operands.end();
+      if (aliased && !elementwise) {
+        *d = st.take(n);
+        if (reads) A4G_CUDA(cudaMemcpyAsync(*d, dc, size_t(n) * sizeof(double), cudaMemcpyDeviceToDevice, s));
+        after.push_back({dc, *d, n, cudaMemcpyDeviceToDevice});
+      } else {
+        *d = dc;
+      }
+      return A4G_OK;
+    }
+    *d = st.take(n);
+    if (reads) {
+      const int rc = h2d(*d, h, n, s);
+      if (rc) return rc;
+    }
+    after.push_back({h, *d, n, cudaMemcpyDeviceToHost});
+    return A4G_OK;
+  }
+  double* scratch(int64_t n) { return st.take(n); }
+  int finish() {
+    for (const Copy& c : after)
+      A4G_CUDA(cudaMemcpyAsync(c.dst, c.src, size_t(c.n) * sizeof(double), c.kind, s));
+    return check_device_flag(s);
+  }
+};
+
 std::map<std::string, std::vector<int>> g_predefined;
 std::mutex g_predef_mu;
 
@@ -125,15 +190,12 @@ void tensor_block_init__(int* nthreads, double* tens, int* tens_rank, int* ext, 
   std::lock_guard<std::mutex> lock(g_host_mu);
   int rc = ensure_init();
   const int64_t n = count(*tens_rank, ext);
-  Staged st;
-  if (!rc) rc = stage(rounded(n), &st);
-  if (!rc) {
-    cudaStream_t s = ctx()->stream;
-    double* d = st.take(n);
-    rc = launch_fill(d, n, *sval, s);
-    if (!rc) rc = d2h(tens, d, n, s);
-    if (!rc) rc = check_device_flag(s);
-  }
+  HostIO io;
+  double* d = nullptr;
+  if (!rc) rc = io.begin(rounded(n));
+  if (!rc) rc = io.out(tens, n, false, true, &d);
+  if (!rc) rc = launch_fill(d, n, *sval, io.s);
+  if (!rc) rc = io.finish();
   *ierr = runtime_ierr(rc);
 }
 
@@ -144,16 +206,12 @@ void tensor_block_scale__(int* nthreads, double* tens, int* tens_rank, int* ext,
   std::lock_guard<std::mutex> lock(g_host_mu);
   int rc = ensure_init();
   const int64_t n = count(*tens_rank, ext);
-  Staged st;
-  if (!rc) rc = stage(rounded(n), &st);
-  if (!rc) {
-    cudaStream_t s = ctx()->stream;
-    double* d = st.take(n);
-    rc = h2d(d, tens, n, s);
-    if (!rc) rc = launch_scale(d, n, *f, s);
-    if (!rc) rc = d2h(tens, d, n, s);
-    if (!rc) rc = check_device_flag(s);
-  }
+  HostIO io;
+  double* d = nullptr;
+  if (!rc) rc = io.begin(rounded(n));
+  if (!rc) rc = io.out(tens, n, true, true, &d);
+  if (!rc) rc = launch_scale(d, n, *f, io.s);
+  if (!rc) rc = io.finish();
   *ierr = runtime_ierr(rc);
 }
 
@@ -167,17 +225,16 @@ double tensor_block_norm2__(int* nthreads, double* tens, int* tens_rank, int* ex
   int rc = ensure_init();
   const int64_t n = count(*tens_rank, ext);
   double result = 0.0;
-  Staged st;
-  if (!rc) rc = stage(rounded(n) + rounded(dot_scratch_len() + 1), &st);
+  HostIO io;
+  double* d = nullptr;
+  if (!rc) rc = io.begin(rounded(n) + rounded(dot_scratch_len() + 1));
+  if (!rc) rc = io.in(tens, n, &d);
   if (!rc) {
-    cudaStream_t s = ctx()->stream;
-    double* d = st.take(n);
-    double* scratch = st.take(dot_scratch_len());
-    double* out = st.take(1);
-    rc = h2d(d, tens, n, s);
-    if (!rc) rc = launch_dot(d, d, nullptr, nullptr, n, out, scratch, dot_scratch_len(), s);
-    if (!rc) rc = d2h(&result, out, 1, s);
-    if (!rc) rc = check_device_flag(s);
+    double* scratch = io.scratch(dot_scratch_len());
+    double* out = io.scratch(1);
+    rc = launch_dot(d, d, nullptr, nullptr, n, out, scratch, dot_scratch_len(), io.s);
+    if (!rc) rc = d2h(&result, out, 1, io.s);
+    if (!rc) rc = io.finish();
   }
   *ierr = runtime_ierr(rc);
   return result;
@@ -190,23 +247,21 @@ static void slice_insert_host(int insert, int* dim_num, double* tens, int* text,
   std::lock_guard<std::mutex> lock(g_host_mu);
   int rc = ensure_init();
   const int64_t nt = count(*dim_num, text), ns = count(*dim_num, sext);
-  Staged st;
-  if (!rc) rc = stage(rounded(nt) + rounded(ns), &st);
-  if (!rc) {
-    cudaStream_t s = ctx()->stream;
-    double* dt = st.take(nt);
-    double* ds = st.take(ns);
-    if (*dim_num == 0) {
-      rc = insert ? h2d(dt, slice, 1, s) : h2d(ds, tens, 1, s);
-      if (!rc) rc = insert ? d2h(tens, dt, 1, s) : d2h(slice, ds, 1, s);
-    } else {
-      rc = h2d(dt, tens, nt, s);
-      if (!rc && insert) rc = h2d(ds, slice, ns, s);
-      if (!rc) rc = launch_slice_insert(insert, *dim_num, dt, text, ds, sext, beg, s);
-      if (!rc) rc = insert ? d2h(tens, dt, nt, s) : d2h(slice, ds, ns, s);
-    }
-    if (!rc) rc = check_device_flag(s);
+  HostIO io;
+  double *dt = nullptr, *ds = nullptr;
+  if (!rc) rc = io.begin(2 * (rounded(nt) + rounded(ns)));
+  if (!rc && *dim_num == 0) {  // scalars: the slice is the tensor
+    rc = insert ? io.in(slice, 1, &ds) : io.in(tens, 1, &dt);
+    if (!rc) rc = insert ? io.out(tens, 1, false, false, &dt) : io.out(slice, 1, false, false, &ds);
+    if (!rc && cudaMemcpyAsync(insert ? dt : ds, insert ? ds : dt, sizeof(double), cudaMemcpyDeviceToDevice,
+                               io.s) != cudaSuccess)
+      rc = cuda_fail(cudaGetLastError(), "cudaMemcpyAsync");
+  } else if (!rc) {
+    rc = insert ? io.in(slice, ns, &ds) : io.in(tens, nt, &dt);
+    if (!rc) rc = insert ? io.out(tens, nt, true, false, &dt) : io.out(slice, ns, false, false, &ds);
+    if (!rc) rc = launch_slice_insert(insert, *dim_num, dt, text, ds, sext, beg, io.s);
   }
+  if (!rc) rc = io.finish();
   *ierr = rc == A4G_ERR_ARG ? 1 : runtime_ierr(rc);
 }
 
@@ -229,18 +284,13 @@ void tensor_block_add__(const int* nthreads, const int* dim_num, int* ext, doubl
   std::lock_guard<std::mutex> lock(g_host_mu);
   int rc = ensure_init();
   const int64_t n = count(*dim_num, ext);
-  Staged st;
-  if (!rc) rc = stage(2 * rounded(n), &st);
-  if (!rc) {
-    cudaStream_t s = ctx()->stream;
-    double* d0 = st.take(n);
-    double* d1 = st.take(n);
-    rc = h2d(d0, t0, n, s);
-    if (!rc) rc = h2d(d1, t1, n, s);
-    if (!rc) rc = launch_add_scaled(d0, d1, n, *scale_fac, s);
-    if (!rc) rc = d2h(t0, d0, n, s);
-    if (!rc) rc = check_device_flag(s);
-  }
+  HostIO io;
+  double *d0 = nullptr, *d1 = nullptr;
+  if (!rc) rc = io.begin(2 * rounded(n));
+  if (!rc) rc = io.in(t1, n, &d1);
+  if (!rc) rc = io.out(t0, n, true, true, &d0);
+  if (!rc) rc = launch_add_scaled(d0, d1, n, *scale_fac, io.s);
+  if (!rc) rc = io.finish();
   *ierr = runtime_ierr(rc);
 }
 
@@ -252,17 +302,13 @@ void tensor_block_copy__(int* nthreads, int* dim_num, int* ext, int* dim_transp,
   std::lock_guard<std::mutex> lock(g_host_mu);
   int rc = ensure_init();
   const int64_t n = count(*dim_num, ext);
-  Staged st;
-  if (!rc) rc = stage(2 * rounded(n), &st);
-  if (!rc) {
-    cudaStream_t s = ctx()->stream;
-    double* din = st.take(n);
-    double* dout = st.take(n);
-    rc = h2d(din, tin, n, s);
-    if (!rc) rc = launch_permute(*dim_num, ext, dim_transp + 1, din, dout, s);
-    if (!rc) rc = d2h(tout, dout, n, s);
-    if (!rc) rc = check_device_flag(s);
-  }
+  HostIO io;
+  double *din = nullptr, *dout = nullptr;
+  if (!rc) rc = io.begin(2 * rounded(n));
+  if (!rc) rc = io.in(tin, n, &din);
+  if (!rc) rc = io.out(tout, n, false, false, &dout);
+  if (!rc) rc = launch_permute(*dim_num, ext, dim_transp + 1, din, dout, io.s);
+  if (!rc) rc = io.finish();
   *ierr = rc == A4G_ERR_ARG ? 1 : runtime_ierr(rc);
 }
 
@@ -279,21 +325,16 @@ void tensor_block_contract__(int* nthreads, int* ptrn, double* ltens, int* lrank
   std::lock_guard<std::mutex> lock(g_host_mu);
   int rc = ensure_init();
   const int64_t nl = count(*lrank, lext), nr = count(*rrank, rext), nd = count(*drank, dext);
-  Staged st;
-  if (!rc) rc = stage(rounded(nl) + rounded(nr) + rounded(nd) + rounded(dot_scratch_len()), &st);
-  if (!rc) {
-    cudaStream_t s = ctx()->stream;
-    double* dl = st.take(nl);
-    double* dr = st.take(nr);
-    double* dd = st.take(nd);
-    double* scratch = st.take(dot_scratch_len());
-    rc = h2d(dl, ltens, nl, s);
-    if (!rc) rc = h2d(dr, rtens, nr, s);
-    if (!rc)
-      rc = contract_device(ptrn, dl, *lrank, lext, dr, *rrank, rext, dd, *drank, dext, 0, scratch, s);
-    if (!rc) rc = d2h(dtens, dd, nd, s);
-    if (!rc) rc = check_device_flag(s);
-  }
+  HostIO io;
+  double *dl = nullptr, *dr = nullptr, *dd = nullptr;
+  if (!rc) rc = io.begin(rounded(nl) + rounded(nr) + rounded(nd) + rounded(dot_scratch_len()));
+  if (!rc) rc = io.in(ltens, nl, &dl);
+  if (!rc) rc = io.in(rtens, nr, &dr);
+  if (!rc) rc = io.out(dtens, nd, false, false, &dd);
+  if (!rc)
+    rc = contract_device(ptrn, dl, *lrank, lext, dr, *rrank, rext, dd, *drank, dext, 0,
+                         io.scratch(dot_scratch_len()), io.s);
+  if (!rc) rc = io.finish();
   *ierr = rc == A4G_ERR_PATTERN ? 1 : runtime_ierr(rc);
 }
 
@@ -441,18 +482,13 @@ void energy_denominator_rhf(int* array_slot_0, int* rank_0, int* index_values_0,
   int rc = ensure_init();
   const int64_t n0 = count(r0, extents_0), n1 = count(r1, extents_1);
   (void)size_0, (void)size_1;
-  Staged st;
-  if (!rc) rc = stage(rounded(n0) + rounded(n1), &st);
-  if (!rc) {
-    cudaStream_t s = ctx()->stream;
-    double* d0 = st.take(n0);
-    double* d1 = st.take(n1);
-    rc = h2d(d0, data_0, n0, s);
-    if (!rc) rc = h2d(d1, data_1, n1, s);
-    if (!rc) rc = launch_denominator(r0, off, extents_0, d0, r1, extents_1[0], d1, s);
-    if (!rc) rc = d2h(data_0, d0, n0, s);
-    if (!rc) rc = check_device_flag(s);
-  }
+  HostIO io;
+  double *d0 = nullptr, *d1 = nullptr;
+  if (!rc) rc = io.begin(2 * (rounded(n0) + rounded(n1)));
+  if (!rc) rc = io.in(data_1, n1, &d1);
+  if (!rc) rc = io.out(data_0, n0, true, false, &d0);
+  if (!rc) rc = launch_denominator(r0, off, extents_0, d0, r1, extents_1[0], d1, io.s);
+  if (!rc) rc = io.finish();
   *ierr = runtime_ierr(rc);
 }
 

@@ -29,6 +29,8 @@ def _ptr(x) -> int:
         return x
     if getattr(x, "is_cuda", False) is False and hasattr(x, "data_ptr"):
         raise TypeError("device API expects CUDA tensors")
+    if str(getattr(x, "dtype", "torch.float64")) != "torch.float64":
+        raise TypeError(f"device API expects float64 tensors, got {x.dtype}")
     return x.data_ptr()
 
 

@@ -12,7 +12,7 @@ import ctypes
 
 import numpy as np
 
-from ._lib import lib
+from ._lib import last_error, lib
 
 _i = ctypes.c_int
 _d = ctypes.c_double
@@ -58,9 +58,10 @@ def contract_labels(dlab, llab, rlab, l, lext, r, rext, dext):
     return tensor_block_contract(ptrn, l, lext, r, rext, d, dext), d
 
 
-def tensor_block_copy(ext, perm_o2n_1based, tin: np.ndarray) -> tuple[int, np.ndarray]:
-    """perm without the sign slot (added here)."""
-    out = np.empty_like(tin)
+def tensor_block_copy(ext, perm_o2n_1based, tin: np.ndarray, out: np.ndarray | None = None) -> tuple[int, np.ndarray]:
+    """perm without the sign slot (added here); out: the destination block
+    (a new array when None)."""
+    out = np.empty_like(tin) if out is None else out
     ierr = _i(0)
     lib().tensor_block_copy__(ctypes.byref(_i(8)), ctypes.byref(_i(len(ext))), _iarr(ext),
                               _iarr([1] + list(perm_o2n_1based)), _dp(tin), _dp(out), ctypes.byref(ierr))
@@ -124,3 +125,60 @@ def energy_denominator_rhf(index_values, ext0, data0, ext1, data1) -> int:
         _iarr(ext0), _dp(data0), ctypes.byref(_i(1)), ctypes.byref(_i(r1)), _iarr([1] * r1),
         ctypes.byref(_i(data1.size)), _iarr(ext1), _dp(data1), ctypes.byref(ierr))
     return ierr.value
+
+
+READ, UPDATE, OVERWRITE = 0, 1, 2
+
+
+class BlockCache:
+    """Device residency of host blocks (a4g_blocks_*): the GPU side of the
+    reference's BlockManager.  Blocks are numpy float64 arrays (their data
+    pointers identify them).  attach() makes the drop-ins above use it."""
+
+    def __init__(self, capacity_bytes: int):
+        h = ctypes.c_void_p(0)
+        rc = lib().a4g_blocks_create(ctypes.byref(h), ctypes.c_size_t(capacity_bytes))
+        if rc:
+            raise RuntimeError(f"a4g_blocks_create failed ({rc}): {last_error()}")
+        self._h = h
+
+    def _ok(self, rc, what):
+        if rc:
+            raise RuntimeError(f"{what} failed ({rc}): {last_error()}")
+
+    def attach(self):
+        self._ok(lib().a4g_blocks_attach(self._h), "a4g_blocks_attach")
+
+    def detach(self):
+        self._ok(lib().a4g_blocks_attach(None), "a4g_blocks_attach")
+
+    def on_device(self, a: np.ndarray, mode: int = READ) -> int:
+        d = ctypes.c_void_p(0)
+        self._ok(lib().a4g_blocks_on_device(self._h, _dp(a), ctypes.c_int64(a.size), mode, ctypes.byref(d), None),
+                 "a4g_blocks_on_device")
+        return d.value
+
+    def on_host(self, a: np.ndarray, mode: int = READ):
+        self._ok(lib().a4g_blocks_on_host(self._h, _dp(a), mode, None), "a4g_blocks_on_host")
+
+    def flush(self):
+        self._ok(lib().a4g_blocks_flush(self._h, None), "a4g_blocks_flush")
+
+    def forget(self, a: np.ndarray):
+        self._ok(lib().a4g_blocks_forget(self._h, _dp(a)), "a4g_blocks_forget")
+
+    def stats(self) -> dict:
+        v = [ctypes.c_int64(0) for _ in range(4)]
+        self._ok(lib().a4g_blocks_stats(self._h, *[ctypes.byref(x) for x in v]), "a4g_blocks_stats")
+        return dict(zip(("h2d_bytes", "d2h_bytes", "resident_bytes", "evictions"), (x.value for x in v)))
+
+    def close(self):
+        if getattr(self, "_h", None) and self._h.value:
+            lib().a4g_blocks_destroy(self._h)
+            self._h = ctypes.c_void_p(0)
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

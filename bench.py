@@ -768,6 +768,134 @@ def run_ladder_full(args, world, rank, local):
         dist.destroy_process_group()
 
 
+DROPIN_METRIC = "FP64 TFLOP/s of the interpreter's per-block-pair contract calls (tensor_block_contract__, host blocks)"
+
+
+def run_dropin(args, world, rank, local):
+    """The drop-in path as the interpreter drives it: one synchronous
+    tensor_block_contract__ per block pair on HOST blocks (interpreter.cpp:1256),
+    the temporary then added into R on the host (Block::accumulate_data), for
+    the o=10/v=48 ladder (all 1024 pairs of 144x25x144) and a sample of the
+    o=40/v=300 ring's pairs (both operands permuted).  Beside it, on the same
+    pairs with the same host accumulation: the reference's CPU algorithm
+    (oracle permute + OpenBLAS dgemm, all host threads); and on device copies
+    of the same blocks: the legacy _gpu_contract (synchronous per call) and
+    a4g_contract (stream-ordered, one synchronisation at the end)."""
+    import numpy as np
+    import torch
+
+    import aces4_gb300 as a4
+    from aces4_gb300.blocks import LADDER_LABELS, RING_LABELS, segments_uniform
+    from oracle import oracle
+
+    torch.cuda.set_device(local)
+    a4.device.init(local)
+    oracle.build()
+    rng = np.random.default_rng(17)
+
+    def pairs_for(name):
+        if name.startswith("ladder"):
+            vs, os_ = [12] * 4, [5, 5]
+            dl, ll, rl = LADDER_LABELS
+            shapes = []
+            for a, b, i, j in np.ndindex(4, 4, 2, 2):
+                for c, d in np.ndindex(4, 4):
+                    shapes.append(([vs[a], vs[b], vs[c], vs[d]], [vs[c], vs[d], os_[i], os_[j]],
+                                   [vs[a], vs[b], os_[i], os_[j]], (a, b, i, j)))
+            scale = 1.0 / 48
+        else:
+            vs, os_ = segments_uniform(300, 24, 40, seed=2), [20, 20]
+            dl, ll, rl = RING_LABELS
+            shapes = []
+            sub = np.random.default_rng(5)
+            for _ in range(args.dropin_pairs):
+                a, b, c = (int(x) for x in sub.integers(0, len(vs), 3))
+                i, j, k = (int(x) for x in sub.integers(0, 2, 3))
+                shapes.append(([vs[a], os_[k], vs[c], os_[i]], [vs[c], vs[b], os_[k], os_[j]],
+                               [vs[a], os_[i], vs[b], os_[j]], (a, i, b, j)))
+            scale = 1.0 / np.sqrt(40 * 300)
+        ierr, ptrn = a4.ref.get_contraction_ptrn(len(dl), len(ll), len(rl), dl + ll + rl)
+        assert ierr == 0
+        blocks = [(rng.uniform(-1, 1, int(np.prod(le))) * scale, rng.normal(0, 0.1, int(np.prod(re))), le, re, de,
+                   key) for le, re, de, key in shapes]
+        return ptrn, (dl, ll, rl), blocks
+
+    res = {}
+    for name in ("ladder o=10 v=48", "ring o=40 v=300 (sampled pairs)"):
+        ptrn, labels, blocks = pairs_for(name)
+        flop = 0.0
+        for _, _, le, re, de, _ in blocks:  # 2 M N K with M N = |D|, K^2 = |L| |R| / |D|
+            mn = float(np.prod(de))
+            flop += 2.0 * mn * np.sqrt(float(np.prod(le)) * float(np.prod(re)) / mn)
+        R, tmp = {}, {}
+        for _, _, le, re, de, key in blocks:
+            R.setdefault(key, np.zeros(int(np.prod(de))))
+            tmp.setdefault(tuple(de), np.empty(int(np.prod(de))))
+
+        def ours():
+            for v, t, le, re, de, key in blocks:
+                d = tmp[tuple(de)]
+                assert a4.ref.tensor_block_contract(ptrn, v, le, t, re, d, de) == 0
+                R[key] += d
+
+        def cpu():
+            for v, t, le, re, de, key in blocks:
+                R[key] += oracle.contract_blas(ptrn, v, le, t, re, de)
+
+        for fn in (ours, cpu):  # warm-up
+            fn()
+        out = {}
+        for tag, fn, reps in (("dropin_host_blocks", ours, args.steps), ("cpu_reference", cpu, 1)):
+            t0 = time.perf_counter()
+            for _ in range(reps):
+                fn()
+            dt = (time.perf_counter() - t0) / reps
+            out[tag] = {"tflops": flop / dt / 1e12, "us_per_call": dt / len(blocks) * 1e6}
+        dv = [(torch.tensor(v, device="cuda"), torch.tensor(t, device="cuda")) for v, t, *_ in blocks]
+        dd = {tuple(b[4]): torch.empty(int(np.prod(b[4])), dtype=torch.float64, device="cuda") for b in blocks}
+        dl_, ll_, rl_ = labels
+        st = torch.cuda.current_stream()
+
+        def dev_legacy():
+            for (tv, tt), (_, _, le, re, de, _) in zip(dv, blocks):
+                a4.device.gpu_contract(dd[tuple(de)], de, dl_, tv, le, ll_, tt, re, rl_)
+
+        def dev_async():
+            for (tv, tt), (_, _, le, re, de, _) in zip(dv, blocks):
+                a4.device.contract(ptrn, tv, le, tt, re, dd[tuple(de)], de, stream=st)
+            torch.cuda.synchronize()
+
+        for tag, fn in (("gpu_contract_device_blocks", dev_legacy), ("a4g_contract_device_async", dev_async)):
+            fn()
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            for _ in range(args.steps):
+                fn()
+            torch.cuda.synchronize()
+            dt = (time.perf_counter() - t0) / args.steps
+            out[tag] = {"tflops": flop / dt / 1e12, "us_per_call": dt / len(blocks) * 1e6}
+        v, t, le, re, de, _ = blocks[0]
+        got = np.empty(int(np.prod(de)))
+        assert a4.ref.tensor_block_contract(ptrn, v, le, t, re, got, de) == 0
+        want = oracle.contract_blas(ptrn, v, le, t, re, de)
+        out["rel_err_first_pair"] = float(np.linalg.norm(got - want) / np.linalg.norm(want))
+        out["pairs"], out["flop"] = len(blocks), flop
+        res[name] = out
+    if rank == 0:
+        lad = res["ladder o=10 v=48"]
+        ours_t = lad["dropin_host_blocks"]["tflops"]
+        print(json.dumps({
+            "metric": DROPIN_METRIC, "value": ours_t, "unit": "TFLOP/s", "n_gpus": 1, "steps": args.steps,
+            "warmup": 1, "ms_per_step": lad["flop"] / ours_t / 1e9, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": "per-pair drop-in calls: ladder o=10/v=48 (1024 pairs), ring o=40/v=300 "
+                                   f"({args.dropin_pairs} sampled pairs)", "timer": "host wall clock, synchronous calls"},
+            "cpu_baseline": {"value": lad["cpu_reference"]["tflops"], "unit": "TFLOP/s", "cores": os.cpu_count(),
+                             "kind": "port", "sample": "the same 1024 ladder pairs"},
+            "workloads": res,
+        }), flush=True)
+
+
 CONFIG_METRIC = "FP64-equiv TFLOP/s per pardo step (batched split vs plain FP64)"
 
 
@@ -982,8 +1110,10 @@ def main():
     ap.add_argument("--e2e-pool", type=int, default=2, help="ladder-full e2e: distinct V slabs in pinned host memory")
     ap.add_argument("--v-pool", type=int, default=8, help="ladder-full: distinct V slabs resident in HBM")
     ap.add_argument("--slabs", type=int, default=0, help="ladder-full: only the first N (a,b) slabs (0: all)")
+    ap.add_argument("--dropin-pairs", type=int, default=200, help="dropin: sampled ring block pairs")
     ap.add_argument("--workload", default="ladder-full",
-                    choices=["ladder-full", "ladder", "triples", "ladder-small", "ring", "sparse", "blockops"],
+                    choices=["ladder-full", "ladder", "triples", "ladder-small", "ring", "sparse", "blockops",
+                             "dropin"],
                     help="ladder-full: the whole o=64/v=512 ladder contraction, all (a,b) slabs (the headline "
                          "metric); ladder: one slab of it; triples: one triples energy step; ladder-small / ring / "
                          "sparse: one pardo step of the o=10/v=48 ladder, the o=40/v=300 ring, the o=48/v=400 "
@@ -1009,6 +1139,9 @@ def main():
         return
     if args.workload == "ladder-full":
         run_ladder_full(args, world, rank, local)
+        return
+    if args.workload == "dropin":
+        run_dropin(args, world, rank, local)
         return
 
     import numpy as np

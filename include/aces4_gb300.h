@@ -324,6 +324,61 @@ int a4g_batch_form(const a4g_batch* b, int* form, float* tuned_ms, int n);
 void a4g_batch_destroy(a4g_batch* b);
 
 /* ----------------------------------------------------------------------------
+ * Device residency of host blocks: the GPU side of the reference's
+ * BlockManager (src/sip/dynamic_data/block_manager.cpp:291-446, lazy copies
+ * between host and GPU) and of the Block status bits onGPU / dirtyOnHost /
+ * dirtyOnGPU (src/sip/dynamic_data/block.h:150-174).  A block is its host
+ * data pointer (Block::data_) and element count; its device copy is made on
+ * first use and kept until it is evicted (least recently used first, written
+ * back first when newer than the host copy) or forgotten.  Blocks must not
+ * overlap; a block whose host memory is freed must be forgotten before the
+ * address is reused.
+ * ------------------------------------------------------------------------- */
+typedef struct a4g_blocks a4g_blocks;
+
+#define A4G_BLOCK_READ 0      /* the copy is read                               */
+#define A4G_BLOCK_UPDATE 1    /* read and modified                              */
+#define A4G_BLOCK_OVERWRITE 2 /* replaced entirely: its old values are not read */
+
+/* capacity_bytes: the most device memory the copies may hold. */
+int a4g_blocks_create(a4g_blocks** out, size_t capacity_bytes);
+/* Frees every device copy without writing any back (flush first to keep
+ * device results); detaches the cache if it is attached. */
+void a4g_blocks_destroy(a4g_blocks* c);
+/* The device copy of host block h (n doubles) for use on `stream`
+ * (lazy_gpu_read/update/write_on_device): READ and UPDATE copy the block in
+ * when there is no device copy or the host copy is newer; OVERWRITE copies
+ * nothing in; UPDATE and OVERWRITE make the device copy the newer one. */
+int a4g_blocks_on_device(a4g_blocks* c, double* h, int64_t n, int mode, double** d, void* stream);
+/* The host copy of block h for use on the host (lazy_gpu_read/update/
+ * write_on_host): READ and UPDATE copy the block back (synchronously) when
+ * the device copy is newer; OVERWRITE copies nothing back; UPDATE and
+ * OVERWRITE make the host copy the newer one (the next device use copies it
+ * in).  A block with no device copy needs nothing. */
+int a4g_blocks_on_host(a4g_blocks* c, double* h, int mode, void* stream);
+/* Writes back every device copy that is newer than its host copy. */
+int a4g_blocks_flush(a4g_blocks* c, void* stream);
+/* Drops block h's device copy without writing it back (the block is being
+ * deleted). */
+int a4g_blocks_forget(a4g_blocks* c, double* h);
+/* Bytes copied host->device and device->host so far, device bytes held, and
+ * the number of evictions. */
+int a4g_blocks_stats(a4g_blocks* c, int64_t* h2d_bytes, int64_t* d2h_bytes, int64_t* resident_bytes,
+                     int64_t* evictions);
+/* Makes the drop-in entry points of group 1 (tensor_block_contract__,
+ * tensor_block_copy__, tensor_block_add__, tensor_block_scale__,
+ * tensor_block_init__, tensor_block_norm2__, tensor_block_slice__,
+ * tensor_block_insert__, energy_denominator_rhf) work through cache c
+ * (NULL: detach).  Their host operands are then taken from their device
+ * copies (copied in only when missing or stale), and their results stay on
+ * the device, newer than the host copy, until a4g_blocks_on_host or
+ * a4g_blocks_flush brings them back: the interpreter calls on_host before it
+ * reads a block on the host, as BlockManager does for GPU blocks.  Detached
+ * (the default), the drop-ins copy every operand in and every result back
+ * on each call, like the Fortran they replace. */
+int a4g_blocks_attach(a4g_blocks* c);
+
+/* ----------------------------------------------------------------------------
  * One batch for a whole pardo loop.  A pardo loop runs the same statement over
  * many segment tuples (src/sip/worker/loop_manager.cpp:289-314): every
  * iteration has the same block shapes and differs only in which blocks it

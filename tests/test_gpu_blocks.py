@@ -346,8 +346,9 @@ def test_golden_energy_gpu(lib, c):
     import torch
 
     esum = torch.zeros(1, dtype=torch.float64, device="cuda")
-    lib.device.energy_contract(c["index_values"], c["ext"], torch.tensor(c["w"], device="cuda"), c["ext1"],
-                               torch.tensor(c["fock"], device="cuda"), c["seg_sizes"], c["efact"], esum,
+    f64 = dict(dtype=torch.float64, device="cuda")
+    lib.device.energy_contract(c["index_values"], c["ext"], torch.tensor(c["w"], **f64), c["ext1"],
+                               torch.tensor(c["fock"], **f64), c["seg_sizes"], c["efact"], esum,
                                den_order=c["den_order"])
     lib.device.sync()
     assert abs(float(esum.item()) - c["expected"]) <= 1e-14 * abs(c["expected"])
