@@ -36,12 +36,19 @@ struct Context {
   void* arena = nullptr;
   size_t arena_bytes = 0;
   int* d_error_flag = nullptr;  // device int: nonzero = a kernel gave up a wait
+  // Stream-ordered allocations of the library (split-K workspaces, block
+  // copies, reduction partials) come from a pool of its own that keeps freed
+  // memory for reuse: the default pool hands memory back to the driver at
+  // every synchronisation, so a synchronous call would allocate from scratch
+  // each time.
+  cudaMemPool_t pool = nullptr;
 };
 Context* ctx();             // initialises on first use (device = current)
 int ensure_init();          // returns A4G_OK or an error code
 cudaStream_t pick(void* stream);
 int arena_reserve(size_t bytes, void** out);  // arena is reused across calls
 int check_device_flag(cudaStream_t s);        // syncs s, reads and clears the flag
+int async_alloc(void** p, size_t bytes, cudaStream_t s);  // from the library pool, stream-ordered (free: cudaFreeAsync)
 
 // ---------------------------------------------------------------- block cache
 // The cache the drop-in entry points use (a4g_blocks_attach), or null; and

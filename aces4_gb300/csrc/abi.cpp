@@ -582,7 +582,7 @@ int a4g_add_sub(int subtract, int rank, const int* d_labels, const int* r_labels
     // d[i,j] += d[j,i]: the right operand must be read before d is written,
     // as the reference does with its temporary block (interpreter.cpp:1919-1927)
     double* tmp = nullptr;
-    A4G_CUDA(cudaMallocAsync(reinterpret_cast<void**>(&tmp), size_t(n) * sizeof(double), s));
+    if (const int rc_ = async_alloc(reinterpret_cast<void**>(&tmp), size_t(n) * sizeof(double), s)) return rc_;
     rc = launch_permute(rank, r_ext, o2n, r, tmp, s);
     int ident[kMaxRank];
     for (int i = 0; i < rank; ++i) ident[i] = i + 1;

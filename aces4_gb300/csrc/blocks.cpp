@@ -127,7 +127,7 @@ int blocks_on_device(a4g_blocks* c, double* h, int64_t n, int mode, double** d, 
   const bool had = e->d != nullptr;
   if (!had) {
     if ((rc = make_room(c, bytes_of(n), e, s))) return rc;
-    A4G_CUDA(cudaMallocAsync(reinterpret_cast<void**>(&e->d), std::max<size_t>(bytes_of(n), 8), s));
+    if (const int rc_ = async_alloc(reinterpret_cast<void**>(&e->d), std::max<size_t>(bytes_of(n), 8), s)) return rc_;
     c->used += bytes_of(n);
   }
   if (mode != A4G_BLOCK_OVERWRITE && (!had || e->dirty_host)) {

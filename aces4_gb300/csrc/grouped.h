@@ -37,11 +37,11 @@ struct GroupedF64Reduce {
   int slot0, nparts;
   int pad;
 };
-int launch_grouped_f64(const GroupedF64Tile* tiles, int ntiles, const GroupedPair* pairs,
-                       const PlanRef* plans, int mode, double* ws, const GroupedF64Reduce* reds, int nreds,
-                       cudaStream_t s);  // mode: bit 0 accumulate, bit 1 negate
+// mode: bit 0 accumulate, bit 1 negate; tile_n: 32 or 64 (grouped_f64_tile_n)
+int launch_grouped_f64(const GroupedF64Tile* tiles, int ntiles, const GroupedPair* pairs, const PlanRef* plans,
+                       int mode, double* ws, const GroupedF64Reduce* reds, int nreds, int tile_n, cudaStream_t s);
 int grouped_f64_tile_m();
-int grouped_f64_tile_n();
+int grouped_f64_tile_n(int max_n);  // tile columns for destination blocks of at most max_n columns
 
 // ------------------------------------------------------------ split precision
 // A panel holds the BF16 slices of every left block that feeds one group of

@@ -838,7 +838,7 @@ int launch_update_t2(const int* off, const int* ext, const double* t2new, const 
   double* partial = d_scratch;
   bool own = false;
   if (gx * gy > scratch_len) {  // more CTAs than the reduction scratch holds
-    A4G_CUDA(cudaMallocAsync(reinterpret_cast<void**>(&partial), size_t(gx * gy) * sizeof(double), s));
+    if (const int rc_ = async_alloc(reinterpret_cast<void**>(&partial), size_t(gx * gy) * sizeof(double), s)) return rc_;
     own = true;
   }
   update_t2_kernel<<<dim3(unsigned(gx), unsigned(gy)), 256, 0, s>>>(p, t2new, t2new_pair, t2old, t2old_pair, err,

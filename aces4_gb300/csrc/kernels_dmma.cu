@@ -5,8 +5,8 @@
 // so no transposed copy of L, R or D is ever written (the reference allocates
 // and fills transposed temporaries, tensor_dil_omp.F90:729-751, 782-785).
 //
-// CTA tile 64x64, k-step 16, 128 threads (2x2 warps, 32x32 per warp = 4x4
-// m8n8k4 DMMA tiles).  Tiles are gathered through the offset tables into
+// CTA tile 64x64 (or 64x32 for narrow destinations), k-step 16, 128 threads
+// (2x2 warps, 4 x BN/16 m8n8k4 DMMA tiles per warp).  Tiles are gathered through the offset tables into
 // registers, then staged in double-buffered shared memory.  FP64 throughput on
 // GB300 is ~2 FMA/clk/SM, so the kernel is bound by the FP64 pipe; the gather
 // traffic is small in comparison.
@@ -14,13 +14,15 @@
 // The grouped form runs a whole pardo step: one CTA owns one 64x64 tile of one
 // destination block and sums the products of every block pair that feeds that
 // block (the contract-accumulate the interpreter lacks), then writes D once.
+#include <algorithm>
+
 #include "a4g_internal.h"
 #include "grouped.h"
 
 namespace a4g {
 namespace {
 
-constexpr int BM = 64, BN = 64, BK = 16, LDS = BM + 4;  // +4 doubles: conflict-free fragment reads
+constexpr int BM = 64, BK = 16;
 constexpr int kThreadsF64 = 128;
 
 __device__ __forceinline__ void dmma_8x8x4(double (&c)[2], double a, double b) {
@@ -29,168 +31,221 @@ __device__ __forceinline__ void dmma_8x8x4(double (&c)[2], double a, double b) {
                : "d"(a), "d"(b));
 }
 
-// Gathers one 64x16 operand tile (rows x k) into 8 registers per thread.
-// KFAST: the operand is unit-stride along k, so threads walk k fastest.
-__device__ __forceinline__ void gather_tile(bool kfast, double (&reg)[8], const double* __restrict__ X,
+// Gathers one ROWS x 16 operand tile (rows x k) into ROWS/8 registers per
+// thread.  KFAST: the operand is unit-stride along k, so threads walk k
+// fastest; otherwise along the rows.
+template <int ROWS>
+__device__ __forceinline__ void gather_tile(bool kfast, double (&reg)[ROWS / 8], const double* __restrict__ X,
                                             const int64_t* __restrict__ offRow,  // smem, per row
                                             const int64_t* __restrict__ offK,    // global, per k
                                             int rows_left, int k0, int K) {
   const int t = threadIdx.x;
 #pragma unroll
-  for (int i = 0; i < 8; ++i) {
-    const int kk = kfast ? (t & (BK - 1)) : ((t >> 6) + 2 * i);
-    const int r = kfast ? ((t >> 4) + 8 * i) : (t & (BM - 1));
+  for (int i = 0; i < ROWS / 8; ++i) {
+    const int kk = kfast ? (t & (BK - 1)) : (t / ROWS + (kThreadsF64 / ROWS) * i);
+    const int r = kfast ? ((t >> 4) + 8 * i) : (t & (ROWS - 1));
     const int k = k0 + kk;
     reg[i] = (r < rows_left && k < K) ? __ldg(&X[offRow[r] + __ldg(&offK[k])]) : 0.0;
   }
 }
 
-__device__ __forceinline__ void store_tile(bool kfast, double (*S)[LDS], const double (&reg)[8]) {
+template <int ROWS, int LD>
+__device__ __forceinline__ void store_tile(bool kfast, double (*S)[LD], const double (&reg)[ROWS / 8]) {
   const int t = threadIdx.x;
 #pragma unroll
-  for (int i = 0; i < 8; ++i) {
-    const int kk = kfast ? (t & (BK - 1)) : ((t >> 6) + 2 * i);
-    const int r = kfast ? ((t >> 4) + 8 * i) : (t & (BM - 1));
+  for (int i = 0; i < ROWS / 8; ++i) {
+    const int kk = kfast ? (t & (BK - 1)) : (t / ROWS + (kThreadsF64 / ROWS) * i);
+    const int r = kfast ? ((t >> 4) + 8 * i) : (t & (ROWS - 1));
     S[kk][r] = reg[i];
   }
 }
 
+// Tile BM x BN: 64 x 64, or 64 x 32 for narrow destinations (the ladder's
+// i,j extent of 25 fills 78 % of a 32-column tile, 39 % of a 64-column one).
+// 4 warps as 2 x 2, each 32 x BN/2 = 4 x (BN/16) m8n8 DMMA tiles.
+template <int BN>
 struct Smem {
-  double As[2][BK][LDS];
-  double Bs[2][BK][LDS];
+  double As[2][BK][BM + 4];  // +4 doubles: conflict-free fragment reads
+  double Bs[2][BK][BN + 4];
   int64_t sLm[BM], sRn[BN];
 };
 
-// acc += L_tile * R_tile over all K of one block pair.
-__device__ void accumulate_pair(Smem& sm, double (&acc)[4][4][2], const double* __restrict__ L,
+template <int BN>
+struct Acc {
+  double v[4][BN / 16][2];
+  __device__ __forceinline__ void zero() {
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+#pragma unroll
+      for (int j = 0; j < BN / 16; ++j) v[i][j][0] = v[i][j][1] = 0.0;
+  }
+};
+
+// acc += L_tile * R_tile over the k steps [ks0, ks1) (16 k each) of one pair.
+template <int BN>
+__device__ void accumulate_pair(Smem<BN>& sm, Acc<BN>& acc, const double* __restrict__ L,
                                 const double* __restrict__ R, const int64_t* __restrict__ offLm,
                                 const int64_t* __restrict__ offLk, const int64_t* __restrict__ offRk,
                                 const int64_t* __restrict__ offRn, int M, int N, int K, int m0, int n0,
-                                bool a_kfast, bool b_kfast) {
+                                bool a_kfast, bool b_kfast, int ks0, int ks1) {
   const int t = threadIdx.x;
   __syncthreads();  // previous pair done with the tables / tiles
   if (t < BM) sm.sLm[t] = (m0 + t < M) ? offLm[m0 + t] : 0;
-  else sm.sRn[t - BM] = (n0 + t - BM < N) ? offRn[n0 + t - BM] : 0;
+  if (t < BN) sm.sRn[t] = (n0 + t < N) ? offRn[n0 + t] : 0;
   __syncthreads();
+  if (ks0 >= ks1) return;
 
   const int warp = t >> 5, lane = t & 31;
   const int g = lane >> 2, tig = lane & 3;
-  const int wm = (warp & 1) * 32, wn = (warp >> 1) * 32;
-  double ra[8], rb[8];
-  const int ksteps = (K + BK - 1) / BK;
-  gather_tile(a_kfast, ra, L, sm.sLm, offLk, M - m0, 0, K);
-  gather_tile(b_kfast, rb, R, sm.sRn, offRk, N - n0, 0, K);
-  store_tile(a_kfast, sm.As[0], ra);
-  store_tile(b_kfast, sm.Bs[0], rb);
+  const int wm = (warp & 1) * 32, wn = (warp >> 1) * (BN / 2);
+  double ra[BM / 8], rb[BN / 8];
+  gather_tile<BM>(a_kfast, ra, L, sm.sLm, offLk, M - m0, ks0 * BK, K);
+  gather_tile<BN>(b_kfast, rb, R, sm.sRn, offRk, N - n0, ks0 * BK, K);
+  store_tile<BM, BM + 4>(a_kfast, sm.As[0], ra);
+  store_tile<BN, BN + 4>(b_kfast, sm.Bs[0], rb);
   __syncthreads();
-  for (int ks = 0; ks < ksteps; ++ks) {
-    const int cur = ks & 1;
-    if (ks + 1 < ksteps) {
-      gather_tile(a_kfast, ra, L, sm.sLm, offLk, M - m0, (ks + 1) * BK, K);
-      gather_tile(b_kfast, rb, R, sm.sRn, offRk, N - n0, (ks + 1) * BK, K);
+  for (int ks = ks0; ks < ks1; ++ks) {
+    const int cur = (ks - ks0) & 1;
+    if (ks + 1 < ks1) {
+      gather_tile<BM>(a_kfast, ra, L, sm.sLm, offLk, M - m0, (ks + 1) * BK, K);
+      gather_tile<BN>(b_kfast, rb, R, sm.sRn, offRk, N - n0, (ks + 1) * BK, K);
     }
 #pragma unroll
     for (int kk = 0; kk < BK; kk += 4) {
-      double af[4], bf[4];
+      double af[4], bf[BN / 16];
 #pragma unroll
       for (int i = 0; i < 4; ++i) af[i] = sm.As[cur][kk + tig][wm + i * 8 + g];
 #pragma unroll
-      for (int j = 0; j < 4; ++j) bf[j] = sm.Bs[cur][kk + tig][wn + j * 8 + g];
+      for (int j = 0; j < BN / 16; ++j) bf[j] = sm.Bs[cur][kk + tig][wn + j * 8 + g];
 #pragma unroll
       for (int i = 0; i < 4; ++i)
 #pragma unroll
-        for (int j = 0; j < 4; ++j) dmma_8x8x4(acc[i][j], af[i], bf[j]);
+        for (int j = 0; j < BN / 16; ++j) dmma_8x8x4(acc.v[i][j], af[i], bf[j]);
     }
-    if (ks + 1 < ksteps) {
-      store_tile(a_kfast, sm.As[cur ^ 1], ra);
-      store_tile(b_kfast, sm.Bs[cur ^ 1], rb);
+    if (ks + 1 < ks1) {
+      store_tile<BM, BM + 4>(a_kfast, sm.As[cur ^ 1], ra);
+      store_tile<BN, BN + 4>(b_kfast, sm.Bs[cur ^ 1], rb);
     }
     __syncthreads();
   }
 }
 
 // mode bit 0: accumulate into D (beta = 1), bit 1: store the negated sum.
-__device__ void write_tile(const double (&acc)[4][4][2], double* __restrict__ D,
-                           const int64_t* __restrict__ offDm, const int64_t* __restrict__ offDn,
-                           int M, int N, int m0, int n0, int mode) {
+template <int BN>
+__device__ void write_tile(const Acc<BN>& acc, double* __restrict__ D, const int64_t* __restrict__ offDm,
+                           const int64_t* __restrict__ offDn, int M, int N, int m0, int n0, int mode) {
   const int t = threadIdx.x, warp = t >> 5, lane = t & 31;
   const int g = lane >> 2, tig = lane & 3;
-  const int wm = (warp & 1) * 32, wn = (warp >> 1) * 32;
+  const int wm = (warp & 1) * 32, wn = (warp >> 1) * (BN / 2);
 #pragma unroll
   for (int i = 0; i < 4; ++i) {
     const int m = m0 + wm + i * 8 + g;
     if (m >= M) continue;
     const int64_t om = offDm[m];
 #pragma unroll
-    for (int j = 0; j < 4; ++j) {
+    for (int j = 0; j < BN / 16; ++j) {
 #pragma unroll
       for (int h = 0; h < 2; ++h) {
         const int n = n0 + wn + j * 8 + 2 * tig + h;
         if (n >= N) continue;
         double* p = &D[om + offDn[n]];
-        const double v = (mode & 2) ? -acc[i][j][h] : acc[i][j][h];
+        const double v = (mode & 2) ? -acc.v[i][j][h] : acc.v[i][j][h];
         *p = (mode & 1) ? *p + v : v;
       }
     }
   }
 }
 
+// A partial tile, column-major BM x BN, into workspace slot `slot`.
+template <int BN>
+__device__ void write_partial(const Acc<BN>& acc, double* __restrict__ ws, int64_t slot) {
+  double* w = ws + slot * BM * BN;
+  const int t = threadIdx.x, warp = t >> 5, lane = t & 31;
+  const int g = lane >> 2, tig = lane & 3;
+  const int wm = (warp & 1) * 32, wn = (warp >> 1) * (BN / 2);
+#pragma unroll
+  for (int i = 0; i < 4; ++i)
+#pragma unroll
+    for (int j = 0; j < BN / 16; ++j)
+#pragma unroll
+      for (int h = 0; h < 2; ++h) w[(wn + j * 8 + 2 * tig + h) * BM + wm + i * 8 + g] = acc.v[i][j][h];
+}
+
+// One block pair.  CTA x = tile + tiles * split: with nsplit == 1 each CTA
+// computes a whole tile and stores it; otherwise each computes the tile over
+// its share of the k steps and writes a partial tile to the workspace, which
+// contract_f64_reduce_kernel sums in split order.  FP64 runs at a few FMA per
+// clock per SM on this GPU, so a small block (the ladder's 144 x 25 x 144)
+// needs its k range spread over many SMs to finish in microseconds.
+template <int BN>
 __global__ void __launch_bounds__(kThreadsF64) contract_f64_kernel(
     const double* __restrict__ L, const double* __restrict__ R, double* __restrict__ D,
     const int64_t* __restrict__ offLm, const int64_t* __restrict__ offLk,
     const int64_t* __restrict__ offRk, const int64_t* __restrict__ offRn,
     const int64_t* __restrict__ offDm, const int64_t* __restrict__ offDn, int M, int N, int K,
-    int tiles_m, int mode, int a_kfast, int b_kfast) {
-  __shared__ __align__(16) Smem sm;
-  const int tm = blockIdx.x % tiles_m, tn = blockIdx.x / tiles_m;
+    int tiles_m, int tiles, int nsplit, int mode, int a_kfast, int b_kfast, double* __restrict__ ws) {
+  __shared__ __align__(16) Smem<BN> sm;
+  const int tile = blockIdx.x % tiles, split = blockIdx.x / tiles;
+  const int tm = tile % tiles_m, tn = tile / tiles_m;
   const int m0 = tm * BM, n0 = tn * BN;
-  double acc[4][4][2];
-#pragma unroll
-  for (int i = 0; i < 4; ++i)
-#pragma unroll
-    for (int j = 0; j < 4; ++j) acc[i][j][0] = acc[i][j][1] = 0.0;
-  accumulate_pair(sm, acc, L, R, offLm, offLk, offRk, offRn, M, N, K, m0, n0, a_kfast, b_kfast);
-  write_tile(acc, D, offDm, offDn, M, N, m0, n0, mode);
+  const int ksteps = (K + BK - 1) / BK;
+  const int ks0 = int(int64_t(ksteps) * split / nsplit), ks1 = int(int64_t(ksteps) * (split + 1) / nsplit);
+  Acc<BN> acc;
+  acc.zero();
+  accumulate_pair<BN>(sm, acc, L, R, offLm, offLk, offRk, offRn, M, N, K, m0, n0, a_kfast, b_kfast, ks0, ks1);
+  if (nsplit > 1) write_partial<BN>(acc, ws, blockIdx.x);
+  else write_tile<BN>(acc, D, offDm, offDn, M, N, m0, n0, mode);
 }
 
-// One CTA per (destination block, 64x64 tile, share of its pairs); the pairs
-// are summed and the tile stored into D, or into a workspace slot when the
-// tile's pairs are spread over several CTAs (few tiles, many pairs).
+// Sums tile `blockIdx.x`'s nsplit partials (slots tile + tiles * split) in
+// split order and stores it: the same bits on every run.
+template <int BN>
+__global__ void __launch_bounds__(256) contract_f64_reduce_kernel(const double* __restrict__ ws, int tiles,
+                                                                  int nsplit, int tiles_m, double* __restrict__ D,
+                                                                  const int64_t* __restrict__ offDm,
+                                                                  const int64_t* __restrict__ offDn, int M, int N,
+                                                                  int mode) {
+  const int tile = blockIdx.x, tm = tile % tiles_m, tn = tile / tiles_m;
+  for (int e = threadIdx.x; e < BM * BN; e += blockDim.x) {
+    const int ml = e % BM, nl = e / BM;
+    const int m = tm * BM + ml, n = tn * BN + nl;
+    if (m >= M || n >= N) continue;
+    double v = 0.0;
+    for (int q = 0; q < nsplit; ++q) v += ws[(int64_t(tile) + int64_t(tiles) * q) * BM * BN + e];
+    if (mode & 2) v = -v;
+    double* p = D + offDm[m] + offDn[n];
+    *p = (mode & 1) ? *p + v : v;
+  }
+}
+
+// One CTA per (destination block, tile, share of its pairs); the pairs are
+// summed and the tile stored into D, or into a workspace slot when the tile's
+// pairs are spread over several CTAs (few tiles, many pairs).
+template <int BN>
 __global__ void __launch_bounds__(kThreadsF64) grouped_f64_kernel(const GroupedF64Tile* __restrict__ tiles,
                                                                   const GroupedPair* __restrict__ pairs,
                                                                   const PlanRef* __restrict__ plans,
                                                                   int mode, double* __restrict__ ws) {
-  __shared__ __align__(16) Smem sm;
+  __shared__ __align__(16) Smem<BN> sm;
   const GroupedF64Tile tl = tiles[blockIdx.x];
-  double acc[4][4][2];
-#pragma unroll
-  for (int i = 0; i < 4; ++i)
-#pragma unroll
-    for (int j = 0; j < 4; ++j) acc[i][j][0] = acc[i][j][1] = 0.0;
+  Acc<BN> acc;
+  acc.zero();
   for (int q = tl.pair_begin; q < tl.pair_end; ++q) {
     const GroupedPair pr = pairs[q];
     const PlanRef pl = plans[pr.plan];
-    accumulate_pair(sm, acc, pr.l, pr.r, pl.offLm, pl.offLk, pl.offRk, pl.offRn, pl.M, pl.N, pl.K,
-                    tl.m0, tl.n0, pl.a_kfast, pl.b_kfast);
+    accumulate_pair<BN>(sm, acc, pr.l, pr.r, pl.offLm, pl.offLk, pl.offRk, pl.offRn, pl.M, pl.N, pl.K, tl.m0,
+                        tl.n0, pl.a_kfast, pl.b_kfast, 0, (pl.K + BK - 1) / BK);
   }
-  if (tl.slot >= 0) {  // partial tile, column-major 64x64 in its slot
-    double* w = ws + size_t(tl.slot) * BM * BN;
-    const int t = threadIdx.x, warp = t >> 5, lane = t & 31;
-    const int g = lane >> 2, tig = lane & 3;
-    const int wm = (warp & 1) * 32, wn = (warp >> 1) * 32;
-#pragma unroll
-    for (int i = 0; i < 4; ++i)
-#pragma unroll
-      for (int j = 0; j < 4; ++j)
-#pragma unroll
-        for (int h = 0; h < 2; ++h) w[(wn + j * 8 + 2 * tig + h) * BM + wm + i * 8 + g] = acc[i][j][h];
+  if (tl.slot >= 0) {
+    write_partial<BN>(acc, ws, tl.slot);
     return;
   }
   const PlanRef dp = plans[tl.dplan];
-  write_tile(acc, tl.d, dp.offDm, dp.offDn, dp.M, dp.N, tl.m0, tl.n0, mode);
+  write_tile<BN>(acc, tl.d, dp.offDm, dp.offDn, dp.M, dp.N, tl.m0, tl.n0, mode);
 }
 
 // Sums a spread tile's partials in slot order (deterministic) and stores it.
+template <int BN>
 __global__ void __launch_bounds__(256) grouped_f64_reduce_kernel(const GroupedF64Reduce* __restrict__ reds,
                                                                  const PlanRef* __restrict__ plans,
                                                                  const double* __restrict__ ws, int mode) {
@@ -216,27 +271,56 @@ int launch_contract_f64(const DevPlan* p, const double* L, const double* R, doub
   if (h.M > 0x7fffffff || h.N > 0x7fffffff || h.K > 0x7fffffff)
     return fail(A4G_ERR_RANGE, "matrix dimension exceeds 2^31");
   const int M = int(h.M), N = int(h.N), K = int(h.K);
-  const int64_t tiles_m = (M + BM - 1) / BM, tiles_n = (N + BN - 1) / BN;
-  const int64_t grid = tiles_m * tiles_n;
-  if (grid > 0x7fffffffLL) return fail(A4G_ERR_RANGE, "contraction grid too large");
-  contract_f64_kernel<<<unsigned(grid), kThreadsF64, 0, s>>>(L, R, D, p->offLm, p->offLk, p->offRk,
-                                                            p->offRn, p->offDm, p->offDn, M, N, K,
-                                                            int(tiles_m), mode, h.a_kfast, h.b_kfast);
+  const int bn = N <= 32 ? 32 : 64;
+  const int64_t tiles_m = (M + BM - 1) / BM, tiles_n = (N + bn - 1) / bn;
+  const int64_t tiles = tiles_m * tiles_n;
+  if (tiles > 0x3fffffffLL) return fail(A4G_ERR_RANGE, "contraction grid too large");
+  // split the k steps when the tiles alone would leave most SMs idle (about
+  // two CTAs per SM, at most 64 splits of at least one k step)
+  const int sms = ctx()->num_sms > 0 ? ctx()->num_sms : 152;
+  const int64_t ksteps = (K + BK - 1) / BK;
+  int nsplit = int(std::max<int64_t>(1, std::min<int64_t>({64, ksteps, (2LL * sms + tiles - 1) / tiles})));
+  if (tiles * nsplit > 0x7fffffffLL) nsplit = 1;
+  double* ws = nullptr;
+  if (nsplit > 1)
+    if (const int rc_ = async_alloc(reinterpret_cast<void**>(&ws), size_t(tiles * nsplit) * BM * bn * sizeof(double), s)) return rc_;
+  const unsigned grid = unsigned(tiles * nsplit);
+  if (bn == 32)
+    contract_f64_kernel<32><<<grid, kThreadsF64, 0, s>>>(L, R, D, p->offLm, p->offLk, p->offRk, p->offRn, p->offDm,
+                                                         p->offDn, M, N, K, int(tiles_m), int(tiles), nsplit, mode,
+                                                         h.a_kfast, h.b_kfast, ws);
+  else
+    contract_f64_kernel<64><<<grid, kThreadsF64, 0, s>>>(L, R, D, p->offLm, p->offLk, p->offRk, p->offRn, p->offDm,
+                                                         p->offDn, M, N, K, int(tiles_m), int(tiles), nsplit, mode,
+                                                         h.a_kfast, h.b_kfast, ws);
+  if (nsplit > 1) {
+    if (bn == 32)
+      contract_f64_reduce_kernel<32><<<unsigned(tiles), 256, 0, s>>>(ws, int(tiles), nsplit, int(tiles_m), D,
+                                                                    p->offDm, p->offDn, M, N, mode);
+    else
+      contract_f64_reduce_kernel<64><<<unsigned(tiles), 256, 0, s>>>(ws, int(tiles), nsplit, int(tiles_m), D,
+                                                                    p->offDm, p->offDn, M, N, mode);
+    A4G_CUDA(cudaFreeAsync(ws, s));
+  }
   A4G_CUDA(cudaGetLastError());
   return A4G_OK;
 }
 
-int launch_grouped_f64(const GroupedF64Tile* tiles, int ntiles, const GroupedPair* pairs,
-                       const PlanRef* plans, int mode, double* ws, const GroupedF64Reduce* reds, int nreds,
-                       cudaStream_t s) {
+int launch_grouped_f64(const GroupedF64Tile* tiles, int ntiles, const GroupedPair* pairs, const PlanRef* plans,
+                       int mode, double* ws, const GroupedF64Reduce* reds, int nreds, int tile_n, cudaStream_t s) {
   if (ntiles <= 0) return A4G_OK;
-  grouped_f64_kernel<<<ntiles, kThreadsF64, 0, s>>>(tiles, pairs, plans, mode, ws);
-  if (nreds > 0) grouped_f64_reduce_kernel<<<nreds, 256, 0, s>>>(reds, plans, ws, mode);
+  if (tile_n == 32) {
+    grouped_f64_kernel<32><<<ntiles, kThreadsF64, 0, s>>>(tiles, pairs, plans, mode, ws);
+    if (nreds > 0) grouped_f64_reduce_kernel<32><<<nreds, 256, 0, s>>>(reds, plans, ws, mode);
+  } else {
+    grouped_f64_kernel<64><<<ntiles, kThreadsF64, 0, s>>>(tiles, pairs, plans, mode, ws);
+    if (nreds > 0) grouped_f64_reduce_kernel<64><<<nreds, 256, 0, s>>>(reds, plans, ws, mode);
+  }
   A4G_CUDA(cudaGetLastError());
   return A4G_OK;
 }
 
 int grouped_f64_tile_m() { return BM; }
-int grouped_f64_tile_n() { return BN; }
+int grouped_f64_tile_n(int max_n) { return max_n <= 32 ? 32 : 64; }
 
 }  // namespace a4g

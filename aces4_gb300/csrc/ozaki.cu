@@ -1587,7 +1587,7 @@ int oz_launch_recombine(const OzTile* tiles, int ntiles, int tile_rows, int tile
 
 int oz_wait_timeout_selftest(int limit_ms, int* waited_ms, cudaStream_t s) {
   int* d_ms = nullptr;
-  A4G_CUDA(cudaMallocAsync(reinterpret_cast<void**>(&d_ms), sizeof(int), s));
+  if (const int rc_ = async_alloc(reinterpret_cast<void**>(&d_ms), sizeof(int), s)) return rc_;
   wait_timeout_selftest_kernel<<<1, 32, 0, s>>>((unsigned long long)limit_ms * 1000000ull, ctx()->d_error_flag, d_ms);
   A4G_CUDA(cudaGetLastError());
   A4G_CUDA(cudaMemcpyAsync(waited_ms, d_ms, sizeof(int), cudaMemcpyDeviceToHost, s));

@@ -44,8 +44,20 @@ int ensure_init() {
   A4G_CUDA(cudaStreamCreateWithFlags(&g_ctx.stream, cudaStreamNonBlocking));
   A4G_CUDA(cudaMalloc(&g_ctx.d_error_flag, sizeof(int)));
   A4G_CUDA(cudaMemset(g_ctx.d_error_flag, 0, sizeof(int)));
+  cudaMemPoolProps props{};
+  props.allocType = cudaMemAllocationTypePinned;
+  props.location.type = cudaMemLocationTypeDevice;
+  props.location.id = dev;
+  A4G_CUDA(cudaMemPoolCreate(&g_ctx.pool, &props));
+  uint64_t keep = ~0ull;  // never hand freed memory back on synchronisation
+  A4G_CUDA(cudaMemPoolSetAttribute(g_ctx.pool, cudaMemPoolAttrReleaseThreshold, &keep));
   g_ctx.num_sms = prop.multiProcessorCount;
   g_ctx.device = dev;
+  return A4G_OK;
+}
+
+int async_alloc(void** p, size_t bytes, cudaStream_t s) {
+  A4G_CUDA(cudaMallocFromPoolAsync(p, std::max<size_t>(bytes, 8), g_ctx.pool, s));
   return A4G_OK;
 }
 
