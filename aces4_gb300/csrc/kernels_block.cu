@@ -464,9 +464,9 @@ __device__ __forceinline__ void block_sum_to(double acc, double* partial, int64_
 // divide).  (An integer form of the subtraction, exact as well, ran slower
 // than the FP64 one.)  Units (x3 [x5], a range of x2) are spread over
 // gridDim.y CTAs in a fixed order.
-constexpr int kEnLoads = 8;  // loads in flight per thread
+constexpr int kEnLoads = 4;  // loads in flight per thread
 constexpr int kEnThreads = 512;
-__global__ void __launch_bounds__(kEnThreads, 1) energy_chain_kernel(DenParams p, const double* __restrict__ w,
+__global__ void __launch_bounds__(kEnThreads, 2) energy_chain_kernel(DenParams p, const double* __restrict__ w,
                                                             const double* __restrict__ e, int x2_per_unit,
                                                             int64_t nunits, double* partial) {
   extern __shared__ double en[];  // e2 energies [ext2], then e4 energies [ext4]
