@@ -56,7 +56,7 @@ struct a4g_batch {
   double* d_f64_ws = nullptr;           // partial tiles when tiles are spread
   GroupedF64Reduce* d_f64_reds = nullptr;
   int n_f64_reds = 0;
-  int f64_tile_n = 64;  // columns of a grouped FP64 tile (32 for narrow destinations)
+  int f64_tile_m = 64, f64_tile_n = 64;  // rows (64 or 48) and columns (64 or 32) of a grouped FP64 tile
   std::vector<GroupedF64Tile> h_f64_tiles;
   std::vector<GroupedPair> h_f64_pairs;
   std::vector<GroupedF64Reduce> h_f64_reds;
@@ -386,10 +386,14 @@ void for_stretches(const DGroup& g, const PanelBuild& pa, const PanelBuild& pb,
 int build_f64(a4g_batch* b, const std::vector<DGroup>& groups, const std::vector<const DevPlan*>& plans) {
   std::vector<GroupedF64Tile> tiles;
   std::vector<GroupedPair> pairs;
-  int64_t max_n = 0;
-  for (const DGroup& g : groups) max_n = std::max(max_n, plans[g.plan]->host.N);
-  const int TM = grouped_f64_tile_m(), TN = grouped_f64_tile_n(int(std::min<int64_t>(max_n, 1 << 30)));
-  b->f64_tile_n = TN;
+  int64_t max_n = 0, pad64 = 0, pad48 = 0;
+  for (const DGroup& g : groups) {
+    const int64_t M = plans[g.plan]->host.M;
+    max_n = std::max(max_n, plans[g.plan]->host.N);
+    pad64 += (M + 63) / 64 * 64, pad48 += (M + 47) / 48 * 48;
+  }
+  const int TM = grouped_f64_tile_m(pad64, pad48), TN = grouped_f64_tile_n(int(std::min<int64_t>(max_n, 1 << 30)));
+  b->f64_tile_m = TM, b->f64_tile_n = TN;
   for (const DGroup& g : groups) {
     const int begin = int(pairs.size());
     for (const Pair& p : g.pairs) pairs.push_back({p.l, p.r, p.plan, 0});
@@ -1267,7 +1271,7 @@ int run(a4g_batch* b, cudaStream_t s, const cudaEvent_t* ev = nullptr) {
   if (b->precision == A4G_PREC_FP64) {
     if ((rc = mark(2)) || (rc = mark(3))) return rc;
     rc = launch_grouped_f64(b->d_f64_tiles, b->n_f64_tiles, b->d_f64_pairs, b->d_plans, b->store_mode(),
-                            b->d_f64_ws, b->d_f64_reds, b->n_f64_reds, b->f64_tile_n, s);
+                            b->d_f64_ws, b->d_f64_reds, b->n_f64_reds, b->f64_tile_m, b->f64_tile_n, s);
     if (rc) return rc;
     if ((rc = mark(4)) || (rc = mark(5))) return rc;
     return A4G_OK;

@@ -37,10 +37,13 @@ struct GroupedF64Reduce {
   int slot0, nparts;
   int pad;
 };
-// mode: bit 0 accumulate, bit 1 negate; tile_n: 32 or 64 (grouped_f64_tile_n)
+// mode: bit 0 accumulate, bit 1 negate; tile_m: 64 or 48 (grouped_f64_tile_m), tile_n: 64 or 32
+// (grouped_f64_tile_n)
 int launch_grouped_f64(const GroupedF64Tile* tiles, int ntiles, const GroupedPair* pairs, const PlanRef* plans,
-                       int mode, double* ws, const GroupedF64Reduce* reds, int nreds, int tile_n, cudaStream_t s);
-int grouped_f64_tile_m();
+                       int mode, double* ws, const GroupedF64Reduce* reds, int nreds, int tile_m, int tile_n,
+                       cudaStream_t s);
+// tile rows given the destination rows padded to 64- and to 48-row tiles (summed over the blocks)
+int grouped_f64_tile_m(int64_t padded64, int64_t padded48);
 int grouped_f64_tile_n(int max_n);  // tile columns for destination blocks of at most max_n columns
 
 // ------------------------------------------------------------ split precision

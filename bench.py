@@ -478,9 +478,16 @@ def run_ladder_full(args, world, rank, local):
     seed = 1234
     T = BlockArray([vs, vs, os_, os_])
     R = BlockArray([vs, vs, os_, os_])
+    # slabs per batch run: one run contracts k slabs (their R blocks are k
+    # stacked destinations over one T panel, so each T tile feeds 4k row tiles)
+    k_run = max(1, args.slabs_per_run)
+    runs = [list(range(q, min(q + k_run, len(slabs)))) for q in range(0, len(slabs), k_run)]
+    if len(runs) > 1 and len(runs[-1]) != k_run:
+        raise SystemExit("--slabs-per-run must divide the slab count")
     # V: a pool of distinct slabs resident in HBM (full V is 550 GB); slab q
     # reads pool[q % P]
-    P = max(2, min(args.v_pool, len(slabs)))
+    P = max(2 * k_run, min(args.v_pool, len(slabs)))
+    P = (P + k_run - 1) // k_run * k_run
     Vb = [BlockArray([[V_SEG], [V_SEG], vs, vs]) for _ in range(P)]
     gen_T(torch, T.buf, seed)
     gvs = torch.Generator(device="cuda")
@@ -489,10 +496,14 @@ def run_ladder_full(args, world, rank, local):
         gen_V_slab(torch, Vb[q], seed, a * nv + bb, gvs)
     ierr, ptrn = a4.ref.get_contraction_ptrn(4, 4, 4, [1, 2, 3, 4, 1, 2, 5, 6, 5, 6, 3, 4])
     assert ierr == 0
-    # the triple arrays of every slab (block addresses), built before timing;
-    # the e2e leg streams slab q into device buffer q % 2
-    arrs = [ladder_slab_array(R, Vb[q % P], T, a, b) for q, (a, b) in enumerate(slabs)]
-    arrs2 = [ladder_slab_array(R, Vb[q % 2], T, a, b) for q, (a, b) in enumerate(slabs)]
+    # the triple arrays of every run (block addresses), built before timing;
+    # the e2e leg streams run r's slabs into device buffers (r % 2) * k + i
+    def run_array(r, buf_of):
+        return np.concatenate([ladder_slab_array(R, Vb[buf_of(r, i, q)], T, *slabs[q])
+                               for i, q in enumerate(runs[r])])
+
+    arrs = [run_array(r, lambda r_, i, q: q % P) for r in range(len(runs))]
+    arrs2 = [run_array(r, lambda r_, i, q: (r_ % 2) * k_run + i) for r in range(len(runs))]
     slab_flop = 2.0 * V_SEG ** 2 * (O_SEG * no) ** 2 * (V_SEG * nv) ** 2
     flops_total = slab_flop * len(all_slabs)
     torch.cuda.synchronize()
@@ -522,9 +533,9 @@ def run_ladder_full(args, world, rank, local):
             ev_hold[0].record(stream)
             bt.hold(1, True, stream=stream)
             ev_hold[1].record(stream)
-            for q in range(len(slabs)):
-                if q:
-                    bt.rebind(arrs[q], stream=stream)
+            for r in range(len(runs)):
+                if r:
+                    bt.rebind(arrs[r], stream=stream)
                 bt.run_timed(stream)
         ph = bt.timings()  # synchronises
         if stats is not None:
@@ -559,8 +570,8 @@ def run_ladder_full(args, world, rank, local):
         dist.barrier()
     ms = max_over_ranks(ev0.elapsed_time(ev1) / args.steps)
     value = flops_total / (ms * 1e-3) / 1e12
-    runs = max(1, stats["runs"])
-    phases = {k: stats[k] / runs for k in a4.device.Batch.PHASES if k != "zero_fill"}
+    n_runs = max(1, stats["runs"])
+    phases = {k: stats[k] / (n_runs * k_run) for k in a4.device.Batch.PHASES if k != "zero_fill"}  # per slab
     per_step = {"create_ms": stats["create_ms"] / args.steps, "hold_T_ms": stats["hold_ms"] / args.steps,
                 "wall_ms": wall_ms}
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -656,8 +667,13 @@ def run_ladder_full(args, world, rank, local):
             o1 = R.offsets[(a, bb, no - 1, no - 1)] + R.size((a, bb, no - 1, no - 1))
             slab_rng.append((o0, o1))
 
-        ev_b = [torch.cuda.Event(enable_timing=True) for _ in slabs]
-        ev_a = [torch.cuda.Event(enable_timing=True) for _ in slabs]
+        ev_b = [torch.cuda.Event(enable_timing=True) for _ in runs]
+        ev_a = [torch.cuda.Event(enable_timing=True) for _ in runs]
+
+        def load(r):  # run r's V slabs into buffer set r % 2 (h2d stream)
+            for i, q in enumerate(runs[r]):
+                Vb[(r % 2) * k_run + i].buf.copy_(Vh[q % PH], non_blocking=True)
+            loaded[r % 2].record(h2d)
 
         def e2e_contraction():
             # the batch first (its set-up copies would queue behind the uploads)
@@ -666,29 +682,27 @@ def run_ladder_full(args, world, rank, local):
             with torch.cuda.stream(h2d):
                 T.buf.copy_(Th, non_blocking=True)
                 t_loaded.record(h2d)
-                Vb[0].buf.copy_(Vh[0], non_blocking=True)
-                loaded[0].record(h2d)
+                load(0)
             stream.wait_event(t_loaded)
             bt.hold(1, True, stream=stream)
-            for q in range(len(slabs)):
-                k = q % 2
-                if q + 1 < len(slabs):  # the next slab's V, once slab q-1 is done with its buffer
+            for r in range(len(runs)):
+                if r + 1 < len(runs):  # the next run's V, once run r-1 is done with its buffers
                     with torch.cuda.stream(h2d):
-                        if q >= 1:
-                            h2d.wait_event(done[(q + 1) % 2])
-                        Vb[(q + 1) % 2].buf.copy_(Vh[(q + 1) % PH], non_blocking=True)
-                        loaded[(q + 1) % 2].record(h2d)
-                stream.wait_event(loaded[k])
-                ev_b[q].record(stream)
-                if q:
-                    bt.rebind(arrs2[q], stream=stream)
+                        if r >= 1:
+                            h2d.wait_event(done[(r + 1) % 2])
+                        load(r + 1)
+                stream.wait_event(loaded[r % 2])
+                ev_b[r].record(stream)
+                if r:
+                    bt.rebind(arrs2[r], stream=stream)
                 bt.run_timed(stream)
-                ev_a[q].record(stream)
-                done[k].record(stream)
+                ev_a[r].record(stream)
+                done[r % 2].record(stream)
                 with torch.cuda.stream(d2h):
-                    d2h.wait_event(done[k])
-                    o0, o1 = slab_rng[q]
-                    Rh[o0:o1].copy_(R.buf[o0:o1], non_blocking=True)
+                    d2h.wait_event(done[r % 2])
+                    for q in runs[r]:
+                        o0, o1 = slab_rng[q]
+                        Rh[o0:o1].copy_(R.buf[o0:o1], non_blocking=True)
             torch.cuda.synchronize()
             e2e_ph.update(bt.timings())
             bt.close()
@@ -702,8 +716,8 @@ def run_ladder_full(args, world, rank, local):
         e2e_ms = max_over_ranks((time.perf_counter() - w0) * 1e3 / args.e2e_steps, device="cuda")
         # last e2e step, per slab on the compute stream: the run itself, and the
         # wait for the slab's V upload before it (from the previous slab's end)
-        run_ms = sum(ev_b[q].elapsed_time(ev_a[q]) for q in range(len(slabs))) / len(slabs)
-        wait_ms = sum(ev_a[q - 1].elapsed_time(ev_b[q]) for q in range(1, len(slabs))) / max(1, len(slabs) - 1)
+        run_ms = sum(ev_b[r].elapsed_time(ev_a[r]) for r in range(len(runs))) / len(slabs)
+        wait_ms = sum(ev_a[r - 1].elapsed_time(ev_b[r]) for r in range(1, len(runs))) / max(1, len(slabs) - 1)
         v_bytes = Vh[0].numel() * 8
         e2e = {"value": flops_total / (e2e_ms * 1e-3) / 1e12, "unit": "TFLOP/s",
                "h2d_bytes_per_step": T.buf.numel() * 8 + v_bytes * len(slabs),
@@ -713,7 +727,7 @@ def run_ladder_full(args, world, rank, local):
                "v_source": f"each slab's V copied from a pool of {PH} pinned host slabs (slab q reads pool[q % {PH}])",
                "pipelining": "slab q+1's V upload and slab q's R download overlap slab q's compute",
                "per_slab_ms": {"run": run_ms, "wait_for_upload": wait_ms,
-                               **{k: e2e_ph[k] / max(1, e2e_ph["runs"]) for k in a4.device.Batch.PHASES
+                               **{k: e2e_ph[k] / max(1, e2e_ph["runs"] * k_run) for k in a4.device.Batch.PHASES
                                   if k != "zero_fill"}}}
         del Th, Rh, Vh
 
@@ -725,12 +739,13 @@ def run_ladder_full(args, world, rank, local):
         peak_key = "bf16_tflops_sustained" if long_run else "bf16_tflops"
         peak = peaks.get(peak_key, 1743.3 if long_run else 1933.6)
         n_v = Vb[0].buf.numel()
-        launches = stats.get("launches_held", 0) * len(slabs) + (launches_full - stats.get("launches_held", 0))
+        launches = stats.get("launches_held", 0) * len(runs) + (launches_full - stats.get("launches_held", 0))
         out = {
             "metric": METRIC, "value": value, "unit": "TFLOP/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "strong",
             "vs_baseline": None, "dtype": f"f64 (Ozaki, {S} BF16 slices)", "data": "synthetic",
             "config": {"workload": full_workload_name(nv, no, len(all_slabs)), "slices": S,
+                       "slabs_per_run": k_run,
                        "digits": "balanced base-256 (8-bit)", "slabs": len(all_slabs), "slabs_this_rank": len(slabs),
                        "block_pairs_per_slab": cold["info"]["pairs"],
                        "l2": f"per slab V {n_v * 8 / 1e9:.2f} GB + T {T.buf.numel() * 8 / 1e9:.2f} GB > 126 MB L2 "
@@ -742,8 +757,9 @@ def run_ladder_full(args, world, rank, local):
             "roofline": {"kernel": "oz_gemm_kernel (tcgen05 BF16 slice products)", "bound": "tensor",
                          "achieved": achieved, "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak,
                          "peak_kind": f"{peak_key} of {peak_kind} (timed region {ms * args.steps / 1e3:.1f} s)",
-                         "algorithmic_per_launch": f"{S * (S + 1) // 2} slice-pair GEMMs x {slab_flop:.3e} flop",
-                         "traffic": _traffic("oz_gemm_kernel")},
+                         "algorithmic_per_launch": f"{S * (S + 1) // 2} slice-pair GEMMs x {k_run} slab(s) x "
+                                                   f"{slab_flop:.3e} flop",
+                         "traffic": _traffic("oz_gemm_kernel") if k_run == 1 else None},
             "fp64_plain": ({"value": fp64_value, "unit": "TFLOP/s", "ms_per_slab": fp64_ms,
                             "kernel": "grouped DMMA (mma.sync f64), one slab",
                             "roofline": {"bound": "fp64 pipe", "peak": dgemm_tflops,
@@ -1109,6 +1125,8 @@ def main():
     ap.add_argument("--tnv", type=int, default=10, help="triples: virtual segments")
     ap.add_argument("--e2e-pool", type=int, default=2, help="ladder-full e2e: distinct V slabs in pinned host memory")
     ap.add_argument("--v-pool", type=int, default=8, help="ladder-full: distinct V slabs resident in HBM")
+    ap.add_argument("--slabs-per-run", type=int, default=1,
+                    help="ladder-full: (a,b) slabs contracted by one batch run (one T panel for all of them)")
     ap.add_argument("--slabs", type=int, default=0, help="ladder-full: only the first N (a,b) slabs (0: all)")
     ap.add_argument("--dropin-pairs", type=int, default=200, help="dropin: sampled ring block pairs")
     ap.add_argument("--workload", default="ladder-full",
