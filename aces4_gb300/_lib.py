@@ -97,6 +97,10 @@ SIGNATURES = {
     "a4g_blocks_attach": (ctypes.c_int, [c_void_p]),
     "a4g_tune_cache_save": (ctypes.c_int, [ctypes.c_char_p]),
     "a4g_tune_cache_load": (ctypes.c_int, [ctypes.c_char_p]),
+    "a4g_fused_create": (ctypes.c_int, None),
+    "a4g_fused_run": (ctypes.c_int, [c_void_p, c_void_p, c_void_p]),
+    "a4g_fused_info": (ctypes.c_int, None),
+    "a4g_fused_destroy": (None, [c_void_p]),
 }
 
 

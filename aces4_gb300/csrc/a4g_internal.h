@@ -90,6 +90,11 @@ struct DevPlan {
 int get_dev_plan(const int* ptrn, int lrank, const int* lext, int rrank, const int* rext,
                  int drank, const int* dext, const DevPlan** out);
 
+// First orbital of each block dimension's segment (energy_denominator_rhf.F:
+// 57-88, 140-220), every orbital index checked against the energy array.
+int denominator_offsets(int rank0, const int* iv, const int* ext0, int rank1, const int* ext1,
+                        const std::vector<int>& segs, int* off);
+
 // ---------------------------------------------------------------- kernels
 // Element-wise / permute / reduction launchers (kernels_block.cu).
 int launch_fill(double* d, int64_t n, double v, cudaStream_t s);

@@ -430,13 +430,15 @@ int a4g_set_predefined_int_array(const char* name, int n, const int* values) {
   return A4G_OK;
 }
 
+}  // extern "C"
+
 // Orbital offsets of each block dimension (energy_denominator_rhf.F:57-88,
 // 140-220): the sum of the segment sizes before the block's segment; for rank
 // 6 an extent of 1 marks a simple index whose offset is its value - 1.
 // Every orbital index the kernel will read is checked against the energy /
 // Fock block here, on the host, so the device never reads out of bounds.
-static int denominator_offsets(int rank0, const int* iv, const int* ext0, int rank1, const int* ext1,
-                               const std::vector<int>& segs, int* off) {
+int a4g::denominator_offsets(int rank0, const int* iv, const int* ext0, int rank1, const int* ext1,
+                             const std::vector<int>& segs, int* off) {
   const int norb = rank1 == 2 ? std::min(ext1[0], ext1[1]) : ext1[0];
   for (int q = 0; q < rank0; ++q) {
     off[q] = 0;
@@ -454,6 +456,8 @@ static int denominator_offsets(int rank0, const int* iv, const int* ext0, int ra
   }
   return A4G_OK;
 }
+
+extern "C" {
 
 void energy_denominator_rhf(int* array_slot_0, int* rank_0, int* index_values_0, int* size_0,
                             int* extents_0, double* data_0, int* array_slot_1, int* rank_1,

@@ -166,4 +166,19 @@ A4G_HD bool div_rn_int(double a, double b, double* q) {
   return true;
 }
 
+// a / b rounded to the nearest double: div_rn_int where it applies, the FP64
+// divide otherwise (zero, subnormal or non-finite operands or results).
+A4G_HD double div_rn(double a, double b) {
+  double q;
+  if (div_rn_int(a, b, &q)) return q;
+#if defined(__CUDA_ARCH__)
+  return __ddiv_rn(a, b);
+#else
+  return a / b;
+#endif
+}
+
+// x != 0 without the FP64 pipe
+A4G_HD bool nonzero(double x) { return (bits_of(x) << 1) != 0ull; }
+
 }  // namespace a4g

@@ -71,6 +71,8 @@ struct OzSplitJob {
   int kfast;  // src is unit-stride along k
   int panel;
   int64_t koff;  // first k column of this block inside the panel (multiple of 16)
+  int negate;    // slice -x instead of x (a term subtracted in a fused two-term step); generic layout only
+  int pad;
 };
 
 // Memory layout of a split job's source block, detected on the host from the
@@ -123,6 +125,21 @@ struct OzUnit {
   int pad;
 };
 
+// Energy form of the direct GEMM (fused two-term step): per destination
+// sub-block, what the epilogue needs to form the orbital-energy denominator of
+// element (m, n) in the reference's order of additions: the chain without its
+// last term, precomputed per sub-block as ptab[rk[m] * ckn + ck[n]], then the
+// last term (a row or a column index) subtracted:
+//     eps(m, n) = ptab[rk[m] * ckn + ck[n]] - elast[last_row ? m : n]
+struct OzEnergyBlock {
+  const double* ptab;
+  const int* rk;        // [M]
+  const int* ck;        // [N]
+  const double* elast;  // [M] or [N]
+  int ckn;
+  int last_row;
+};
+
 struct OzGemmArgs {
   const void* maps_a;  // CUtensorMap[n_panels_a], 64-byte aligned, device memory
   const void* maps_b;
@@ -145,6 +162,12 @@ struct OzGemmArgs {
   int mode;  // direct: bit 0 accumulate into D, bit 1 negate
   int dry;   // direct: compute everything but store nothing (timing)
   const OzDBlock* dblocks;
+  // Energy form (direct, one SM per tile): nothing is stored; each epilogue
+  // thread accumulates sum D(x) * fl(D(x) / eps(x)) over its elements in FP64
+  // and writes it to epart[(blockIdx.x * 16 + epilogue warp) * 32 + lane].
+  int energy;
+  const OzEnergyBlock* eblocks;  // one per destination sub-block (tile.dblock)
+  double* epart;
 };
 
 }  // namespace a4g

@@ -366,15 +366,9 @@ __device__ __forceinline__ double eps_at(const DenParams& p, const double* e, in
 // Denominator of the element with storage coordinates x, in the reference's
 // order of additions (energy_denominator_rhf.F do_rhf_den2/4/6): positions
 // 0, 2, 4 are virtual (subtracted), 1, 3, 5 occupied (added).
-// a / b rounded to the nearest double: integer arithmetic (exact_fp.h) for
-// normal operands and results, the FP64 divide otherwise.
-__device__ __forceinline__ double div_rn(double a, double b) {
-  double q;
-  return div_rn_int(a, b, &q) ? q : __ddiv_rn(a, b);
-}
-
-// x != 0 without the FP64 pipe
-__device__ __forceinline__ bool nonzero(double x) { return (bits_of(x) << 1) != 0ull; }
+// div_rn (a / b rounded to the nearest double: integer arithmetic for normal
+// operands and results, the FP64 divide otherwise) and nonzero come from
+// exact_fp.h.
 
 __device__ __forceinline__ double den_eps(const DenParams& p, const double* e, const int (&x)[6]) {
   const double ea = eps_at(p, e, pick6(x, p.pos[0]) + p.poff[0]);

@@ -26,7 +26,7 @@
 //   oz_exp_*_kernel     max exponent per panel row          (HBM: 8 B/elem read)
 //   oz_split_*_kernel   FP64 -> BF16 digit slices, K-major   (HBM: 8 B read + 2*slices B write)
 //                       with the block's index permute folded into the gather
-//   oz_gemm_kernel<PAIR, BN, DIRECT>
+//   oz_gemm_kernel<PAIR, BN, DIRECT, ENERGY>
 //                       persistent warp-specialised tcgen05 GEMM: TMA (SW128)
 //                       -> smem ring -> tcgen05.mma into TMEM (2 accumulators)
 //                       -> epilogue warps fold each exact chunk into the level
@@ -441,14 +441,27 @@ struct DirectCol {
   int F;         // biased column exponent (at least 1)
   int pad;
 };
+// Energy form: a second per-warp table (only that kernel declares it, so the
+// store forms keep their shared memory).
+struct EnergyCol {
+  double ec;  // the column's last-term orbital energy (when the last term is a column index)
+  int ck;     // the column's index into the prefix table (-1: outside D)
+  int pad;
+};
 struct DirectTile {
   long long roff;   // the row's offset from a column base
   DirectCol* cols;  // this warp's 32 entries
   int ebase;        // row scale and constant part of the result's exponent
   bool mlive;
   bool nonfinite;   // the row holds a non-finite operand value
+  // energy form
+  EnergyCol* ecols;    // this warp's 32 entries
+  const double* prow;  // the row's prefix-table row
+  double er;           // the row's last-term orbital energy (when the last term is a row index)
+  bool last_row;
 };
 
+template <bool ENERGY>
 __device__ __forceinline__ void direct_tile(DirectTile& t, const OzGemmArgs& a, const OzTile& tl, int row,
                                             int col0, int lane) {
   const OzDBlock db = a.dblocks[tl.dblock];
@@ -457,21 +470,40 @@ __device__ __forceinline__ void direct_tile(DirectTile& t, const OzGemmArgs& a, 
   int Em = 1;
   t.roff = 0;
   t.nonfinite = false;
+  [[maybe_unused]] OzEnergyBlock eb{};
+  if constexpr (ENERGY) {
+    eb = a.eblocks[tl.dblock];
+    t.last_row = eb.last_row != 0;
+    t.prow = eb.ptab;
+    t.er = 0.0;
+  }
   if (t.mlive) {
     const int e = a.panels_a[tl.panel_a].exps[m];
     Em = e ? e : 1;
     t.nonfinite = e == kNonFiniteExp;
-    t.roff = db.rowoff[m];
+    if constexpr (ENERGY) {
+      t.prow = eb.ptab + int64_t(eb.rk[m]) * eb.ckn;
+      if (t.last_row) t.er = eb.elast[m];
+    } else {
+      t.roff = db.rowoff[m];
+    }
   }
   t.ebase = Em - 1022 - 1022 + 2 - kDigitBits * (a.slices + 1);
   DirectCol c{nullptr, 1, 0};
+  [[maybe_unused]] EnergyCol ec{0.0, -1, 0};
   if (n < db.N) {
     const int f = a.panels_b[tl.panel_b].exps[n];
     c.F = f ? f : 1;
-    c.colp = db.colptr[n];
+    if constexpr (ENERGY) {
+      ec.ck = eb.ck[n];
+      if (!eb.last_row) ec.ec = eb.elast[n];
+    } else {
+      c.colp = db.colptr[n];
+    }
   }
   __syncwarp();  // the previous tile's entries are read
   t.cols[lane] = c;
+  if constexpr (ENERGY) t.ecols[lane] = ec;
   __syncwarp();
 }
 
@@ -526,6 +558,38 @@ __device__ __forceinline__ void store_direct(const OzGemmArgs& a, const DirectTi
   }
 }
 
+// Energy form, after the last chunk of a tile's last level: the same rounding
+// of the 32 exact sums as store_direct, then per element (nothing stored)
+//     acc += x * fl(x / eps),   eps = fl(prefix - e_last)
+// in FP64: the prefix is the denominator chain without its last term, formed
+// on the host in the reference's order; the quotient is the exactly rounded
+// FP64 quotient (div_rn); zeros add nothing and skip the division.  A
+// non-finite operand value in the row or column makes x (and the sum) NaN.
+// Every lane of the warp runs the TMEM loads (.sync.aligned: the whole warp
+// together); rows outside the block are skipped per element.
+__device__ __forceinline__ void energy_direct(const OzGemmArgs& a, const DirectTile& t, uint32_t w0addr,
+                                              double& acc) {
+#pragma unroll 1
+  for (int p = 0; p < 4; ++p) {
+    uint32_t w0[8], w1[8];
+    tc_ld8_nowait(w0addr + 8 * p, w0);
+    tc_ld8_nowait(w0addr + (kTmemW1 - kTmemW0) + 8 * p, w1);
+    tc_wait_ld();
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+      const EnergyCol ec = t.ecols[8 * p + j];
+      if (!t.mlive || ec.ck < 0) continue;
+      const int F = t.cols[8 * p + j].F;
+      const long long v = (long long)(((unsigned long long)w1[j] << 32) | w0[j]);
+      double x = i64_scaled_to_double(v, t.ebase + F, false);
+      if (t.nonfinite || F == kNonFiniteExp) x = __longlong_as_double(0x7FF8000000000000ll);
+      if (!nonzero(x)) continue;
+      const double eps = __dsub_rn(t.prow[ec.ck], t.last_row ? t.er : ec.ec);
+      acc = fma(x, div_rn(x, eps), acc);
+    }
+  }
+}
+
 // Eight warps, two per TMEM lane quadrant (warp % 4); each thread owns one
 // accumulator row and 64 of its 128 columns, in two groups of 32.  The three
 // TMEM loads of a group (chunk, hi, lo) are issued before one wait.  In the
@@ -537,7 +601,7 @@ __device__ __forceinline__ void store_direct(const OzGemmArgs& a, const DirectTi
 // TMEM words per element; the host admits a batch to this form only when the
 // sum stays below 2^63.  The last chunk of the last level is rounded once and
 // stored into D.
-template <bool PAIR, bool DIRECT>
+template <bool PAIR, bool DIRECT, bool ENERGY = false>
 __device__ void epilogue(const OzGemmArgs& a, OzSmemT<PAIR, 128>& sm, uint32_t tmem, int warp, int lane,
                          uint32_t rank) {
   constexpr int kRows = PAIR ? 2 * kOzBM : kOzBM;  // rows of a tile
@@ -549,9 +613,14 @@ __device__ void epilogue(const OzGemmArgs& a, OzSmemT<PAIR, 128>& sm, uint32_t t
   for (int b = 0; b < 2; ++b) empty_bar[b] = PAIR ? mapa_shared(&sm.acc_empty[b], 0) : smem_u32(&sm.acc_empty[b]);
   uint32_t chunk = 0;
   [[maybe_unused]] DirectTile dt{};
+  [[maybe_unused]] double eacc = 0.0;
   if constexpr (DIRECT) {
     __shared__ DirectCol direct_cols[kThreadsOzDirect / 32 - 2][32];  // one table per epilogue warp
     dt.cols = direct_cols[warp - 2];
+    if constexpr (ENERGY) {
+      __shared__ EnergyCol energy_cols[kThreadsOzDirect / 32 - 2][32];
+      dt.ecols = energy_cols[warp - 2];
+    }
   }
   auto release = [&](uint32_t buf) {
     tc_fence_before();
@@ -568,8 +637,9 @@ __device__ void epilogue(const OzGemmArgs& a, OzSmemT<PAIR, 128>& sm, uint32_t t
     if constexpr (DIRECT) {
       const bool last_level = un.level == a.slices - 1;
       if (un.level == 0) {
-        direct_tile(dt, a, a.tiles[un.tile], row, kCols * h, lane);
-        if ((a.mode & 1) && !a.dry) prefetch_direct(dt);
+        direct_tile<ENERGY>(dt, a, a.tiles[un.tile], row, kCols * h, lane);
+        if constexpr (!ENERGY)
+          if ((a.mode & 1) && !a.dry) prefetch_direct(dt);
       }
       for (int c = 0; c < nchunks; ++c) {
         const uint32_t buf = chunk & 1;
@@ -606,7 +676,10 @@ __device__ void epilogue(const OzGemmArgs& a, OzSmemT<PAIR, 128>& sm, uint32_t t
         tc_wait_st();
         release(buf);  // the next MMAs may start while this thread stores D
         ++chunk;
-        if (final) store_direct(a, dt, lane_addr + kTmemW0);
+        if (final) {
+          if constexpr (ENERGY) energy_direct(a, dt, lane_addr + kTmemW0, eacc);
+          else store_direct(a, dt, lane_addr + kTmemW0);
+        }
       }
       return true;
     } else {
@@ -661,6 +734,7 @@ __device__ void epilogue(const OzGemmArgs& a, OzSmemT<PAIR, 128>& sm, uint32_t t
     return true;
     }
   });
+  if constexpr (ENERGY) a.epart[(size_t(blockIdx.x) * 16 + size_t(warp - 2)) * 32 + lane] = eacc;
 }
 
 // 256-column tiles: the two FP32 accumulators use all 512 TMEM columns, so the
@@ -714,7 +788,7 @@ __device__ void epilogue_int(const OzGemmArgs& a, OzSmemT<PAIR, 256>& sm, uint32
   });
 }
 
-template <bool PAIR, int BN, bool DIRECT = false>
+template <bool PAIR, int BN, bool DIRECT = false, bool ENERGY = false>
 __global__ void __launch_bounds__(DIRECT ? kThreadsOzDirect : kThreadsOz, 1)
     oz_gemm_kernel(const __grid_constant__ OzGemmArgs a) {
   using SM = OzSmemT<PAIR, BN>;
@@ -767,7 +841,7 @@ __global__ void __launch_bounds__(DIRECT ? kThreadsOzDirect : kThreadsOz, 1)
     }
   } else {
     if constexpr (BN == 256) epilogue_int<PAIR>(a, sm, tmem, warp, lane, rank);
-    else epilogue<PAIR, DIRECT>(a, sm, tmem, warp, lane, rank);
+    else epilogue<PAIR, DIRECT, ENERGY>(a, sm, tmem, warp, lane, rank);
   }
   tc_fence_before();
   __syncthreads();
@@ -811,7 +885,7 @@ __device__ __forceinline__ void load_job_tile(const OzSplitJob& jb, int r0, int 
     unsigned long long v = 0;
     if (r0 + r < jb.rows && k0 + k < jb.K)
       v = __double_as_longlong(__ldg(&jb.src[__ldg(&jb.offRow[r0 + r]) + __ldg(&jb.offK[k0 + k])]));
-    tile[r][k] = v;
+    tile[r][k] = v ^ (jb.negate ? (1ull << 63) : 0ull);  // -x: the sign bit (exponents unchanged)
   }
 }
 
@@ -1367,6 +1441,23 @@ __global__ void wait_timeout_selftest_kernel(unsigned long long limit_ns, int* e
   if (!done) atomicExch(err, 6);
 }
 
+// esum += efact * (sum of the n partial energies), the partials added in a
+// fixed order (one CTA: strided per-thread sums, then a fixed tree), so a GPU
+// gives the same bits every run.
+__global__ void __launch_bounds__(1024) oz_energy_reduce_kernel(const double* __restrict__ part, int n,
+                                                                double efact, double* esum) {
+  __shared__ double red[1024];
+  double acc = 0.0;
+  for (int i = threadIdx.x; i < n; i += 1024) acc += part[i];
+  red[threadIdx.x] = acc;
+  __syncthreads();
+  for (int w = 512; w > 0; w >>= 1) {
+    if (int(threadIdx.x) < w) red[threadIdx.x] += red[threadIdx.x + w];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) *esum += efact * red[0];
+}
+
 using EncodeTiled = PFN_cuTensorMapEncodeTiled_v12000;
 EncodeTiled get_encoder() {
   static EncodeTiled fn = nullptr;
@@ -1454,10 +1545,10 @@ int oz_launch_split(int layout, const OzSplitJob* jobs, const int64_t* prefix, i
   return A4G_OK;
 }
 
-template <bool PAIR, int BN, bool DIRECT = false>
+template <bool PAIR, int BN, bool DIRECT = false, bool ENERGY = false>
 int set_smem_attr() {
-  A4G_CUDA(cudaFuncSetAttribute(oz_gemm_kernel<PAIR, BN, DIRECT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                int(sizeof(OzSmemT<PAIR, BN>)) + 1024));
+  A4G_CUDA(cudaFuncSetAttribute(oz_gemm_kernel<PAIR, BN, DIRECT, ENERGY>,
+                                cudaFuncAttributeMaxDynamicSharedMemorySize, int(sizeof(OzSmemT<PAIR, BN>)) + 1024));
   return A4G_OK;
 }
 
@@ -1476,7 +1567,8 @@ int oz_prepare() {
     int rc;
     if ((rc = set_smem_attr<false, 128>()) || (rc = set_smem_attr<true, 128>()) ||
         (rc = set_smem_attr<false, 256>()) || (rc = set_smem_attr<true, 256>()) ||
-        (rc = set_smem_attr<false, 128, true>()) || (rc = set_smem_attr<true, 128, true>())) {
+        (rc = set_smem_attr<false, 128, true>()) || (rc = set_smem_attr<true, 128, true>()) ||
+        (rc = set_smem_attr<false, 128, true, true>())) {
       done.store(0);
       return rc;
     }
@@ -1504,11 +1596,11 @@ int oz_max_pairs(int* pairs) {
   return A4G_OK;
 }
 
-template <bool PAIR, int BN, bool DIRECT = false>
+template <bool PAIR, int BN, bool DIRECT = false, bool ENERGY = false>
 int launch_form(const OzGemmArgs& args, int grid, cudaStream_t s) {
   const size_t smem = sizeof(OzSmemT<PAIR, BN>) + 1024;
   if constexpr (!PAIR) {
-    oz_gemm_kernel<false, BN, DIRECT><<<grid, DIRECT ? kThreadsOzDirect : kThreadsOz, smem, s>>>(args);
+    oz_gemm_kernel<false, BN, DIRECT, ENERGY><<<grid, DIRECT ? kThreadsOzDirect : kThreadsOz, smem, s>>>(args);
   } else {
     if (grid % 2) return fail(A4G_ERR_ARG, "CTA-pair grid must be even");
     cudaLaunchConfig_t cfg = {};
@@ -1535,6 +1627,10 @@ int oz_launch_gemm(const OzGemmArgs& args, int grid, bool pair, int tile_cols, c
   if (args.direct) {
     if (tile_cols != 128 || args.nsplit != 1 || args.n_units % args.slices)
       return fail(A4G_ERR_ARG, "direct form: 128-column tiles, one split, whole tiles");
+    if (args.energy) {
+      if (pair || !args.eblocks || !args.epart) return fail(A4G_ERR_ARG, "energy form: one SM per tile, tables");
+      return launch_form<false, 128, true, true>(args, grid, s);
+    }
     return pair ? launch_form<true, 128, true>(args, grid, s) : launch_form<false, 128, true>(args, grid, s);
   }
   if (tile_cols == 256) return pair ? launch_form<true, 256>(args, grid, s) : launch_form<false, 256>(args, grid, s);
@@ -1581,6 +1677,12 @@ int oz_launch_recombine(const OzTile* tiles, int ntiles, int tile_rows, int tile
 #undef A4G_RECOMBINE
     default: return fail(A4G_ERR_ARG, "recombine: slices must be 1..7");
   }
+  A4G_CUDA(cudaGetLastError());
+  return A4G_OK;
+}
+
+int oz_launch_energy_reduce(const double* part, int n, double efact, double* esum, cudaStream_t s) {
+  oz_energy_reduce_kernel<<<1, 1024, 0, s>>>(part, n, efact, esum);
   A4G_CUDA(cudaGetLastError());
   return A4G_OK;
 }

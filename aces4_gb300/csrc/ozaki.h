@@ -23,6 +23,8 @@ int oz_launch_split(int layout, const OzSplitJob* jobs, const int64_t* prefix, i
 // tile_cols: 128 (exact sums kept in TMEM) or 256 (exact sums in registers).
 int oz_launch_gemm(const OzGemmArgs& args, int grid, bool pair, int tile_cols, cudaStream_t s);
 int oz_wait_timeout_selftest(int limit_ms, int* waited_ms, cudaStream_t s);
+// esum (device) += efact * the sum of the energy form's n partials, in a fixed order.
+int oz_launch_energy_reduce(const double* part, int n, double efact, double* esum, cudaStream_t s);
 int oz_launch_recombine(const OzTile* tiles, int ntiles, int tile_rows, int tile_cols, const OzDBlock* dblocks,
                         const OzPanel* pa, const OzPanel* pb, const int* ws, int slices,
                         int nsplit, int mode, cudaStream_t s);  // mode: bit 0 accumulate, bit 1 negate

@@ -222,6 +222,82 @@ def _triples_arg(triples):
     return ctypes.cast(_triple_array(tl), ctypes.c_void_p), len(tl), tl
 
 
+class _Term(ctypes.Structure):
+    _fields_ = [("contr_ptrn", ctypes.c_void_p), ("triples", ctypes.c_void_p), ("n_triples", ctypes.c_int64),
+                ("sign", ctypes.c_int)]
+
+
+class _FusedEnergy(ctypes.Structure):
+    _fields_ = [("n_blocks", ctypes.c_int64), ("blocks", ctypes.c_void_p), ("index_values", ctypes.c_void_p),
+                ("den_order", ctypes.c_void_p), ("rank1", ctypes.c_int), ("ext1", ctypes.c_void_p),
+                ("e_or_fock", ctypes.c_void_p), ("nsegs", ctypes.c_int), ("seg_sizes", ctypes.c_void_p),
+                ("efact", ctypes.c_double)]
+
+
+class Fused:
+    """One or two contraction statements into the same destination blocks in
+    one split-precision pass (a4g_fused_*).
+
+    terms: [(ptrn, triples, sign), ...] with triples as for Batch and sign +1
+    or -1.  energy=None: run() stores D = sum of sign * L R (beta 1: adds).
+    energy=dict(blocks, index_values, ext1, e_or_fock, seg_sizes, efact=1.0,
+    den_order=None): run(esum) adds efact * sum D * fl(D / eps) to esum (a
+    1-element CUDA float64 tensor) and stores nothing.
+    """
+
+    def __init__(self, drank, lrank, rrank, terms, slices=5, beta=0, energy=None):
+        keep, tarr = [], (_Term * max(1, len(terms)))()
+        for i, (ptrn, triples, sign) in enumerate(terms):
+            arr, n, k = _triples_arg(triples)
+            pt = _iarr(ptrn)
+            keep += [k, arr, pt]
+            tarr[i].contr_ptrn = ctypes.cast(pt, ctypes.c_void_p)
+            tarr[i].triples = arr
+            tarr[i].n_triples = n
+            tarr[i].sign = int(sign)
+        en = None
+        if energy is not None:
+            blocks = energy["blocks"]
+            bl = (ctypes.c_uint64 * max(1, len(blocks)))(*[_ptr(x) for x in blocks])
+            iv = _iarr([int(v) for row in energy["index_values"] for v in row])
+            e1, sg = _iarr(energy["ext1"]), _iarr(energy["seg_sizes"])
+            do = _iarr(energy["den_order"]) if energy.get("den_order") is not None else None
+            keep += [bl, iv, e1, sg, do, energy["e_or_fock"]]
+            en = _FusedEnergy(len(blocks), ctypes.cast(bl, ctypes.c_void_p), ctypes.cast(iv, ctypes.c_void_p),
+                              ctypes.cast(do, ctypes.c_void_p) if do is not None else None, len(energy["ext1"]),
+                              ctypes.cast(e1, ctypes.c_void_p), _ptr(energy["e_or_fock"]),
+                              len(energy["seg_sizes"]), ctypes.cast(sg, ctypes.c_void_p),
+                              float(energy.get("efact", 1.0)))
+        opts = _Opts(PREC_OZAKI_BF16, slices, beta, 0, 0, 0)
+        h = ctypes.c_void_p(0)
+        rc = lib().a4g_fused_create(ctypes.byref(h), _i(drank), _i(lrank), _i(rrank), tarr, _i(len(terms)),
+                                    ctypes.byref(en) if en is not None else None, ctypes.byref(opts))
+        _check(rc, "a4g_fused_create")
+        self._h = h
+        self._keep = keep  # the caller's buffers must outlive the step
+        self.energy = energy is not None
+
+    def run(self, esum=None, stream=None):
+        _check(lib().a4g_fused_run(self._h, ctypes.c_void_p(_ptr(esum)), _stream(stream)), "a4g_fused_run")
+
+    def info(self):
+        pairs, flops, el, nb = ctypes.c_int64(0), ctypes.c_double(0), ctypes.c_int64(0), ctypes.c_int64(0)
+        _check(lib().a4g_fused_info(self._h, ctypes.byref(pairs), ctypes.byref(flops), ctypes.byref(el),
+                                    ctypes.byref(nb)), "a4g_fused_info")
+        return {"pairs": pairs.value, "flops": flops.value, "elements": el.value, "device_bytes": nb.value}
+
+    def close(self):
+        if getattr(self, "_h", None) and self._h.value:
+            lib().a4g_fused_destroy(self._h)
+            self._h = ctypes.c_void_p(0)
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 def tune_cache_clear():
     """Forget every autotuned choice of this process (a4g_tune_cache_clear)."""
     lib().a4g_tune_cache_clear()

@@ -283,7 +283,6 @@ def run_triples(args, world, rank, local):
     import aces4_gb300 as a4
     from aces4_gb300.blocks import (TRIPLES_TERM1_LABELS, TRIPLES_TERM2_LABELS, BlockArray,
                                     triples_index_values, triples_step)
-    from oracle import oracle
 
     torch.cuda.set_device(local)
     if world > 1:
@@ -307,8 +306,8 @@ def run_triples(args, world, rank, local):
     fock = torch.tensor(np.diag(e).ravel(order="F"), device="cuda")
     W = BlockArray([v_segs, o_segs, v_segs, o_segs, v_segs, o_segs], present=lambda k: k[0] == a and k[2] == b)
     t1, t2 = triples_step(W, V1, V2, T, a, b)
-    p1 = oracle.get_contraction_ptrn(6, 4, 4, sum(TRIPLES_TERM1_LABELS, []))[1]
-    p2 = oracle.get_contraction_ptrn(6, 4, 4, sum(TRIPLES_TERM2_LABELS, []))[1]
+    p1 = a4.ref.get_contraction_ptrn(6, 4, 4, sum(TRIPLES_TERM1_LABELS, []))[1]
+    p2 = a4.ref.get_contraction_ptrn(6, 4, 4, sum(TRIPLES_TERM2_LABELS, []))[1]
     segs = o_segs + v_segs
     norb = sum(segs)
     esum = torch.zeros(1, dtype=torch.float64, device="cuda")
@@ -323,16 +322,19 @@ def run_triples(args, world, rank, local):
         return (a4.device.Batch(p1, 6, 4, 4, t1, variant=args.variant if prec else 0, **kw),
                 a4.device.Batch(p2, 6, 4, 4, t2, beta=1, negate=True, variant=args.variant if prec else 0, **kw))
 
-    b1, b2 = batches(a4.device.PREC_OZAKI_BF16)
-    flops = b1.info()["flops"] + b2.info()["flops"]
+    # the fused step (both terms and the energy in one pass, W never stored)
+    terms = [(p1, t1, 1), (p2, t2, -1)]
+    energy_args = dict(blocks=[blk for _, _, blk in ivs], index_values=[iv for iv, _, _ in ivs],
+                       ext1=[norb, norb], e_or_fock=fock, seg_sizes=segs, efact=1.0)
+    t0 = time.perf_counter()
+    fe = a4.device.Fused(6, 4, 4, terms, slices=args.slices, energy=energy_args)
+    create_s = time.perf_counter() - t0
+    finfo = fe.info()
+    flops = finfo["flops"]
     for _ in range(args.warmup):
-        b1.run(stream)
-        b2.run(stream)
-        energy()
+        fe.run(esum, stream)
     torch.cuda.synchronize()
-    b1.timings(), b2.timings()
     ev = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
-    t_terms = t_energy = 0.0
     if world > 1:
         dist.barrier()
     torch.cuda.synchronize()
@@ -341,28 +343,44 @@ def run_triples(args, world, rank, local):
     with ClockSampler(gpu_id) as clk:
         ev[0].record(stream)
         for _ in range(args.steps):
-            ev[1].record(stream)
-            b1.run_timed(stream)
-            b2.run_timed(stream)
-            ev[2].record(stream)
-            energy()
-            ev[3].record(stream)
-            torch.cuda.synchronize()
-            t_terms += ev[1].elapsed_time(ev[2])
-            t_energy += ev[2].elapsed_time(ev[3])
+            fe.run(esum, stream)
+        ev[1].record(stream)
+        torch.cuda.synchronize()
+    ms = max_over_ranks(ev[0].elapsed_time(ev[1]) / args.steps)
+    esum.zero_()
+    fe.run(esum, stream)
+    E_split = float(esum.item())
+    fe.close()
+    # the same step through two batches and a separate energy pass (W stored, then read)
+    b1, b2 = batches(a4.device.PREC_OZAKI_BF16)
+    for _ in range(max(1, min(args.warmup, 2))):
+        b1.run(stream)
+        b2.run(stream)
+        energy()
+    torch.cuda.synchronize()
+    b1.timings(), b2.timings()
+    t_terms = t_energy = 0.0
+    n_unfused = max(1, min(args.steps, 3))
+    for _ in range(n_unfused):
+        ev[1].record(stream)
+        b1.run_timed(stream)
+        b2.run_timed(stream)
+        ev[2].record(stream)
+        energy()
         ev[3].record(stream)
         torch.cuda.synchronize()
-    ms = max_over_ranks(ev[0].elapsed_time(ev[3]) / args.steps)
+        t_terms += ev[1].elapsed_time(ev[2])
+        t_energy += ev[2].elapsed_time(ev[3])
     ph1, ph2 = b1.timings(), b2.timings()
-    esum.zero_()
-    b1.run(stream)
-    b2.run(stream)
-    energy()
-    E_split = float(esum.item())
-    W_split = W.buf.clone()
     form = b1.form()
     b1.close()
     b2.close()
+    # W of the fused pass (store form) against plain FP64
+    fs = a4.device.Fused(6, 4, 4, terms, slices=args.slices)
+    fs.run(stream=stream)
+    torch.cuda.synchronize()
+    fs.close()
+    W_split = W.buf.clone()
     f1, f2 = batches(a4.device.PREC_FP64)
     torch.cuda.synchronize()
     ev[0].record(stream)
@@ -382,21 +400,25 @@ def run_triples(args, world, rank, local):
     if rank == 0:
         runs = max(1, ph1["runs"])
         n_w = sum(W.size(k) for k in W.keys())
-        e_ms = t_energy / args.steps
+        e_ms = t_energy / n_unfused
         line = {
             "metric": TRIPLES_METRIC, "value": world * flops / (ms * 1e-3) / 1e12, "unit": "TFLOP/s",
             "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
-            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "bf16", "data": "synthetic",
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": f"f64 (Ozaki, {args.slices} BF16 slices)", "data": "synthetic",
             "config": {"workload": f"triples o={o} (1x{seg}), v={v} ({nv}x{seg}), one (a,b) step: "
                                    f"{len(W.keys())} W blocks of {seg}^6, {len(t1)}+{len(t2)} block pairs "
-                                   f"({flops:.3g} flop)", "slices": args.slices},
-            "phases_ms_per_step": {
+                                   f"({flops:.3g} flop), W and E = sum W fl(W/D) in one fused pass "
+                                   f"(W never stored)", "slices": args.slices},
+            "fused": {"elements": finfo["elements"], "device_bytes": finfo["device_bytes"],
+                      "create_s": create_s, "gelem_per_s": finfo["elements"] / (ms * 1e-3) / 1e9},
+            "unfused_two_batches": {
+                "ms_per_step": (t_terms + t_energy) / n_unfused,
                 "term1": {k: ph1[k] / runs for k in ("zero_fill", "exponents", "split", "gemm", "recombine")},
                 "term2": {k: ph2[k] / runs for k in ("zero_fill", "exponents", "split", "gemm", "recombine")},
-                "terms_total": t_terms / args.steps, "energy": e_ms},
-            "energy_pass": {"elements": n_w, "ms": e_ms, "gelem_per_s": n_w / (e_ms * 1e-3) / 1e9,
-                            "hbm_gbs": n_w * 8 / (e_ms * 1e-3) / 1e9},
-            "gemm_form": {"chosen": form["name"], "autotune_ms": form["tuned_ms"]},
+                "terms_total": t_terms / n_unfused, "energy": e_ms,
+                "energy_gelem_per_s": n_w / (e_ms * 1e-3) / 1e9,
+                "gemm_form": {"chosen": form["name"], "autotune_ms": form["tuned_ms"]}},
             "fp64_plain": {"value": flops / (fp64_ms * 1e-3) / 1e12, "unit": "TFLOP/s",
                            "ms_per_step_terms": fp64_ms},
             "energy": {"split": E_split, "fp64": E64, "rel_diff": abs(E_split - E64) / abs(E64)},
@@ -968,7 +990,6 @@ def run_config(args, world, rank, local):
     import torch
 
     import aces4_gb300 as a4
-    from oracle import oracle
 
     torch.cuda.set_device(local)
     a4.device.init(local)
@@ -976,7 +997,7 @@ def run_config(args, world, rank, local):
     R, trip, labels, desc = build_config(torch, args.workload, 11 + rank)
     torch.cuda.synchronize()
     d, l, r = labels
-    ptrn = oracle.get_contraction_ptrn(len(d), len(l), len(r), d + l + r)[1]
+    ptrn = a4.ref.get_contraction_ptrn(len(d), len(l), len(r), d + l + r)[1]
     res = {}
     for prec in (a4.device.PREC_OZAKI_BF16, a4.device.PREC_FP64):
         b = a4.device.Batch(ptrn, 4, 4, 4, trip, precision=prec, slices=args.slices)

@@ -443,6 +443,63 @@ void a4g_tune_cache_clear(void);
 int a4g_tune_cache_save(const char* path);
 int a4g_tune_cache_load(const char* path);
 
+/* ----------------------------------------------------------------------------
+ * Fused pardo step: one or two contraction statements into the same
+ * destination blocks in one split-precision pass, and optionally the (T)
+ * energy of the result without storing it (rccsdpt_aaa.sialx:2163-2172:
+ * W = V1*T - V2*T, then energy_denominator_rhf on a copy and the contraction
+ * of the two to a scalar, esum += etemp).
+ *
+ * Store form (energy NULL): every destination block becomes
+ *     D = sign1 * L1 R1 + sign2 * L2 R2        (beta 1: D += ...)
+ * with both terms' integer level sums added before the one rounding (the two
+ * statements of the reference round after each).  Energy form: nothing is
+ * written; for every element x of every destination block
+ *     *esum += efact * D(x) * fl(D(x) / eps(x))
+ * eps(x) the orbital-energy denominator of a4g_energy_contract (the same
+ * terms added in the same order: the chain without its last term is
+ * tabulated once at creation, the last subtraction and the exactly rounded
+ * quotient are formed per element), the products summed in FP64 in a fixed
+ * order.  D exists only one 128 x 128 tile at a time, as exact 64-bit level
+ * sums in tensor memory.
+ *
+ * Both terms share the destination ranks and the operand ranks.  Every
+ * destination index is a row (left operand in both terms), a column (right
+ * in both), or fixed per sub-problem (left in one term, right in the other:
+ * the triples' b and j); the energy form needs the denominator's last term
+ * on a row or column index.  Split precision only (opts->precision
+ * A4G_PREC_OZAKI_BF16); opts->slices and opts->beta apply, the other options
+ * are ignored.  A triple with a NULL operand is skipped. */
+typedef struct a4g_term {
+  const int* contr_ptrn; /* as for a4g_batch_create (lrank + rrank entries)  */
+  const a4g_triple* triples;
+  int64_t n_triples;
+  int sign; /* +1: the term is added, -1: subtracted                       */
+} a4g_term;
+
+typedef struct a4g_fused_energy {
+  int64_t n_blocks;
+  double* const* blocks;   /* the destination blocks (the triples' d pointers) */
+  const int* index_values; /* [n_blocks * drank]: as a4g_energy_contract's index_values0 */
+  const int* den_order;    /* NULL or [drank], as for a4g_energy_contract */
+  int rank1;
+  const int* ext1;
+  const double* e_or_fock; /* device */
+  int nsegs;
+  const int* seg_sizes;
+  double efact;
+} a4g_fused_energy;
+
+typedef struct a4g_fused a4g_fused;
+
+int a4g_fused_create(a4g_fused** out, int drank, int lrank, int rrank, const a4g_term* terms, int nterms,
+                     const a4g_fused_energy* energy, const a4g_batch_opts* opts);
+/* esum: a device double (energy form), else NULL.  Operands are read at run
+ * time (their values may change between runs; their addresses may not). */
+int a4g_fused_run(a4g_fused* f, double* esum, void* stream);
+int a4g_fused_info(const a4g_fused* f, int64_t* pairs, double* flops, int64_t* elements, int64_t* device_bytes);
+void a4g_fused_destroy(a4g_fused* f);
+
 #ifdef __cplusplus
 }
 #endif

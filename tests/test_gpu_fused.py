@@ -1,0 +1,193 @@
+"""The fused triples step on the GPU (a4g_fused_*): both contraction terms of
+W(a,i,b,j,c,k) = sum_d V1(b,c,d,k) T(a,d,i,j) - sum_l V2(l,c,j,k) T(a,b,i,l)
+in one split-precision pass (rccsdpt_aaa.sialx:2163-2172), W either stored or
+reduced straight to the (T) energy E = sum W fl(W / eps) without being
+stored.
+
+Tolerances (relative, 5 slices): W against the oracle's BLAS path 1e-10 per
+block (Frobenius), E against the oracle's (T) energy pattern 1e-10, the same
+bound the two-batch split path is held to; two runs of the energy form give
+the same bits."""
+import numpy as np
+import pytest
+
+from oracle import oracle
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def a4():
+    import aces4_gb300
+
+    aces4_gb300.build()
+    aces4_gb300.device.init(0)
+    return aces4_gb300
+
+
+def _problem(o_segs, v_segs, seed):
+    import torch
+
+    from aces4_gb300.blocks import BlockArray
+
+    o, v = sum(o_segs), sum(v_segs)
+    V1 = BlockArray([v_segs, v_segs, v_segs, o_segs])
+    V2 = BlockArray([o_segs, v_segs, o_segs, o_segs])
+    T = BlockArray([v_segs, v_segs, o_segs, o_segs])
+    g = torch.Generator(device="cuda")
+    g.manual_seed(seed)
+    V1.buf.uniform_(-1.0, 1.0, generator=g).div_(v)
+    V2.buf.uniform_(-1.0, 1.0, generator=g).div_(v)
+    T.buf.normal_(0.0, 0.1, generator=g)
+    rng = np.random.default_rng(seed)
+    e = np.concatenate([rng.uniform(-2.0, -0.5, o), rng.uniform(0.2, 5.0, v)])
+    fock = np.diag(e).ravel(order="F").copy()
+    return V1, V2, T, fock
+
+
+def _step(V1, V2, T, o_segs, v_segs, a, b):
+    from aces4_gb300.blocks import (TRIPLES_TERM1_LABELS, TRIPLES_TERM2_LABELS, BlockArray, triples_step)
+
+    W = BlockArray([v_segs, o_segs, v_segs, o_segs, v_segs, o_segs], present=lambda k: k[0] == a and k[2] == b)
+    W.buf.fill_(float("nan"))
+    t1, t2 = triples_step(W, V1, V2, T, a, b)
+    p1 = oracle.get_contraction_ptrn(6, 4, 4, sum(TRIPLES_TERM1_LABELS, []))[1]
+    p2 = oracle.get_contraction_ptrn(6, 4, 4, sum(TRIPLES_TERM2_LABELS, []))[1]
+    return W, [(p1, t1, 1), (p2, t2, -1)]
+
+
+def _energy_args(W, o_segs, v_segs, fock_t):
+    from aces4_gb300.blocks import triples_index_values
+
+    segs = list(o_segs) + list(v_segs)
+    norb = sum(segs)
+    keys = list(W.keys())
+    return dict(blocks=[W.block(k) for k in keys], index_values=[triples_index_values(k, len(o_segs)) for k in keys],
+                ext1=[norb, norb], e_or_fock=fock_t, seg_sizes=segs, efact=1.0)
+
+
+def _oracle_W_E(W, terms, o_segs, v_segs, fock):
+    from aces4_gb300.blocks import triples_index_values
+
+    segs = list(o_segs) + list(v_segs)
+    norb = sum(segs)
+    Ws, E = {}, 0.0
+    for key in W.keys():
+        dptr, de = W.block(key).data_ptr(), W.ext(key)
+        want = np.zeros(W.size(key))
+        for p, trip, sign in terms:
+            for d, l, r, _, le, re in trip:
+                if d.data_ptr() == dptr:
+                    want += sign * oracle.contract_blas(p, l.cpu().numpy(), le, r.cpu().numpy(), re, de)
+        Ws[key] = want
+        E += oracle.energy_contract(triples_index_values(key, len(o_segs)), de, want, [norb, norb], fock, segs, 1.0)
+    return Ws, E
+
+
+@pytest.mark.parametrize("o_segs,v_segs,a,b", [([6], [12, 12], 0, 1),         # even segments
+                                               ([3, 5], [5, 7, 4], 0, 2)])   # uneven, odd k lengths
+def test_fused_store_and_energy_match_oracle(a4, o_segs, v_segs, a, b):
+    import torch
+
+    V1, V2, T, fock = _problem(o_segs, v_segs, 21 + len(v_segs))
+    ft = torch.tensor(fock, device="cuda")
+    W, terms = _step(V1, V2, T, o_segs, v_segs, a, b)
+    Wref, Eref = _oracle_W_E(W, terms, o_segs, v_segs, fock)
+    f = a4.device.Fused(6, 4, 4, terms)
+    f.run()
+    a4.device.sync()
+    for key in W.keys():
+        got = W.block(key).cpu().numpy()
+        nrm = np.linalg.norm(Wref[key])
+        assert np.all(np.isfinite(got)), key  # every element written
+        assert np.linalg.norm(got - Wref[key]) <= 1e-10 * nrm, key
+    f.close()
+    W.buf.fill_(float("nan"))  # the energy form stores nothing
+    fe = a4.device.Fused(6, 4, 4, terms, energy=_energy_args(W, o_segs, v_segs, ft))
+    esum = torch.full((1,), 0.5, dtype=torch.float64, device="cuda")
+    fe.run(esum)
+    a4.device.sync()
+    got = float(esum.item()) - 0.5
+    assert Eref < 0
+    assert abs(got - Eref) <= 1e-10 * abs(Eref)
+    assert bool(torch.isnan(W.buf).all())
+    info = fe.info()
+    assert info["elements"] == sum(W.size(k) for k in W.keys())
+    o, v = sum(o_segs), sum(v_segs)
+    va, vb = v_segs[a], v_segs[b]
+    assert abs(info["flops"] - 2 * va * vb * v * o ** 3 * (v + o)) < 1
+    fe.close()
+
+
+def test_fused_energy_is_deterministic_and_accumulates(a4):
+    import torch
+
+    o_segs, v_segs = [8], [16, 16, 16]
+    V1, V2, T, fock = _problem(o_segs, v_segs, 5)
+    ft = torch.tensor(fock, device="cuda")
+    W, terms = _step(V1, V2, T, o_segs, v_segs, 1, 2)
+    ea = _energy_args(W, o_segs, v_segs, ft)
+    ea["efact"] = 0.5
+    fe = a4.device.Fused(6, 4, 4, terms, energy=ea)
+    e1 = torch.zeros(1, dtype=torch.float64, device="cuda")
+    e2 = torch.zeros(1, dtype=torch.float64, device="cuda")
+    fe.run(e1)
+    fe.run(e2)
+    fe.run(e2)
+    a4.device.sync()
+    assert float(e1.item()) != 0.0
+    assert abs(float(e2.item()) - 2 * float(e1.item())) <= 1e-15 * abs(float(e2.item()))
+    e3 = torch.zeros(1, dtype=torch.float64, device="cuda")
+    fe.run(e3)
+    a4.device.sync()
+    assert float(e3.item()) == float(e1.item())
+    _, Eref = _oracle_W_E(W, terms, o_segs, v_segs, fock)
+    assert abs(float(e1.item()) - 0.5 * Eref) <= 1e-10 * abs(0.5 * Eref)
+    fe.close()
+
+
+def test_fused_store_beta_and_single_term(a4):
+    """beta = 1 adds the fused sum to D; one term alone is a plain direct-form
+    contraction."""
+    import torch
+
+    o_segs, v_segs = [6], [12, 12]
+    V1, V2, T, fock = _problem(o_segs, v_segs, 8)
+    W, terms = _step(V1, V2, T, o_segs, v_segs, 1, 0)
+    W.buf.fill_(0.25)
+    f = a4.device.Fused(6, 4, 4, terms, beta=1)
+    f.run()
+    a4.device.sync()
+    Wref, _ = _oracle_W_E(W, terms, o_segs, v_segs, fock)
+    for key in W.keys():
+        want = Wref[key] + 0.25
+        got = W.block(key).cpu().numpy()
+        assert np.linalg.norm(got - want) <= 1e-10 * np.linalg.norm(want), key
+    f.close()
+    W.buf.fill_(float("nan"))
+    f1 = a4.device.Fused(6, 4, 4, terms[:1])
+    f1.run()
+    a4.device.sync()
+    Wref1, _ = _oracle_W_E(W, terms[:1], o_segs, v_segs, fock)
+    for key in W.keys():
+        got = W.block(key).cpu().numpy()
+        assert np.linalg.norm(got - Wref1[key]) <= 1e-10 * np.linalg.norm(Wref1[key]), key
+    f1.close()
+
+
+def test_fused_rejects_what_it_does_not_cover(a4):
+    import torch
+
+    o_segs, v_segs = [4], [6, 6]
+    V1, V2, T, fock = _problem(o_segs, v_segs, 3)
+    W, terms = _step(V1, V2, T, o_segs, v_segs, 0, 1)
+    with pytest.raises(a4.device.A4GError):
+        a4.device.Fused(6, 4, 4, [terms[0], terms[1], terms[0]])  # at most two terms
+    with pytest.raises(a4.device.A4GError):
+        a4.device.Fused(6, 4, 4, [(terms[0][0], terms[0][1], 2)])  # sign must be +-1
+    ft = torch.tensor(fock, device="cuda")
+    ea = _energy_args(W, o_segs, v_segs, ft)
+    ea["den_order"] = [0, 1, 4, 3, 2, 5]  # the last term on b, a fixed index of the sub-problems
+    with pytest.raises(a4.device.A4GError) as ei:
+        a4.device.Fused(6, 4, 4, terms, energy=ea)
+    assert ei.value.rc == 6
