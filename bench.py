@@ -697,10 +697,16 @@ def run_ladder_full(args, world, rank, local):
                 Vb[(r % 2) * k_run + i].buf.copy_(Vh[q % PH], non_blocking=True)
             loaded[r % 2].record(h2d)
 
+        g_start, g_end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        host = {}
+
         def e2e_contraction():
+            c0 = time.perf_counter()
+            g_start.record(stream)
             # the batch first (its set-up copies would queue behind the uploads)
             bt = a4.device.Batch(ptrn, 4, 4, 4, arrs2[0], precision=a4.device.PREC_OZAKI_BF16, slices=S,
                                  variant=args.variant)
+            c1 = time.perf_counter()
             with torch.cuda.stream(h2d):
                 T.buf.copy_(Th, non_blocking=True)
                 t_loaded.record(h2d)
@@ -725,9 +731,21 @@ def run_ladder_full(args, world, rank, local):
                     for q in runs[r]:
                         o0, o1 = slab_rng[q]
                         Rh[o0:o1].copy_(R.buf[o0:o1], non_blocking=True)
+            stream.wait_stream(d2h)
+            g_end.record(stream)
+            c2 = time.perf_counter()
             torch.cuda.synchronize()
+            c3 = time.perf_counter()
             e2e_ph.update(bt.timings())
             bt.close()
+            c4 = time.perf_counter()
+            gaps = [ev_a[r - 1].elapsed_time(ev_b[r]) for r in range(1, len(runs))]
+            host.update(create_ms=(c1 - c0) * 1e3, issue_ms=(c2 - c1) * 1e3, drain_ms=(c3 - c2) * 1e3,
+                        close_ms=(c4 - c3) * 1e3, gpu_span_ms=g_start.elapsed_time(g_end),
+                        gpu_before_first_slab_ms=g_start.elapsed_time(ev_b[0]),
+                        gpu_after_last_slab_ms=ev_a[-1].elapsed_time(g_end),
+                        gpu_slab_runs_ms=sum(ev_b[r].elapsed_time(ev_a[r]) for r in range(len(runs))),
+                        gpu_max_gap_ms=max(gaps) if gaps else 0.0)
 
         e2e_ph = {}
         e2e_contraction()  # warm-up (pinned pages touched, tuning cached)
@@ -748,6 +766,7 @@ def run_ladder_full(args, world, rank, local):
                "h2d_gbs_alone": h2d_gbs,
                "v_source": f"each slab's V copied from a pool of {PH} pinned host slabs (slab q reads pool[q % {PH}])",
                "pipelining": "slab q+1's V upload and slab q's R download overlap slab q's compute",
+               "host_ms_last_step": host,
                "per_slab_ms": {"run": run_ms, "wait_for_upload": wait_ms,
                                **{k: e2e_ph[k] / max(1, e2e_ph["runs"] * k_run) for k in a4.device.Batch.PHASES
                                   if k != "zero_fill"}}}
