@@ -227,9 +227,94 @@ def reference_pairs(n_pairs: int):
     return [(rng.uniform(-1, 1, vblk) / 512.0, rng.normal(0, 0.1, tblk)) for _ in range(n_pairs)], False
 
 
+def run_reference_dropin(args):
+    """--impl reference --workload dropin: the reference's CPU path on the
+    drop-in workloads' pairs (the same blocks as the library's arm), and its
+    legacy GPU path (_gpu_contract: its own reorder kernels from the reference
+    source, 40 MB scratch buffers per call, cuBLAS DGEMM issued twice) on
+    device copies of the same blocks, one synchronous call per pair."""
+    import numpy as np
+
+    from oracle import oracle
+
+    oracle.build()
+    rng = np.random.default_rng(17)
+    gpu_ok, why = False, "no CUDA device"
+    try:
+        import torch
+
+        if torch.cuda.is_available():
+            gpu_ok = oracle.ref_gpu_available()
+            why = "" if gpu_ok else "reference GPU cubin not built (the reference tree was absent at build time)"
+    except Exception as e:  # torch missing
+        why = str(e)
+    res = {}
+    for name in DROPIN_WORKLOADS:
+        ptrn, labels, blocks = dropin_pairs(name, args.dropin_pairs, rng, oracle.get_contraction_ptrn)
+        flop = dropin_flop(blocks)
+        R = {}
+        for _, _, le, re, de, key in blocks:
+            R.setdefault(key, np.zeros(int(np.prod(de))))
+
+        def cpu():
+            for v, t, le, re, de, key in blocks:
+                R[key] += oracle.contract_blas(ptrn, v, le, t, re, de)
+
+        cpu()
+        t0 = time.perf_counter()
+        for _ in range(max(1, args.steps)):
+            cpu()
+        dt = (time.perf_counter() - t0) / max(1, args.steps)
+        out = {"cpu_reference": {"tflops": flop / dt / 1e12, "us_per_call": dt / len(blocks) * 1e6},
+               "pairs": len(blocks), "flop": flop}
+        if gpu_ok:
+            import torch
+
+            dl, ll, rl = labels
+            dv = [(torch.tensor(v, device="cuda"), torch.tensor(t, device="cuda")) for v, t, *_ in blocks]
+            dd = {tuple(b[4]): torch.empty(int(np.prod(b[4])), dtype=torch.float64, device="cuda") for b in blocks}
+
+            def gpu():
+                for (tv, tt), (_, _, le, re, de, _) in zip(dv, blocks):
+                    oracle.ref_gpu_contract(dd[tuple(de)].data_ptr(), de, dl, tv.data_ptr(), le, ll, tt.data_ptr(),
+                                            re, rl)
+
+            gpu()
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            for _ in range(max(1, args.steps)):
+                gpu()
+            torch.cuda.synchronize()
+            dt = (time.perf_counter() - t0) / max(1, args.steps)
+            out["reference_gpu_contract_device_blocks"] = {"tflops": flop / dt / 1e12,
+                                                           "us_per_call": dt / len(blocks) * 1e6}
+        res[name] = out
+    lad = res[DROPIN_WORKLOADS[0]]
+    value = lad["cpu_reference"]["tflops"]
+    cores = os.cpu_count()
+    line = {
+        "impl": "reference", "metric": DROPIN_METRIC, "value": value, "unit": "TFLOP/s", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": 1, "ms_per_step": lad["flop"] / value / 1e9, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": "per-pair calls: ladder o=10/v=48 (1024 pairs), ring o=40/v=300 "
+                               f"({args.dropin_pairs} sampled pairs), the library arm's blocks",
+                   "reference_gpu_path": "the reference's own kernels (gpu_super_instructions.cu compiled for "
+                                         "sm_103a), host steps of __gpu_contract_helper restated" if gpu_ok
+                   else "unavailable: " + why},
+        "cpu_baseline": {"value": value, "unit": "TFLOP/s", "cores": cores, "kind": "port",
+                         "sample": "the 1024 ladder pairs per step, oracle permute + OpenBLAS dgemm, all host threads"},
+        "e2e": {"value": value, "unit": "TFLOP/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "workloads": res,
+    }
+    print(json.dumps(line), flush=True)
+
+
 def run_reference_arm(args, rank: int):
     """--impl reference: CPU arm, rank 0 only."""
     if rank != 0:
+        return
+    if args.workload == "dropin":
+        run_reference_dropin(args)
         return
     from oracle import oracle
 
@@ -828,6 +913,55 @@ def run_ladder_full(args, world, rank, local):
 DROPIN_METRIC = "FP64 TFLOP/s of the interpreter's per-block-pair contract calls (tensor_block_contract__, host blocks)"
 
 
+DROPIN_WORKLOADS = ("ladder o=10 v=48", "ring o=40 v=300 (sampled pairs)")
+
+
+def dropin_pairs(name, n_ring_pairs, rng, get_ptrn):
+    """Host blocks of the drop-in workloads: every (a,b,i,j) x (c,d) pair of
+    the o=10/v=48 ladder, or n_ring_pairs sampled pairs of the o=40/v=300
+    ring; (pattern, labels, [(V, T, lext, rext, dext, R key)])."""
+    import numpy as np
+
+    from aces4_gb300.blocks import LADDER_LABELS, RING_LABELS, segments_uniform
+
+    if name.startswith("ladder"):
+        vs, os_ = [12] * 4, [5, 5]
+        dl, ll, rl = LADDER_LABELS
+        shapes = []
+        for a, b, i, j in np.ndindex(4, 4, 2, 2):
+            for c, d in np.ndindex(4, 4):
+                shapes.append(([vs[a], vs[b], vs[c], vs[d]], [vs[c], vs[d], os_[i], os_[j]],
+                               [vs[a], vs[b], os_[i], os_[j]], (a, b, i, j)))
+        scale = 1.0 / 48
+    else:
+        vs, os_ = segments_uniform(300, 24, 40, seed=2), [20, 20]
+        dl, ll, rl = RING_LABELS
+        shapes = []
+        sub = np.random.default_rng(5)
+        for _ in range(n_ring_pairs):
+            a, b, c = (int(x) for x in sub.integers(0, len(vs), 3))
+            i, j, k = (int(x) for x in sub.integers(0, 2, 3))
+            shapes.append(([vs[a], os_[k], vs[c], os_[i]], [vs[c], vs[b], os_[k], os_[j]],
+                           [vs[a], os_[i], vs[b], os_[j]], (a, i, b, j)))
+        scale = 1.0 / np.sqrt(40 * 300)
+    ierr, ptrn = get_ptrn(len(dl), len(ll), len(rl), dl + ll + rl)
+    assert ierr == 0
+    blocks = [(rng.uniform(-1, 1, int(np.prod(le))) * scale, rng.normal(0, 0.1, int(np.prod(re))), le, re, de,
+               key) for le, re, de, key in shapes]
+    return ptrn, (dl, ll, rl), blocks
+
+
+def dropin_flop(blocks):
+    """2 M N K per pair, with M N = |D| and K^2 = |L| |R| / |D|."""
+    import numpy as np
+
+    flop = 0.0
+    for _, _, le, re, de, _ in blocks:
+        mn = float(np.prod(de))
+        flop += 2.0 * mn * np.sqrt(float(np.prod(le)) * float(np.prod(re)) / mn)
+    return flop
+
+
 def run_dropin(args, world, rank, local):
     """The drop-in path as the interpreter drives it: one synchronous
     tensor_block_contract__ per block pair on HOST blocks (interpreter.cpp:1256),
@@ -842,7 +976,6 @@ def run_dropin(args, world, rank, local):
     import torch
 
     import aces4_gb300 as a4
-    from aces4_gb300.blocks import LADDER_LABELS, RING_LABELS, segments_uniform
     from oracle import oracle
 
     torch.cuda.set_device(local)
@@ -850,40 +983,10 @@ def run_dropin(args, world, rank, local):
     oracle.build()
     rng = np.random.default_rng(17)
 
-    def pairs_for(name):
-        if name.startswith("ladder"):
-            vs, os_ = [12] * 4, [5, 5]
-            dl, ll, rl = LADDER_LABELS
-            shapes = []
-            for a, b, i, j in np.ndindex(4, 4, 2, 2):
-                for c, d in np.ndindex(4, 4):
-                    shapes.append(([vs[a], vs[b], vs[c], vs[d]], [vs[c], vs[d], os_[i], os_[j]],
-                                   [vs[a], vs[b], os_[i], os_[j]], (a, b, i, j)))
-            scale = 1.0 / 48
-        else:
-            vs, os_ = segments_uniform(300, 24, 40, seed=2), [20, 20]
-            dl, ll, rl = RING_LABELS
-            shapes = []
-            sub = np.random.default_rng(5)
-            for _ in range(args.dropin_pairs):
-                a, b, c = (int(x) for x in sub.integers(0, len(vs), 3))
-                i, j, k = (int(x) for x in sub.integers(0, 2, 3))
-                shapes.append(([vs[a], os_[k], vs[c], os_[i]], [vs[c], vs[b], os_[k], os_[j]],
-                               [vs[a], os_[i], vs[b], os_[j]], (a, i, b, j)))
-            scale = 1.0 / np.sqrt(40 * 300)
-        ierr, ptrn = a4.ref.get_contraction_ptrn(len(dl), len(ll), len(rl), dl + ll + rl)
-        assert ierr == 0
-        blocks = [(rng.uniform(-1, 1, int(np.prod(le))) * scale, rng.normal(0, 0.1, int(np.prod(re))), le, re, de,
-                   key) for le, re, de, key in shapes]
-        return ptrn, (dl, ll, rl), blocks
-
     res = {}
-    for name in ("ladder o=10 v=48", "ring o=40 v=300 (sampled pairs)"):
-        ptrn, labels, blocks = pairs_for(name)
-        flop = 0.0
-        for _, _, le, re, de, _ in blocks:  # 2 M N K with M N = |D|, K^2 = |L| |R| / |D|
-            mn = float(np.prod(de))
-            flop += 2.0 * mn * np.sqrt(float(np.prod(le)) * float(np.prod(re)) / mn)
+    for name in DROPIN_WORKLOADS:
+        ptrn, labels, blocks = dropin_pairs(name, args.dropin_pairs, rng, a4.ref.get_contraction_ptrn)
+        flop = dropin_flop(blocks)
         R, tmp = {}, {}
         for _, _, le, re, de, key in blocks:
             R.setdefault(key, np.zeros(int(np.prod(de))))

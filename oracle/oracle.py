@@ -279,3 +279,40 @@ def update_t2(index_values, ext, t2new, t2new_pair, t2old, t2old_pair, ext1, foc
     nrm, ierr = tensor_block_norm2(err, ext)
     assert ierr == 0
     return err, t2, nrm
+
+
+# ------------------------------------------------------------ reference GPU path
+# The reference's legacy GPU contraction (gpu_super_instructions.cu:369-586):
+# its own kernels from oracle/_ref/gpu_super_instructions.cubin (compiled from
+# the reference tree by the Makefile, where that tree is present), driven by
+# the host steps restated in ref_gpu.cpp.  Test and baseline use only.
+_REF_CUBIN = os.path.join(_HERE, "_ref", "gpu_super_instructions.cubin")
+_REF_GPU_SO = os.path.join(_HERE, "_build", "libref_gpu.so")
+_ref_gpu = None
+
+
+def ref_gpu_available() -> bool:
+    return os.path.exists(_REF_CUBIN) and os.path.exists(_REF_GPU_SO)
+
+
+def ref_gpu():
+    """The loaded driver (raises when the cubin or the driver is missing)."""
+    global _ref_gpu
+    if _ref_gpu is None:
+        if not ref_gpu_available():
+            raise RuntimeError("reference GPU path unavailable: " + _REF_CUBIN + " not built")
+        L = ctypes.CDLL(_REF_GPU_SO)
+        L.ref_gpu_error.restype = ctypes.c_char_p
+        if L.ref_gpu_load(_REF_CUBIN.encode()) != 0:
+            raise RuntimeError("ref_gpu_load: " + L.ref_gpu_error().decode())
+        _ref_gpu = L
+    return _ref_gpu
+
+
+def ref_gpu_contract(y: int, ydims, yinds, x1: int, x1dims, x1inds, x2: int, x2dims, x2inds):
+    """_gpu_contract on device addresses: y = x1 * x2 (synchronous, like the reference)."""
+    L = ref_gpu()
+    rc = L.ref_gpu_contract(ctypes.c_void_p(y), len(ydims), _i(ydims), _i(yinds), ctypes.c_void_p(x1), len(x1dims),
+                            _i(x1dims), _i(x1inds), ctypes.c_void_p(x2), len(x2dims), _i(x2dims), _i(x2inds))
+    if rc != 0:
+        raise RuntimeError("ref_gpu_contract: " + L.ref_gpu_error().decode())
