@@ -746,8 +746,15 @@ def run_ladder_full(args, world, rank, local):
     e2e = None
     if args.e2e_steps > 0:
         PH = max(1, min(args.e2e_pool, P))
-        Th = torch.empty_like(T.buf, device="cpu").pin_memory()
-        Th.copy_(T.buf)
+        # T's host copy as pinned pieces of a V slab's size (one 8.6 GB pinned
+        # buffer uploads at a third of the rate of slab-sized ones on this host)
+        t_chunk = max(1, Vb[0].buf.numel())
+        t_pieces = [(o, min(T.buf.numel(), o + t_chunk)) for o in range(0, T.buf.numel(), t_chunk)]
+        Th = []
+        for o0, o1 in t_pieces:
+            h = torch.empty(o1 - o0, dtype=T.buf.dtype).pin_memory()
+            h.copy_(T.buf[o0:o1])
+            Th.append(h)
         Rh = torch.empty_like(R.buf, device="cpu").pin_memory()
         Vh = []
         for q in range(PH):
@@ -765,9 +772,18 @@ def run_ladder_full(args, world, rank, local):
             h1.record(h2d)
         torch.cuda.synchronize()
         h2d_gbs = 4 * Vh[0].numel() * 8 / (h0.elapsed_time(h1) * 1e-3) / 1e9
+        def upload_T():
+            for (o0, o1), h in zip(t_pieces, Th):
+                T.buf[o0:o1].copy_(h, non_blocking=True)
+
+        with torch.cuda.stream(h2d):
+            h0.record(h2d)
+            upload_T()
+            h1.record(h2d)
+        torch.cuda.synchronize()
+        t_gbs = T.buf.numel() * 8 / (h0.elapsed_time(h1) * 1e-3) / 1e9
         loaded = [torch.cuda.Event(), torch.cuda.Event()]
         done = [torch.cuda.Event(), torch.cuda.Event()]
-        t_loaded = torch.cuda.Event()
         slab_rng = []
         for (a, bb) in slabs:
             o0 = R.offsets[(a, bb, 0, 0)]
@@ -783,6 +799,8 @@ def run_ladder_full(args, world, rank, local):
             loaded[r % 2].record(h2d)
 
         g_start, g_end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        t_loaded = torch.cuda.Event(enable_timing=True)
+        g_hold, g_v0 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         host = {}
 
         def e2e_contraction():
@@ -793,11 +811,13 @@ def run_ladder_full(args, world, rank, local):
                                  variant=args.variant)
             c1 = time.perf_counter()
             with torch.cuda.stream(h2d):
-                T.buf.copy_(Th, non_blocking=True)
+                upload_T()
                 t_loaded.record(h2d)
                 load(0)
+                g_v0.record(h2d)
             stream.wait_event(t_loaded)
             bt.hold(1, True, stream=stream)
+            g_hold.record(stream)
             for r in range(len(runs)):
                 if r + 1 < len(runs):  # the next run's V, once run r-1 is done with its buffers
                     with torch.cuda.stream(h2d):
@@ -806,6 +826,8 @@ def run_ladder_full(args, world, rank, local):
                         load(r + 1)
                 stream.wait_event(loaded[r % 2])
                 ev_b[r].record(stream)
+                if r == 0:
+                    c_first = time.perf_counter()
                 if r:
                     bt.rebind(arrs2[r], stream=stream)
                 bt.run_timed(stream)
@@ -825,9 +847,13 @@ def run_ladder_full(args, world, rank, local):
             bt.close()
             c4 = time.perf_counter()
             gaps = [ev_a[r - 1].elapsed_time(ev_b[r]) for r in range(1, len(runs))]
-            host.update(create_ms=(c1 - c0) * 1e3, issue_ms=(c2 - c1) * 1e3, drain_ms=(c3 - c2) * 1e3,
+            host.update(create_ms=(c1 - c0) * 1e3, first_slab_issued_ms=(c_first - c0) * 1e3,
+                        issue_ms=(c2 - c1) * 1e3, drain_ms=(c3 - c2) * 1e3,
                         close_ms=(c4 - c3) * 1e3, gpu_span_ms=g_start.elapsed_time(g_end),
                         gpu_before_first_slab_ms=g_start.elapsed_time(ev_b[0]),
+                        gpu_T_uploaded_at_ms=g_start.elapsed_time(t_loaded),
+                        gpu_T_held_at_ms=g_start.elapsed_time(g_hold),
+                        gpu_V0_uploaded_at_ms=g_start.elapsed_time(g_v0),
                         gpu_after_last_slab_ms=ev_a[-1].elapsed_time(g_end),
                         gpu_slab_runs_ms=sum(ev_b[r].elapsed_time(ev_a[r]) for r in range(len(runs))),
                         gpu_max_gap_ms=max(gaps) if gaps else 0.0)
@@ -848,7 +874,7 @@ def run_ladder_full(args, world, rank, local):
                "h2d_bytes_per_step": T.buf.numel() * 8 + v_bytes * len(slabs),
                "d2h_bytes_per_step": sum(o1 - o0 for o0, o1 in slab_rng) * 8, "ms_per_step": e2e_ms,
                "steps": args.e2e_steps, "timer": "host wall clock around whole contractions (synchronised)",
-               "h2d_gbs_alone": h2d_gbs,
+               "h2d_gbs_alone": h2d_gbs, "T_upload_gbs_alone": t_gbs, "T_pinned": all(h.is_pinned() for h in Th),
                "v_source": f"each slab's V copied from a pool of {PH} pinned host slabs (slab q reads pool[q % {PH}])",
                "pipelining": "slab q+1's V upload and slab q's R download overlap slab q's compute",
                "host_ms_last_step": host,
