@@ -1117,6 +1117,12 @@ __global__ void __launch_bounds__(256) oz_split_kmaj_kernel(const OzSplitJob* __
   }
 }
 
+// Column of k inside a row of the transpose tile: within each 16-column group
+// the low two bits are rotated by the group index, so that the store phase's
+// half-warp (one row, columns 4 kq + u for kq = 0..15) hits 16 distinct bank
+// pairs instead of 4 (k = 16 b + 4 a + u is kept at 16 b + 4 a + (u + b) mod 4).
+__device__ __forceinline__ int rows_tile_col(int k) { return (k & ~3) | (((k & 3) + (k >> 4)) & 3); }
+
 // Slices of a column-major [rows x K] block: 64x64 tiles transposed through
 // shared memory (16-byte loads along rows, 8-byte stores along k).
 template <int S>
@@ -1147,8 +1153,8 @@ __global__ void __launch_bounds__(256) oz_split_rows_kernel(const OzSplitJob* __
         if (r + 1 < jb.rows) x1 = __double_as_longlong(__ldg(src + 1));
       }
     }
-    tile[2 * rp][k] = x0;
-    tile[2 * rp + 1][k] = x1;
+    tile[2 * rp][rows_tile_col(k)] = x0;
+    tile[2 * rp + 1][rows_tile_col(k)] = x1;
   }
   __syncthreads();
   // store: thread -> (row, 4 consecutive k): 16 k-quads x 16 rows per pass, 4 passes
@@ -1162,7 +1168,7 @@ __global__ void __launch_bounds__(256) oz_split_rows_kernel(const OzSplitJob* __
     int d[4][S];
 #pragma unroll
     for (int u = 0; u < 4; ++u) {
-      const unsigned long long b = (k0 + 4 * kq + u < jb.K) ? tile[r][4 * kq + u] : 0ull;
+      const unsigned long long b = (k0 + 4 * kq + u < jb.K) ? tile[r][rows_tile_col(4 * kq + u)] : 0ull;
       balanced_digits<S>(quantize(b, mx, S), d[u]);
     }
     uint2* dst = reinterpret_cast<uint2*>(pn.base + (size_t(r0 + r) * pn.kpad + jb.koff + k0 + 4 * kq));
