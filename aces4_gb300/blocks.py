@@ -130,16 +130,20 @@ TRIPLES_TERM1_LABELS = ([1, 2, 3, 4, 5, 6], [3, 5, 7, 6], [1, 7, 2, 4])
 TRIPLES_TERM2_LABELS = ([1, 2, 3, 4, 5, 6], [8, 5, 4, 6], [1, 3, 2, 8])
 
 
-def triples_step(W: BlockArray, V1: BlockArray, V2: BlockArray, T: BlockArray, a: int, b: int):
+def triples_step(W: BlockArray, V1: BlockArray, V2: BlockArray, T: BlockArray, a: int, b: int, w_key=None):
     """Block triples of one pardo step of the triples energy: the fixed
     virtual segments (a, b), every c and every occupied (i, j, k).  Returns
     (term-1 triples, term-2 triples); the second term is run with negate=1
-    and beta=1 into the same W blocks."""
+    and beta=1 into the same W blocks.  w_key maps a W block key to the key
+    of the W block that stands for it (a step whose W is never stored can
+    name another step's blocks of the same extents)."""
     nv, no = len(T.segs[0]), len(T.segs[2])
     t1, t2 = [], []
     for c in range(nv):
         for i, j, k in itertools.product(range(no), repeat=3):
             wk = (a, i, b, j, c, k)
+            if w_key is not None:
+                wk = w_key(wk)
             wb, we = W.block(wk), W.ext(wk)
             for d in range(nv):
                 lk, rk = (b, c, d, k), (a, d, i, j)

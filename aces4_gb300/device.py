@@ -246,6 +246,26 @@ class Fused:
     """
 
     def __init__(self, drank, lrank, rrank, terms, slices=5, beta=0, energy=None):
+        tarr, en, keep = self._args(terms, energy)
+        opts = _Opts(PREC_OZAKI_BF16, slices, beta, 0, 0, 0)
+        h = ctypes.c_void_p(0)
+        rc = lib().a4g_fused_create(ctypes.byref(h), _i(drank), _i(lrank), _i(rrank), tarr, _i(len(terms)),
+                                    ctypes.byref(en) if en is not None else None, ctypes.byref(opts))
+        _check(rc, "a4g_fused_create")
+        self._h = h
+        self._keep = keep  # the caller's buffers must outlive the step
+        self.energy = energy is not None
+
+    def rebind(self, terms, energy=None, stream=None):
+        """The same structure on other blocks / index values (a4g_fused_rebind)."""
+        tarr, en, keep = self._args(terms, energy)
+        rc = lib().a4g_fused_rebind(self._h, tarr, _i(len(terms)), ctypes.byref(en) if en is not None else None,
+                                    _stream(stream))
+        _check(rc, "a4g_fused_rebind")
+        self._keep = keep
+
+    @staticmethod
+    def _args(terms, energy):
         keep, tarr = [], (_Term * max(1, len(terms)))()
         for i, (ptrn, triples, sign) in enumerate(terms):
             arr, n, k = _triples_arg(triples)
@@ -268,14 +288,7 @@ class Fused:
                               ctypes.cast(e1, ctypes.c_void_p), _ptr(energy["e_or_fock"]),
                               len(energy["seg_sizes"]), ctypes.cast(sg, ctypes.c_void_p),
                               float(energy.get("efact", 1.0)))
-        opts = _Opts(PREC_OZAKI_BF16, slices, beta, 0, 0, 0)
-        h = ctypes.c_void_p(0)
-        rc = lib().a4g_fused_create(ctypes.byref(h), _i(drank), _i(lrank), _i(rrank), tarr, _i(len(terms)),
-                                    ctypes.byref(en) if en is not None else None, ctypes.byref(opts))
-        _check(rc, "a4g_fused_create")
-        self._h = h
-        self._keep = keep  # the caller's buffers must outlive the step
-        self.energy = energy is not None
+        return tarr, en, keep + [tarr, en]
 
     def run(self, esum=None, stream=None):
         _check(lib().a4g_fused_run(self._h, ctypes.c_void_p(_ptr(esum)), _stream(stream)), "a4g_fused_run")

@@ -351,16 +351,22 @@ def run_reference_arm(args, rank: int):
     print(json.dumps(line), flush=True)
 
 
-TRIPLES_METRIC = "FP64-equiv TFLOP/s per triples step (W = V1*T - V2*T, E = sum W^2/D; split vs plain FP64)"
+TRIPLES_METRIC = "FP64-equiv TFLOP/s of the whole triples energy (W = V1*T - V2*T, E = sum W^2/D; split vs plain FP64)"
 
 
 def run_triples(args, world, rank, local):
-    """Triples energy step, by default at o=24 (1 x 24), v=240 (10 x 24):
-    fixed virtual segments (a, b), every c: 10 W blocks of 24^6 (1.53 GB
-    each), 100 + 10 block pairs, 1.01e12 flop, then the fused denominator +
-    contraction pass over the 1.9e9 W elements.  V1, V2 ~ U[-1,1]/v,
-    T ~ N(0, 1e-2), e_occ ~ U[-2,-0.5], e_virt ~ U[0.2,5] (seeded,
-    synthetic)."""
+    """The whole (T) energy, by default at o=24 (1 x 24), v=240 (10 x 24):
+    every (a, b) pair of virtual segments is one pardo step (every c and
+    every occupied i, j, k: 10 W blocks of 24^6, 100 + 10 block pairs,
+    1.01e12 flop), 100 steps and 1.01e14 flop in all, E = sum W fl(W / D).
+    Each step is one fused pass (both terms and the energy; W is never
+    stored): the fused step is created on the first (a, b) inside the timed
+    region and rebound to each next one.  The (a, b) steps are split over the
+    ranks (no collective; the per-rank sums would be added on the host).
+    V1, V2 ~ U[-1,1]/v, T ~ N(0, 1e-2), e_occ ~ U[-2,-0.5], e_virt ~
+    U[0.2,5] (seeded, synthetic).  Checks: per-step E of two steps against
+    plain FP64 (two batches, a stored W, the energy pass), W of one step (the
+    fused pass's store form) against FP64."""
     import numpy as np
     import torch
     import torch.distributed as dist
@@ -373,140 +379,165 @@ def run_triples(args, world, rank, local):
     if world > 1:
         dist.init_process_group("nccl", device_id=torch.device("cuda", local))
     a4.device.init(local)
-    stream = torch.cuda.current_stream()
+    stream = torch.cuda.Stream()
     seg, nv = args.tseg, args.tnv
     o_segs, v_segs = [seg], [seg] * nv
     o, v = seg, seg * nv
-    a, b = rank % nv, (rank + 1) % nv
     V1 = BlockArray([v_segs, v_segs, v_segs, o_segs])
     V2 = BlockArray([o_segs, v_segs, o_segs, o_segs])
     T = BlockArray([v_segs, v_segs, o_segs, o_segs])
     g = torch.Generator(device="cuda")
-    g.manual_seed(77 + rank)
+    g.manual_seed(77)
     V1.buf.uniform_(-1.0, 1.0, generator=g).div_(v)
     V2.buf.uniform_(-1.0, 1.0, generator=g).div_(v)
     T.buf.normal_(0.0, 0.1, generator=g)
-    rng = np.random.default_rng(77 + rank)  # orbital energies
+    rng = np.random.default_rng(77)  # orbital energies
     e = np.concatenate([rng.uniform(-2.0, -0.5, o), rng.uniform(0.2, 5.0, v)])
     fock = torch.tensor(np.diag(e).ravel(order="F"), device="cuda")
-    W = BlockArray([v_segs, o_segs, v_segs, o_segs, v_segs, o_segs], present=lambda k: k[0] == a and k[2] == b)
-    t1, t2 = triples_step(W, V1, V2, T, a, b)
-    p1 = a4.ref.get_contraction_ptrn(6, 4, 4, sum(TRIPLES_TERM1_LABELS, []))[1]
-    p2 = a4.ref.get_contraction_ptrn(6, 4, 4, sum(TRIPLES_TERM2_LABELS, []))[1]
     segs = o_segs + v_segs
     norb = sum(segs)
+    # the W blocks of step (0, 1); every step's fused pass names them (its W is never stored)
+    a0, b0 = 0, 1
+    W = BlockArray([v_segs, o_segs, v_segs, o_segs, v_segs, o_segs], present=lambda k: k[0] == a0 and k[2] == b0)
+    p1 = a4.ref.get_contraction_ptrn(6, 4, 4, sum(TRIPLES_TERM1_LABELS, []))[1]
+    p2 = a4.ref.get_contraction_ptrn(6, 4, 4, sum(TRIPLES_TERM2_LABELS, []))[1]
+    steps_all = [(a, b) for a in range(nv) for b in range(nv)]
+    mine = steps_all[rank::world]
+
+    def step_args(a, b):
+        stand_in = lambda k: (a0, k[1], b0, k[3], k[4], k[5])
+        t1, t2 = triples_step(W, V1, V2, T, a, b, w_key=stand_in)
+        keys = [(a, i, b, j, c, k) for c in range(nv) for i in range(1) for j in range(1) for k in range(1)]
+        en = dict(blocks=[W.block(stand_in(k)) for k in keys], index_values=[triples_index_values(k, 1) for k in keys],
+                  ext1=[norb, norb], e_or_fock=fock, seg_sizes=segs, efact=1.0)
+        return [(p1, t1, 1), (p2, t2, -1)], en
+
+    args_of = {ab: step_args(*ab) for ab in mine}
     esum = torch.zeros(1, dtype=torch.float64, device="cuda")
-    ivs = [(triples_index_values(k, 1), W.ext(k), W.block(k)) for k in W.keys()]
 
-    def energy():
-        for iv, ext, blk in ivs:
-            a4.device.energy_contract(iv, ext, blk, [norb, norb], fock, segs, 1.0, esum, stream=stream)
+    def whole(timing=None):
+        """One pass over this rank's (a, b) steps; creation included."""
+        t0 = time.perf_counter()
+        fe = a4.device.Fused(6, 4, 4, args_of[mine[0]][0], slices=args.slices, energy=args_of[mine[0]][1])
+        create_ms = (time.perf_counter() - t0) * 1e3
+        for q, ab in enumerate(mine):
+            if q:
+                fe.rebind(args_of[ab][0], energy=args_of[ab][1], stream=stream)
+            fe.run(esum, stream)
+        info = fe.info()
+        stream.synchronize()
+        fe.close()
+        if timing is not None:
+            timing.update(create_ms=create_ms, info=info)
+        return info
 
-    def batches(prec):
-        kw = dict(precision=prec, slices=args.slices)
-        return (a4.device.Batch(p1, 6, 4, 4, t1, variant=args.variant if prec else 0, **kw),
-                a4.device.Batch(p2, 6, 4, 4, t2, beta=1, negate=True, variant=args.variant if prec else 0, **kw))
-
-    # the fused step (both terms and the energy in one pass, W never stored)
-    terms = [(p1, t1, 1), (p2, t2, -1)]
-    energy_args = dict(blocks=[blk for _, _, blk in ivs], index_values=[iv for iv, _, _ in ivs],
-                       ext1=[norb, norb], e_or_fock=fock, seg_sizes=segs, efact=1.0)
-    t0 = time.perf_counter()
-    fe = a4.device.Fused(6, 4, 4, terms, slices=args.slices, energy=energy_args)
-    create_s = time.perf_counter() - t0
-    finfo = fe.info()
-    flops = finfo["flops"]
+    first = {}
     for _ in range(args.warmup):
-        fe.run(esum, stream)
+        esum.zero_()
+        whole(first)
     torch.cuda.synchronize()
-    ev = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
+    flops_rank = first["info"]["flops"] * len(mine)
+    flops_total = first["info"]["flops"] * len(steps_all)
     if world > 1:
         dist.barrier()
     torch.cuda.synchronize()
     props = torch.cuda.get_device_properties(local)
     gpu_id = f"GPU-{props.uuid}" if getattr(props, "uuid", None) else str(local)
+    tim = {}
     with ClockSampler(gpu_id) as clk:
-        ev[0].record(stream)
+        w0 = time.perf_counter()
         for _ in range(args.steps):
-            fe.run(esum, stream)
-        ev[1].record(stream)
+            esum.zero_()
+            whole(tim)
         torch.cuda.synchronize()
-    ms = max_over_ranks(ev[0].elapsed_time(ev[1]) / args.steps)
-    esum.zero_()
+        wall_ms = (time.perf_counter() - w0) * 1e3 / args.steps
+    ms = max_over_ranks(wall_ms, device="cuda")
+    E_rank = float(esum.item())
+    # per-step device time of one fused pass (CUDA events; rebound, so no creation)
+    fe = a4.device.Fused(6, 4, 4, args_of[mine[0]][0], slices=args.slices, energy=args_of[mine[0]][1])
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
     fe.run(esum, stream)
-    E_split = float(esum.item())
+    ev[0].record(stream)
+    fe.run(esum, stream)
+    ev[1].record(stream)
+    stream.synchronize()
+    step_ms = ev[0].elapsed_time(ev[1])
+    t0 = time.perf_counter()
+    fe.rebind(args_of[mine[-1]][0], energy=args_of[mine[-1]][1], stream=stream)
+    stream.synchronize()
+    rebind_ms = (time.perf_counter() - t0) * 1e3
     fe.close()
-    # the same step through two batches and a separate energy pass (W stored, then read)
-    b1, b2 = batches(a4.device.PREC_OZAKI_BF16)
-    for _ in range(max(1, min(args.warmup, 2))):
+    # checks on two steps: split E per step against plain FP64 (two batches, W stored, the energy pass)
+    checks = []
+    for ab in (mine[0], mine[-1]):
+        terms, en = args_of[ab]
+        e1 = torch.zeros(1, dtype=torch.float64, device="cuda")
+        f1 = a4.device.Fused(6, 4, 4, terms, slices=args.slices, energy=en)
+        f1.run(e1, stream)
+        stream.synchronize()
+        f1.close()
+        b1 = a4.device.Batch(p1, 6, 4, 4, terms[0][1], precision=a4.device.PREC_FP64)
+        b2 = a4.device.Batch(p2, 6, 4, 4, terms[1][1], beta=1, negate=True, precision=a4.device.PREC_FP64)
+        ev[0].record(stream)
         b1.run(stream)
         b2.run(stream)
-        energy()
-    torch.cuda.synchronize()
-    b1.timings(), b2.timings()
-    t_terms = t_energy = 0.0
-    n_unfused = max(1, min(args.steps, 3))
-    for _ in range(n_unfused):
         ev[1].record(stream)
-        b1.run_timed(stream)
-        b2.run_timed(stream)
-        ev[2].record(stream)
-        energy()
-        ev[3].record(stream)
-        torch.cuda.synchronize()
-        t_terms += ev[1].elapsed_time(ev[2])
-        t_energy += ev[2].elapsed_time(ev[3])
-    ph1, ph2 = b1.timings(), b2.timings()
-    form = b1.form()
-    b1.close()
-    b2.close()
-    # W of the fused pass (store form) against plain FP64
-    fs = a4.device.Fused(6, 4, 4, terms, slices=args.slices)
+        e64 = torch.zeros(1, dtype=torch.float64, device="cuda")
+        for blk, iv in zip(en["blocks"], en["index_values"]):
+            a4.device.energy_contract(iv, W.ext(W.keys()[0]), blk, [norb, norb], fock, segs, 1.0, e64, stream=stream)
+        stream.synchronize()
+        fp64_ms = ev[0].elapsed_time(ev[1])
+        checks.append({"step": list(ab), "E_split": float(e1.item()), "E_fp64": float(e64.item()),
+                       "rel_diff": abs(float(e1.item()) - float(e64.item())) / abs(float(e64.item())),
+                       "fp64_terms_ms": fp64_ms})
+        b1.close(), b2.close()
+    # W of the last checked step: the fused pass's store form against the FP64 W just computed
+    W64 = W.buf.clone()
+    fs = a4.device.Fused(6, 4, 4, args_of[mine[-1]][0], slices=args.slices)
     fs.run(stream=stream)
-    torch.cuda.synchronize()
+    stream.synchronize()
     fs.close()
-    W_split = W.buf.clone()
-    f1, f2 = batches(a4.device.PREC_FP64)
-    torch.cuda.synchronize()
-    ev[0].record(stream)
-    f1.run(stream)
-    f2.run(stream)
-    ev[1].record(stream)
-    esum.zero_()
-    energy()
-    torch.cuda.synchronize()
-    fp64_ms = ev[0].elapsed_time(ev[1])
-    E64 = float(esum.item())
-    werr = max(float(torch.linalg.norm(W_split[W.offsets[k]:W.offsets[k] + W.size(k)] -
-                                       W.buf[W.offsets[k]:W.offsets[k] + W.size(k)]) /
-                     torch.linalg.norm(W.buf[W.offsets[k]:W.offsets[k] + W.size(k)])) for k in W.keys())
-    f1.close()
-    f2.close()
+    werr = max(float(torch.linalg.norm(W.buf[W.offsets[k]:W.offsets[k] + W.size(k)] -
+                                       W64[W.offsets[k]:W.offsets[k] + W.size(k)]) /
+                     torch.linalg.norm(W64[W.offsets[k]:W.offsets[k] + W.size(k)])) for k in W.keys())
+    del W64
+    # the same step through two split batches and a separate energy pass (W written, read, rewritten)
+    terms, en = args_of[mine[0]]
+    bs1 = a4.device.Batch(p1, 6, 4, 4, terms[0][1], precision=a4.device.PREC_OZAKI_BF16, slices=args.slices)
+    bs2 = a4.device.Batch(p2, 6, 4, 4, terms[1][1], beta=1, negate=True, precision=a4.device.PREC_OZAKI_BF16,
+                          slices=args.slices)
+    for rep in range(2):
+        ev[0].record(stream)
+        bs1.run(stream)
+        bs2.run(stream)
+        ev[1].record(stream)
+        for blk, iv in zip(en["blocks"], en["index_values"]):
+            a4.device.energy_contract(iv, W.ext(W.keys()[0]), blk, [norb, norb], fock, segs, 1.0, esum, stream=stream)
+        ev[2].record(stream)
+        stream.synchronize()
+    unfused = {"terms_ms": ev[0].elapsed_time(ev[1]), "energy_ms": ev[1].elapsed_time(ev[2]),
+               "ms": ev[0].elapsed_time(ev[2])}
+    bs1.close(), bs2.close()
     if rank == 0:
-        runs = max(1, ph1["runs"])
-        n_w = sum(W.size(k) for k in W.keys())
-        e_ms = t_energy / n_unfused
+        fp64_rate = first["info"]["flops"] / (checks[0]["fp64_terms_ms"] * 1e-3) / 1e12
+        value = flops_total / (ms * 1e-3) / 1e12
         line = {
-            "metric": TRIPLES_METRIC, "value": world * flops / (ms * 1e-3) / 1e12, "unit": "TFLOP/s",
-            "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
-            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-            "dtype": f"f64 (Ozaki, {args.slices} BF16 slices)", "data": "synthetic",
-            "config": {"workload": f"triples o={o} (1x{seg}), v={v} ({nv}x{seg}), one (a,b) step: "
-                                   f"{len(W.keys())} W blocks of {seg}^6, {len(t1)}+{len(t2)} block pairs "
-                                   f"({flops:.3g} flop), W and E = sum W fl(W/D) in one fused pass "
-                                   f"(W never stored)", "slices": args.slices},
-            "fused": {"elements": finfo["elements"], "device_bytes": finfo["device_bytes"],
-                      "create_s": create_s, "gelem_per_s": finfo["elements"] / (ms * 1e-3) / 1e9},
-            "unfused_two_batches": {
-                "ms_per_step": (t_terms + t_energy) / n_unfused,
-                "term1": {k: ph1[k] / runs for k in ("zero_fill", "exponents", "split", "gemm", "recombine")},
-                "term2": {k: ph2[k] / runs for k in ("zero_fill", "exponents", "split", "gemm", "recombine")},
-                "terms_total": t_terms / n_unfused, "energy": e_ms,
-                "energy_gelem_per_s": n_w / (e_ms * 1e-3) / 1e9,
-                "gemm_form": {"chosen": form["name"], "autotune_ms": form["tuned_ms"]}},
-            "fp64_plain": {"value": flops / (fp64_ms * 1e-3) / 1e12, "unit": "TFLOP/s",
-                           "ms_per_step_terms": fp64_ms},
-            "energy": {"split": E_split, "fp64": E64, "rel_diff": abs(E_split - E64) / abs(E64)},
+            "metric": TRIPLES_METRIC, "value": value, "unit": "TFLOP/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "strong",
+            "vs_baseline": None, "dtype": f"f64 (Ozaki, {args.slices} BF16 slices)", "data": "synthetic",
+            "config": {"workload": f"the whole (T) energy at o={o} (1x{seg}), v={v} ({nv}x{seg}): {len(steps_all)} "
+                                   f"(a,b) steps of {nv} W blocks of {seg}^6 and "
+                                   f"{len(args_of[mine[0]][0][0][1])}+{len(args_of[mine[0]][0][1][1])} block pairs, "
+                                   f"{flops_total:.3g} flop, E = sum W fl(W/D); each step one fused pass (W never "
+                                   f"stored), the step rebound from one (a,b) to the next", "slices": args.slices,
+                       "steps_this_rank": len(mine), "timer": "host wall clock around whole computations"},
+            "E_total_this_rank": E_rank,
+            "per_step": {"device_ms": step_ms, "rebind_host_ms": rebind_ms, "create_ms": tim.get("create_ms"),
+                         "elements": first["info"]["elements"], "device_bytes": first["info"]["device_bytes"]},
+            "unfused_two_batches_one_step": unfused,
+            "fp64_plain": {"value": fp64_rate, "unit": "TFLOP/s", "ms_per_step_terms": checks[0]["fp64_terms_ms"]},
+            "split_over_fp64": value / world / fp64_rate,
+            "energy_checks": checks,
             "rel_err_max_w_block_vs_fp64_gpu": werr,
             "clocks": clk.summary(),
         }

@@ -497,6 +497,15 @@ int a4g_fused_create(a4g_fused** out, int drank, int lrank, int rrank, const a4g
 /* esum: a device double (energy form), else NULL.  Operands are read at run
  * time (their values may change between runs; their addresses may not). */
 int a4g_fused_run(a4g_fused* f, double* esum, void* stream);
+/* The next iteration of the same loop (the triples' next (a, b) step): the
+ * same terms with other blocks and, in the energy form, other index values,
+ * in the same structure (triple counts, extents, zero blocks, which blocks
+ * share a destination or a right operand, which destination blocks share a
+ * denominator table).  Re-plans on the host, then updates on `stream` only the
+ * split jobs' sources, the destination column bases and the denominator
+ * tables; the tiles, panels and kernel arguments stay.  A4G_ERR_ARG when the
+ * structure differs (create a new step then). */
+int a4g_fused_rebind(a4g_fused* f, const a4g_term* terms, int nterms, const a4g_fused_energy* energy, void* stream);
 int a4g_fused_info(const a4g_fused* f, int64_t* pairs, double* flops, int64_t* elements, int64_t* device_bytes);
 void a4g_fused_destroy(a4g_fused* f);
 

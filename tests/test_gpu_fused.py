@@ -191,3 +191,46 @@ def test_fused_rejects_what_it_does_not_cover(a4):
     with pytest.raises(a4.device.A4GError) as ei:
         a4.device.Fused(6, 4, 4, terms, energy=ea)
     assert ei.value.rc == 6
+
+
+def test_fused_rebind_equals_fresh_creation(a4):
+    """The (T) loop's next (a, b) step through a4g_fused_rebind: the same bits
+    as a step created on those blocks, in the energy and the store form; a
+    structure that differs is rejected."""
+    import torch
+
+    o_segs, v_segs = [6], [12, 12, 12]
+    V1, V2, T, fock = _problem(o_segs, v_segs, 31)
+    ft = torch.tensor(fock, device="cuda")
+    W01, terms01 = _step(V1, V2, T, o_segs, v_segs, 0, 1)
+    W20, terms20 = _step(V1, V2, T, o_segs, v_segs, 2, 0)
+    fe = a4.device.Fused(6, 4, 4, terms01, energy=_energy_args(W01, o_segs, v_segs, ft))
+    e = torch.zeros(2, dtype=torch.float64, device="cuda")
+    fe.run(e[0:1])
+    fe.rebind(terms20, energy=_energy_args(W20, o_segs, v_segs, ft))
+    fe.run(e[1:2])
+    fresh = a4.device.Fused(6, 4, 4, terms20, energy=_energy_args(W20, o_segs, v_segs, ft))
+    e2 = torch.zeros(1, dtype=torch.float64, device="cuda")
+    fresh.run(e2)
+    a4.device.sync()
+    assert float(e[1].item()) == float(e2.item())
+    _, Eref = _oracle_W_E(W20, terms20, o_segs, v_segs, fock)
+    assert abs(float(e[1].item()) - Eref) <= 1e-10 * abs(Eref)
+    _, Eref01 = _oracle_W_E(W01, terms01, o_segs, v_segs, fock)
+    assert abs(float(e[0].item()) - Eref01) <= 1e-10 * abs(Eref01)
+    fresh.close()
+    # store form: rebound W20 equals a fresh creation's W20, bit for bit
+    fs = a4.device.Fused(6, 4, 4, terms01)
+    fs.rebind(terms20)
+    fs.run()
+    a4.device.sync()
+    got = W20.buf.clone()
+    W20.buf.fill_(float("nan"))
+    f2 = a4.device.Fused(6, 4, 4, terms20)
+    f2.run()
+    a4.device.sync()
+    assert torch.equal(got.view(torch.int64), W20.buf.view(torch.int64))
+    # another structure: one term only
+    with pytest.raises(a4.device.A4GError):
+        fs.rebind(terms20[:1])
+    fe.close(), fs.close(), f2.close()
