@@ -42,6 +42,11 @@ struct Context {
   // every synchronisation, so a synchronous call would allocate from scratch
   // each time.
   cudaMemPool_t pool = nullptr;
+  // Kernels can read and write pageable host memory through the host's page
+  // tables (address translation services over the CPU-GPU link): the
+  // drop-ins then run on the caller's host blocks in place.
+  bool host_access = false;
+  int host_direct = 1;  // a4g_host_direct: 1 in place when host_access, 0 always staged
 };
 Context* ctx();             // initialises on first use (device = current)
 int ensure_init();          // returns A4G_OK or an error code

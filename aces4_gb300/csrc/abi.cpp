@@ -68,8 +68,12 @@ int d2h(double* h, const double* d, int64_t n, cudaStream_t s) {
 std::mutex g_host_mu;  // host-buffer entries share one arena
 
 // Device views of one drop-in call's host blocks.  Detached (the default):
-// operands staged through the arena, results copied back before the call
-// returns, like the Fortran kernels.  With a block cache attached: the
+// where the GPU reads and writes pageable host memory through the host's page
+// tables (Grace-Blackwell), the kernels run on the host blocks in place (no
+// copies; a result that aliases an operand of a non-element-wise operation
+// goes through a device temporary); elsewhere operands are staged through the
+// arena and results copied back; either way the call returns when the results
+// are in the host blocks, like the Fortran kernels.  With a block cache attached: the
 // cache's device copies (copied in only when missing or stale); results stay
 // there, newer than the host copy, until the host asks for them.  Operands
 // are declared before results, so a result that is also an operand (the same
@@ -78,6 +82,7 @@ std::mutex g_host_mu;  // host-buffer entries share one arena
 struct HostIO {
   cudaStream_t s = nullptr;
   a4g_blocks* cache = nullptr;
+  bool direct = false;
   Staged st;
   struct Copy {
     double* dst;
@@ -91,11 +96,16 @@ struct HostIO {
   int begin(size_t arena_bytes) {
     s = ctx()->stream;
     cache = attached_blocks();
+    direct = !cache && ctx()->host_access && ctx()->host_direct;
     return stage(arena_bytes, &st);
   }
   int in(const double* h, int64_t n, double** d) {
     operands.push_back(h);
     if (cache) return blocks_on_device(cache, const_cast<double*>(h), n, A4G_BLOCK_READ, d, s);
+    if (direct) {
+      *d = const_cast<double*>(h);
+      return A4G_OK;
+    }
     *d = st.take(n);
     return h2d(*d, h, n, s);
   }
@@ -114,6 +124,17 @@ struct HostIO {
       } else {
         *d = dc;
       }
+      return A4G_OK;
+    }
+    if (direct) {
+      const bool aliased = std::find(operands.begin(), operands.end(), h) != operands.end();
+      if (!aliased || elementwise) {
+        *d = h;
+        return A4G_OK;
+      }
+      *d = st.take(n);
+      if (reads) A4G_CUDA(cudaMemcpyAsync(*d, h, size_t(n) * sizeof(double), cudaMemcpyDefault, s));
+      after.push_back({h, *d, n, cudaMemcpyDefault});
       return A4G_OK;
     }
     *d = st.take(n);
@@ -423,6 +444,13 @@ void _gpu_free(double* g_addr) {
 }
 
 // ============================================================ super instruction
+int a4g_host_direct(int enable) {
+  const int rc = ensure_init();
+  if (rc) return rc;
+  ctx()->host_direct = enable ? 1 : 0;
+  return ctx()->host_access ? A4G_OK : A4G_ERR_UNSUPPORTED;
+}
+
 int a4g_set_predefined_int_array(const char* name, int n, const int* values) {
   if (!name || n < 0 || (n > 0 && !values)) return fail(A4G_ERR_ARG, "bad predefined array");
   std::lock_guard<std::mutex> lock(g_predef_mu);

@@ -52,6 +52,10 @@ int ensure_init() {
   uint64_t keep = ~0ull;  // never hand freed memory back on synchronisation
   A4G_CUDA(cudaMemPoolSetAttribute(g_ctx.pool, cudaMemPoolAttrReleaseThreshold, &keep));
   g_ctx.num_sms = prop.multiProcessorCount;
+  int pageable = 0, host_tables = 0;
+  A4G_CUDA(cudaDeviceGetAttribute(&pageable, cudaDevAttrPageableMemoryAccess, dev));
+  A4G_CUDA(cudaDeviceGetAttribute(&host_tables, cudaDevAttrPageableMemoryAccessUsesHostPageTables, dev));
+  g_ctx.host_access = pageable == 1 && host_tables == 1;
   g_ctx.device = dev;
   return A4G_OK;
 }

@@ -111,6 +111,13 @@ def tensor_block_insert(t, text, s, sext, beg) -> int:
     return ierr.value
 
 
+def host_direct(enable: bool) -> int:
+    """Drop-ins run on the host blocks in place where the GPU reads host
+    memory through the host's page tables (default), or stage them through
+    device memory (False).  Returns the a4g status (6: no host access)."""
+    return lib().a4g_host_direct(int(bool(enable)))
+
+
 def set_predefined_int_array(name: str, values) -> int:
     arr = _iarr(values)
     return lib().a4g_set_predefined_int_array(name.encode(), len(values), ctypes.cast(arr, ctypes.c_void_p))

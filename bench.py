@@ -1062,12 +1062,23 @@ def run_dropin(args, world, rank, local):
         for fn in (ours, cpu):  # warm-up
             fn()
         out = {}
+        in_place = a4.ref.host_direct(True) == 0
         for tag, fn, reps in (("dropin_host_blocks", ours, args.steps), ("cpu_reference", cpu, 1)):
             t0 = time.perf_counter()
             for _ in range(reps):
                 fn()
             dt = (time.perf_counter() - t0) / reps
             out[tag] = {"tflops": flop / dt / 1e12, "us_per_call": dt / len(blocks) * 1e6}
+        out["dropin_host_blocks"]["in_place"] = in_place
+        if in_place:  # the same calls with the blocks staged through device memory
+            a4.ref.host_direct(False)
+            ours()
+            t0 = time.perf_counter()
+            for _ in range(args.steps):
+                ours()
+            dt = (time.perf_counter() - t0) / args.steps
+            out["dropin_host_blocks_staged"] = {"tflops": flop / dt / 1e12, "us_per_call": dt / len(blocks) * 1e6}
+            a4.ref.host_direct(True)
         dv = [(torch.tensor(v, device="cuda"), torch.tensor(t, device="cuda")) for v, t, *_ in blocks]
         dd = {tuple(b[4]): torch.empty(int(np.prod(b[4])), dtype=torch.float64, device="cuda") for b in blocks}
         dl_, ll_, rl_ = labels

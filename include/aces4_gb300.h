@@ -46,6 +46,15 @@ extern "C" {
 #define A4G_ERR_RANGE 7      /* size beyond a documented maximum                              */
 #define A4G_ERR_PRECISION 8  /* a certified error bound exceeds the requested target           */
 
+/* Drop-ins on host blocks (group 1 and energy_denominator_rhf): where the GPU
+ * reads and writes pageable host memory through the host's page tables
+ * (Grace-Blackwell; cudaDevAttrPageableMemoryAccessUsesHostPageTables), the
+ * kernels run on the caller's host blocks in place, with no copies; elsewhere
+ * (or after a4g_host_direct(0)) the blocks are staged through device memory.
+ * The results and the synchronous return are the same either way.  Returns
+ * A4G_ERR_UNSUPPORTED when the GPU cannot access host memory (staging then). */
+int a4g_host_direct(int enable);
+
 /* Text of the last error on the calling thread ("" when none). */
 const char* a4g_last_error(void);
 /* Forget the recorded error (the legacy _gpu_* calls record failures and
