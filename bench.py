@@ -837,13 +837,14 @@ def run_ladder_full(args, world, rank, local):
         def e2e_contraction():
             c0 = time.perf_counter()
             g_start.record(stream)
-            # the batch first (its set-up copies would queue behind the uploads)
+            # T's upload first: the batch's creation (host planning) runs meanwhile
+            with torch.cuda.stream(h2d):
+                upload_T()
+                t_loaded.record(h2d)
             bt = a4.device.Batch(ptrn, 4, 4, 4, arrs2[0], precision=a4.device.PREC_OZAKI_BF16, slices=S,
                                  variant=args.variant)
             c1 = time.perf_counter()
             with torch.cuda.stream(h2d):
-                upload_T()
-                t_loaded.record(h2d)
                 load(0)
                 g_v0.record(h2d)
             stream.wait_event(t_loaded)
