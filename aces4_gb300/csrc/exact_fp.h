@@ -122,46 +122,64 @@ A4G_HD double i128_scaled_to_double(__int128 N, int e2) {
 
 // a / b rounded to the nearest double (ties to even; a quotient of two
 // doubles is never exactly halfway) for normal a, b and a normal result;
-// false otherwise (the caller divides in FP64).  Method: a reciprocal
-// R ~ 2^116/mb of the divisor's 53-bit significand by Newton-Raphson (seed:
-// the FP32 reciprocal of its top 24 bits; two steps R += R(2^116 - mb R)/2^116
-// in 64-bit fixed point), the 55-bit quotient estimate Q = ma 2^s R / 2^116,
-// and the exact remainder ma 2^s - Q mb, which corrects Q to
-// floor(ma 2^s / mb) (Knuth, TAOCP vol. 2, 4.3.1: estimate a quotient digit,
-// then fix it from the remainder) and gives the sticky bit for the rounding.
+// false otherwise (the caller divides in FP64).  With A = ma or 2 ma (the
+// dividend's significand doubled when it is below the divisor's, so that
+// A / mb lies in [1, 2)), the 55-bit quotient Q = floor(A 2^54 / mb) is
+// estimated through a reciprocal R ~ 2^116 / mb of the divisor's 53-bit
+// significand and corrected from the exact remainder A 2^54 - Q mb (Knuth,
+// TAOCP vol. 2, 4.3.1: estimate a quotient digit, then fix it from the
+// remainder), which also gives the sticky bit for the rounding.  R comes from
+// Newton-Raphson, x' = x + x (1 - d x), in fixed point: the FP32 reciprocal
+// of mb's top 24 bits (relative error below 2^-22), one step in 32-bit
+// arithmetic on mb's top 32 bits (below 2^-30), one step in 64-bit arithmetic
+// on all of mb (below 2^-59).  Q is then off by at most one unit, so one
+// correction each way suffices, and the remainder, below 2 mb < 2^54 in
+// magnitude, is exact in wrapping 64-bit arithmetic.
 A4G_HD bool div_rn_int(double a, double b, double* q) {
   const unsigned long long ua = bits_of(a), ub = bits_of(b);
   const int ea = int((ua >> 52) & 0x7FF), eb = int((ub >> 52) & 0x7FF);
   if (ea == 0 || ea == 2047 || eb == 0 || eb == 2047) return false;
   const unsigned long long ma = (ua & ((1ull << 52) - 1)) | (1ull << 52);
   const unsigned long long mb = (ub & ((1ull << 52) - 1)) | (1ull << 52);
-  const float rf = frcp_rn(float(uint32_t(mb >> 29)));  // mb's top 24 bits: exact in FP32
+  const int adj = ma < mb ? 1 : 0;
+  const unsigned long long A = ma << adj;  // [mb, 2 mb)
+  const int field = ea - eb + 1023 - adj;  // biased exponent of the quotient's leading bit
+  if (field < 1 || field > 2045) return false;
+  // seed R32 ~ 2^84 / mb: the FP32 reciprocal of mb's top 24 bits (exact in
+  // FP32) lies in (2^-24, 2^-23]; its significand shifted into place, 2^-23
+  // itself (2^32) clamped to 2^32 - 1
+  const float rf = frcp_rn(float(uint32_t(mb >> 29)));
   uint32_t rb;
   memcpy(&rb, &rf, 4);
-  const int er = int((rb >> 23) & 0xFF) - 127;  // the reciprocal lies in (2^-24, 2^-23]
-  const unsigned long long rm = (rb & 0x7FFFFFu) | 0x800000u;
-  unsigned long long R = er == -23 ? ~0ull : rm << (er + 64);  // 2^-23 exactly would be 2^64
-  for (int it = 0; it < 2; ++it) {
+  unsigned long long R32 = ((rb >> 23) & 0xFFu) == 103u ? ((unsigned long long)((rb & 0x7FFFFFu) | 0x800000u) << 8)
+                                                         : 0xFFFFFFFFull;
+  // 32-bit step on m32 = mb's top 32 bits: R32 += R32 (2^63 - m32 R32) / 2^63
+  {
+    const unsigned long long m32 = mb >> 21;
+    const unsigned long long t = m32 * R32;  // ~2^63, |2^63 - t| < 2^42
+    const bool up = t < (1ull << 63);
+    const unsigned long long e = up ? (1ull << 63) - t : t - (1ull << 63);
+    const unsigned long long d = mulhi64(R32 << 1, e);
+    R32 = up ? R32 + d : R32 - d;
+    if (R32 > 0xFFFFFFFFull) R32 = 0xFFFFFFFFull;
+  }
+  // 64-bit step on mb: R += R (2^116 - mb R) / 2^116
+  unsigned long long R = R32 << 32;
+  {
     const unsigned long long plo = mb * R, phi = mulhi64(mb, R);  // mb R (117 bits)
     const unsigned long long elo = 0ull - plo, ehi = (1ull << 52) - phi - (plo != 0 ? 1ull : 0ull);  // 2^116 - mb R
-    const long long e52 = (long long)((ehi << 12) | (elo >> 52));  // (2^116 - mb R) / 2^52, |.| < 2^43
+    const long long e52 = (long long)((ehi << 12) | (elo >> 52));  // (2^116 - mb R) / 2^52, |.| < 2^35
     const unsigned long long d = mulhi64(R, e52 < 0 ? (unsigned long long)(-e52) : (unsigned long long)e52);
     R = e52 < 0 ? R - d : R + d;
   }
-  const int adj = ma < mb ? 1 : 0;
-  const int sh = 54 + adj;  // floor(ma 2^sh / mb) lies in [2^54, 2^55)
-  const int rs = 116 - sh;
-  unsigned long long Q = (mulhi64(ma, R) << (64 - rs)) | ((ma * R) >> rs);
-  long long rem = (long long)((ma << sh) - Q * mb);  // exact: |rem| < 2^63
-  for (int it = 0; it < 3; ++it)
-    if (rem < 0) --Q, rem += (long long)mb;
-  for (int it = 0; it < 3; ++it)
-    if (rem >= (long long)mb) ++Q, rem -= (long long)mb;
+  // Q = floor(A 2^10 R / 2^64) / 2^8 ~ A 2^54 / mb, within one unit
+  unsigned long long Q = mulhi64(A << 10, R) >> 8;
+  long long rem = (long long)(((A & 0x3FFull) << 54) - Q * mb);  // A 2^54 - Q mb, exact: |.| < 2^55
+  if (rem < 0) --Q, rem += (long long)mb;
+  if (rem >= (long long)mb) ++Q, rem -= (long long)mb;
   unsigned long long mant = Q >> 2;
   const unsigned long long guard = (Q >> 1) & 1ull, sticky = (Q & 1ull) | (rem != 0 ? 1ull : 0ull);
   mant += (guard && (sticky || (mant & 1ull))) ? 1ull : 0ull;
-  const int field = ea - eb + 1023 - adj;  // biased exponent of the quotient's leading bit
-  if (field < 1 || field > 2045) return false;
   *q = double_of(((ua ^ ub) & (1ull << 63)) | ((((unsigned long long)(field - 1)) << 52) + mant));
   return true;
 }
