@@ -234,3 +234,105 @@ def test_fused_rebind_equals_fresh_creation(a4):
     with pytest.raises(a4.device.A4GError):
         fs.rebind(terms20[:1])
     fe.close(), fs.close(), f2.close()
+
+
+def test_fused_permuted_storage_and_rank4(a4):
+    """Other storage orders and ranks through the same planner: W stored as
+    (a,b,c,i,j,k) with the denominator's order given (den_order), and a
+    single-term rank-4 ring contraction R(a,i,b,j) = V(a,k,c,i) T(c,b,k,j)
+    with a 1-D orbital-energy array, whose denominator's last term (b) is a
+    column index.  Store and energy forms against the oracle."""
+    import itertools
+
+    import torch
+
+    from aces4_gb300.blocks import BlockArray, ring_triples
+
+    # (a,b,c,i,j,k) storage; labels a=1 i=2 b=3 j=4 c=5 k=6 d=7 l=8
+    o_segs, v_segs = [5], [6, 7]
+    nocc = len(o_segs)
+    V1, V2, T, fock = _problem(o_segs, v_segs, 41)
+    a, b = 1, 0
+    W = BlockArray([v_segs, v_segs, v_segs, o_segs, o_segs, o_segs], present=lambda k: k[0] == a and k[1] == b)
+    W.buf.fill_(float("nan"))
+    wl = [1, 3, 5, 2, 4, 6]
+    p1 = oracle.get_contraction_ptrn(6, 4, 4, wl + [3, 5, 7, 6] + [1, 7, 2, 4])[1]
+    p2 = oracle.get_contraction_ptrn(6, 4, 4, wl + [8, 5, 4, 6] + [1, 3, 2, 8])[1]
+    t1, t2 = [], []
+    nv, no = len(v_segs), len(o_segs)
+    for c in range(nv):
+        for i, j, k in itertools.product(range(no), repeat=3):
+            wk = (a, b, c, i, j, k)
+            for d in range(nv):
+                t1.append((W.block(wk), V1.block((b, c, d, k)), T.block((a, d, i, j)), W.ext(wk),
+                           V1.ext((b, c, d, k)), T.ext((a, d, i, j))))
+            for l in range(no):
+                t2.append((W.block(wk), V2.block((l, c, j, k)), T.block((a, b, i, l)), W.ext(wk),
+                           V2.ext((l, c, j, k)), T.ext((a, b, i, l))))
+    terms = [(p1, t1, 1), (p2, t2, -1)]
+    segs = list(o_segs) + list(v_segs)
+    norb = sum(segs)
+    den_order = [0, 3, 1, 4, 2, 5]  # denominator positions (a,i,b,j,c,k) -> storage dims
+    keys = W.keys()
+    ivs = {k: [nocc + k[0] + 1, nocc + k[1] + 1, nocc + k[2] + 1, k[3] + 1, k[4] + 1, k[5] + 1] for k in keys}
+    Wref, Eref = {}, 0.0
+    for key in keys:
+        dp, de = W.block(key).data_ptr(), W.ext(key)
+        want = np.zeros(W.size(key))
+        for p, trip, sign in terms:
+            for d_, l_, r_, _, le, re in trip:
+                if d_.data_ptr() == dp:
+                    want += sign * oracle.contract_blas(p, l_.cpu().numpy(), le, r_.cpu().numpy(), re, de)
+        Wref[key] = want
+        Eref += oracle.energy_contract(ivs[key], de, want, [norb, norb], fock, segs, 1.0, den_order=den_order)
+    f = a4.device.Fused(6, 4, 4, terms)
+    f.run()
+    a4.device.sync()
+    for key in keys:
+        got = W.block(key).cpu().numpy()
+        assert np.linalg.norm(got - Wref[key]) <= 1e-10 * np.linalg.norm(Wref[key]), key
+    f.close()
+    ft = torch.tensor(fock, device="cuda")
+    fe = a4.device.Fused(6, 4, 4, terms, energy=dict(blocks=[W.block(k) for k in keys],
+                                                    index_values=[ivs[k] for k in keys], ext1=[norb, norb],
+                                                    e_or_fock=ft, seg_sizes=segs, den_order=den_order))
+    e = torch.zeros(1, dtype=torch.float64, device="cuda")
+    fe.run(e)
+    a4.device.sync()
+    assert abs(float(e.item()) - Eref) <= 1e-10 * abs(Eref)
+    fe.close()
+
+    # rank 4, one term: R(a,i,b,j) = V(a,k,c,i) T(c,b,k,j), labels a=1 i=3 b=2 j=4 c=5 k=7
+    o_s, v_s = [4, 3], [5, 6]
+    R = BlockArray([v_s, o_s, v_s, o_s])
+    V = BlockArray([v_s, o_s, v_s, o_s])
+    T4 = BlockArray([v_s, v_s, o_s, o_s])
+    g = torch.Generator(device="cuda")
+    g.manual_seed(43)
+    V.buf.uniform_(-1.0, 1.0, generator=g)
+    T4.buf.normal_(0.0, 0.1, generator=g)
+    trip = ring_triples(R, V, T4)
+    ptrn = oracle.get_contraction_ptrn(4, 4, 4, [1, 3, 2, 4] + [1, 7, 5, 3] + [5, 2, 7, 4])[1]
+    rng = np.random.default_rng(43)
+    n_o, n_v = sum(o_s), sum(v_s)
+    e1 = np.concatenate([rng.uniform(-2.0, -0.5, n_o), rng.uniform(0.2, 5.0, n_v)])
+    segs4 = list(o_s) + list(v_s)
+    no4 = len(o_s)
+    keys4 = R.keys()
+    iv4 = {k: [no4 + k[0] + 1, k[1] + 1, no4 + k[2] + 1, k[3] + 1] for k in keys4}
+    E4 = 0.0
+    for key in keys4:
+        dp, de = R.block(key).data_ptr(), R.ext(key)
+        want = np.zeros(R.size(key))
+        for d_, l_, r_, _, le, re in trip:
+            if d_.data_ptr() == dp:
+                want += oracle.contract_blas(ptrn, l_.cpu().numpy(), le, r_.cpu().numpy(), re, de)
+        E4 += oracle.energy_contract(iv4[key], de, want, [n_o + n_v], e1, segs4, 0.25)
+    f4 = a4.device.Fused(4, 4, 4, [(ptrn, trip, 1)], energy=dict(
+        blocks=[R.block(k) for k in keys4], index_values=[iv4[k] for k in keys4], ext1=[n_o + n_v],
+        e_or_fock=torch.tensor(e1, device="cuda"), seg_sizes=segs4, efact=0.25))
+    e4 = torch.zeros(1, dtype=torch.float64, device="cuda")
+    f4.run(e4)
+    a4.device.sync()
+    assert abs(float(e4.item()) - E4) <= 1e-10 * abs(E4)
+    f4.close()
