@@ -102,6 +102,7 @@ SIGNATURES = {
     "a4g_fused_rebind": (ctypes.c_int, None),
     "a4g_host_direct": (ctypes.c_int, [ctypes.c_int]),
     "a4g_fused_info": (ctypes.c_int, None),
+    "a4g_fused_form": (ctypes.c_int, [c_void_p]),
     "a4g_fused_destroy": (None, [c_void_p]),
 }
 

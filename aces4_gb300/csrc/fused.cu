@@ -58,6 +58,8 @@ struct PtabTable {
 
 struct a4g_fused {
   int slices = 5;
+  int variant = 0;      // as created: 0 automatic, 5 one level at a time, 7 all levels at once
+  bool levels = false;  // the all-levels GEMM form runs
   int drank = 0, lrank = 0, rrank = 0;
   int nterms = 0;
   int beta = 0;
@@ -248,6 +250,7 @@ namespace {
 // are held as offsets (cast to pointers) and relocated at creation.
 struct Plan {
   uint64_t sig = 0;
+  bool levels = false;  // the all-levels GEMM form (128 x 64 tiles), else one level at a time (128 x 128)
   double flops = 0.0;
   int64_t pairs = 0, elements = 0;
   std::vector<OzPanel> panels;  // A panels then B panels; exps as an int offset
@@ -278,14 +281,15 @@ P* as_offset(size_t off) {
 size_t offset_of(const void* p) { return reinterpret_cast<size_t>(p); }
 
 int plan_fused(int drank, int lrank, int rrank, const a4g_term* terms, int nterms, const a4g_fused_energy* energy,
-               int S, int beta, Plan* out) {
+               int S, int beta, int variant, Plan* out) {
   Plan& P = *out;
   if (!terms || nterms < 1 || nterms > 2) return fail(A4G_ERR_ARG, "fused step: one or two terms");
   if (drank < 1 || drank > kMaxRank || lrank < 1 || lrank > kMaxRank || rrank < 1 || rrank > kMaxRank)
     return fail(A4G_ERR_ARG, "fused step: ranks out of range (tensor-tensor contractions only)");
   Fnv64 sig;
   sig.put(uint32_t(0x46555344));  // format tag
-  sig.put(S), sig.put(beta), sig.put(nterms), sig.put(drank), sig.put(lrank), sig.put(rrank);
+  if (variant != 0 && variant != 5 && variant != 7) return fail(A4G_ERR_ARG, "fused step: variant 0, 5 or 7");
+  sig.put(S), sig.put(beta), sig.put(variant), sig.put(nterms), sig.put(drank), sig.put(lrank), sig.put(rrank);
   sig.put(int(energy != nullptr));
 
   // ---- the terms' index maps
@@ -425,6 +429,7 @@ int plan_fused(int drank, int lrank, int rrank, const a4g_term* terms, int nterm
   struct SubH {
     size_t w;
     int b, j;
+    int trip_begin, trip_end, kb_total;
   };
   std::vector<SubH> subs;
   struct WInfo {
@@ -563,8 +568,6 @@ int plan_fused(int drank, int lrank, int rrank, const a4g_term* terms, int nterm
     // stretch (1, j), trip 2 = A stretch (2, j) x B stretch (2, b)
     for (int64_t b = 0; b < NB1; ++b)
       for (int64_t j = 0; j < NB2; ++j) {
-        const int sub = int(subs.size());
-        subs.push_back({w, int(b), int(j)});
         const int trip_begin = int(P.trips.size());
         int kb_total = 0;
         if (!W.pairs[0].empty()) {
@@ -579,15 +582,27 @@ int plan_fused(int drank, int lrank, int rrank, const a4g_term* terms, int nterm
           P.trips.push_back(tr);
           kb_total += tr.nkb;
         }
-        for (int64_t m0 = 0; m0 < M; m0 += kOzBM)
-          for (int64_t n0 = 0; n0 < N; n0 += kOzBN) {
-            OzTile tl{};
-            tl.dblock = sub, tl.m0 = int(m0), tl.n0 = int(n0);
-            tl.panel_a = I.pa, tl.panel_b = I.pb;
-            tl.trip_begin = trip_begin, tl.trip_end = int(P.trips.size());
-            tl.kb_total = kb_total;
-            P.tiles.push_back(tl);
-          }
+        subs.push_back({w, int(b), int(j), trip_begin, int(P.trips.size()), kb_total});
+      }
+  }
+  // ---- the GEMM form, then the tiles of every sub-problem (n fastest)
+  bool fit = true;
+  for (const SubH& sb : subs) fit = fit && oz_levels_fit(S, sb.kb_total);
+  if (variant == 7 && !fit)
+    return fail(A4G_ERR_UNSUPPORTED, "fused step: the all-levels form needs at most 5 slices and k <= 320");
+  P.levels = variant == 7 || (variant == 0 && fit);
+  const int tile_n = P.levels ? kOzLevelsTileCols : kOzBN;
+  for (size_t q = 0; q < subs.size(); ++q) {
+    const SubH& sb = subs[q];
+    const WInfo& I = wi[sb.w];
+    for (int64_t m0 = 0; m0 < I.M; m0 += kOzBM)
+      for (int64_t n0 = 0; n0 < I.N; n0 += tile_n) {
+        OzTile tl{};
+        tl.dblock = int(q), tl.m0 = int(m0), tl.n0 = int(n0);
+        tl.panel_a = I.pa, tl.panel_b = I.pb;
+        tl.trip_begin = sb.trip_begin, tl.trip_end = sb.trip_end;
+        tl.kb_total = sb.kb_total;
+        P.tiles.push_back(tl);
       }
   }
   if (P.tiles.size() > size_t(0x7fffffff / kOzMaxSlices)) return fail(A4G_ERR_RANGE, "fused step: too many tiles");
@@ -777,10 +792,12 @@ int a4g_fused_create(a4g_fused** out, int drank, int lrank, int rrank, const a4g
   if (S < 1 || S > kOzMaxUsableSlices) return fail(A4G_ERR_ARG, "slices must be 1..7");
   const int beta = opts ? opts->beta : 0;
   if (beta != 0 && beta != 1) return fail(A4G_ERR_ARG, "beta must be 0 or 1");
+  const int variant = opts ? opts->variant : 0;
   Plan P;
-  if ((rc = plan_fused(drank, lrank, rrank, terms, nterms, energy, S, beta, &P))) return rc;
+  if ((rc = plan_fused(drank, lrank, rrank, terms, nterms, energy, S, beta, variant, &P))) return rc;
   std::unique_ptr<a4g_fused> f(new a4g_fused());
   f->slices = S, f->drank = drank, f->lrank = lrank, f->rrank = rrank, f->nterms = nterms, f->beta = beta;
+  f->variant = variant, f->levels = P.levels;
   f->energy = P.energy, f->efact = P.efact, f->signature = P.sig;
   f->flops = P.flops, f->pairs = P.pairs, f->elements = P.elements;
   f->zero_blocks = P.zero_blocks;
@@ -807,7 +824,10 @@ int a4g_fused_create(a4g_fused** out, int drank, int lrank, int rrank, const a4g
     for (size_t i = 0; i < hp.size(); ++i) {
       hp[i].base = reinterpret_cast<__nv_bfloat16*>(static_cast<char*>(p) + at[i]);
       hp[i].exps = f->d_exps + offset_of(hp[i].exps);
-      if ((rc = oz_make_tensor_map(maps[i].b, hp[i].base, hp[i].kpad, int64_t(S) * hp[i].rows_pad, kOzBM)))
+      // all-levels form: 32-wide k boxes of 128 rows (A) or 64 columns (B)
+      const int box_rows = P.levels && int(i) >= P.nA ? kOzLevelsTileCols : kOzBM;
+      if ((rc = oz_make_tensor_map_k(maps[i].b, hp[i].base, hp[i].kpad, int64_t(S) * hp[i].rows_pad, box_rows,
+                                     P.levels ? 32 : kOzBK)))
         return rc;
     }
     MapImage* d_maps = nullptr;
@@ -859,10 +879,12 @@ int a4g_fused_create(a4g_fused** out, int drank, int lrank, int rrank, const a4g
     }
   }
 
-  // ---- the GEMM: direct form, one SM per 128 x 128 tile, all levels of a tile in a row
+  // ---- the GEMM: direct form, one SM per tile; one level at a time: work
+  // units (tile, level), all levels of a tile in a row; all levels at once:
+  // the tiles themselves
   std::vector<OzUnit> units;
-  units.reserve(P.tiles.size() * size_t(S));
-  for (size_t g = 0; g < P.tiles.size(); ++g)
+  if (!P.levels) units.reserve(P.tiles.size() * size_t(S));
+  for (size_t g = 0; g < (P.levels ? 0 : P.tiles.size()); ++g)
     for (int lv = 0; lv < S; ++lv) {
       OzUnit u{};
       u.tile = int(g), u.level = lv, u.split = 0;
@@ -914,7 +936,7 @@ int a4g_fused_rebind(a4g_fused* f, const a4g_term* terms, int nterms, const a4g_
   if (!f) return fail(A4G_ERR_ARG, "null fused step");
   if ((energy != nullptr) != f->energy) return fail(A4G_ERR_ARG, "fused rebind: energy form differs from the creation's");
   Plan P;
-  int rc = plan_fused(f->drank, f->lrank, f->rrank, terms, nterms, energy, f->slices, f->beta, &P);
+  int rc = plan_fused(f->drank, f->lrank, f->rrank, terms, nterms, energy, f->slices, f->beta, f->variant, &P);
   if (rc) return rc;
   if (P.sig != f->signature || P.jobs.size() != f->h_jobs.size() || P.colptr.size() != f->n_colptr ||
       P.elast.size() != f->n_elast || int(P.ptabs.size()) != f->n_ptabs)
@@ -943,12 +965,12 @@ int a4g_fused_run(a4g_fused* f, double* esum, void* stream) {
   int rc;
   for (auto& z : f->zero_blocks)
     if ((rc = launch_fill(z.first, z.second, 0.0, s))) return rc;
-  if (f->args.n_units <= 0) return A4G_OK;
+  if (f->args.n_tiles <= 0) return A4G_OK;
   A4G_CUDA(cudaMemsetAsync(f->d_exps, 0, f->exps_bytes, s));
   if ((rc = oz_launch_exp(kOzGeneric, f->d_jobs, f->d_prefix_exp, f->njobs, f->tiles_exp, f->d_panels, s)) ||
       (rc = oz_launch_split(kOzGeneric, f->d_jobs, f->d_prefix_split, f->njobs, f->tiles_split, f->d_panels,
                             f->slices, s)) ||
-      (rc = oz_launch_gemm(f->args, f->grid, false, kOzBN, s)))
+      (rc = f->levels ? oz_launch_levels(f->args, f->grid, s) : oz_launch_gemm(f->args, f->grid, false, kOzBN, s)))
     return rc;
   if (f->energy) return oz_launch_energy_reduce(f->d_epart, f->epart_len, f->efact, esum, s);
   return A4G_OK;
@@ -962,6 +984,8 @@ int a4g_fused_info(const a4g_fused* f, int64_t* pairs, double* flops, int64_t* e
   if (device_bytes) *device_bytes = f->device_bytes;
   return A4G_OK;
 }
+
+int a4g_fused_form(const a4g_fused* f) { return f ? (f->levels ? 7 : 5) : -1; }
 
 void a4g_fused_destroy(a4g_fused* f) { delete f; }
 

@@ -855,6 +855,294 @@ __global__ void __launch_bounds__(DIRECT ? kThreadsOzDirect : kThreadsOz, 1)
   }
 }
 
+// ------------------------------------------------------------------ all levels at once
+// Form of the direct GEMM for sub-problems whose k range fits one exact FP32
+// flush per level (at most 5 slices, k at most 320): every level accumulator
+// of a 128 x 64 tile lives in TMEM at once (levels 0-2 one each; levels 3 and
+// 4, whose sums over 320 k could pass 2^24, one per half of the k range:
+// 7 x 64 = 448 columns).  Each 32-wide k block of the tile's S A-slices and S
+// B-slices is then loaded once for all S (S + 1) / 2 slice pairs, where the
+// level-by-level form loads two tiles per pair.  When the tile's MMAs
+// complete, the epilogue reads each accumulator once, forms the exact sum
+// over levels (the same 64-bit integer as the level-by-level Horner sum) in
+// registers and releases TMEM before it rounds and divides, sums or stores:
+// the tensor cores run the next tile meanwhile.
+constexpr int kLvBN = 64, kLvBK = 32, kLvMaxS = 5, kLvSt = 3, kLvAcc = 7;
+constexpr uint32_t kLvATile = kOzBM * kLvBK * 2;  // 8 KB: 128 rows x 32 k
+constexpr uint32_t kLvBTile = kLvBN * kLvBK * 2;  // 4 KB: 64 columns x 32 k
+struct __align__(1024) LvSmem {
+  uint8_t a[kLvSt][kLvMaxS][kLvATile];
+  uint8_t b[kLvSt][kLvMaxS][kLvBTile];
+  uint64_t full[kLvSt], empty[kLvSt];
+  uint64_t acc_full, acc_empty, drain;
+  uint32_t tmem_base;
+  volatile int abort;
+};
+static_assert(kLvBN == kOzLevelsTileCols, "tile columns of the all-levels form");
+// TMEM accumulator (in 64-column units) of level t; levels 3 and 4: of k half h.
+__device__ __forceinline__ int lv_acc(int t, int h) { return t < 3 ? t : 2 * t - 3 + h; }
+
+// Shared-memory matrix descriptor: K-major, 64-byte swizzle, rows of 64 B,
+// 8-row core groups 512 B apart.
+__device__ __forceinline__ uint64_t sw64_desc(const void* tile) {
+  const uint32_t addr = smem_u32(tile);
+  uint64_t d = uint64_t((addr & 0x3FFFF) >> 4);
+  d |= uint64_t(1) << 16;          // leading byte offset (unused for swizzled K-major)
+  d |= uint64_t(512 >> 4) << 32;   // stride byte offset
+  d |= uint64_t(1) << 46;
+  d |= uint64_t(4) << 61;          // SWIZZLE_64B
+  return d;
+}
+
+// Per 32-wide k block of a tile, one stage: the S A-slices (rows m0..m0+127)
+// and the S B-slices (columns n0..n0+63).
+__device__ void lv_producer(const OzGemmArgs& a, LvSmem& sm) {
+  const int S = a.slices;
+  const uint32_t bytes = uint32_t(S) * (kLvATile + kLvBTile);
+  uint32_t it = 0;
+  for (int g = int(blockIdx.x); g < a.n_tiles; g += int(gridDim.x)) {
+    const OzTile tl = a.tiles[g];
+    const void* ma = static_cast<const uint8_t*>(a.maps_a) + size_t(tl.panel_a) * 128;
+    const void* mb = static_cast<const uint8_t*>(a.maps_b) + size_t(tl.panel_b) * 128;
+    const int rpa = a.panels_a[tl.panel_a].rows_pad, rpb = a.panels_b[tl.panel_b].rows_pad;
+    for (int q = tl.trip_begin; q < tl.trip_end; ++q) {
+      const OzTrip tr = a.trips[q];
+      for (int j = 0; j < 2 * tr.nkb; ++j) {
+        const int s = int(it % kLvSt);
+        const uint32_t ph = (it / kLvSt) & 1;
+        if (!mbar_wait(&sm.empty[s], ph ^ 1, sm, a.err_flag, 1)) return;
+        mbar_expect_tx(&sm.full[s], bytes);
+        const int ka = int(tr.koff_a) + j * kLvBK, kb = int(tr.koff_b) + j * kLvBK;
+        for (int i = 0; i < S; ++i) {
+          tma_load_2d(sm.a[s][i], ma, &sm.full[s], ka, i * rpa + tl.m0);
+          tma_load_2d(sm.b[s][i], mb, &sm.full[s], kb, i * rpb + tl.n0);
+        }
+        ++it;
+      }
+    }
+  }
+}
+
+// One thread issues every MMA: per stage, slice pair (i, j) with i + j < S
+// into the accumulator of level i + j (k half h for levels 3 and 4: the
+// tile's 2 kb_total 32-wide blocks split in two equal halves, at most 160 k
+// each).  The first MMA into an accumulator overwrites it.
+__device__ void lv_mma(const OzGemmArgs& a, LvSmem& sm, uint32_t tmem) {
+  const int S = a.slices;
+  uint32_t it = 0, nt = 0;
+  for (int g = int(blockIdx.x); g < a.n_tiles; g += int(gridDim.x), ++nt) {
+    const OzTile tl = a.tiles[g];
+    const int half = tl.kb_total;
+    if (!mbar_wait(&sm.acc_empty, (nt & 1) ^ 1, sm, a.err_flag, 2)) return;
+    tc_fence_after();
+    int kb = 0;
+    for (int q = tl.trip_begin; q < tl.trip_end; ++q) {
+      const int nk = 2 * a.trips[q].nkb;
+      for (int j = 0; j < nk; ++j, ++kb) {
+        const int s = int(it % kLvSt);
+        const uint32_t ph = (it / kLvSt) & 1;
+        if (!mbar_wait(&sm.full[s], ph, sm, a.err_flag, 3)) return;
+        tc_fence_after();
+        // one issue slot per MMA: the slices' descriptors are the stage's first
+        // plus the tile offset (in 16-byte units), the accumulator columns and
+        // the overwrite flags fixed per stage
+        const uint32_t h64 = kb >= half ? uint32_t(kLvBN) : 0u;  // levels 3, 4: second k half
+        const uint32_t acc_lo = kb == 0 ? 0u : 1u;                // levels 0-2: overwrite at the first block
+        const uint32_t acc_hi = kb == 0 || kb == half ? 0u : 1u;  // levels 3, 4: at the first block of a half
+        const uint64_t ad0 = sw64_desc(sm.a[s][0]), bd0 = sw64_desc(sm.b[s][0]);
+#pragma unroll
+        for (int i = 0; i < kLvMaxS; ++i) {
+#pragma unroll
+          for (int jj = 0; jj < kLvMaxS - i; ++jj) {
+            const int t = i + jj;
+            if (t >= S) continue;
+            const uint32_t d = tmem + uint32_t(kLvBN * lv_acc(t, 0)) + (t >= 3 ? h64 : 0u);
+            const uint32_t acc = i > 0 ? 1u : (t < 3 ? acc_lo : acc_hi);
+            const uint64_t ad = ad0 + uint64_t(i) * (kLvATile >> 4), bd = bd0 + uint64_t(jj) * (kLvBTile >> 4);
+            tc_mma<kLvBN>(d, ad, bd, acc);
+            tc_mma<kLvBN>(d, ad + 2, bd + 2, 1u);  // the block's second 16 k: 32 B further
+          }
+        }
+        tc_commit(&sm.empty[s]);
+        ++it;
+      }
+    }
+    tc_commit(&sm.acc_full);
+  }
+}
+
+// What a thread needs of one of its warp's 16 columns (a table per warp in
+// shared memory, filled while the tensor cores work on the tile).
+struct LvCol {
+  double* colp;  // store form: column base in D (null: outside D)
+  double ec;     // energy form: the column's last-term orbital energy
+  int F;         // biased column exponent (at least 1)
+  int ck;        // energy form: prefix-table column (-1: outside D)
+};
+
+// Sixteen warps, four per TMEM lane quadrant; a thread owns one row and 16
+// columns.  Per tile: the row's scale and tables, the 16 columns' table, the
+// wait for the tile's MMAs, the exact sums (two groups of 8 columns, each
+// accumulator read once), TMEM released, then per element the rounding to
+// FP64 with the row and column scales and
+//   energy form: acc += x * fl(x / eps), eps = fl(prefix - e_last)
+//   (the chain without its last term tabulated in the reference's order; the
+//   quotient exactly rounded; zeros add nothing);
+//   store form: D = x or D += x.
+// A non-finite operand value in the row or column makes x NaN.
+template <bool ENERGY>
+__device__ void lv_epilogue(const OzGemmArgs& a, LvSmem& sm, uint32_t tmem, int warp, int lane) {
+  __shared__ LvCol lv_cols[kThreadsOzDirect / 32 - 2][16];
+  LvCol* tab = lv_cols[warp - 2];
+  const int q = warp & 3, h = (warp - 2) >> 2;
+  const int row = 32 * q + lane;
+  const uint32_t lane_addr = tmem + (uint32_t(32 * q) << 16) + uint32_t(16 * h);
+  const int S = a.slices;
+  [[maybe_unused]] double eacc = 0.0;
+  uint32_t nt = 0;
+  for (int g = int(blockIdx.x); g < a.n_tiles; g += int(gridDim.x), ++nt) {
+    const OzTile tl = a.tiles[g];
+    const OzDBlock db = a.dblocks[tl.dblock];
+    const int m = tl.m0 + row;
+    const bool mlive = m < db.M;
+    int Em = 1;
+    bool nonfinite = false;
+    [[maybe_unused]] long long roff = 0;
+    [[maybe_unused]] const double* prow = nullptr;
+    [[maybe_unused]] double er = 0.0;
+    [[maybe_unused]] bool last_row = false;
+    [[maybe_unused]] OzEnergyBlock eb{};
+    if constexpr (ENERGY) {
+      eb = a.eblocks[tl.dblock];
+      last_row = eb.last_row != 0;
+    }
+    if (mlive) {
+      const int e = a.panels_a[tl.panel_a].exps[m];
+      Em = e ? e : 1;
+      nonfinite = e == kNonFiniteExp;
+      if constexpr (ENERGY) {
+        prow = eb.ptab + int64_t(eb.rk[m]) * eb.ckn;
+        if (last_row) er = eb.elast[m];
+      } else {
+        roff = db.rowoff[m];
+      }
+    }
+    const int ebase = Em - 1022 - 1022 + 2 - kDigitBits * (S + 1);
+    __syncwarp();  // the previous tile's entries are read
+    if (lane < 16) {
+      const int n = tl.n0 + 16 * h + lane;
+      LvCol c{nullptr, 0.0, 1, -1};
+      if (n < db.N) {
+        const int f = a.panels_b[tl.panel_b].exps[n];
+        c.F = f ? f : 1;
+        if constexpr (ENERGY) {
+          c.ck = eb.ck[n];
+          if (!last_row) c.ec = eb.elast[n];
+        } else {
+          c.colp = db.colptr[n];
+        }
+      }
+      tab[lane] = c;
+    }
+    __syncwarp();
+    if (!mbar_wait(&sm.acc_full, nt & 1, sm, a.err_flag, 4)) break;
+    tc_fence_after();
+    long long sum[16];
+#pragma unroll
+    for (int gg = 0; gg < 2; ++gg) {
+      uint32_t v[kLvAcc][8];
+#pragma unroll
+      for (int c = 0; c < kLvAcc; ++c) tc_ld8_nowait(lane_addr + uint32_t(kLvBN * c + 8 * gg), v[c]);
+      tc_wait_ld();
+#pragma unroll
+      for (int j = 0; j < 8; ++j) {
+        // sum_t S_t 256^(S-1-t), S_t an integer below 2^24 in FP32 (levels
+        // 3 and 4: the sum of the two halves)
+        long long r = 0;
+#pragma unroll
+        for (int t = 0; t < kLvMaxS; ++t)
+          if (t < S) {
+            long long st = __float2int_rz(__uint_as_float(v[lv_acc(t, 0)][j]));
+            if (t >= 3) st += __float2int_rz(__uint_as_float(v[lv_acc(t, 1)][j]));
+            r = r * 256 + st;
+          }
+        sum[8 * gg + j] = r;
+      }
+    }
+    tc_fence_before();
+    __syncwarp();
+    if (lane == 0) mbar_arrive(&sm.acc_empty);  // the next tile's MMAs may start
+    if constexpr (ENERGY) {
+#pragma unroll
+      for (int j = 0; j < 16; ++j) {
+        const LvCol c = tab[j];
+        if (!mlive || c.ck < 0) continue;
+        double x = i64_scaled_to_double(sum[j], ebase + c.F, false);
+        if (nonfinite || c.F == kNonFiniteExp) x = __longlong_as_double(0x7FF8000000000000ll);
+        if (!nonzero(x)) continue;
+        const double eps = __dsub_rn(prow[c.ck], last_row ? er : c.ec);
+        eacc = fma(x, div_rn(x, eps), eacc);
+      }
+    } else {
+      const bool acc = a.mode & 1;
+#pragma unroll
+      for (int j = 0; j < 16; ++j) {
+        const LvCol c = tab[j];
+        if (!mlive || !c.colp) continue;
+        double x = i64_scaled_to_double(sum[j], ebase + c.F, a.mode & 2);
+        if (nonfinite || c.F == kNonFiniteExp) x = __longlong_as_double(0x7FF8000000000000ll);
+        double* p = c.colp + roff;
+        *p = acc ? *p + x : x;
+      }
+    }
+  }
+  if constexpr (ENERGY) a.epart[(size_t(blockIdx.x) * 16 + size_t(warp - 2)) * 32 + lane] = eacc;
+}
+
+template <bool ENERGY>
+__global__ void __launch_bounds__(kThreadsOzDirect, 1) oz_levels_kernel(const __grid_constant__ OzGemmArgs a) {
+  extern __shared__ uint8_t smem_raw[];
+  LvSmem& sm = *reinterpret_cast<LvSmem*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < kLvSt; ++s) {
+      mbar_init(&sm.full[s], 1);
+      mbar_init(&sm.empty[s], 1);
+    }
+    mbar_init(&sm.acc_full, 1);
+    mbar_init(&sm.acc_empty, 16);  // one arrive per epilogue warp
+    mbar_init(&sm.drain, 1);
+    sm.abort = 0;
+    fence_mbar_init();
+  }
+  if (warp == 1) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&sm.tmem_base)),
+                 "r"(kTmemCols));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = sm.tmem_base;
+  if (warp == 0) {
+    if (lane == 0) lv_producer(a, sm);
+  } else if (warp == 1) {
+    if (lane == 0) {
+      lv_mma(a, sm, tmem);
+      tc_commit(&sm.drain);  // all MMAs this thread issued have completed before TMEM is released
+      mbar_wait(&sm.drain, 0, sm, a.err_flag, 5);
+    }
+  } else {
+    lv_epilogue<ENERGY>(a, sm, tmem, warp, lane);
+  }
+  tc_fence_before();
+  __syncthreads();
+  if (warp == 1) {
+    tc_fence_after();
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kTmemCols));
+  }
+}
+
 // ------------------------------------------------------------------ split side
 // Tiles of 64 rows x 64 k over the jobs; job_tiles[j] is the prefix count.
 __device__ __forceinline__ int find_job(const int64_t* prefix, int njobs, int64_t t) {
@@ -1489,18 +1777,24 @@ int oz_chunk_kb(int level) {
 }
 
 int oz_make_tensor_map(void* map128, const void* base, int64_t kpad, int64_t rows_total, int box_rows) {
+  return oz_make_tensor_map_k(map128, base, kpad, rows_total, box_rows, kOzBK);
+}
+
+int oz_make_tensor_map_k(void* map128, const void* base, int64_t kpad, int64_t rows_total, int box_rows, int box_k) {
   EncodeTiled enc = get_encoder();
   if (!enc) return fail(A4G_ERR_CUDA, "cuTensorMapEncodeTiled unavailable");
+  if (box_k != kOzBK && box_k != kLvBK) return fail(A4G_ERR_ARG, "tensor map: k box of 64 or 32");
   if (kpad % kOzBK != 0 || (reinterpret_cast<uintptr_t>(base) & 15) != 0)
     return fail(A4G_ERR_ARG, "panel not aligned for TMA");
   cuuint64_t dims[2] = {cuuint64_t(kpad), cuuint64_t(rows_total)};
   cuuint64_t strides[1] = {cuuint64_t(kpad) * 2};
-  cuuint32_t box[2] = {kOzBK, cuuint32_t(box_rows)};
+  cuuint32_t box[2] = {cuuint32_t(box_k), cuuint32_t(box_rows)};
   cuuint32_t estr[2] = {1, 1};
+  // rows of 128 B (64 k) with the 128-byte swizzle, of 64 B (32 k) with the 64-byte one
   CUresult r = enc(reinterpret_cast<CUtensorMap*>(map128), CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2,
                    const_cast<void*>(base), dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
-                   CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
-                   CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+                   box_k == kOzBK ? CU_TENSOR_MAP_SWIZZLE_128B : CU_TENSOR_MAP_SWIZZLE_64B,
+                   CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
   if (r != CUDA_SUCCESS) return fail(A4G_ERR_CUDA, "cuTensorMapEncodeTiled failed: " + std::to_string(int(r)));
   return A4G_OK;
 }
@@ -1558,6 +1852,13 @@ int set_smem_attr() {
   return A4G_OK;
 }
 
+template <bool ENERGY>
+int set_levels_attr() {
+  A4G_CUDA(cudaFuncSetAttribute(oz_levels_kernel<ENERGY>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                int(sizeof(LvSmem)) + 1024));
+  return A4G_OK;
+}
+
 // Function attributes are set once per device (they belong to the device's
 // instance of the kernel).
 bool first_on_device(std::atomic<unsigned long long>& mask) {
@@ -1574,7 +1875,8 @@ int oz_prepare() {
     if ((rc = set_smem_attr<false, 128>()) || (rc = set_smem_attr<true, 128>()) ||
         (rc = set_smem_attr<false, 256>()) || (rc = set_smem_attr<true, 256>()) ||
         (rc = set_smem_attr<false, 128, true>()) || (rc = set_smem_attr<true, 128, true>()) ||
-        (rc = set_smem_attr<false, 128, true, true>())) {
+        (rc = set_smem_attr<false, 128, true, true>()) || (rc = set_levels_attr<false>()) ||
+        (rc = set_levels_attr<true>())) {
       done.store(0);
       return rc;
     }
@@ -1641,6 +1943,24 @@ int oz_launch_gemm(const OzGemmArgs& args, int grid, bool pair, int tile_cols, c
   }
   if (tile_cols == 256) return pair ? launch_form<true, 256>(args, grid, s) : launch_form<false, 256>(args, grid, s);
   return pair ? launch_form<true, 128>(args, grid, s) : launch_form<false, 128>(args, grid, s);
+}
+
+bool oz_levels_fit(int slices, int kb_total) { return slices >= 1 && slices <= kLvMaxS && kb_total <= 5; }
+
+int oz_launch_levels(const OzGemmArgs& args, int grid, cudaStream_t s) {
+  if (!oz_levels_fit(args.slices, 0) || !args.direct) return fail(A4G_ERR_ARG, "all-levels form: 1..5 slices, direct");
+  int rc = oz_prepare();
+  if (rc) return rc;
+  if (args.n_tiles <= 0) return A4G_OK;
+  const size_t smem = sizeof(LvSmem) + 1024;
+  if (args.energy) {
+    if (!args.eblocks || !args.epart) return fail(A4G_ERR_ARG, "energy form: tables");
+    oz_levels_kernel<true><<<grid, kThreadsOzDirect, smem, s>>>(args);
+  } else {
+    oz_levels_kernel<false><<<grid, kThreadsOzDirect, smem, s>>>(args);
+  }
+  A4G_CUDA(cudaGetLastError());
+  return A4G_OK;
 }
 
 int oz_launch_recombine(const OzTile* tiles, int ntiles, int tile_rows, int tile_cols, const OzDBlock* dblocks,

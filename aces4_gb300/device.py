@@ -242,12 +242,13 @@ class Fused:
     or -1.  energy=None: run() stores D = sum of sign * L R (beta 1: adds).
     energy=dict(blocks, index_values, ext1, e_or_fock, seg_sizes, efact=1.0,
     den_order=None): run(esum) adds efact * sum D * fl(D / eps) to esum (a
-    1-element CUDA float64 tensor) and stores nothing.
+    1-element CUDA float64 tensor) and stores nothing.  variant: the GEMM form
+    (0 automatic, 5 one level at a time, 7 all levels at once).
     """
 
-    def __init__(self, drank, lrank, rrank, terms, slices=5, beta=0, energy=None):
+    def __init__(self, drank, lrank, rrank, terms, slices=5, beta=0, energy=None, variant=0):
         tarr, en, keep = self._args(terms, energy)
-        opts = _Opts(PREC_OZAKI_BF16, slices, beta, 0, 0, 0)
+        opts = _Opts(PREC_OZAKI_BF16, slices, beta, variant, 0, 0)
         h = ctypes.c_void_p(0)
         rc = lib().a4g_fused_create(ctypes.byref(h), _i(drank), _i(lrank), _i(rrank), tarr, _i(len(terms)),
                                     ctypes.byref(en) if en is not None else None, ctypes.byref(opts))
@@ -297,7 +298,8 @@ class Fused:
         pairs, flops, el, nb = ctypes.c_int64(0), ctypes.c_double(0), ctypes.c_int64(0), ctypes.c_int64(0)
         _check(lib().a4g_fused_info(self._h, ctypes.byref(pairs), ctypes.byref(flops), ctypes.byref(el),
                                     ctypes.byref(nb)), "a4g_fused_info")
-        return {"pairs": pairs.value, "flops": flops.value, "elements": el.value, "device_bytes": nb.value}
+        return {"pairs": pairs.value, "flops": flops.value, "elements": el.value, "device_bytes": nb.value,
+                "form": int(lib().a4g_fused_form(self._h))}
 
     def close(self):
         if getattr(self, "_h", None) and self._h.value:

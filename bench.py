@@ -533,7 +533,9 @@ def run_triples(args, world, rank, local):
                        "steps_this_rank": len(mine), "timer": "host wall clock around whole computations"},
             "E_total_this_rank": E_rank,
             "per_step": {"device_ms": step_ms, "rebind_host_ms": rebind_ms, "create_ms": tim.get("create_ms"),
-                         "elements": first["info"]["elements"], "device_bytes": first["info"]["device_bytes"]},
+                         "elements": first["info"]["elements"], "device_bytes": first["info"]["device_bytes"],
+                         "gemm_form": {5: "one level at a time, 128x128 tiles",
+                                       7: "all levels at once, 128x64 tiles"}.get(first["info"]["form"])},
             "unfused_two_batches_one_step": unfused,
             "fp64_plain": {"value": fp64_rate, "unit": "TFLOP/s", "ms_per_step_terms": checks[0]["fp64_terms_ms"]},
             "split_over_fp64": value / world / fp64_rate,

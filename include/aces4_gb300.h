@@ -469,16 +469,28 @@ int a4g_tune_cache_load(const char* path);
  * terms added in the same order: the chain without its last term is
  * tabulated once at creation, the last subtraction and the exactly rounded
  * quotient are formed per element), the products summed in FP64 in a fixed
- * order.  D exists only one 128 x 128 tile at a time, as exact 64-bit level
- * sums in tensor memory.
+ * order.  D exists only one tile at a time, as exact integer level sums in
+ * tensor memory.
+ *
+ * GEMM form (opts->variant): 0 automatic (7 where it fits, else 5); 5 one
+ * level at a time: 128 x 128 tiles, the exact 64-bit sum over levels folded
+ * in tensor memory level by level; 7 all levels at once: 128 x 64 tiles,
+ * every level's accumulator in tensor memory together, each k block of the
+ * slices loaded once for all slice pairs, the sum over levels formed in
+ * registers and tensor memory released before the rounding, the division and
+ * the store; it fits at most 5 slices and k <= 320 per sub-problem (the sum
+ * of both terms' contracted extents, each stretch rounded up to 64; the
+ * triples at segments of 24 and 10 virtual segments: 256 + 64) and is
+ * A4G_ERR_UNSUPPORTED beyond.  Both forms give the same D bits; the energy
+ * sums differ in the order of the partial sums only.
  *
  * Both terms share the destination ranks and the operand ranks.  Every
  * destination index is a row (left operand in both terms), a column (right
  * in both), or fixed per sub-problem (left in one term, right in the other:
  * the triples' b and j); the energy form needs the denominator's last term
  * on a row or column index.  Split precision only (opts->precision
- * A4G_PREC_OZAKI_BF16); opts->slices and opts->beta apply, the other options
- * are ignored.  A triple with a NULL operand is skipped. */
+ * A4G_PREC_OZAKI_BF16); opts->slices, opts->beta and opts->variant apply, the
+ * other options are ignored.  A triple with a NULL operand is skipped. */
 typedef struct a4g_term {
   const int* contr_ptrn; /* as for a4g_batch_create (lrank + rrank entries)  */
   const a4g_triple* triples;
@@ -516,6 +528,8 @@ int a4g_fused_run(a4g_fused* f, double* esum, void* stream);
  * structure differs (create a new step then). */
 int a4g_fused_rebind(a4g_fused* f, const a4g_term* terms, int nterms, const a4g_fused_energy* energy, void* stream);
 int a4g_fused_info(const a4g_fused* f, int64_t* pairs, double* flops, int64_t* elements, int64_t* device_bytes);
+/* The GEMM form the step runs: 5 (one level at a time) or 7 (all levels at once); -1 for NULL. */
+int a4g_fused_form(const a4g_fused* f);
 void a4g_fused_destroy(a4g_fused* f);
 
 #ifdef __cplusplus

@@ -336,3 +336,81 @@ def test_fused_permuted_storage_and_rank4(a4):
     a4.device.sync()
     assert abs(float(e4.item()) - E4) <= 1e-10 * abs(E4)
     f4.close()
+
+
+@pytest.mark.parametrize("o_segs,v_segs,a,b,slices", [([6], [12, 12], 0, 1, 5),          # one tile column
+                                                      ([3, 5], [5, 7, 4], 0, 2, 5),     # ragged tiles, odd k
+                                                      ([8], [16, 16, 16], 1, 2, 4),     # 256-row sub-problems
+                                                      ([8], [16, 16, 16], 2, 0, 3)])
+def test_fused_forms_agree(a4, o_segs, v_segs, a, b, slices):
+    """The two GEMM forms of the fused step: all levels at once (variant 7,
+    128 x 64 tiles, levels 3 and 4 over two k halves) and one level at a time
+    (variant 5, 128 x 128 tiles) form the same exact integer sums, so the
+    stored W has the same bits (overwrite and beta = 1); the energies differ
+    in the order of the partial sums only."""
+    import torch
+
+    V1, V2, T, fock = _problem(o_segs, v_segs, 50 + slices)
+    ft = torch.tensor(fock, device="cuda")
+    W, terms = _step(V1, V2, T, o_segs, v_segs, a, b)
+    out = {}
+    for variant in (5, 7):
+        for beta in (0, 1):
+            W.buf.fill_(0.375 if beta else float("nan"))
+            f = a4.device.Fused(6, 4, 4, terms, slices=slices, beta=beta, variant=variant)
+            assert f.info()["form"] == variant
+            f.run()
+            a4.device.sync()
+            out[variant, beta] = W.buf.clone()
+            f.close()
+    for beta in (0, 1):
+        for key in W.keys():  # every element written (the gaps between blocks are not)
+            off = W.offsets[key]
+            assert bool(torch.isfinite(out[7, beta][off:off + W.size(key)]).all()), (key, beta)
+        assert torch.equal(out[5, beta].view(torch.int64), out[7, beta].view(torch.int64)), beta
+    if slices == 5:
+        Wref, Eref = _oracle_W_E(W, terms, o_segs, v_segs, fock)
+        for key in W.keys():
+            off = W.offsets[key]
+            got = out[7, 0][off:off + W.size(key)].cpu().numpy()
+            assert np.linalg.norm(got - Wref[key]) <= 1e-10 * np.linalg.norm(Wref[key]), key
+    e = {}
+    for variant in (5, 7):
+        fe = a4.device.Fused(6, 4, 4, terms, slices=slices, energy=_energy_args(W, o_segs, v_segs, ft),
+                             variant=variant)
+        e[variant] = torch.zeros(1, dtype=torch.float64, device="cuda")
+        fe.run(e[variant])
+        a4.device.sync()
+        fe.close()
+    e5, e7 = float(e[5].item()), float(e[7].item())
+    assert e5 < 0 and abs(e7 - e5) <= 1e-13 * abs(e5)
+    if slices == 5:
+        assert abs(e7 - Eref) <= 1e-10 * abs(Eref)
+
+
+def test_fused_form_choice(a4):
+    """Automatic choice: the all-levels form where it fits, else one level at
+    a time (six slices; a k range above 320); variant 7 beyond its range is
+    A4G_ERR_UNSUPPORTED."""
+    o_segs, v_segs = [4], [6, 6]
+    V1, V2, T, _ = _problem(o_segs, v_segs, 3)
+    W, terms = _step(V1, V2, T, o_segs, v_segs, 0, 1)
+    f = a4.device.Fused(6, 4, 4, terms)
+    assert f.info()["form"] == 7
+    f.close()
+    f6 = a4.device.Fused(6, 4, 4, terms, slices=6)
+    assert f6.info()["form"] == 5
+    f6.close()
+    with pytest.raises(a4.device.A4GError) as ei:
+        a4.device.Fused(6, 4, 4, terms, slices=6, variant=7)
+    assert ei.value.rc == 6
+    # k of term 1: 41 virtual segments of 8 = 328, a stretch of 384 (> 320)
+    o_segs, v_segs = [1], [8] * 41
+    V1, V2, T, _ = _problem(o_segs, v_segs, 4)
+    W, terms = _step(V1, V2, T, o_segs, v_segs, 0, 1)
+    f = a4.device.Fused(6, 4, 4, terms)
+    assert f.info()["form"] == 5
+    f.close()
+    with pytest.raises(a4.device.A4GError) as ei:
+        a4.device.Fused(6, 4, 4, terms, variant=7)
+    assert ei.value.rc == 6
