@@ -125,22 +125,23 @@ A4G_HD double i128_scaled_to_double(__int128 N, int e2) {
 // false otherwise (the caller divides in FP64).  With A = ma or 2 ma (the
 // dividend's significand doubled when it is below the divisor's, so that
 // A / mb lies in [1, 2)), the 55-bit quotient Q = floor(A 2^54 / mb) is
-// estimated through a reciprocal R ~ 2^116 / mb of the divisor's 53-bit
-// significand and corrected from the exact remainder A 2^54 - Q mb (Knuth,
-// TAOCP vol. 2, 4.3.1: estimate a quotient digit, then fix it from the
-// remainder), which also gives the sticky bit for the rounding.  R comes from
-// Newton-Raphson, x' = x + x (1 - d x), in fixed point: the FP32 reciprocal
-// of mb's top 24 bits (relative error below 2^-22), one step in 32-bit
-// arithmetic on mb's top 32 bits (below 2^-30), one step in 64-bit arithmetic
-// on all of mb (below 2^-59).  Q is then off by at most one unit, so one
-// correction each way suffices, and the remainder, below 2 mb < 2^54 in
-// magnitude, is exact in wrapping 64-bit arithmetic.
-A4G_HD bool div_rn_int(double a, double b, double* q) {
-  const unsigned long long ua = bits_of(a), ub = bits_of(b);
-  const int ea = int((ua >> 52) & 0x7FF), eb = int((ub >> 52) & 0x7FF);
-  if (ea == 0 || ea == 2047 || eb == 0 || eb == 2047) return false;
-  const unsigned long long ma = (ua & ((1ull << 52) - 1)) | (1ull << 52);
-  const unsigned long long mb = (ub & ((1ull << 52) - 1)) | (1ull << 52);
+// formed in two digits, each estimated through a 32-bit reciprocal
+// R32 ~ 2^84 / mb and the next one taken from the exact remainder (Knuth,
+// TAOCP vol. 2, 4.3.1: estimate a quotient digit, then continue from the
+// remainder), and the last one corrected from the remainder, which also gives
+// the sticky bit for the rounding.  R32 comes from Newton-Raphson,
+// x' = x + x (1 - d x), in fixed point: the FP32 reciprocal of mb's top 24
+// bits (relative error below 2^-22), one step in 32-bit arithmetic on mb's top
+// 32 bits (below 2^-30).  Digit 1, q1 = (A's top 32 bits) R32 / 2^32, lies
+// within (-2, 4.01) units of A 2^30 / mb, so s1 = A 2^30 - q1 mb (exact in
+// wrapping 64-bit arithmetic) is below 4.01 mb in magnitude; digit 2,
+// q2 = floor((s1 >> 25) R32 / 2^35), lies within one unit of s1 2^24 / mb
+// (the estimate is off by less than 0.19 below and 0.07 above).  So
+// Q = q1 2^24 + q2 is off by at most one unit, one correction each way
+// suffices, and the remainder, below 2 mb < 2^54 in magnitude, is exact in
+// wrapping 64-bit arithmetic.
+A4G_HD bool div_rn_sig(unsigned long long ma, int ea, unsigned long long mb, int eb, unsigned long long sign,
+                       double* q) {
   const int adj = ma < mb ? 1 : 0;
   const unsigned long long A = ma << adj;  // [mb, 2 mb)
   const int field = ea - eb + 1023 - adj;  // biased exponent of the quotient's leading bit
@@ -151,37 +152,42 @@ A4G_HD bool div_rn_int(double a, double b, double* q) {
   const float rf = frcp_rn(float(uint32_t(mb >> 29)));
   uint32_t rb;
   memcpy(&rb, &rf, 4);
-  unsigned long long R32 = ((rb >> 23) & 0xFFu) == 103u ? ((unsigned long long)((rb & 0x7FFFFFu) | 0x800000u) << 8)
-                                                         : 0xFFFFFFFFull;
-  // 32-bit step on m32 = mb's top 32 bits: R32 += R32 (2^63 - m32 R32) / 2^63
+  uint32_t R32 = ((rb >> 23) & 0xFFu) == 103u ? (((rb & 0x7FFFFFu) | 0x800000u) << 8) : 0xFFFFFFFFu;
+  // 32-bit step on m32 = mb's top 32 bits: R32 += R32 (2^63 - m32 R32) / 2^63,
+  // the correction formed from e's top 32 bits (|e| < 2^42: the seed is within
+  // 2^-21 of 2^63 / m32)
   {
-    const unsigned long long m32 = mb >> 21;
-    const unsigned long long t = m32 * R32;  // ~2^63, |2^63 - t| < 2^42
+    const uint32_t m32 = uint32_t(mb >> 21);
+    const unsigned long long t = (unsigned long long)m32 * R32;  // ~2^63
     const bool up = t < (1ull << 63);
     const unsigned long long e = up ? (1ull << 63) - t : t - (1ull << 63);
-    const unsigned long long d = mulhi64(R32 << 1, e);
-    R32 = up ? R32 + d : R32 - d;
-    if (R32 > 0xFFFFFFFFull) R32 = 0xFFFFFFFFull;
+    const unsigned long long d = ((unsigned long long)R32 * uint32_t(e >> 10)) >> 53;
+    const unsigned long long r = up ? (unsigned long long)R32 + d : (unsigned long long)R32 - d;
+    R32 = r > 0xFFFFFFFFull ? 0xFFFFFFFFu : uint32_t(r);
   }
-  // 64-bit step on mb: R += R (2^116 - mb R) / 2^116
-  unsigned long long R = R32 << 32;
-  {
-    const unsigned long long plo = mb * R, phi = mulhi64(mb, R);  // mb R (117 bits)
-    const unsigned long long elo = 0ull - plo, ehi = (1ull << 52) - phi - (plo != 0 ? 1ull : 0ull);  // 2^116 - mb R
-    const long long e52 = (long long)((ehi << 12) | (elo >> 52));  // (2^116 - mb R) / 2^52, |.| < 2^35
-    const unsigned long long d = mulhi64(R, e52 < 0 ? (unsigned long long)(-e52) : (unsigned long long)e52);
-    R = e52 < 0 ? R - d : R + d;
-  }
-  // Q = floor(A 2^10 R / 2^64) / 2^8 ~ A 2^54 / mb, within one unit
-  unsigned long long Q = mulhi64(A << 10, R) >> 8;
-  long long rem = (long long)(((A & 0x3FFull) << 54) - Q * mb);  // A 2^54 - Q mb, exact: |.| < 2^55
+  // digit 1: the quotient's top 31 bits; s1 = A 2^30 - q1 mb
+  const uint32_t q1 = uint32_t(((unsigned long long)uint32_t(A >> 22) * R32) >> 32);
+  const long long s1 = (long long)((A << 30) - (unsigned long long)q1 * mb);
+  // digit 2: floor(s1 2^24 / mb), within one unit
+  const long long q2 = ((s1 >> 25) * (long long)R32) >> 35;
+  unsigned long long Q = ((unsigned long long)q1 << 24) + (unsigned long long)q2;
+  long long rem = (long long)(((A & 0x3FFull) << 54) - Q * mb);  // A 2^54 - Q mb, exact: |.| < 2 mb
   if (rem < 0) --Q, rem += (long long)mb;
   if (rem >= (long long)mb) ++Q, rem -= (long long)mb;
   unsigned long long mant = Q >> 2;
   const unsigned long long guard = (Q >> 1) & 1ull, sticky = (Q & 1ull) | (rem != 0 ? 1ull : 0ull);
   mant += (guard && (sticky || (mant & 1ull))) ? 1ull : 0ull;
-  *q = double_of(((ua ^ ub) & (1ull << 63)) | ((((unsigned long long)(field - 1)) << 52) + mant));
+  *q = double_of((sign << 63) | ((((unsigned long long)(field - 1)) << 52) + mant));
   return true;
+}
+
+A4G_HD bool div_rn_int(double a, double b, double* q) {
+  const unsigned long long ua = bits_of(a), ub = bits_of(b);
+  const int ea = int((ua >> 52) & 0x7FF), eb = int((ub >> 52) & 0x7FF);
+  if (ea == 0 || ea == 2047 || eb == 0 || eb == 2047) return false;
+  const unsigned long long ma = (ua & ((1ull << 52) - 1)) | (1ull << 52);
+  const unsigned long long mb = (ub & ((1ull << 52) - 1)) | (1ull << 52);
+  return div_rn_sig(ma, ea, mb, eb, (ua ^ ub) >> 63, q);
 }
 
 // a / b rounded to the nearest double: div_rn_int where it applies, the FP64

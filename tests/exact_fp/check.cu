@@ -6,6 +6,7 @@
 
 #include <cmath>
 #include <random>
+#include <vector>
 
 #include "exact_fp.h"
 
@@ -62,6 +63,26 @@ int main(int argc, char** argv) {
       if (bad < 5) printf("div: unexpected fallback a=%a b=%a\n", a, b);
       ++bad;
     }
+  }
+  // division: every pair of edge significands (the ends of [2^52, 2^53), one
+  // bit set or cleared above the leading one), both orders of magnitude
+  {
+    std::vector<unsigned long long> sig;
+    for (int k = 0; k < 4; ++k) sig.push_back((1ull << 52) + k), sig.push_back((2ull << 52) - 1 - k);
+    for (int k = 0; k < 52; ++k) sig.push_back((1ull << 52) | (1ull << k)), sig.push_back(((2ull << 52) - 1) & ~(1ull << k));
+    for (int k = 0; k < 40; ++k) sig.push_back((1ull << 52) | (g() >> 12));
+    for (unsigned long long sa : sig)
+      for (unsigned long long sb : sig)
+        for (int de = -1; de <= 1; ++de) {
+          const double a = double_of(((unsigned long long)(1023 + de) << 52) | (sa & ((1ull << 52) - 1)));
+          const double b = double_of((1023ull << 52) | (sb & ((1ull << 52) - 1)));
+          double q;
+          if (!div_rn_int(a, b, &q) || !same(q, a / b)) {
+            if (bad < 10) printf("div edge: a=%a b=%a\n", a, b);
+            ++bad;
+          }
+          ++fast;
+        }
   }
   // scaled integer -> double, both signs, ties and near-ties
   for (long i = 0; i < n; ++i) {
