@@ -71,6 +71,8 @@ SIGNATURES = {
     "a4g_energy_contract": (ctypes.c_int, None),
     "a4g_batch_splits": (ctypes.c_int, None),
     "a4g_selftest_wait_timeout": (ctypes.c_int, None),
+    "a4g_selftest_round": (ctypes.c_int, [ctypes.c_int, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p]),
+    "a4g_selftest_div": (ctypes.c_int, [ctypes.c_int, c_void_p, c_void_p, c_void_p, c_void_p]),
     "a4g_clear_error": (None, []),
     "a4g_update_t2": (ctypes.c_int, None),
     "a4g_batch_launches": (ctypes.c_int, None),

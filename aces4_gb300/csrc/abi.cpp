@@ -702,6 +702,20 @@ int a4g_selftest_wait_timeout(int limit_ms, int* waited_ms, void* stream) {
   return check_device_flag(s);  // A4G_ERR_TIMEOUT when the wait gave up, as intended
 }
 
+int a4g_selftest_round(int n, const long long* v, const int* e2, const int* neg, double* out, void* stream) {
+  int rc = ensure_init();
+  if (rc) return rc;
+  if (n < 0 || (n > 0 && (!v || !e2 || !neg || !out))) return fail(A4G_ERR_ARG, "rounding self-test: arguments");
+  return oz_round_selftest(n, v, e2, neg, out, pick(stream));
+}
+
+int a4g_selftest_div(int n, const double* a, const double* b, double* out, void* stream) {
+  int rc = ensure_init();
+  if (rc) return rc;
+  if (n < 0 || (n > 0 && (!a || !b || !out))) return fail(A4G_ERR_ARG, "division self-test: arguments");
+  return oz_div_selftest(n, a, b, out, pick(stream));
+}
+
 int a4g_energy_contract(int rank0, const int* iv, const int* ext0, const double* data0, const int* den_order,
                         int rank1, const int* ext1, const double* e, int nsegs, const int* segs, double efact,
                         double* esum, void* stream) {

@@ -59,11 +59,27 @@ A4G_HD float frcp_rn(float x) {
 }
 
 // The double nearest (ties to even) to u * 2^e2 with sign `neg`, u an
-// unsigned 64-bit magnitude.  Results outside the normal range take an FP64
-// path (ldexp).
+// unsigned 64-bit magnitude, rounded once: to 53 bits in the normal range, to
+// a multiple of 2^-1074 below it (subnormal results and zero), to infinity
+// beyond the largest double.
 A4G_HD double u64_scaled_to_double(unsigned long long u, bool neg, int e2) {
   if (u == 0) return 0.0;
+  const unsigned long long sbit = neg ? (1ull << 63) : 0ull;
   const int nbits = 64 - clz64(u);
+  if (e2 + nbits - 1 < -1022) {  // below 2^-1022: the unit is 2^-1074
+    const int sh = -1074 - e2;    // bits of u below the unit
+    unsigned long long q;
+    if (sh <= 0) {
+      q = u << (-sh);  // exact: a multiple of the unit below 2^-1022
+    } else if (sh > 64) {
+      q = 0;  // below half a unit
+    } else {
+      q = sh == 64 ? 0ull : u >> sh;
+      const unsigned long long rem = sh == 64 ? u : u & ((1ull << sh) - 1), half = 1ull << (sh - 1);
+      if (rem > half || (rem == half && (q & 1ull))) ++q;
+    }
+    return double_of(sbit | q);  // q = 2^52 (rounded up to the least normal) has the right bits too
+  }
   unsigned long long mant;
   int e = e2;
   if (nbits <= 53) {
@@ -78,10 +94,8 @@ A4G_HD double u64_scaled_to_double(unsigned long long u, bool neg, int e2) {
     if (mant == (1ull << 53)) mant >>= 1, ++e;
   }
   const int field = e + 52 + 1023;  // value = mant * 2^e, mant in [2^52, 2^53)
-  if (field >= 1 && field <= 2046)
-    return double_of((neg ? (1ull << 63) : 0ull) | ((unsigned long long)field << 52) | (mant & ((1ull << 52) - 1)));
-  const double v = ldexp(double(mant), e);
-  return neg ? -v : v;
+  if (field > 2046) return double_of(sbit | 0x7FF0000000000000ull);
+  return double_of(sbit | ((unsigned long long)field << 52) | (mant & ((1ull << 52) - 1)));
 }
 
 // (neg ? -1 : 1) * v * 2^e2 rounded once to the nearest double (ties to
@@ -92,6 +106,18 @@ A4G_HD double u64_scaled_to_double(unsigned long long u, bool neg, int e2) {
 // the result of u64_scaled_to_double (a zero keeps the sign the negation
 // gives it).
 A4G_HD double i64_scaled_to_double(long long v, int e2, bool neg) {
+#if defined(__CUDA_ARCH__)
+  // On the GPU the integer-to-FP64 conversion rounds v once to 53 bits (to
+  // nearest, ties to even), and the scaling by 2^e2 is an exact addition to
+  // the exponent field while the result stays normal: the same bits as the
+  // integer construction below, in three instructions.
+  if (v != 0) {
+    const unsigned long long b = bits_of(__ll2double_rn(v));
+    const int field = int((b >> 52) & 0x7FF) + e2;
+    if (field >= 1 && field <= 2046)
+      return double_of((b + ((unsigned long long)(long long)e2 << 52)) ^ (neg ? (1ull << 63) : 0ull));
+  }
+#endif
   const unsigned long long sign = (v < 0) != neg ? (1ull << 63) : 0ull;
   const unsigned long long u = v < 0 ? (unsigned long long)(-v) : (unsigned long long)v;
   const int n = clz64(u | 1ull);  // u = 0 is mapped to a signed zero at the end

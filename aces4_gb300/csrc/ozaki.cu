@@ -1735,6 +1735,20 @@ __global__ void wait_timeout_selftest_kernel(unsigned long long limit_ns, int* e
   if (!done) atomicExch(err, 6);
 }
 
+// Self-tests of the one-rounding helpers exactly as the kernels run them: the
+// integer-to-FP64 rounding of every split-precision epilogue and the exact
+// division of the denominator and energy passes, one element per thread.
+__global__ void round_selftest_kernel(int n, const long long* __restrict__ v, const int* __restrict__ e2,
+                                      const int* __restrict__ neg, double* __restrict__ out) {
+  const int i = int(blockIdx.x) * int(blockDim.x) + int(threadIdx.x);
+  if (i < n) out[i] = i64_scaled_to_double(v[i], e2[i], neg[i] != 0);
+}
+__global__ void div_selftest_kernel(int n, const double* __restrict__ a, const double* __restrict__ b,
+                                    double* __restrict__ out) {
+  const int i = int(blockIdx.x) * int(blockDim.x) + int(threadIdx.x);
+  if (i < n) out[i] = div_rn(a[i], b[i]);
+}
+
 // esum += efact * (sum of the n partial energies), the partials added in a
 // fixed order (one CTA: strided per-thread sums, then a fixed tree), so a GPU
 // gives the same bits every run.
@@ -2020,6 +2034,20 @@ int oz_wait_timeout_selftest(int limit_ms, int* waited_ms, cudaStream_t s) {
   A4G_CUDA(cudaGetLastError());
   A4G_CUDA(cudaMemcpyAsync(waited_ms, d_ms, sizeof(int), cudaMemcpyDeviceToHost, s));
   A4G_CUDA(cudaFreeAsync(d_ms, s));
+  return A4G_OK;
+}
+
+int oz_round_selftest(int n, const long long* v, const int* e2, const int* neg, double* out, cudaStream_t s) {
+  if (n <= 0) return A4G_OK;
+  round_selftest_kernel<<<unsigned((n + 255) / 256), 256, 0, s>>>(n, v, e2, neg, out);
+  A4G_CUDA(cudaGetLastError());
+  return A4G_OK;
+}
+
+int oz_div_selftest(int n, const double* a, const double* b, double* out, cudaStream_t s) {
+  if (n <= 0) return A4G_OK;
+  div_selftest_kernel<<<unsigned((n + 255) / 256), 256, 0, s>>>(n, a, b, out);
+  A4G_CUDA(cudaGetLastError());
   return A4G_OK;
 }
 

@@ -31,6 +31,9 @@ constexpr int kOzLevelsTileCols = 64;
 bool oz_levels_fit(int slices, int kb_total);
 int oz_launch_levels(const OzGemmArgs& args, int grid, cudaStream_t s);
 int oz_wait_timeout_selftest(int limit_ms, int* waited_ms, cudaStream_t s);
+// device runs of the one-rounding helpers (exact_fp.h) over device arrays
+int oz_round_selftest(int n, const long long* v, const int* e2, const int* neg, double* out, cudaStream_t s);
+int oz_div_selftest(int n, const double* a, const double* b, double* out, cudaStream_t s);
 // esum (device) += efact * the sum of the energy form's n partials, in a fixed order.
 int oz_launch_energy_reduce(const double* part, int n, double efact, double* esum, cudaStream_t s);
 int oz_launch_recombine(const OzTile* tiles, int ntiles, int tile_rows, int tile_cols, const OzDBlock* dblocks,

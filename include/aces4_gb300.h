@@ -209,6 +209,15 @@ int a4g_energy_denominator(int rank0, const int* index_values0, const int* ext0,
  * CUDA context still usable.  Every pipeline wait (TMA stages, MMA
  * accumulators, bulk copies) takes the same path with a 20 s limit. */
 int a4g_selftest_wait_timeout(int limit_ms, int* waited_ms, void* stream);
+/* Self-tests of the exact-rounding helpers as the kernels run them (no
+ * reference counterpart), over n elements of device arrays:
+ * a4g_selftest_round: out[i] = (neg[i] ? -1 : 1) * v[i] * 2^e2[i] rounded
+ * once to the nearest double (ties to even), the rounding of every
+ * split-precision result; a4g_selftest_div: out[i] = a[i] / b[i] rounded to
+ * the nearest double, the division of the denominators and the (T) energy.
+ * Both are expected to equal IEEE arithmetic bit for bit. */
+int a4g_selftest_round(int n, const long long* v, const int* e2, const int* neg, double* out, void* stream);
+int a4g_selftest_div(int n, const double* a, const double* b, double* out, void* stream);
 
 /* Amplitude update of one block (a,i,b,j): procedure updatet2 of
  * src/sialx/qm/cc/rlccd_rhf.sialx:557-600, both of its pardo passes fused

@@ -124,6 +124,22 @@ int main(int argc, char** argv) {
       ++bad;
     }
   }
+  // scaled integer -> double at the ends of the range: subnormal results,
+  // underflow to zero and overflow to infinity, rounded once
+  for (long i = 0; i < n; ++i) {
+    const int bits = 1 + int(g() % 63);
+    long long v = (long long)(g() >> (64 - bits));
+    if (g() & 1) v = -v;
+    const int e2 = (i & 1) ? -1150 + int(g() % 130) : 940 + int(g() % 80);
+    const bool neg = g() & 1;
+    const long double r = std::ldexp((long double)v, e2);
+    const double want = v == 0 ? (neg ? -0.0 : 0.0) : (double)(neg ? -r : r);
+    const double got = i64_scaled_to_double(v, e2, neg);
+    if (!same(got, want)) {
+      if (bad < 10) printf("i64 extreme: v=%lld e2=%d neg=%d got %a want %a\n", v, e2, int(neg), got, want);
+      ++bad;
+    }
+  }
   printf("division checked %ld on the integer path, mismatches %ld\n", fast, bad);
   return bad == 0 && fast > n / 2 ? 0 : 1;
 }
