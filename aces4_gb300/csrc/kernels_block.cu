@@ -460,7 +460,11 @@ __device__ __forceinline__ void block_sum_to(double acc, double* partial, int64_
 // gridDim.y CTAs in a fixed order.
 constexpr int kEnLoads = 4;  // loads in flight per thread
 constexpr int kEnThreads = 512;
-__global__ void __launch_bounds__(kEnThreads, 2) energy_chain_kernel(DenParams p, const double* __restrict__ w,
+// DIVIDE: the denominator drop-in on the same walk, in place: each element
+// becomes fl(w / eps) (zeros included: 0 / eps keeps the IEEE sign), nothing
+// is summed.
+template <bool DIVIDE>
+__global__ void __launch_bounds__(kEnThreads, 2) energy_chain_kernel(DenParams p, double* w,
                                                             const double* __restrict__ e, int x2_per_unit,
                                                             int64_t nunits, double* partial) {
   extern __shared__ double en[];  // e2 energies [ext2], then e4 energies [ext4]
@@ -474,6 +478,11 @@ __global__ void __launch_bounds__(kEnThreads, 2) energy_chain_kernel(DenParams p
   const int64_t n01 = int64_t(n0) * n1;
   const int64_t pp = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
   const int x2_chunks = (n2 + x2_per_unit - 1) / x2_per_unit;
+  // the energy form only reads w (read-only cache); the divide form writes it
+  auto load = [](const double* q) -> double {
+    if constexpr (DIVIDE) return *q;
+    else return __ldg(q);
+  };
   double acc = 0.0;
   if (pp < n01) {
     const int x0 = int(pp % n0), x1 = int(pp / n0);
@@ -487,33 +496,43 @@ __global__ void __launch_bounds__(kEnThreads, 2) energy_chain_kernel(DenParams p
       t = __dsub_rn(t, e0v);
       const int x2b = chunk * x2_per_unit, x2e = min(n2, x2b + x2_per_unit);
       if (!r6) {
-        const double* base = w + pp + n01 * (int64_t(n2) * x3);
+        double* base = w + pp + n01 * (int64_t(n2) * x3);
         for (int x2 = x2b; x2 < x2e; x2 += kEnLoads) {
           double v[kEnLoads];
 #pragma unroll
-          for (int k = 0; k < kEnLoads; ++k) v[k] = x2 + k < x2e ? __ldg(base + n01 * (x2 + k)) : 0.0;
+          for (int k = 0; k < kEnLoads; ++k) v[k] = x2 + k < x2e ? load(base + n01 * (x2 + k)) : 0.0;
 #pragma unroll
-          for (int k = 0; k < kEnLoads; ++k)
-            if (nonzero(v[k])) acc = fma(v[k], div_rn(v[k], __dsub_rn(t, en[x2 + k])), acc);
+          for (int k = 0; k < kEnLoads; ++k) {
+            if constexpr (DIVIDE) {
+              if (x2 + k < x2e) base[n01 * (x2 + k)] = div_rn(v[k], __dsub_rn(t, en[x2 + k]));
+            } else if (nonzero(v[k])) {
+              acc = fma(v[k], div_rn(v[k], __dsub_rn(t, en[x2 + k])), acc);
+            }
+          }
         }
       } else {
         const int64_t s4 = n01 * int64_t(n2) * n3;  // stride of x4
         for (int x2 = x2b; x2 < x2e; ++x2) {
           const double t2 = __dsub_rn(t, en[x2]);
-          const double* base = w + pp + n01 * (x2 + int64_t(n2) * x3) + s4 * int64_t(n4) * x5;
+          double* base = w + pp + n01 * (x2 + int64_t(n2) * x3) + s4 * int64_t(n4) * x5;
           for (int x4 = 0; x4 < n4; x4 += kEnLoads) {
             double v[kEnLoads];
 #pragma unroll
-            for (int k = 0; k < kEnLoads; ++k) v[k] = x4 + k < n4 ? __ldg(base + s4 * (x4 + k)) : 0.0;
+            for (int k = 0; k < kEnLoads; ++k) v[k] = x4 + k < n4 ? load(base + s4 * (x4 + k)) : 0.0;
 #pragma unroll
-            for (int k = 0; k < kEnLoads; ++k)
-              if (nonzero(v[k])) acc = fma(v[k], div_rn(v[k], __dsub_rn(t2, en[n2 + x4 + k])), acc);
+            for (int k = 0; k < kEnLoads; ++k) {
+              if constexpr (DIVIDE) {
+                if (x4 + k < n4) base[s4 * (x4 + k)] = div_rn(v[k], __dsub_rn(t2, en[n2 + x4 + k]));
+              } else if (nonzero(v[k])) {
+                acc = fma(v[k], div_rn(v[k], __dsub_rn(t2, en[n2 + x4 + k])), acc);
+              }
+            }
           }
         }
       }
     }
   }
-  block_sum_to(acc, partial, int64_t(blockIdx.y) * gridDim.x + blockIdx.x);
+  if constexpr (!DIVIDE) block_sum_to(acc, partial, int64_t(blockIdx.y) * gridDim.x + blockIdx.x);
 }
 
 // Any other storage order or rank: the whole chain per element (den_eps, the
@@ -809,10 +828,46 @@ static DenParams den_params(int rank0, const int* off, const int* ext0, const in
   return p;
 }
 
+// Grid of the chain walk (rank 4 or 6 in the denominator's order): a thread
+// per (x0, x1) position (the positions split evenly over gx CTAs of at most
+// 512 threads); units (x3 [x5], an x2 range) spread over enough CTAs to fill
+// the GPU a few times, at most max_ctas in all.
+struct ChainGrid {
+  int64_t gx = 0, gy = 0, nunits = 0;
+  int threads = 0, per = 0;
+  size_t smem = 0;
+};
+ChainGrid chain_grid(int rank0, const int* ext0, int64_t max_ctas) {
+  ChainGrid g;
+  const int sms = ctx()->num_sms > 0 ? ctx()->num_sms : 152;
+  const int64_t n01 = int64_t(ext0[0]) * ext0[1];
+  g.gx = (n01 + kEnThreads - 1) / kEnThreads;
+  g.threads = int(((n01 + g.gx - 1) / g.gx + 31) / 32 * 32);
+  const int64_t nocc = rank0 == 6 ? int64_t(ext0[3]) * ext0[5] : ext0[3];
+  const int64_t want = 16LL * sms;  // CTAs
+  const int chunks = int(std::max<int64_t>(1, std::min<int64_t>(ext0[2], (want / g.gx + nocc - 1) / nocc)));
+  g.per = (ext0[2] + chunks - 1) / chunks;
+  g.nunits = nocc * ((ext0[2] + g.per - 1) / g.per);
+  g.gy = std::max<int64_t>(1, std::min<int64_t>({g.nunits, std::max<int64_t>(1, want / g.gx), max_ctas / g.gx}));
+  g.smem = size_t(ext0[2] + (rank0 == 6 ? ext0[4] : 0)) * sizeof(double);
+  return g;
+}
+
 int launch_denominator(int rank0, const int* off, const int* ext0, double* data, int rank1,
                        int ld1, const double* e_or_fock, cudaStream_t s) {
   int64_t n = 0;
   const DenParams p = den_params(rank0, off, ext0, nullptr, rank1, ld1, &n);
+  if (n == 0) return A4G_OK;
+  if (rank0 == 4 || rank0 == 6) {
+    // the chain's prefix formed once per unit: one FP64 subtraction per element
+    const ChainGrid g = chain_grid(rank0, ext0, 0x7fffffffLL);
+    if (g.smem <= 48 * 1024 && g.gx <= 0x7fffffffLL && g.gy <= 65535) {
+      energy_chain_kernel<true><<<dim3(unsigned(g.gx), unsigned(g.gy)), g.threads, g.smem, s>>>(
+          p, data, e_or_fock, g.per, g.nunits, nullptr);
+      A4G_CUDA(cudaGetLastError());
+      return A4G_OK;
+    }
+  }
   denominator_kernel<<<grid_for((n + kDenRun - 1) / kDenRun), kThreads, 0, s>>>(p, data, e_or_fock, n);
   A4G_CUDA(cudaGetLastError());
   return A4G_OK;
@@ -854,23 +909,12 @@ int launch_energy_contract(int rank0, const int* off, const int* ext0, const int
   const int sms = ctx()->num_sms > 0 ? ctx()->num_sms : 152;
   const int64_t n01 = rank0 >= 2 ? int64_t(ext0[0]) * ext0[1] : n;
   if (identity && (rank0 == 4 || rank0 == 6) && n01 <= kEnThreads * int64_t(scratch_len)) {
-    // a thread per (x0, x1) position (the positions split evenly over gx
-    // CTAs of at most 512 threads); units (x3 [x5], x2 range) spread over
-    // enough CTAs to fill the GPU a few times, at most scratch_len partials
-    const int64_t gx = (n01 + kEnThreads - 1) / kEnThreads;
-    const int threads = int(((n01 + gx - 1) / gx + 31) / 32 * 32);
-    const int64_t nocc = rank0 == 6 ? int64_t(ext0[3]) * ext0[5] : ext0[3];
-    const int64_t want = 16LL * sms;  // CTAs
-    const int chunks = int(std::max<int64_t>(1, std::min<int64_t>(ext0[2], (want / gx + nocc - 1) / nocc)));
-    const int per = (ext0[2] + chunks - 1) / chunks;
-    const int64_t nunits = nocc * ((ext0[2] + per - 1) / per);
-    const int64_t gy = std::max<int64_t>(1, std::min<int64_t>({nunits, std::max<int64_t>(1, want / gx),
-                                                                scratch_len / gx}));
-    const size_t smem = size_t(ext0[2] + (rank0 == 6 ? ext0[4] : 0)) * sizeof(double);
-    if (smem > 48 * 1024) return fail(A4G_ERR_RANGE, "energy contraction: segments too large");
-    energy_chain_kernel<<<dim3(unsigned(gx), unsigned(gy)), threads, smem, s>>>(p, w, e_or_fock, per, nunits,
-                                                                                d_scratch);
-    energy_final_kernel<<<1, kThreads, 0, s>>>(d_scratch, int(gx * gy), efact, esum);
+    // at most scratch_len partials (one per CTA)
+    const ChainGrid g = chain_grid(rank0, ext0, scratch_len);
+    if (g.smem > 48 * 1024) return fail(A4G_ERR_RANGE, "energy contraction: segments too large");
+    energy_chain_kernel<false><<<dim3(unsigned(g.gx), unsigned(g.gy)), g.threads, g.smem, s>>>(
+        p, const_cast<double*>(w), e_or_fock, g.per, g.nunits, d_scratch);
+    energy_final_kernel<<<1, kThreads, 0, s>>>(d_scratch, int(g.gx * g.gy), efact, esum);
   } else {
     const int g = int(std::min<int64_t>({int64_t(scratch_len), 8LL * sms,
                                          std::max<int64_t>(1, (n + kThreads * kDenRun - 1) / (kThreads * kDenRun))}));

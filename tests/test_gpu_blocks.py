@@ -255,6 +255,29 @@ def test_energy_denominator_bit_exact(lib, rank0, rank1):
     np.testing.assert_array_equal(a, b)
 
 
+@pytest.mark.parametrize("rank0,rank1,ext0", [(4, 2, [40, 30, 37, 11]), (4, 1, [17, 33, 5, 3]),
+                                               (6, 2, [24, 7, 23, 6, 13, 5])])
+def test_energy_denominator_large_bit_exact(lib, rank0, rank1, ext0):
+    """Blocks that spread over several CTAs, with x2 (and x4) ranges that are
+    not multiples of the loads in flight, zeros among the data (0 / eps keeps
+    the IEEE sign): bit for bit against the oracle."""
+    rng = np.random.default_rng(sum(ext0))
+    segs = [40, 30, 37, 11, 17, 33, 5, 3, 24, 7, 23, 6, 13]
+    norb = sum(segs)
+    eps = np.concatenate([rng.uniform(-2, -0.3, norb // 3), rng.uniform(0.2, 5, norb - norb // 3)])
+    fock = np.diag(eps) + 0.01 * rng.standard_normal((norb, norb))
+    f1 = fock.ravel(order="F").copy() if rank1 == 2 else eps.copy()
+    ext1 = [norb, norb] if rank1 == 2 else [norb]
+    iv = [segs.index(x) + 1 for x in ext0]
+    data = rng.standard_normal(kat.size(ext0))
+    data[::17] = 0.0
+    a, b = data.copy(), data.copy()
+    assert lib.ref.set_predefined_int_array("moa_seg_ranges", segs) == 0
+    assert lib.ref.energy_denominator_rhf(iv, ext0, a, ext1, f1) == 0
+    assert oracle.energy_denominator_rhf(iv, ext0, b, ext1, f1, segs) == 0
+    assert np.array_equal(a.view(np.int64), b.view(np.int64))
+
+
 def test_legacy_gpu_api(lib):
     import ctypes
 
