@@ -588,6 +588,14 @@ __device__ __forceinline__ double eps_at_upd(const UpdParams& p, const double* e
   return p.rank1 == 2 ? e[int64_t(orb) + int64_t(orb) * p.ld1] : e[orb];
 }
 
+// x / 2 without the FP64 pipe where that is an exponent decrement (normal x
+// whose half is normal); the FP64 multiply otherwise (the same bits either way)
+__device__ __forceinline__ double half_of(double x) {
+  const unsigned long long b = bits_of(x);
+  const unsigned f = unsigned(b >> 52) & 0x7FFu;
+  return f >= 2u && f != 0x7FFu ? double_of(b - (1ull << 52)) : __dmul_rn(x, 0.5);
+}
+
 __global__ void __launch_bounds__(256) update_t2_kernel(UpdParams p, const double* __restrict__ xn,
                                                         const double* __restrict__ xnp,
                                                         const double* __restrict__ xo,
@@ -613,19 +621,23 @@ __global__ void __launch_bounds__(256) update_t2_kernel(UpdParams p, const doubl
     po[k][tx] = vo;
   }
   __syncthreads();
-  const double eij = __dadd_rn(eps_at_upd(p, e, p.oi + i), eps_at_upd(p, e, p.oj + j));
+  // (e_i + e_j) - e_a once per thread (a is fixed per thread), - e_b per element
+  const int a = a0 + tx;
+  const double eija = a < p.ea ? __dsub_rn(__dadd_rn(eps_at_upd(p, e, p.oi + i), eps_at_upd(p, e, p.oj + j)),
+                                           eps_at_upd(p, e, p.oa + a))
+                               : 0.0;
   double acc = 0.0;
   for (int k = ty; k < 32; k += 8) {
-    const int a = a0 + tx, b = b0 + k;
+    const int b = b0 + k;
     if (a >= p.ea || b >= p.eb) continue;
     const int64_t q = a + int64_t(p.ea) * (i + int64_t(p.ei) * (b + int64_t(p.eb) * j));
     const double t = __dadd_rn(pn[tx][k], __ldg(xn + q));
     const double t1 = __dadd_rn(po[tx][k], __ldg(xo + q));
-    const double eps = __dsub_rn(__dsub_rn(eij, eps_at_upd(p, e, p.oa + a)), eps_at_upd(p, e, p.ob + b));
+    const double eps = __dsub_rn(eija, eps_at_upd(p, e, p.ob + b));
     const double td = div_rn(t, eps);
-    const double ev = __dmul_rn(__dsub_rn(t1, td), -0.5);
+    const double ev = double_of(bits_of(half_of(__dsub_rn(t1, td))) ^ (1ull << 63));  // -0.5 (t1 - td)
     if (err) err[q] = ev;
-    next[q] = fabs(td) >= 0x1p-1021 ? __dmul_rn(td, 0.5) : __ddiv_rn(__dmul_rn(t, 0.5), eps);
+    next[q] = fabs(td) >= 0x1p-1021 ? half_of(td) : __ddiv_rn(__dmul_rn(t, 0.5), eps);
     acc = fma(ev, ev, acc);
   }
   __shared__ double red[8];
